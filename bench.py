@@ -1,0 +1,298 @@
+"""Benchmark: fwd+bwd field samples/s on the 3-D SDF regression workload (262,144 points/step).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl native|reference]
+
+One step = one fwd+bwd pass of the field hot path over one batch: gradients zeroed, field
+forward (mapping, basis + coefficient gathers, product, MLP head), L1 loss gradient, MLP
+backward and the scatter of the grid gradients. Inputs (262,144 points + SDF targets) are
+resident in HBM for `value`; `e2e` times the public API from pinned host buffers (H2D copy of
+the batch and D2H of the loss inside the timed region). L2 is flushed (256 MB write) before
+every timed step and each step is timed alone with CUDA events.
+
+--impl reference times the reference's own CPU PyTorch op sequence (oracle/ref_torch.py) on
+the host cores, on a bounded sample of the same workload. Under torchrun each rank runs an
+independent replica on its own GPU (the path shards by points: no collective on the data
+path); `value` is the sum over ranks of points / max-over-ranks time.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+import torch
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = "cfg1: 3-D SDF fit, 6-level grid basis [4,4,4,2,2,2] @ [32..128]^3, coeff 18x32^3, 2x64 ReLU head, L1"
+N_POINTS = 262144
+METRIC = "fwd+bwd field samples/s"
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index, self.rows, self.proc = index, [], None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm = [float(r[1]) for r in self.rows if len(r) > 8 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) > 8 and r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            if len(r) > 8:
+                for nm, v in zip(names, r[5:9]):
+                    if v.lower().startswith("active"):
+                        reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def flush_l2(buf):
+    buf.zero_()
+
+
+def make_model(precision):
+    from factor_fields_gb300 import FactorFields
+    from factor_fields_gb300 import workloads as W
+    torch.manual_seed(0)
+    m = FactorFields(W.field_cfg("cfg1"), device="cuda", precision=precision)
+    g = torch.Generator(device="cpu").manual_seed(1)
+    with torch.no_grad():  # a mid-training-like state: random coefficients
+        for c in m.coeffs:
+            c.copy_(torch.rand(c.shape, generator=g) * 2 - 1)
+    return m
+
+
+def bytes_per_point(m, gathers, param_bytes):
+    """Algorithmic bytes per point: `gathers` passes over K corners x (sum C + C_coeff)
+    channels at param_bytes, one float32 scatter of the same, coords (12 B) + target (4 B)."""
+    k = 2 ** m.in_dim
+    ch = m.n_feat * 2
+    return gathers * k * ch * param_bytes + k * ch * 4 + 12 + 4
+
+
+def run_native(args, ws, rank, local):
+    from factor_fields_gb300 import _native as N
+    from factor_fields_gb300 import workloads as W
+    from factor_fields_gb300 import train as T
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    n = N_POINTS
+    nb = 8  # distinct batches cycled through (seeded, generated on the host)
+    batches = [W.sdf_batch(1000 * rank + i, n) for i in range(nb)]
+    host = [(torch.from_numpy(x).pin_memory(), torch.from_numpy(y).pin_memory()) for x, y in batches]
+    devb = [(x.to(dev), y.to(dev)) for x, y in host]
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MB > L2
+
+    res = {}
+    # ---- fast path: fused BF16 (falls back to the float32 drop-in step only if absent) ----
+    m = make_model("bf16")
+    runner = T.FieldFitRunner(m, loss="l1")
+    stream = torch.cuda.current_stream()
+
+    def timed(step_fn, k, with_kernel_events):
+        times, ktimes = [], []
+        for i in range(k):
+            flush_l2(flush)
+            torch.cuda.synchronize()
+            if ws > 1:
+                torch.distributed.barrier()
+            s0 = torch.cuda.Event(enable_timing=True)
+            s1 = torch.cuda.Event(enable_timing=True)
+            s0.record(stream)
+            kev = step_fn(i)
+            s1.record(stream)
+            torch.cuda.synchronize()
+            times.append(s0.elapsed_time(s1))
+            if with_kernel_events and kev is not None:
+                ktimes.append(kev[0].elapsed_time(kev[1]))
+        return times, ktimes
+
+    for i in range(args.warmup):
+        runner.step(*devb[i % nb])
+    torch.cuda.synchronize()
+    clocks = Clocks(local)
+    clocks.start()
+    N.reset_launch_count()
+    t_fast, k_fast = timed(lambda i: runner.step(*devb[i % nb], kernel_events=True), args.steps, True)
+    launches = N.launch_count()
+    ck = clocks.stop()
+    ms = float(np.sum(t_fast))
+
+    # ---- end to end through the public API from pinned host memory ----
+    loss_host = torch.empty(1, pin_memory=True)
+
+    def e2e_step(i):
+        x, y = host[i % nb]
+        xd = x.to(dev, non_blocking=True)
+        yd = y.to(dev, non_blocking=True)
+        loss = runner.step(xd, yd)
+        loss_host.copy_(loss.reshape(1), non_blocking=True)
+        return None
+
+    for i in range(args.warmup):
+        e2e_step(i)
+    t_e2e, _ = timed(e2e_step, args.steps, False)
+
+    # ---- the float32 drop-in path (autograd through get_coding / linear_mat) ----
+    md = make_model("fp32")
+
+    def dropin_step(i):
+        x, y = devb[i % nb]
+        md.zero_grad(set_to_none=True)
+        feats, _ = md.get_coding(x)
+        pred = md.linear_mat(feats)
+        (pred - y).abs().mean().backward()
+        return None
+
+    for i in range(args.warmup):
+        dropin_step(i)
+    t_drop, _ = timed(dropin_step, args.steps, False)
+
+    # ---- max over ranks ----
+    tot = torch.tensor([ms, float(np.sum(t_e2e)), float(np.sum(t_drop))], device=dev)
+    if ws > 1:
+        torch.distributed.all_reduce(tot, op=torch.distributed.ReduceOp.MAX)
+    ms, ms_e2e, ms_drop = [float(v) for v in tot.tolist()]
+    pts = n * args.steps * ws
+    value = pts / (ms / 1e3)
+    kern_ms = float(np.mean(k_fast)) if k_fast else None
+    bpp = bytes_per_point(m, runner.gathers_per_point, 2 if m.precision == "bf16" else 4)
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except OSError:
+        pass
+    peak = peaks.get("hbm_gbs", 6800.0)
+    achieved = (bpp * n) / (kern_ms / 1e3) / 1e9 if kern_ms else None
+    res = {
+        "metric": METRIC, "value": value, "unit": "samples/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "bf16 storage, fp32 accumulation" if m.precision == "bf16" else "fp32",
+        "data": "synthetic (seeded analytic SDF: 16 spheres + 8 boxes)",
+        "config": {"workload": WORKLOAD, "points_per_step": n, "loss": "l1", "path": runner.path_name,
+                   "l2": "flushed (256 MB write) before every timed step", "parallelism": f"replicas x{ws}"},
+        "e2e": {"value": pts / (ms_e2e / 1e3), "unit": "samples/s", "h2d_bytes_per_step": n * 16,
+                "d2h_bytes_per_step": 4},
+        "fp32_dropin": {"value": pts / (ms_drop / 1e3), "unit": "samples/s",
+                        "ms_per_step": ms_drop / args.steps},
+        "roofline": {"bound": "hbm", "kernel": runner.dominant_kernel, "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": (achieved / peak) if achieved else None, "traffic": None,
+                     "bytes_per_point": bpp, "kernel_ms": kern_ms,
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if "hbm_gbs" in peaks else "fallback"},
+        "gpu_launches": launches,
+        "clocks": ck,
+    }
+    return res
+
+
+def run_cpu_baseline(n_points, steps, warmup=1):
+    """The reference's CPU op sequence on a bounded sample of the workload: samples/s."""
+    from factor_fields_gb300 import workloads as W
+    from oracle.ref_torch import RefField
+    from factor_fields_gb300.config import FieldGeometry
+    from factor_fields_gb300.field import dct_dict
+    cores = os.cpu_count() or 1
+    torch.set_num_threads(cores)
+    cfg = W.field_cfg("cfg1")
+    g = FieldGeometry(cfg)
+    levels = [dct_dict(int(np.power(c, 1.0 / 3) + 1), r, c, 3).reshape([1, c] + [r] * 3)
+              for c, r in zip(g.basis_dims, g.basis_reso)]
+    gen = torch.Generator().manual_seed(1)
+    coeff = torch.rand([1, 18] + g.coeff_reso, generator=gen) * 2 - 1
+    torch.manual_seed(0)
+    l0, l1 = torch.nn.Linear(18, 64), torch.nn.Linear(64, 1, bias=False)
+    r = RefField("reconstruction", cfg.dataset.aabb, levels, coeff, [l0.weight.detach(), l1.weight.detach()],
+                 [l0.bias.detach(), None], g.freq_bands, "sawtooth")
+    x, y = W.sdf_batch(7, n_points)
+    x, y = torch.from_numpy(x), torch.from_numpy(y)
+    for _ in range(warmup):
+        r.fit_step(x, y)
+    best = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        r.fit_step(x, y)
+        best.append(time.perf_counter() - t0)
+    t = min(best)
+    return {"value": n_points / t, "unit": "samples/s", "cores": cores, "kind": "port",
+            "sample": f"{n_points} points of the same workload per step, best of {steps} after {warmup} warm-up "
+                      "(torch CPU restatement of the reference's grid_sample/MLPMixer op sequence, "
+                      "oracle/ref_torch.py)"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="native", choices=["native", "reference"])
+    ap.add_argument("--cpu-points", type=int, default=32768)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    ws, rank, local = dist_env()
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        cb = run_cpu_baseline(args.cpu_points, max(args.steps // 5, 3), warmup=min(args.warmup, 1))
+        line = {"metric": METRIC, "value": cb["value"], "unit": "samples/s", "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "fp32", "data": "synthetic (seeded analytic SDF: 16 spheres + 8 boxes)",
+                "config": {"workload": WORKLOAD, "points_per_step": args.cpu_points}, "impl": "reference",
+                "cpu_baseline": cb, "e2e": {"value": cb["value"], "unit": "samples/s", "h2d_bytes_per_step": 0,
+                                            "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return 0
+    if ws > 1:
+        torch.distributed.init_process_group("nccl", device_id=torch.device("cuda", local))
+    res = run_native(args, ws, rank, local)
+    if rank == 0:
+        if not args.no_cpu_baseline:
+            res["cpu_baseline"] = run_cpu_baseline(args.cpu_points, 3)
+        print(json.dumps(res))
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

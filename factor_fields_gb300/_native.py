@@ -1,0 +1,128 @@
+"""ctypes binding of libffgb.so (the C ABI declared in include/ff_native.h).
+
+The library is built in-tree by factor_fields_gb300.build and loaded from this package's
+directory. There is no fallback: if the library is missing or cannot be loaded, every
+operation raises. Device pointers come from torch tensors; work is enqueued on torch's
+current CUDA stream.
+"""
+import ctypes
+import os
+import threading
+
+import torch
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "libffgb.so")
+
+FF_MAX_LEVELS = 8
+FF_MAX_MLP_LAYERS = 4
+FF_OK, FF_ERR_ARG, FF_ERR_UNSUPPORTED, FF_ERR_ALIGN, FF_ERR_CUDA, FF_ERR_SIZE = 0, -1, -2, -3, -4, -5
+FF_MAP = {"sawtooth": 0, "triangle": 1}
+FF_INTERP = {"bilinear": 0, "linear": 0, "trilinear": 0, "nearest": 1}
+FF_F32, FF_BF16 = 0, 1
+FF_LOSS = {"l1": 0, "mse": 1}
+
+c_i32, c_i64, c_f32, c_vp = ctypes.c_int32, ctypes.c_int64, ctypes.c_float, ctypes.c_void_p
+
+
+class FFField(ctypes.Structure):
+    _fields_ = [
+        ("basis_dim", c_i32), ("coord_dim", c_i32), ("n_levels", c_i32), ("mapping", c_i32),
+        ("basis_interp", c_i32), ("coeff_interp", c_i32), ("param_dtype", c_i32), ("n_feat", c_i32),
+        ("level_channels", c_i32 * FF_MAX_LEVELS), ("level_stride", c_i32 * FF_MAX_LEVELS),
+        ("level_vec", c_i32 * FF_MAX_LEVELS), ("level_reso", c_i32 * FF_MAX_LEVELS),
+        ("level_offset", c_i64 * FF_MAX_LEVELS), ("level_scale", c_f32 * FF_MAX_LEVELS),
+        ("map_origin", c_f32 * 3), ("coeff_reso", c_i32 * 3), ("coeff_stride", c_i32),
+        ("coeff_origin", c_f32 * 3), ("coeff_inv_size", c_f32 * 3),
+    ]
+
+
+class FFMlp(ctypes.Structure):
+    _fields_ = [("n_layers", c_i32), ("in_dim", c_i32), ("hidden_dim", c_i32), ("out_dim", c_i32),
+                ("weight", c_vp * FF_MAX_MLP_LAYERS), ("bias", c_vp * FF_MAX_MLP_LAYERS)]
+
+
+class FFMlpGrad(ctypes.Structure):
+    _fields_ = [("weight", c_vp * FF_MAX_MLP_LAYERS), ("bias", c_vp * FF_MAX_MLP_LAYERS)]
+
+
+# (name, restype, argtypes) of every exported entry point.
+_P = ctypes.POINTER
+SIGNATURES = {
+    "ff_abi_version": (c_i32, []),
+    "ff_last_error": (ctypes.c_char_p, []),
+    "ff_struct_size": (c_i64, [c_i32]),
+    "ff_device_info": (c_i32, [_P(c_i32), _P(c_i32)]),
+    "ff_field_forward": (c_i32, [_P(FFField), c_vp, c_vp, c_vp, c_i64, c_vp, c_vp, c_vp, c_vp]),
+    "ff_field_backward": (c_i32, [_P(FFField), c_vp, c_vp, c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
+    "ff_mlp_forward": (c_i32, [_P(FFMlp), c_vp, c_i64, c_vp, c_vp]),
+    "ff_mlp_backward": (c_i32, [_P(FFMlp), c_vp, c_i64, c_vp, c_vp, _P(FFMlpGrad), c_vp]),
+}
+
+_lib = None
+_lock = threading.Lock()
+
+
+class NativeError(RuntimeError):
+    pass
+
+
+def load(path=LIB_PATH):
+    """Load (once) and return the ctypes handle of libffgb.so; raises if it is absent."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if not os.path.exists(path):
+            raise NativeError(f"{path} is not built: run `python -m factor_fields_gb300.build` "
+                              "(the CUDA extension is required; there is no fallback)")
+        lib = ctypes.CDLL(path)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+        return lib
+
+
+def lib():
+    return _lib if _lib is not None else load()
+
+
+def check(rc, what):
+    if rc != FF_OK:
+        msg = lib().ff_last_error().decode(errors="replace")
+        raise NativeError(f"{what} failed (code {rc}): {msg}")
+
+
+def ptr(t):
+    """Device pointer of a tensor (or None -> NULL)."""
+    if t is None:
+        return None
+    if not t.is_cuda:
+        raise NativeError("expected a CUDA tensor")
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def stream_ptr():
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+_launches = [0]
+_NON_LAUNCHING = {"ff_abi_version", "ff_last_error", "ff_device_info", "ff_struct_size"}
+
+
+def reset_launch_count():
+    _launches[0] = 0
+
+
+def launch_count():
+    """Entry-point calls that enqueue kernels since the last reset (each enqueues one kernel)."""
+    return _launches[0]
+
+
+def call(name, *args):
+    rc = getattr(lib(), name)(*args)
+    check(rc, name)
+    if name not in _NON_LAUNCHING:
+        _launches[0] += 1

@@ -1,0 +1,162 @@
+// extern "C" entry points of libffgb.so (declared in include/ff_native.h): argument
+// validation, error reporting and dispatch to the kernel launchers.
+#include <cstdio>
+#include <string>
+
+#include "ff_common.cuh"
+#include "ff_internal.h"
+
+namespace ffgb {
+
+namespace {
+thread_local std::string g_last_error;
+}
+
+int set_error(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+int sm_count() {
+  static int cached[64] = {0};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 148;
+  if (cached[dev] == 0) {
+    int v = 0;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0) v = 148;
+    cached[dev] = v;
+  }
+  return cached[dev];
+}
+
+static int cuda_status(cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return FF_OK;
+  return set_error(FF_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+static bool aligned(const void* p, int bytes) { return (reinterpret_cast<uintptr_t>(p) % bytes) == 0; }
+
+// Validates an FFField; returns FF_OK or an error code with ff_last_error set.
+static int validate_field(const FFField* f, const void* basis, const void* coeff) {
+  if (!f) return set_error(FF_ERR_ARG, "field descriptor is NULL");
+  if (!(f->basis_dim == 2 || f->basis_dim == 3)) return set_error(FF_ERR_ARG, "basis_dim must be 2 or 3");
+  if (!(f->coord_dim == f->basis_dim || (f->basis_dim == 2 && f->coord_dim == 3)))
+    return set_error(FF_ERR_UNSUPPORTED, "coord_dim must equal basis_dim (or be 3 with a 2-D basis: 'images' mode)");
+  if (f->n_levels < 1 || f->n_levels > FF_MAX_LEVELS) return set_error(FF_ERR_ARG, "n_levels out of range 1..8");
+  if (f->mapping != FF_MAP_SAWTOOTH && f->mapping != FF_MAP_TRIANGLE)
+    return set_error(FF_ERR_UNSUPPORTED, "basis_mapping must be sawtooth or triangle");
+  if ((f->basis_interp != FF_INTERP_LINEAR && f->basis_interp != FF_INTERP_NEAREST) ||
+      (f->coeff_interp != FF_INTERP_LINEAR && f->coeff_interp != FF_INTERP_NEAREST))
+    return set_error(FF_ERR_ARG, "interpolation mode must be linear or nearest");
+  if (f->param_dtype != FF_F32 && f->param_dtype != FF_BF16) return set_error(FF_ERR_ARG, "param_dtype must be F32 or BF16");
+  const int es = f->param_dtype == FF_F32 ? 4 : 2;
+  if (!basis || !coeff) return set_error(FF_ERR_ARG, "basis/coeff pointer is NULL");
+  if (!aligned(basis, 16) || !aligned(coeff, 16)) return set_error(FF_ERR_ALIGN, "basis/coeff must be 16-byte aligned");
+  int sum = 0;
+  for (int l = 0; l < f->n_levels; ++l) {
+    const int c = f->level_channels[l], v = f->level_vec[l];
+    if (c < 1 || f->level_reso[l] < 1 || f->level_stride[l] < c) return set_error(FF_ERR_ARG, "bad level channels/reso/stride");
+    if (!(v == 1 || v == 2 || v == 4) || c % v || f->level_stride[l] % v || f->level_offset[l] % v || sum % v ||
+        f->coeff_stride % v)
+      return set_error(FF_ERR_ALIGN, "level_vec does not divide channels/stride/offset of level " + std::to_string(l));
+    if (f->level_scale[l] <= 0.f) return set_error(FF_ERR_ARG, "level_scale must be > 0");
+    int64_t cells = 1;
+    for (int k = 0; k < f->basis_dim; ++k) cells *= f->level_reso[l];
+    if (cells > (1ll << 31) / 8) return set_error(FF_ERR_SIZE, "basis level too large");
+    sum += c;
+  }
+  if (sum != f->n_feat) return set_error(FF_ERR_ARG, "n_feat != sum(level_channels)");
+  if (f->coeff_stride < f->n_feat) return set_error(FF_ERR_ARG, "coeff_stride < n_feat");
+  int64_t cells = 1;
+  for (int k = 0; k < f->coord_dim; ++k) {
+    if (f->coeff_reso[k] < 1) return set_error(FF_ERR_ARG, "coeff_reso must be >= 1");
+    cells *= f->coeff_reso[k];
+  }
+  if (cells > (1ll << 31) / 8) return set_error(FF_ERR_SIZE, "coefficient grid too large");
+  (void)es;
+  return FF_OK;
+}
+
+static int validate_mlp(const FFMlp* m) {
+  if (!m) return set_error(FF_ERR_ARG, "mlp descriptor is NULL");
+  if (m->n_layers < 1 || m->n_layers > FF_MAX_MLP_LAYERS) return set_error(FF_ERR_UNSUPPORTED, "n_layers must be 1..4");
+  if (m->in_dim < 1 || m->out_dim < 1 || (m->n_layers > 1 && m->hidden_dim < 1))
+    return set_error(FF_ERR_ARG, "bad MLP dims");
+  for (int l = 0; l < m->n_layers; ++l)
+    if (!m->weight[l]) return set_error(FF_ERR_ARG, "MLP weight pointer is NULL");
+  return FF_OK;
+}
+
+}  // namespace ffgb
+
+using namespace ffgb;
+
+extern "C" {
+
+int ff_abi_version(void) { return FF_ABI_VERSION; }
+
+const char* ff_last_error(void) { return g_last_error.c_str(); }
+
+int64_t ff_struct_size(int32_t which) {
+  switch (which) {
+    case 0: return (int64_t)sizeof(FFField);
+    case 1: return (int64_t)sizeof(FFMlp);
+    case 2: return (int64_t)sizeof(FFMlpGrad);
+    default: return -1;
+  }
+}
+
+int ff_device_info(int32_t* sms, int32_t* cc) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_status(e, "cudaGetDevice");
+  int ma = 0, mi = 0;
+  cudaDeviceGetAttribute(&ma, cudaDevAttrComputeCapabilityMajor, dev);
+  cudaDeviceGetAttribute(&mi, cudaDevAttrComputeCapabilityMinor, dev);
+  if (sms) *sms = sm_count();
+  if (cc) *cc = ma * 10 + mi;
+  return FF_OK;
+}
+
+int ff_field_forward(const FFField* f, const void* basis, const void* coeff, const float* x, int64_t n, float* feats,
+                     float* coeff_out, float* basis_out, void* stream) {
+  int rc = validate_field(f, basis, coeff);
+  if (rc) return rc;
+  if (n < 0 || (n > 0 && !x)) return set_error(FF_ERR_ARG, "bad points pointer or count");
+  return cuda_status(launch_field_forward(*f, basis, coeff, x, n, feats, coeff_out, basis_out, (cudaStream_t)stream),
+                     "ff_field_forward launch");
+}
+
+int ff_field_backward(const FFField* f, const void* basis, const void* coeff, const float* x, int64_t n,
+                      const float* grad_feats, const float* grad_coeff_out, const float* grad_basis_out,
+                      float* grad_basis, float* grad_coeff_grid, void* stream) {
+  int rc = validate_field(f, basis, coeff);
+  if (rc) return rc;
+  if (n < 0 || (n > 0 && !x)) return set_error(FF_ERR_ARG, "bad points pointer or count");
+  if ((grad_basis && !aligned(grad_basis, 16)) || (grad_coeff_grid && !aligned(grad_coeff_grid, 16)))
+    return set_error(FF_ERR_ALIGN, "gradient buffers must be 16-byte aligned");
+  return cuda_status(launch_field_backward(*f, basis, coeff, x, n, grad_feats, grad_coeff_out, grad_basis_out,
+                                           grad_basis, grad_coeff_grid, (cudaStream_t)stream),
+                     "ff_field_backward launch");
+}
+
+int ff_mlp_forward(const FFMlp* m, const float* x, int64_t n, float* out, void* stream) {
+  int rc = validate_mlp(m);
+  if (rc) return rc;
+  if (n < 0 || (n > 0 && (!x || !out))) return set_error(FF_ERR_ARG, "bad x/out pointer or count");
+  if (mlp_smem_bytes(*m, false, nullptr) < 0) return set_error(FF_ERR_UNSUPPORTED, "MLP too large for shared memory");
+  return cuda_status(launch_mlp_forward(*m, x, n, out, (cudaStream_t)stream), "ff_mlp_forward launch");
+}
+
+int ff_mlp_backward(const FFMlp* m, const float* x, int64_t n, const float* grad_out, float* grad_x, const FFMlpGrad* g,
+                    void* stream) {
+  int rc = validate_mlp(m);
+  if (rc) return rc;
+  if (n < 0 || (n > 0 && (!x || !grad_out))) return set_error(FF_ERR_ARG, "bad x/grad_out pointer or count");
+  if (mlp_smem_bytes(*m, true, nullptr) < 0) return set_error(FF_ERR_UNSUPPORTED, "MLP too large for shared memory");
+  FFMlpGrad none = {};
+  return cuda_status(launch_mlp_backward(*m, x, n, grad_out, grad_x, g ? *g : none, (cudaStream_t)stream),
+                     "ff_mlp_backward launch");
+}
+
+}  // extern "C"

@@ -1,0 +1,191 @@
+// Shared device helpers for the Factor Fields sm_103a kernels.
+//
+// Arithmetic that decides which grid cell, sample or occupancy bit is used is written with
+// explicitly rounded intrinsics (__fadd_rn, __fmul_rn, __fdiv_rn ...) in the same operation
+// order as the reference's PyTorch ops, so that the compiler cannot contract it into FMAs and
+// indices / interpolation weights come out bit-identical to the reference's float32 values.
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/ff_native.h"
+
+namespace ffgb {
+
+constexpr int kMapSawtooth = FF_MAP_SAWTOOTH;
+constexpr int kMapTriangle = FF_MAP_TRIANGLE;
+
+// ---------------------------------------------------------------------------------------
+// float32 arithmetic with Python / ATen semantics
+// ---------------------------------------------------------------------------------------
+
+// torch.remainder for floats: fmod (exact) shifted into the divisor's sign.
+__device__ __forceinline__ float py_rem(float a, float b) {
+  float m = fmodf(a, b);
+  if (m != 0.f && ((b < 0.f) != (m < 0.f))) m = __fadd_rn(m, b);
+  return m;
+}
+
+// torch.floor_divide for floats (c10::div_floor_floating).
+__device__ __forceinline__ float py_floordiv(float a, float b) {
+  float mod = fmodf(a, b);
+  float div = __fdiv_rn(__fsub_rn(a, mod), b);
+  if (mod != 0.f && ((b < 0.f) != (mod < 0.f))) div = __fsub_rn(div, 1.f);
+  float fl;
+  if (div != 0.f) {
+    fl = floorf(div);
+    if (__fsub_rn(div, fl) > 0.5f) fl = __fadd_rn(fl, 1.f);
+  } else {
+    fl = copysignf(0.f, __fdiv_rn(a, b));
+  }
+  return fl;
+}
+
+// grid_mapping (models/FactorFields.py:11-22) for one coordinate and one level.
+__device__ __forceinline__ float map_coord(float p, float origin, float scale, int mapping) {
+  const float rel = __fsub_rn(p, origin);
+  const float half = __fmul_rn(scale, 0.5f);  // scale / 2, exact
+  const float m = py_rem(rel, scale);
+  float loc = __fsub_rn(__fdiv_rn(m, half), 1.f);
+  if (mapping == kMapTriangle) {
+    const float odd = py_rem(py_floordiv(rel, scale), 2.f);
+    if (odd == 1.f) loc = -loc;
+  } else {
+    loc = fminf(fmaxf(loc, -1.f), 1.f);
+  }
+  return loc;
+}
+
+// ATen grid_sampler_unnormalize + border clip (grid_sampler_compute_source_index).
+__device__ __forceinline__ float unnorm_align(float c, int size) {  // align_corners=True
+  return __fmul_rn(__fmul_rn(__fadd_rn(c, 1.f), 0.5f), (float)(size - 1));
+}
+__device__ __forceinline__ float unnorm_noalign_border(float c, int size) {  // False + border
+  float ix = __fmul_rn(__fsub_rn(__fmul_rn(__fadd_rn(c, 1.f), (float)size), 1.f), 0.5f);
+  return fminf((float)(size - 1), fmaxf(ix, 0.f));
+}
+
+// normalize_coord (models/FactorFields.py:635-637).
+__device__ __forceinline__ float normalize_coord(float x, float origin, float inv) {
+  return __fsub_rn(__fmul_rn(__fsub_rn(x, origin), inv), 1.f);
+}
+
+// ---------------------------------------------------------------------------------------
+// interpolation corners
+// ---------------------------------------------------------------------------------------
+
+// Corner set of one bi/trilinear (or nearest) lookup. idx < 0 marks an out-of-bounds corner
+// (zero padding): it is neither read nor scattered to. Order: x fastest, then y, then z
+// (ATen's nw, ne, sw, se, [bnw ... bse]).
+template <int D>
+struct Corners {
+  static constexpr int K = 1 << D;
+  int32_t idx[K];
+  float w[K];
+};
+
+// Linear corners for coordinates already unnormalised to grid units (ix[k] along axis k,
+// size[k] cells). Weights: low corner (x0 + 1) - ix, high corner ix - x0 (both exact), and
+// the product is formed x*y*z in that order like ATen.
+template <int D>
+__device__ __forceinline__ void linear_corners(const float* ix, const int* size, Corners<D>& c) {
+  int lo[D];
+  float wl[D], wh[D];
+#pragma unroll
+  for (int k = 0; k < D; ++k) {
+    const float f = floorf(ix[k]);
+    lo[k] = (int)f;
+    wl[k] = __fsub_rn(__fadd_rn(f, 1.f), ix[k]);
+    wh[k] = __fsub_rn(ix[k], f);
+  }
+#pragma unroll
+  for (int b = 0; b < (1 << D); ++b) {
+    float w;
+    int flat = 0;
+    bool ok = true;
+#pragma unroll
+    for (int k = D - 1; k >= 0; --k) {
+      const int ck = lo[k] + ((b >> k) & 1);
+      ok = ok && (ck >= 0) && (ck < size[k]);
+      flat = flat * size[k] + ck;
+    }
+    w = (b & 1) ? wh[0] : wl[0];
+#pragma unroll
+    for (int k = 1; k < D; ++k) w = __fmul_rn(w, ((b >> k) & 1) ? wh[k] : wl[k]);
+    c.idx[b] = ok ? flat : -1;
+    c.w[b] = ok ? w : 0.f;
+  }
+}
+
+// Nearest corner (nearbyint = round half to even), stored in slot 0 with weight 1.
+template <int D>
+__device__ __forceinline__ void nearest_corner(const float* ix, const int* size, Corners<D>& c) {
+  int flat = 0;
+  bool ok = true;
+#pragma unroll
+  for (int k = D - 1; k >= 0; --k) {
+    const float r = rintf(ix[k]);
+    ok = ok && (r >= 0.f) && (r < (float)size[k]);
+    flat = flat * size[k] + (int)r;
+  }
+  c.idx[0] = ok ? flat : -1;
+  c.w[0] = ok ? 1.f : 0.f;
+#pragma unroll
+  for (int b = 1; b < (1 << D); ++b) {
+    c.idx[b] = -1;
+    c.w[b] = 0.f;
+  }
+}
+
+// ---------------------------------------------------------------------------------------
+// vector loads (float32 / bf16 storage -> float32 registers) and vector atomics
+// ---------------------------------------------------------------------------------------
+
+template <int V>
+__device__ __forceinline__ void load_vec(const float* __restrict__ p, float* v) {
+  if constexpr (V == 4) {
+    const float4 t = __ldg(reinterpret_cast<const float4*>(p));
+    v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
+  } else if constexpr (V == 2) {
+    const float2 t = __ldg(reinterpret_cast<const float2*>(p));
+    v[0] = t.x; v[1] = t.y;
+  } else {
+    v[0] = __ldg(p);
+  }
+}
+
+template <int V>
+__device__ __forceinline__ void load_vec(const __nv_bfloat16* __restrict__ p, float* v) {
+  if constexpr (V == 4) {
+    const uint2 t = __ldg(reinterpret_cast<const uint2*>(p));
+    v[0] = __uint_as_float(t.x << 16); v[1] = __uint_as_float(t.x & 0xffff0000u);
+    v[2] = __uint_as_float(t.y << 16); v[3] = __uint_as_float(t.y & 0xffff0000u);
+  } else if constexpr (V == 2) {
+    const uint32_t t = __ldg(reinterpret_cast<const unsigned int*>(p));
+    v[0] = __uint_as_float(t << 16); v[1] = __uint_as_float(t & 0xffff0000u);
+  } else {
+    const unsigned short t = __ldg(reinterpret_cast<const unsigned short*>(p));
+    v[0] = __uint_as_float(((uint32_t)t) << 16);
+  }
+}
+
+template <int V>
+__device__ __forceinline__ void atomic_add_vec(float* p, const float* v) {
+  if constexpr (V == 4) {
+    atomicAdd(reinterpret_cast<float4*>(p), make_float4(v[0], v[1], v[2], v[3]));
+  } else if constexpr (V == 2) {
+    atomicAdd(reinterpret_cast<float2*>(p), make_float2(v[0], v[1]));
+  } else {
+    atomicAdd(p, v[0]);
+  }
+}
+
+// ---------------------------------------------------------------------------------------
+// misc
+// ---------------------------------------------------------------------------------------
+
+__host__ __device__ __forceinline__ int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+}  // namespace ffgb

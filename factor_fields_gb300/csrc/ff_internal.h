@@ -1,0 +1,34 @@
+// Host-side launchers shared between the kernel translation units and the C-ABI layer.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "../../include/ff_native.h"
+
+namespace ffgb {
+
+// Records an error message for ff_last_error() and returns the code.
+int set_error(int code, const std::string& msg);
+int check_launch(const char* what);  // reads cudaGetLastError after a launch
+int sm_count();                      // SMs of the current device (cached per device)
+
+// field_kernels.cu
+cudaError_t launch_field_forward(const FFField& f, const void* basis, const void* coeff, const float* x,
+                                 int64_t n, float* feats, float* coeff_out, float* basis_out,
+                                 cudaStream_t s);
+cudaError_t launch_field_backward(const FFField& f, const void* basis, const void* coeff, const float* x,
+                                  int64_t n, const float* grad_feats, const float* grad_coeff_out,
+                                  const float* grad_basis_out, float* grad_basis, float* grad_coeff_grid,
+                                  cudaStream_t s);
+
+// mlp_kernels.cu
+// Returns the dynamic shared memory an MLP launch needs, or -1 if the shape cannot fit.
+int64_t mlp_smem_bytes(const FFMlp& m, bool backward, int* tile_points);
+cudaError_t launch_mlp_forward(const FFMlp& m, const float* x, int64_t n, float* out, cudaStream_t s);
+cudaError_t launch_mlp_backward(const FFMlp& m, const float* x, int64_t n, const float* grad_out,
+                                float* grad_x, const FFMlpGrad& g, cudaStream_t s);
+
+}  // namespace ffgb

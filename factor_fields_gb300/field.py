@@ -1,0 +1,285 @@
+"""FactorFields: the reference's model surface (models/FactorFields.py:206) on the native kernels.
+
+The module keeps the reference's constructor, attributes (basis_dims, basis_reso, freq_bands,
+coeff_reso, aabb, in_dim, basises, coeffs, linear_mat, renderModule, alphaMask, stepSize,
+nSamples, scene_idx) and methods (get_coding, get_basis, get_coeff, linear_mat(feats,
+is_train), forward(rays...), get_optparam_groups, n_parameters, save/load), for
+basis_type = coeff_type = 'grid'.
+
+Storage differs from the reference: the grids are channels-last flat float32 parameters
+(basis_flat, coeff_flat; see layout.py). `basises[l]` / `coeffs[s]` return strided views of
+that storage in the reference's [1, C, R, R(, R)] shape, so reading, in-place writes and
+autograd through them work as in the reference.
+
+precision='fp32' is the drop-in path (float32 storage and math, parity 1e-5 with the
+reference). precision='bf16' reads BF16 copies of the grids (refreshed automatically after
+the float32 master parameters change) with float32 accumulation and float32 gradients.
+"""
+import math
+
+import numpy as np
+import torch
+import torch.nn.functional as F
+
+from . import _native as N
+from . import functional as FN
+from .config import FieldGeometry, make_cfg, n_to_reso, render_step
+from .layout import FieldLayout
+
+
+def dct_dict(n_atoms_fre, size, n_select, dim=2):
+    """DCT dictionary used to initialise each basis level (models/FactorFields.py:36-71):
+    cosine atoms cos(pi*k*i/p) with the mean removed (k > 0), their Kronecker product over the
+    dims, n_select evenly spaced atoms, each normalised to unit L2 norm."""
+    p = n_atoms_fre
+    rows = []
+    for k in range(p):
+        atom = np.cos(np.arange(size) * k * math.pi / p)
+        rows.append(atom - np.mean(atom) if k > 0 else atom)
+    table = np.stack(rows)
+    kron = np.kron(table, table)
+    if dim == 3:
+        kron = np.kron(kron, table)
+    if n_select < kron.shape[0]:
+        pick = [chunk[0] for chunk in np.array_split(np.arange(kron.shape[0]), n_select)]
+        kron = kron[pick]
+    for r in range(kron.shape[0]):  # row by row, as the reference does, for a bit-identical init
+        kron[r] /= np.linalg.norm(kron[r]) or 1
+    return torch.from_numpy(kron.astype(np.float32))
+
+
+class MLPMixer(torch.nn.Module):
+    """models/FactorFields.py:113-159: Linear(+bias)+ReLU per hidden layer, last layer without
+    bias and activation. Same parameter names (backbone.i.weight/bias) and init as the
+    reference; the math runs on the native float32 kernels."""
+
+    def __init__(self, in_dim, out_dim=16, num_layers=2, hidden_dim=64, pe=0, with_dropout=False):
+        super().__init__()
+        if pe:
+            raise NotImplementedError("positional encoding inside MLPMixer is not on the grid/grid path")
+        self.with_dropout = with_dropout
+        self.in_dim, self.out_dim = in_dim, out_dim
+        self.num_layers, self.hidden_dim, self.pe = num_layers, hidden_dim, pe
+        layers = []
+        for l in range(num_layers):
+            din = in_dim if l == 0 else hidden_dim
+            last = l == num_layers - 1
+            layers.append(torch.nn.Linear(din, out_dim if last else hidden_dim, bias=not last))
+        self.backbone = torch.nn.ModuleList(layers)
+
+    def weights(self):
+        return [l.weight for l in self.backbone], [l.bias for l in self.backbone]
+
+    def forward(self, x, is_train=False):
+        h = x
+        if self.with_dropout and is_train:
+            h = F.dropout(h, p=0.1)
+        w, b = self.weights()
+        return FN.mlp(h, w, b, self.in_dim, self.hidden_dim, self.out_dim)
+
+
+class FactorFields(torch.nn.Module):
+    def __init__(self, cfg, device="cuda", precision="fp32"):
+        super().__init__()
+        cfg = make_cfg(cfg)
+        if precision not in ("fp32", "bf16"):
+            raise ValueError("precision must be 'fp32' or 'bf16'")
+        self.cfg, self.device, self.precision = cfg, torch.device(device), precision
+        self.matMode, self.vecMode = [[0, 1], [0, 2], [1, 2]], [2, 1, 0]
+        self.n_scene, self.scene_idx = 1, 0
+        self.alphaMask = None
+        self.coeff_type, self.basis_type = cfg.model.coeff_type, cfg.model.basis_type
+        self._setup(cfg)
+        self.linear_mat = MLPMixer(self.n_feat, cfg.model.out_dim, num_layers=cfg.model.num_layers,
+                                   hidden_dim=cfg.model.hidden_dim,
+                                   with_dropout=bool(cfg.model.with_dropout)).to(self.device)
+        if "reconstruction" in cfg.defaults.mode:
+            from .renderer import make_render_module
+            self.renderModule = make_render_module(cfg, cfg.model.out_dim - 1).to(self.device)
+            self.is_unbound = bool(cfg.dataset.is_unbound)
+            if self.is_unbound:
+                raise NotImplementedError("unbounded scenes (sample_point_unbound) are not on this path")
+            self.inward_aabb = self.aabb
+            self.cur_volumeSize = n_to_reso(cfg.training.volume_resoInit ** self.in_dim, self.aabb.cpu())
+            self.update_renderParams(self.cur_volumeSize)
+
+    # ---- construction -----------------------------------------------------------------
+    def _setup(self, cfg):
+        g = FieldGeometry(cfg)
+        self.geom = g
+        self.in_dim = g.in_dim
+        self.aabb = g.aabb.to(self.device)
+        self.basis_dims, self.basis_reso = g.basis_dims, g.basis_reso
+        self.T_basis, self.T_coeff = g.T_basis, g.T_coeff
+        self.coeff_reso = g.coeff_reso
+        self.n_scene = g.n_scene
+        self.n_feat = g.n_feat
+        self._freq_bands = g.freq_bands.to(self.device)
+        self.layout = FieldLayout(g.basis_dims, g.basis_reso, g.in_dim, g.coeff_reso, g.n_scene)
+        levels = [dct_dict(int(np.power(c, 1.0 / self.in_dim) + 1), r, n_select=c, dim=self.in_dim)
+                  .reshape([1, c] + [r] * self.in_dim) for c, r in zip(g.basis_dims, g.basis_reso)]
+        self.basis_flat = torch.nn.Parameter(self.layout.basis_from_reference(levels, device=self.device))
+        coef = torch.zeros(self.layout.coeff_numel, device=self.device)
+        for s in range(self.n_scene):
+            self.layout.coeff_view(coef, s).fill_(float(cfg.model.coef_init))
+        self.coeff_flat = torch.nn.Parameter(coef)
+        self._desc_cache = {}
+        self._bf16 = None
+
+    @property
+    def freq_bands(self):
+        return self._freq_bands
+
+    @freq_bands.setter
+    def freq_bands(self, v):
+        self._freq_bands = torch.as_tensor(v, dtype=torch.float32).to(self.device)
+        self._desc_cache = {}
+
+    @property
+    def basises(self):
+        """Each basis level as the reference's [1, C, R, R(, R)] tensor (a view of basis_flat)."""
+        return [self.layout.basis_view(self.basis_flat, l) for l in range(len(self.basis_dims))]
+
+    @property
+    def coeffs(self):
+        """Each scene's coefficient grid as the reference's [1, C, (D,) H, W] (a view)."""
+        return [self.layout.coeff_view(self.coeff_flat, s) for s in range(self.n_scene)]
+
+    def descriptor(self, dtype):
+        key = (dtype, tuple(self._freq_bands.tolist()))
+        d = self._desc_cache.get(key)
+        if d is None:
+            self.geom.freq_bands = self._freq_bands.cpu()
+            d = self.layout.descriptor(self.geom, self.cfg.model.basis_mapping, self.cfg.model.basis_mode,
+                                       self.cfg.model.coef_mode, dtype)
+            self._desc_cache[key] = d
+        return d
+
+    def _read_buffers(self):
+        """(basis, coeff, dtype code) the kernels read: float32 params or their BF16 copies."""
+        if self.precision == "fp32":
+            return self.basis_flat, self.coeff_flat, N.FF_F32
+        ver = (self.basis_flat._version, self.coeff_flat._version, self.basis_flat.data_ptr(),
+               self.coeff_flat.data_ptr())
+        if self._bf16 is None or self._bf16[0] != ver:
+            with torch.no_grad():
+                self._bf16 = (ver, self.basis_flat.detach().to(torch.bfloat16),
+                              self.coeff_flat.detach().to(torch.bfloat16))
+        return self._bf16[1], self._bf16[2], N.FF_BF16
+
+    def _coeff_scene(self, buf):
+        n = self.layout.coeff_scene_numel
+        return buf[self.scene_idx * n:(self.scene_idx + 1) * n]
+
+    def _field(self, x, want):
+        basis_r, coeff_r, dt = self._read_buffers()
+        desc = self.descriptor(dt)
+        coeff_param = self.coeff_flat
+        if self.n_scene > 1:
+            coeff_param = self._coeff_scene(self.coeff_flat)
+            coeff_r = self._coeff_scene(coeff_r)
+        return FN.FieldCoding.apply(x, self.basis_flat, coeff_param, basis_r, coeff_r, desc, want)
+
+    # ---- reference methods --------------------------------------------------------------
+    def get_coding(self, x):
+        """models/FactorFields.py:523-527: (basis * coeff, coeff)."""
+        feats, coeff, _ = self._field(x, (True, True, False))
+        return feats, coeff
+
+    def get_basis(self, x):
+        """models/FactorFields.py:467-513 (grid basis)."""
+        return self._field(x, (False, False, True))[2]
+
+    def get_coeff(self, x):
+        """models/FactorFields.py:425-434 (grid coefficients)."""
+        return self._field(x, (False, True, False))[1]
+
+    def n_parameters(self):
+        """Logical parameter count (models/FactorFields.py:535-539), padding excluded."""
+        basis = sum(c * r ** self.in_dim for c, r in zip(self.basis_dims, self.basis_reso))
+        coeff = self.n_feat * self.layout.coeff_cells * self.n_scene
+        rest = sum(p.numel() for n, p in self.named_parameters() if n not in ("basis_flat", "coeff_flat"))
+        return basis + coeff + rest
+
+    def get_optparam_groups(self, lr_small=0.001, lr_large=0.02):
+        """models/FactorFields.py:541-554."""
+        t = self.cfg.training or {}
+        groups = []
+        if t.get("linear_mat", True):
+            groups.append({"params": self.linear_mat.parameters(), "lr": lr_small})
+        if t.get("coeff", True):
+            groups.append({"params": [self.coeff_flat], "lr": lr_large})
+        if t.get("basis", True):
+            groups.append({"params": [self.basis_flat], "lr": lr_large})
+        if "reconstruction" in self.cfg.defaults.mode and t.get("renderModule", True):
+            groups.append({"params": self.renderModule.parameters(), "lr": lr_small})
+        return groups
+
+    def normalize_coord(self, xyz):
+        """models/FactorFields.py:635-637."""
+        inv = 2.0 / (self.aabb[1] - self.aabb[0])
+        return (xyz - self.aabb[0]) * inv - 1
+
+    def basis2density(self, density_features):
+        """models/FactorFields.py:639-643."""
+        if self.cfg.renderer.fea2denseAct == "softplus":
+            return F.softplus(density_features + self.cfg.renderer.density_shift)
+        return F.relu(density_features + self.cfg.renderer.density_shift)
+
+    def update_renderParams(self, gridSize):
+        """models/FactorFields.py:693-699."""
+        aabb = self.aabb.cpu()
+        self.aabbSize = (aabb[1] - aabb[0]).to(self.device)
+        self.gridSize = torch.tensor(gridSize, dtype=torch.long, device=self.device)
+        step, n = render_step(aabb, gridSize, self.cfg.renderer.step_ratio)
+        self.stepSize = step.to(self.device)
+        self.nSamples = n
+
+    def forward(self, rays_chunk, white_bg=True, is_train=False, ndc_ray=False, N_samples=-1):
+        """models/FactorFields.py:843-898 (bounded scenes): (rgb_map, depth_map, coeffs)."""
+        from .renderer import render_forward
+        return render_forward(self, rays_chunk, white_bg=white_bg, is_train=is_train, ndc_ray=ndc_ray,
+                              N_samples=N_samples)
+
+    # ---- checkpoints (models/FactorFields.py:669-691) --------------------------------------
+    def reference_state_dict(self):
+        """state_dict with the reference's keys and layouts (basises.l, coeffs.s as [1,C,...])."""
+        sd = {}
+        for k, v in self.state_dict().items():
+            if k not in ("basis_flat", "coeff_flat"):
+                sd[k] = v.detach().clone()
+        for l, b in enumerate(self.basises):
+            sd[f"basises.{l}"] = b.detach().contiguous().clone()
+        for s, c in enumerate(self.coeffs):
+            sd[f"coeffs.{s}"] = c.detach().contiguous().clone()
+        return sd
+
+    @torch.no_grad()
+    def load_reference_state_dict(self, sd):
+        own = {k: v for k, v in sd.items() if not (k.startswith("basises.") or k.startswith("coeffs."))}
+        missing, unexpected = self.load_state_dict(
+            {**own, "basis_flat": self.basis_flat, "coeff_flat": self.coeff_flat}, strict=False)
+        for l in range(len(self.basis_dims)):
+            self.layout.basis_view(self.basis_flat, l).copy_(sd[f"basises.{l}"].to(self.device))
+        for s in range(self.n_scene):
+            key = f"coeffs.{s}" if f"coeffs.{s}" in sd else "coeffs.0"
+            self.layout.coeff_view(self.coeff_flat, s).copy_(sd[key].to(self.device))
+        return unexpected
+
+    def save(self, path):
+        ckpt = {"state_dict": self.reference_state_dict(), "cfg": dict(self.cfg)}
+        if self.alphaMask is not None:
+            vol = self.alphaMask.alpha_volume.bool().cpu().numpy()
+            ckpt.update({"alphaMask.shape": vol.shape, "alphaMask.mask": np.packbits(vol.reshape(-1)),
+                         "alphaMask.aabb": self.alphaMask.aabb.cpu()})
+        torch.save(ckpt, path)
+
+    def load(self, ckpt):
+        if "alphaMask.aabb" in ckpt:
+            from .renderer import AlphaGridMask
+            length = int(np.prod(ckpt["alphaMask.shape"]))
+            vol = torch.from_numpy(np.unpackbits(ckpt["alphaMask.mask"])[:length].reshape(ckpt["alphaMask.shape"]))
+            self.alphaMask = AlphaGridMask(self.device, ckpt["alphaMask.aabb"].to(self.device), vol.float().to(self.device))
+        self.load_reference_state_dict(ckpt["state_dict"])
+        if "reconstruction" in self.cfg.defaults.mode:
+            self.update_renderParams(n_to_reso(self.cfg.training.volume_resoFinal ** self.in_dim, self.aabb.cpu()))

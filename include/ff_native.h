@@ -1,0 +1,143 @@
+/*
+ * ff_native.h — C ABI of the GB300 (sm_103a) Factor Fields field-evaluation and ray-rendering
+ * library (libffgb.so).
+ *
+ * Conventions for every entry point:
+ *   - Pointers named x, out, grad_* ... are DEVICE pointers owned by the caller. The library
+ *     allocates no device memory; where an operation needs scratch space the caller passes it
+ *     (see each function) and ff_*_workspace_bytes() says how much.
+ *   - Work is enqueued on `stream` (a cudaStream_t passed as void*; NULL = legacy default
+ *     stream) and returns without synchronising.
+ *   - The return value is FF_OK (0) or a negative FF_ERR_* code; ff_last_error() returns a
+ *     thread-local description of the most recent failure on the calling thread.
+ *   - Gradient outputs are ACCUMULATED (+=) in float32, like autograd's .grad: zero them first.
+ *   - Launches are stream-ordered. There is no mutable global state: two calls on different
+ *     streams are independent unless they write the same output buffers.
+ *
+ * Every entry point replaces a specific piece of the reference's PyTorch code
+ * (autonomousvision/factor-fields); the citation is given beside each declaration.
+ */
+#ifndef FF_NATIVE_H
+#define FF_NATIVE_H
+
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define FF_API __attribute__((visibility("default")))
+#else
+#define FF_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FF_ABI_VERSION 1
+#define FF_MAX_LEVELS 8
+#define FF_MAX_MLP_LAYERS 4
+
+enum {
+  FF_OK = 0,
+  FF_ERR_ARG = -1,         /* bad pointer / size / enum value */
+  FF_ERR_UNSUPPORTED = -2, /* a shape or mode this library does not implement */
+  FF_ERR_ALIGN = -3,       /* a pointer is not aligned as documented */
+  FF_ERR_CUDA = -4,        /* a CUDA runtime call failed (see ff_last_error) */
+  FF_ERR_SIZE = -5         /* a size exceeds a documented maximum */
+};
+
+enum { FF_MAP_SAWTOOTH = 0, FF_MAP_TRIANGLE = 1 };
+enum { FF_INTERP_LINEAR = 0, FF_INTERP_NEAREST = 1 };
+enum { FF_F32 = 0, FF_BF16 = 1 };
+enum { FF_LOSS_L1 = 0, FF_LOSS_MSE = 1 };
+
+/*
+ * Description of one grid/grid factor field (models/FactorFields.py:262-309 setup_params,
+ * :397-409 init_basis, :311-317 init_coef). Filled in by the host from the model config.
+ *
+ * Storage (channels-last, all offsets/strides in ELEMENTS of param_dtype):
+ *   basis level l : [R_l]^basis_dim cells x level_stride[l] channels, starting at
+ *                   level_offset[l]; cell (x, y[, z]) is at ((z*R + y)*R + x).
+ *   coefficients  : [coeff_reso.z][coeff_reso.y][coeff_reso.x] cells x coeff_stride channels.
+ *   The float32 gradient buffers use exactly the same element offsets and strides.
+ * Alignment: basis/coeff base pointers 16-byte aligned; level_offset[l]*elem_size and
+ * level_stride[l]*elem_size multiples of the vector width used for level l (vec_l below).
+ */
+typedef struct FFField {
+  int32_t basis_dim;     /* 2 or 3: dims of the basis grids (in_dim of the reference) */
+  int32_t coord_dim;     /* 2 or 3: dims of the input points and of the coefficient grid */
+  int32_t n_levels;      /* 1..FF_MAX_LEVELS */
+  int32_t mapping;       /* FF_MAP_*: basis_mapping (:11-33) */
+  int32_t basis_interp;  /* FF_INTERP_*: cfg.model.basis_mode */
+  int32_t coeff_interp;  /* FF_INTERP_*: cfg.model.coef_mode */
+  int32_t param_dtype;   /* FF_F32 or FF_BF16: element type of basis and coeff */
+  int32_t n_feat;        /* sum(basis_dims) == coefficient channels */
+  int32_t level_channels[FF_MAX_LEVELS];
+  int32_t level_stride[FF_MAX_LEVELS];
+  int32_t level_vec[FF_MAX_LEVELS];  /* 1, 2 or 4: channels per vector access on level l, valid
+                                        for the basis level AND its coefficient channel segment */
+  int32_t level_reso[FF_MAX_LEVELS];
+  int64_t level_offset[FF_MAX_LEVELS];
+  float level_scale[FF_MAX_LEVELS];  /* max(aabb size) / freq_bands[l] in float32 (:12-13) */
+  float map_origin[3];               /* aabb[0] over the basis dims (:15, :20) */
+  int32_t coeff_reso[3];             /* x (W), y (H), z (D) */
+  int32_t coeff_stride;              /* channels per coefficient cell (>= n_feat) */
+  float coeff_origin[3];             /* aabb[0] over coord dims (:635-637) */
+  float coeff_inv_size[3];           /* 2 / (aabb[1] - aabb[0]) in float32 (:636) */
+} FFField;
+
+/* MLPMixer (models/FactorFields.py:113-159): Linear+ReLU per layer, no ReLU after the last.
+ * weight[i] is row-major [out_i, in_i] float32 (torch layout); bias[i] may be NULL. */
+typedef struct FFMlp {
+  int32_t n_layers; /* 1..FF_MAX_MLP_LAYERS */
+  int32_t in_dim;
+  int32_t hidden_dim;
+  int32_t out_dim;
+  const float* weight[FF_MAX_MLP_LAYERS];
+  const float* bias[FF_MAX_MLP_LAYERS];
+} FFMlp;
+
+/* Accumulated (+=) float32 gradients of an FFMlp; NULL entries are skipped. */
+typedef struct FFMlpGrad {
+  float* weight[FF_MAX_MLP_LAYERS];
+  float* bias[FF_MAX_MLP_LAYERS];
+} FFMlpGrad;
+
+/* ---- library ------------------------------------------------------------------------- */
+FF_API int ff_abi_version(void);
+FF_API const char* ff_last_error(void);
+/* sizeof of the ABI structs, for binding checks: which = 0 FFField, 1 FFMlp, 2 FFMlpGrad. */
+FF_API int64_t ff_struct_size(int32_t which);
+/* Number of SMs of the current device and the compute capability (major*10+minor). */
+FF_API int ff_device_info(int32_t* sm_count, int32_t* cc);
+
+/* ---- field: drop-in (unfused, float32 math) ------------------------------------------ */
+
+/* get_coding (models/FactorFields.py:523-527) = get_coeff (:425-434) * get_basis (:467-513)
+ * for basis_type=coeff_type='grid'. x: [n, coord_dim] float32. Outputs (each optional, NULL
+ * to skip): feats = basis*coeff [n, n_feat], coeff [n, n_feat], basis [n, n_feat], float32. */
+FF_API int ff_field_forward(const FFField* f, const void* basis, const void* coeff, const float* x,
+                     int64_t n, float* feats, float* coeff_out, float* basis_out, void* stream);
+
+/* Backward of ff_field_forward: the grid_sample backward scatter of F.grid_sample (:433, :488)
+ * and of the product (:527). Incoming gradients of the three outputs, each [n, n_feat] and
+ * each optional (NULL = zero): grad_feats, grad_coeff_out, grad_basis_out. grad_basis /
+ * grad_coeff_grid: float32 buffers laid out like the parameters (NULL = not wanted). */
+FF_API int ff_field_backward(const FFField* f, const void* basis, const void* coeff, const float* x,
+                             int64_t n, const float* grad_feats, const float* grad_coeff_out,
+                             const float* grad_basis_out, float* grad_basis, float* grad_coeff_grid,
+                             void* stream);
+
+/* ---- MLP: drop-in float32 -------------------------------------------------------------- */
+
+/* MLPMixer.forward (models/FactorFields.py:144-159), dropout off. x [n, in_dim] -> out [n, out_dim]. */
+FF_API int ff_mlp_forward(const FFMlp* m, const float* x, int64_t n, float* out, void* stream);
+
+/* Backward of ff_mlp_forward: grad_x [n, in_dim] (optional, overwritten) and accumulated
+ * weight/bias gradients. */
+FF_API int ff_mlp_backward(const FFMlp* m, const float* x, int64_t n, const float* grad_out, float* grad_x,
+                    const FFMlpGrad* g, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FF_NATIVE_H */

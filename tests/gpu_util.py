@@ -1,0 +1,58 @@
+"""Helpers shared by the GPU tests: build models from golden fixtures, error metrics."""
+import glob
+import json
+import os
+
+import numpy as np
+import pytest
+import torch
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def need_gpu():
+    if not torch.cuda.is_available():
+        pytest.skip("needs a CUDA device")
+    from factor_fields_gb300 import build
+    build.build()
+
+
+def load_golden(name):
+    d = dict(np.load(os.path.join(GOLD, name)))
+    meta = json.loads(str(d.pop("meta"))) if "meta" in d else None
+    return d, meta
+
+
+def field_cases():
+    return sorted(os.path.basename(p) for p in glob.glob(os.path.join(GOLD, "field_*.npz")))
+
+
+def render_cases():
+    return sorted(os.path.basename(p) for p in glob.glob(os.path.join(GOLD, "render_*.npz")))
+
+
+def reference_sd(d, n_levels, prefix_mlp="mlp"):
+    sd = {f"basises.{i}": torch.from_numpy(d[f"basis{i}"]) for i in range(n_levels)}
+    sd["coeffs.0"] = torch.from_numpy(d["coeffs0"])
+    i = 0
+    while f"{prefix_mlp}_w{i}" in d:
+        sd[f"linear_mat.backbone.{i}.weight"] = torch.from_numpy(d[f"{prefix_mlp}_w{i}"])
+        if f"{prefix_mlp}_b{i}" in d:
+            sd[f"linear_mat.backbone.{i}.bias"] = torch.from_numpy(d[f"{prefix_mlp}_b{i}"])
+        i += 1
+    return sd
+
+
+def model_from_golden(d, meta, precision="fp32"):
+    from factor_fields_gb300 import FactorFields, make_cfg
+    m = FactorFields(make_cfg(meta["cfg"]), device="cuda", precision=precision)
+    m.freq_bands = meta["freq_bands"]
+    m.load_reference_state_dict(reference_sd(d, len(m.basis_dims)))
+    return m
+
+
+def rel_err(a, b):
+    """max |a - b| / max |b| (the tolerance convention of every parity test)."""
+    a = np.asarray(a.detach().cpu().numpy() if torch.is_tensor(a) else a, np.float64)
+    b = np.asarray(b.detach().cpu().numpy() if torch.is_tensor(b) else b, np.float64)
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-30))

@@ -173,3 +173,24 @@ def test_sample_pdf():
         ok = _well_conditioned(w, u)
         assert ok.mean() > 0.95
         assert rel_err(got[ok], ref[ok]) < 1e-5
+
+
+@pytest.mark.parametrize("case", FIELD_CASES)
+def test_torch_cpu_baseline_matches_reference(case):
+    """oracle/ref_torch.py (the timed CPU baseline) reproduces the reference's outputs/grads."""
+    import torch
+    from oracle.ref_torch import RefField
+    d, meta = load(case)
+    ws, bs = mlp_params(d)
+    r = RefField(meta["cfg"]["defaults"]["mode"], meta["cfg"]["dataset"]["aabb"],
+                 [d[f"basis{i}"] for i in range(meta["n_levels"])], d["coeffs0"], ws, bs, meta["freq_bands"],
+                 meta["cfg"]["model"]["basis_mapping"], meta["cfg"]["model"]["basis_mode"],
+                 meta["cfg"]["model"]["coef_mode"])
+    x = torch.from_numpy(d["x"])
+    feats, coeff = r.get_coding(x)
+    np.testing.assert_array_equal(feats.detach().numpy(), d["feats"])
+    loss = (feats * torch.from_numpy(d["g_feats"])).sum() + (coeff * torch.from_numpy(d["g_coeff"])).sum()
+    loss.backward()
+    for i in range(meta["n_levels"]):
+        assert rel_err(r.basises[i].grad.numpy(), d[f"grad_basis{i}"]) < 1e-6
+    assert rel_err(r.coeff.grad.numpy(), d["grad_coeffs0"]) < 1e-6
