@@ -159,4 +159,53 @@ int ff_mlp_backward(const FFMlp* m, const float* x, int64_t n, const float* grad
                      "ff_mlp_backward launch");
 }
 
+static int validate_fused(const FFField* f, const void* basis, const void* coeff, const FFMlp* m, const float* x,
+                          int64_t n) {
+  int rc = validate_field(f, basis, coeff);
+  if (rc) return rc;
+  rc = validate_mlp(m);
+  if (rc) return rc;
+  if (const char* why = fused_unsupported(*f, *m)) return set_error(FF_ERR_UNSUPPORTED, why);
+  if (n < 0 || (n > 0 && !x)) return set_error(FF_ERR_ARG, "bad points pointer or count");
+  return FF_OK;
+}
+
+int ff_field_mlp_forward(const FFField* f, const void* basis, const void* coeff, const FFMlp* m, const float* x,
+                         int64_t n, float* out, void* stream) {
+  int rc = validate_fused(f, basis, coeff, m, x, n);
+  if (rc) return rc;
+  if (n > 0 && !out) return set_error(FF_ERR_ARG, "out is NULL");
+  return cuda_status(launch_fused_forward(*f, basis, coeff, *m, x, n, out, (cudaStream_t)stream),
+                     "ff_field_mlp_forward launch");
+}
+
+int ff_field_mlp_backward(const FFField* f, const void* basis, const void* coeff, const FFMlp* m, const float* x,
+                          int64_t n, const float* grad_out, float* grad_basis, float* grad_coeff_grid,
+                          const FFMlpGrad* g, void* stream) {
+  int rc = validate_fused(f, basis, coeff, m, x, n);
+  if (rc) return rc;
+  if (n > 0 && !grad_out) return set_error(FF_ERR_ARG, "grad_out is NULL");
+  if (!grad_basis || !grad_coeff_grid || !aligned(grad_basis, 16) || !aligned(grad_coeff_grid, 16))
+    return set_error(FF_ERR_ARG, "grid gradient buffers must be non-NULL and 16-byte aligned");
+  FFMlpGrad none = {};
+  return cuda_status(launch_fused_backward(*f, basis, coeff, *m, x, n, grad_out, grad_basis, grad_coeff_grid,
+                                           g ? *g : none, (cudaStream_t)stream),
+                     "ff_field_mlp_backward launch");
+}
+
+int ff_field_fit_step(const FFField* f, const void* basis, const void* coeff, const FFMlp* m, const float* x,
+                      const float* target, int64_t n, int32_t loss_kind, float loss_scale, float* loss_sum,
+                      float* grad_basis, float* grad_coeff_grid, const FFMlpGrad* g, void* stream) {
+  int rc = validate_fused(f, basis, coeff, m, x, n);
+  if (rc) return rc;
+  if (n > 0 && !target) return set_error(FF_ERR_ARG, "target is NULL");
+  if (loss_kind != FF_LOSS_L1 && loss_kind != FF_LOSS_MSE) return set_error(FF_ERR_ARG, "loss_kind must be L1 or MSE");
+  if (!grad_basis || !grad_coeff_grid || !aligned(grad_basis, 16) || !aligned(grad_coeff_grid, 16))
+    return set_error(FF_ERR_ARG, "grid gradient buffers must be non-NULL and 16-byte aligned");
+  FFMlpGrad none = {};
+  return cuda_status(launch_fused_fit(*f, basis, coeff, *m, x, target, n, loss_kind, loss_scale, loss_sum,
+                                      grad_basis, grad_coeff_grid, g ? *g : none, (cudaStream_t)stream),
+                     "ff_field_fit_step launch");
+}
+
 }  // extern "C"

@@ -183,6 +183,72 @@ __device__ __forceinline__ void atomic_add_vec(float* p, const float* v) {
 }
 
 // ---------------------------------------------------------------------------------------
+// per-point corner sets of the coefficient grid and of one basis level; gather / scatter
+// ---------------------------------------------------------------------------------------
+
+template <int CD>
+__device__ __forceinline__ void coeff_corners(const FFField& f, const float* p, Corners<CD>& cc) {
+  float ix[CD];
+  int sz[CD];
+#pragma unroll
+  for (int k = 0; k < CD; ++k) {
+    sz[k] = f.coeff_reso[k];
+    ix[k] = unnorm_noalign_border(normalize_coord(p[k], f.coeff_origin[k], f.coeff_inv_size[k]), sz[k]);
+  }
+  if (f.coeff_interp == FF_INTERP_NEAREST)
+    nearest_corner<CD>(ix, sz, cc);
+  else
+    linear_corners<CD>(ix, sz, cc);
+}
+
+template <int BD>
+__device__ __forceinline__ void basis_corners(const FFField& f, int l, const float* p, Corners<BD>& bc) {
+  float ix[BD];
+  int sz[BD];
+  const int r = f.level_reso[l];
+#pragma unroll
+  for (int k = 0; k < BD; ++k) {
+    sz[k] = r;
+    ix[k] = unnorm_align(map_coord(p[k], f.map_origin[k], f.level_scale[l], f.mapping), r);
+  }
+  if (f.basis_interp == FF_INTERP_NEAREST)
+    nearest_corner<BD>(ix, sz, bc);
+  else
+    linear_corners<BD>(ix, sz, bc);
+}
+
+// Gather V channels at channel offset c of every valid corner (ATen corner order).
+template <int V, int D, typename T>
+__device__ __forceinline__ void gather(const T* __restrict__ grid, int64_t stride, int c, const Corners<D>& cn,
+                                       float* acc) {
+#pragma unroll
+  for (int v = 0; v < V; ++v) acc[v] = 0.f;
+#pragma unroll
+  for (int k = 0; k < Corners<D>::K; ++k) {
+    if (cn.idx[k] >= 0 && cn.w[k] != 0.f) {
+      float t[V];
+      load_vec<V>(grid + (int64_t)cn.idx[k] * stride + c, t);
+#pragma unroll
+      for (int v = 0; v < V; ++v) acc[v] += t[v] * cn.w[k];
+    }
+  }
+}
+
+template <int V, int D>
+__device__ __forceinline__ void scatter(float* __restrict__ grad, int64_t stride, int c, const Corners<D>& cn,
+                                        const float* g) {
+#pragma unroll
+  for (int k = 0; k < Corners<D>::K; ++k) {
+    if (cn.idx[k] >= 0 && cn.w[k] != 0.f) {
+      float t[V];
+#pragma unroll
+      for (int v = 0; v < V; ++v) t[v] = g[v] * cn.w[k];
+      atomic_add_vec<V>(grad + (int64_t)cn.idx[k] * stride + c, t);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------------------
 // misc
 // ---------------------------------------------------------------------------------------
 

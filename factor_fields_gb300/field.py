@@ -194,6 +194,22 @@ class FactorFields(torch.nn.Module):
         """models/FactorFields.py:425-434 (grid coefficients)."""
         return self._field(x, (False, True, False))[1]
 
+    def field_mlp(self, x):
+        """linear_mat(get_coding(x)[0]) through the fused kernel (one launch forward, one
+        backward): BF16 tensor-core MLP with FP32 accumulation, grids read at self.precision."""
+        basis_r, coeff_r, dt = self._read_buffers()
+        desc = self.descriptor(dt)
+        coeff_param = self.coeff_flat
+        if self.n_scene > 1:
+            coeff_param = self._coeff_scene(self.coeff_flat)
+            coeff_r = self._coeff_scene(coeff_r)
+        lm = self.linear_mat
+        if lm.num_layers != 2:
+            raise NotImplementedError("the fused path needs an MLPMixer with num_layers=2")
+        l0, l1 = lm.backbone
+        return FN.FusedFieldMLP.apply(x, self.basis_flat, coeff_param, l0.weight, l0.bias, l1.weight, basis_r,
+                                      coeff_r, desc, (lm.in_dim, lm.hidden_dim, lm.out_dim))
+
     def n_parameters(self):
         """Logical parameter count (models/FactorFields.py:535-539), padding excluded."""
         basis = sum(c * r ** self.in_dim for c, r in zip(self.basis_dims, self.basis_reso))

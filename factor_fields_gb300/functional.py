@@ -104,6 +104,39 @@ class MLPFunction(torch.autograd.Function):
         return (gx, None, None, *gw, *gbias)
 
 
+class FusedFieldMLP(torch.autograd.Function):
+    """linear_mat(get_coding(x)[0]) in one fused launch (BF16 tensor-core MLP, FP32 accumulation).
+
+    apply(x, basis_param, coeff_param, w0, b0, w1, basis_read, coeff_read, desc, dims)."""
+
+    @staticmethod
+    def forward(ctx, x, basis_param, coeff_param, w0, b0, w1, basis_read, coeff_read, desc, dims):
+        x = _contig_f32(x, "points")
+        w0, b0, w1 = w0.contiguous(), b0.contiguous(), w1.contiguous()
+        m = mlp_struct([w0, w1], [b0, None], *dims)
+        out = torch.empty(x.shape[0], dims[2], device=x.device, dtype=torch.float32)
+        N.call("ff_field_mlp_forward", ctypes.byref(desc), N.ptr(basis_read), N.ptr(coeff_read), ctypes.byref(m),
+               N.ptr(x), x.shape[0], N.ptr(out), N.stream_ptr())
+        ctx.save_for_backward(x, w0, b0, w1, basis_read, coeff_read)
+        ctx.desc, ctx.dims = desc, dims
+        ctx.shapes = (basis_param.shape, coeff_param.shape)
+        return out
+
+    @staticmethod
+    def backward(ctx, g_out):
+        x, w0, b0, w1, basis_read, coeff_read = ctx.saved_tensors
+        m = mlp_struct([w0, w1], [b0, None], *ctx.dims)
+        gb = torch.zeros(ctx.shapes[0], device=x.device)
+        gc = torch.zeros(ctx.shapes[1], device=x.device)
+        gw0, gb0, gw1 = torch.zeros_like(w0), torch.zeros_like(b0), torch.zeros_like(w1)
+        g = N.FFMlpGrad()
+        g.weight[0], g.bias[0], g.weight[1] = gw0.data_ptr(), gb0.data_ptr(), gw1.data_ptr()
+        N.call("ff_field_mlp_backward", ctypes.byref(ctx.desc), N.ptr(basis_read), N.ptr(coeff_read),
+               ctypes.byref(m), N.ptr(x), x.shape[0], N.ptr(g_out.contiguous()), N.ptr(gb), N.ptr(gc),
+               ctypes.byref(g), N.stream_ptr())
+        return None, gb, gc, gw0, gb0, gw1, None, None, None, None
+
+
 def mlp(x, weights, biases, in_dim, hidden_dim, out_dim):
     L = len(weights)
     return MLPFunction.apply(x, (in_dim, hidden_dim, out_dim), L, *weights, *biases)

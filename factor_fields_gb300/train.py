@@ -11,37 +11,72 @@ from . import functional as FN
 class FieldFitRunner:
     """One fwd+bwd regression step of a FactorFields model on (points, targets).
 
-    Gradients are written into the model's .grad buffers (zeroed at the start of each step);
-    returns the loss as a 0-d device tensor (no host sync)."""
+    fused=True: ONE ff_field_fit_step launch (gathers, BF16 tensor-core MLP, loss, backward,
+    scatter) after zeroing the gradient buffers. fused=False: the drop-in kernels launched one
+    after the other (field fwd, MLP fwd, MLP bwd, field bwd) with the loss in PyTorch.
+    Gradients land in the model's .grad buffers; step() returns the mean loss as a 0-d device
+    tensor (no host synchronisation)."""
 
-    def __init__(self, model, loss="l1"):
+    def __init__(self, model, loss="l1", fused=True):
         if loss not in N.FF_LOSS:
             raise ValueError("loss must be 'l1' or 'mse'")
-        self.m, self.loss = model, loss
-        self.path_name = "explicit drop-in kernels (field fwd, MLP fwd, MLP bwd, field bwd)"
-        self.dominant_kernel = "ff_field_backward"
-        self.gathers_per_point = 2
+        self.m, self.loss, self.fused = model, loss, fused
+        if fused:
+            self.path_name = "fused: one ff_field_fit_step launch per step (+ gradient zeroing)"
+            self.dominant_kernel = "ff_field_fit_step"
+            self.gathers_per_point = 1
+        else:
+            self.path_name = "explicit drop-in kernels (field fwd, MLP fwd, MLP bwd, field bwd)"
+            self.dominant_kernel = "ff_field_backward"
+            self.gathers_per_point = 2
         for p in self._params():
             if p.grad is None:
                 p.grad = torch.zeros_like(p)
+        self.loss_buf = torch.zeros(1, device=model.basis_flat.device)
 
     def _params(self):
         ws, bs = self.m.linear_mat.weights()
         return [self.m.basis_flat, self.m.coeff_flat] + ws + [b for b in bs if b is not None]
 
-    def step(self, x, y, kernel_events=False):
-        m = self.m
+    def _grad_struct(self):
+        ws, bs = self.m.linear_mat.weights()
+        g = N.FFMlpGrad()
+        for i, (w, b) in enumerate(zip(ws, bs)):
+            g.weight[i] = w.grad.data_ptr()
+            g.bias[i] = b.grad.data_ptr() if b is not None else None
+        return g
+
+    def zero_grad(self):
         for p in self._params():
             p.grad.zero_()
+
+    def step(self, x, y, kernel_events=False):
+        m = self.m
+        self.zero_grad()
         basis_r, coeff_r, dt = m._read_buffers()
         desc = m.descriptor(dt)
         n = x.shape[0]
-        feats = torch.empty(n, m.n_feat, device=x.device)
-        st = N.stream_ptr()
-        N.call("ff_field_forward", ctypes.byref(desc), N.ptr(basis_r), N.ptr(coeff_r), N.ptr(x), n, N.ptr(feats),
-               None, None, st)
         ws, bs = m.linear_mat.weights()
         mlp = FN.mlp_struct(ws, bs, m.linear_mat.in_dim, m.linear_mat.hidden_dim, m.linear_mat.out_dim)
+        st = N.stream_ptr()
+        g = self._grad_struct()
+        ev = None
+        if kernel_events:
+            ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+        if self.fused:
+            self.loss_buf.zero_()
+            if ev:
+                ev[0].record()
+            N.call("ff_field_fit_step", ctypes.byref(desc), N.ptr(basis_r), N.ptr(coeff_r), ctypes.byref(mlp),
+                   N.ptr(x), N.ptr(y), n, N.FF_LOSS[self.loss], 1.0 / (n * m.linear_mat.out_dim),
+                   N.ptr(self.loss_buf), N.ptr(m.basis_flat.grad), N.ptr(m.coeff_flat.grad), ctypes.byref(g), st)
+            if ev:
+                ev[1].record()
+            loss = self.loss_buf[0] / (n * m.linear_mat.out_dim)
+            return ev if kernel_events else loss
+        feats = torch.empty(n, m.n_feat, device=x.device)
+        N.call("ff_field_forward", ctypes.byref(desc), N.ptr(basis_r), N.ptr(coeff_r), N.ptr(x), n, N.ptr(feats),
+               None, None, st)
         pred = torch.empty(n, m.linear_mat.out_dim, device=x.device)
         N.call("ff_mlp_forward", ctypes.byref(mlp), N.ptr(feats), n, N.ptr(pred), st)
         err = pred - y
@@ -51,19 +86,13 @@ class FieldFitRunner:
         else:
             loss = (err * err).mean()
             g_out = 2 * err / err.numel()
-        g = N.FFMlpGrad()
-        for i, (w, b) in enumerate(zip(ws, bs)):
-            g.weight[i] = w.grad.data_ptr()
-            g.bias[i] = b.grad.data_ptr() if b is not None else None
         g_feats = torch.empty_like(feats)
         N.call("ff_mlp_backward", ctypes.byref(mlp), N.ptr(feats), n, N.ptr(g_out), N.ptr(g_feats), ctypes.byref(g), st)
-        ev = None
-        if kernel_events:
-            ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+        if ev:
             ev[0].record()
         N.call("ff_field_backward", ctypes.byref(desc), N.ptr(basis_r), N.ptr(coeff_r), N.ptr(x), n, N.ptr(g_feats),
                None, None, N.ptr(m.basis_flat.grad), N.ptr(m.coeff_flat.grad), st)
-        if kernel_events:
+        if ev:
             ev[1].record()
             return ev
         return loss

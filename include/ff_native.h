@@ -137,6 +137,32 @@ FF_API int ff_mlp_forward(const FFMlp* m, const float* x, int64_t n, float* out,
 FF_API int ff_mlp_backward(const FFMlp* m, const float* x, int64_t n, const float* grad_out, float* grad_x,
                     const FFMlpGrad* g, void* stream);
 
+/* ---- field + MLP fused (the fast path; BF16 or float32 grids, BF16 tensor-core MLP) ---- */
+/* Requirements (else FF_ERR_UNSUPPORTED): basis_dims = [4,4,4,2,2,2] stored unpadded, and an
+ * MLPMixer with num_layers = 2, hidden_dim = 64, in_dim = 18, out_dim <= 32, bias on layer 0
+ * only. MLP weights are read as float32 and rounded to BF16 inside the kernel. */
+
+/* linear_mat(get_coding(x)[0]) (models/FactorFields.py:523-527 then :144-159) in one launch:
+ * out [n, out_dim] float32. */
+FF_API int ff_field_mlp_forward(const FFField* f, const void* basis, const void* coeff, const FFMlp* m,
+                                const float* x, int64_t n, float* out, void* stream);
+
+/* Backward of ff_field_mlp_forward given grad_out [n, out_dim]: accumulates the grid
+ * gradients (as ff_field_backward) and the MLP weight/bias gradients. Recomputes the forward. */
+FF_API int ff_field_mlp_backward(const FFField* f, const void* basis, const void* coeff, const FFMlp* m,
+                                 const float* x, int64_t n, const float* grad_out, float* grad_basis,
+                                 float* grad_coeff_grid, const FFMlpGrad* g, void* stream);
+
+/* One regression step of the notebooks' field fit (scripts/2D_regression.ipynb cell 4,
+ * scripts/sdf_regression.ipynb cell 2) up to the optimizer: forward, loss against target
+ * [n, out_dim] (FF_LOSS_L1: mean |o - t|, FF_LOSS_MSE: mean (o - t)^2; gradients scaled by
+ * loss_scale, normally 1 / (n * out_dim)), and the full backward, in ONE launch.
+ * loss_sum (optional, device float) accumulates sum |o - t| or sum (o - t)^2. */
+FF_API int ff_field_fit_step(const FFField* f, const void* basis, const void* coeff, const FFMlp* m,
+                             const float* x, const float* target, int64_t n, int32_t loss_kind,
+                             float loss_scale, float* loss_sum, float* grad_basis, float* grad_coeff_grid,
+                             const FFMlpGrad* g, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

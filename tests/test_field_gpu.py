@@ -95,9 +95,7 @@ def test_full_size_configs_against_oracle(key):
     g = torch.Generator(device="cpu").manual_seed(3)
     with torch.no_grad():
         m.coeff_flat.copy_(torch.rand(m.coeff_flat.shape, generator=g) * 2 - 1)
-        m.basis_flat.add_(torch.rand(m.basis_flat.shape, generator=g) * 0.2 - 0.1)
-        for l in range(len(m.basis_dims)):  # re-zero padding channels
-            pass
+        m.basis_flat.add_((torch.rand(m.basis_flat.shape, generator=g) * 0.2 - 0.1).cuda())
     n = 16384
     aabb = np.array(m.cfg.dataset.aabb, np.float32)
     rng = np.random.default_rng(5)

@@ -1,0 +1,165 @@
+"""GPU parity of the fused field+MLP kernels (ff_field_mlp_forward / _backward / ff_field_fit_step)
+against the FP64 oracle, on the golden fixtures and on the full-size benchmark configurations.
+
+The fused MLP stores its weights in BF16 and runs on BF16 tensor cores with FP32
+accumulation, so the tolerances are the BF16 ones: forward 2e-2 (against the reference's own
+float32 output), gradients 3e-2 (relative = max|a-b| / max|ref|) against the FP64 oracle of
+the BF16-stored model (MLP weights, and the grids when stored in BF16, rounded to BF16).
+Against float32 weights the gradients of these adversarial fixtures (random weights and
+upstream gradients, tiny grids) differ by up to ~7% even with exact activations: rounding a
+weight to BF16 moves some pre-activations across the ReLU kink."""
+import numpy as np
+import pytest
+import torch
+
+from gpu_util import field_cases, load_golden, model_from_golden, need_gpu, rel_err
+from oracle import ff_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+FWD_TOL, GRAD_TOL = 2e-2, 3e-2
+
+
+@pytest.fixture(autouse=True)
+def _gpu():
+    need_gpu()
+
+
+def _stored(t, bf16):
+    t = t.detach()
+    return (t.to(torch.bfloat16).float() if bf16 else t).cpu().numpy()
+
+
+def oracle_of(m):
+    """Oracle inputs for the model as the fused kernel stores it: MLP weights in BF16 (the
+    bias stays float32), grids in BF16 when precision == 'bf16'."""
+    spec = O.FieldSpec(m.cfg.defaults.mode, m.cfg.dataset.aabb, m.basis_dims, m.basis_reso,
+                       m.freq_bands.cpu().numpy(), m.coeff_reso, m.cfg.model.basis_mapping, m.cfg.model.basis_mode,
+                       m.cfg.model.coef_mode)
+    gb = m.precision == "bf16"
+    bg = [_stored(b[0], gb) for b in m.basises]
+    cg = _stored(m.coeffs[m.scene_idx][0], gb)
+    ws, bs = m.linear_mat.weights()
+    ws = [_stored(w, True) for w in ws]
+    bs = [None if b is None else b.detach().cpu().numpy() for b in bs]
+    return spec, bg, cg, ws, bs
+
+
+def oracle_fwd_bwd(m, x, g_out):
+    spec, bg, cg, ws, bs = oracle_of(m)
+    feats, _ = O.get_coding(spec, bg, cg, x)
+    out, _ = O.mlp_fwd(ws, bs, feats)
+    if g_out is None:
+        return out, None
+    gin, gw, gb = O.mlp_bwd(ws, bs, feats, g_out)
+    gbasis, gcoef = O.get_coding_bwd(spec, bg, cg, x, gin)
+    return out, (gbasis, gcoef, gw, gb)
+
+
+def check_grads(m, ref):
+    gbasis, gcoef, gw, gb = ref
+    for l in range(len(m.basis_dims)):
+        assert rel_err(m.layout.basis_view(m.basis_flat.grad, l)[0], gbasis[l]) < GRAD_TOL, f"basis level {l}"
+    assert rel_err(m.layout.coeff_view(m.coeff_flat.grad, m.scene_idx)[0], gcoef) < GRAD_TOL, "coeff"
+    for i, lin in enumerate(m.linear_mat.backbone):
+        assert rel_err(lin.weight.grad, gw[i]) < GRAD_TOL, f"w{i}"
+        if lin.bias is not None:
+            assert rel_err(lin.bias.grad, gb[i]) < GRAD_TOL, f"b{i}"
+
+
+FUSED_CASES = [c for c in field_cases() if "aniso" not in c]  # aniso uses a 3-layer MLP
+
+
+@pytest.mark.parametrize("precision", ["bf16", "fp32"])
+@pytest.mark.parametrize("case", FUSED_CASES)
+def test_field_mlp_fwd_bwd_golden(case, precision):
+    d, meta = load_golden(case)
+    m = model_from_golden(d, meta, precision=precision)
+    x = torch.from_numpy(d["x"]).cuda()
+    out = m.field_mlp(x)
+    assert rel_err(out, d["mlp_out"]) < FWD_TOL  # the reference's own output
+    g_out = d["g_out"]
+    (out * torch.from_numpy(g_out).cuda()).sum().backward()
+    _, ref = oracle_fwd_bwd(m, d["x"], g_out)
+    check_grads(m, ref)
+
+
+@pytest.mark.parametrize("loss", ["l1", "mse"])
+@pytest.mark.parametrize("key", ["cfg0", "cfg1", "cfg2", "cfg4"])
+def test_fit_step_full_size(key, loss):
+    from factor_fields_gb300 import FactorFields
+    from factor_fields_gb300 import workloads as W
+    from factor_fields_gb300.train import FieldFitRunner
+    torch.manual_seed(0)
+    m = FactorFields(W.field_cfg(key), device="cuda", precision="bf16")
+    if key == "cfg0":
+        m.freq_bands = W.FREQ6
+    gen = torch.Generator().manual_seed(2)
+    with torch.no_grad():
+        m.coeff_flat.copy_((torch.rand(m.coeff_flat.shape, generator=gen) * 2 - 1).cuda())
+        # round the float32 masters to BF16 so the oracle sees exactly the grids the kernel reads
+        m.basis_flat.copy_(m.basis_flat.to(torch.bfloat16).float())
+        m.coeff_flat.copy_(m.coeff_flat.to(torch.bfloat16).float())
+    n = 4096
+    aabb = np.array(m.cfg.dataset.aabb, np.float32)
+    rng = np.random.default_rng(11)
+    x = rng.uniform(aabb[0], aabb[1], (n, aabb.shape[1])).astype(np.float32)
+    if key == "cfg4":
+        x[:, 2] = rng.integers(0, 256, n) + 0.5
+    out_ref, _ = oracle_fwd_bwd(m, x, None)
+    # targets at a distance >= 0.1 from the prediction so that sign(err) is not ambiguous
+    off = rng.uniform(0.1, 1.0, out_ref.shape) * rng.choice([-1.0, 1.0], out_ref.shape)
+    y = (out_ref + off).astype(np.float32)
+    err = out_ref - y
+    if loss == "l1":
+        g_out = np.sign(err) / err.size
+        loss_ref = np.abs(err).mean()
+    else:
+        g_out = 2 * err / err.size
+        loss_ref = (err * err).mean()
+    _, ref = oracle_fwd_bwd(m, x, g_out)
+    runner = FieldFitRunner(m, loss=loss, fused=True)
+    lv = runner.step(torch.from_numpy(x).cuda(), torch.from_numpy(y).cuda())
+    torch.cuda.synchronize()
+    assert abs(float(lv) - loss_ref) <= FWD_TOL * abs(loss_ref)
+    check_grads(m, ref)
+    # the fused forward agrees with the oracle too
+    with torch.no_grad():
+        out = m.field_mlp(torch.from_numpy(x).cuda())
+    assert rel_err(out, out_ref) < FWD_TOL
+
+
+def test_fused_matches_dropin_step():
+    """Fused and drop-in runner steps produce the same gradients (within BF16 tolerance)."""
+    from factor_fields_gb300 import FactorFields
+    from factor_fields_gb300 import workloads as W
+    from factor_fields_gb300.train import FieldFitRunner
+    xs, ys = W.sdf_batch(3, 8192)
+    x, y = torch.from_numpy(xs).cuda(), torch.from_numpy(ys).cuda()
+    grads = []
+    for fused in (False, True):
+        torch.manual_seed(0)
+        m = FactorFields(W.field_cfg("cfg1"), device="cuda", precision="bf16")
+        with torch.no_grad():  # the stored-BF16 MLP for both paths
+            for w in m.linear_mat.weights()[0]:
+                w.copy_(w.to(torch.bfloat16).float())
+        r = FieldFitRunner(m, loss="mse", fused=fused)
+        r.step(x, y)
+        grads.append([p.grad.clone() for p in r._params()])
+    for a, b in zip(*grads):
+        assert rel_err(b, a) < GRAD_TOL
+
+
+def test_unsupported_shapes_fail_loudly():
+    from factor_fields_gb300 import FactorFields, merged_cfg
+    from factor_fields_gb300._native import NativeError
+    cfg = merged_cfg({"defaults": {"mode": "reconstruction"},
+                      "model": {"basis_dims": [4, 4, 2], "basis_resos": [8, 9, 10], "freq_bands": [1.0, 2.0, 3.0],
+                                "coeff_reso": 4, "total_params": 10 * 4 ** 3 + 8 ** 3 * 4 + 9 ** 3 * 4 + 10 ** 3 * 2,
+                                "out_dim": 1},
+                      "dataset": {"aabb": [[-1, -1, -1], [1, 1, 1]], "scene_reso": 10}})
+    m = FactorFields(cfg, device="cuda")
+    with pytest.raises(NativeError, match="fused path"):
+        m.field_mlp(torch.zeros(8, 3, device="cuda"))
+    feats, _ = m.get_coding(torch.zeros(8, 3, device="cuda"))  # the drop-in path handles it
+    assert feats.shape == (8, 10)
