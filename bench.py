@@ -147,14 +147,19 @@ def run_native(args, ws, rank, local):
                 ktimes.append(kev[0].elapsed_time(kev[1]))
         return times, ktimes
 
+    # launches of this library per step (the captured graph replays exactly these)
+    N.reset_launch_count()
+    runner.step(*devb[0])
+    per_step = N.launch_count()
     for i in range(args.warmup):
-        runner.step(*devb[i % nb])
+        runner.graph_step(*devb[i % nb])
     torch.cuda.synchronize()
     clocks = Clocks(local)
     clocks.start()
-    N.reset_launch_count()
-    t_fast, k_fast = timed(lambda i: runner.step(*devb[i % nb], kernel_events=True), args.steps, True)
-    launches = N.launch_count()
+    t_fast, _ = timed(lambda i: runner.graph_step(*devb[i % nb]), args.steps, False)
+    launches = per_step * args.steps
+    # the dominant kernel alone, CUDA events around its launch on the launching stream
+    _, k_fast = timed(lambda i: runner.step(*devb[i % nb], kernel_events=True), args.steps, True)
     ck = clocks.stop()
     ms = float(np.sum(t_fast))
 
@@ -163,9 +168,7 @@ def run_native(args, ws, rank, local):
 
     def e2e_step(i):
         x, y = host[i % nb]
-        xd = x.to(dev, non_blocking=True)
-        yd = y.to(dev, non_blocking=True)
-        loss = runner.step(xd, yd)
+        loss = runner.graph_step(x, y)  # H2D copies from pinned host memory into the graph's inputs
         loss_host.copy_(loss.reshape(1), non_blocking=True)
         return None
 

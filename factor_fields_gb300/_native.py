@@ -34,6 +34,7 @@ class FFField(ctypes.Structure):
         ("level_offset", c_i64 * FF_MAX_LEVELS), ("level_scale", c_f32 * FF_MAX_LEVELS),
         ("map_origin", c_f32 * 3), ("coeff_reso", c_i32 * 3), ("coeff_stride", c_i32),
         ("coeff_origin", c_f32 * 3), ("coeff_inv_size", c_f32 * 3),
+        ("level_inv_scale", c_f32 * FF_MAX_LEVELS), ("level_inv_half", c_f32 * FF_MAX_LEVELS),
     ]
 
 

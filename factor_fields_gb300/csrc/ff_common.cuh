@@ -58,6 +58,31 @@ __device__ __forceinline__ float map_coord(float p, float origin, float scale, i
   return loc;
 }
 
+// Division-free grid_mapping for the fused kernels: q = floor(rel / scale) from a reciprocal,
+// m = rel - q*scale corrected into [0, scale), loc = m * (2/scale) - 1. Within a few ulp of
+// map_coord; both mappings are continuous at the period boundaries where it matters (the
+// triangle wave is continuous there, the sawtooth jump is at m = 0 which both compute exactly).
+__device__ __forceinline__ float map_coord_fast(float p, float origin, float scale, float inv_scale,
+                                                float inv_half, int mapping) {
+  const float rel = p - origin;
+  float q = floorf(rel * inv_scale);
+  float m = fmaf(-q, scale, rel);
+  if (m < 0.f) {
+    m += scale;
+    q -= 1.f;
+  } else if (m >= scale) {
+    m -= scale;
+    q += 1.f;
+  }
+  float loc = fmaf(m, inv_half, -1.f);
+  if (mapping == kMapTriangle) {
+    if (((int)q) & 1) loc = -loc;
+  } else {
+    loc = fminf(fmaxf(loc, -1.f), 1.f);
+  }
+  return loc;
+}
+
 // ATen grid_sampler_unnormalize + border clip (grid_sampler_compute_source_index).
 __device__ __forceinline__ float unnorm_align(float c, int size) {  // align_corners=True
   return __fmul_rn(__fmul_rn(__fadd_rn(c, 1.f), 0.5f), (float)(size - 1));
@@ -244,6 +269,91 @@ __device__ __forceinline__ void scatter(float* __restrict__ grad, int64_t stride
 #pragma unroll
       for (int v = 0; v < V; ++v) t[v] = g[v] * cn.w[k];
       atomic_add_vec<V>(grad + (int64_t)cn.idx[k] * stride + c, t);
+    }
+  }
+}
+
+// Basis corners with the division-free mapping (fused kernels).
+template <int BD>
+__device__ __forceinline__ void basis_corners_fast(const FFField& f, int l, const float* p, Corners<BD>& bc) {
+  float ix[BD];
+  int sz[BD];
+  const int r = f.level_reso[l];
+#pragma unroll
+  for (int k = 0; k < BD; ++k) {
+    sz[k] = r;
+    ix[k] = unnorm_align(
+        map_coord_fast(p[k], f.map_origin[k], f.level_scale[l], f.level_inv_scale[l], f.level_inv_half[l], f.mapping),
+        r);
+  }
+  if (f.basis_interp == FF_INTERP_NEAREST)
+    nearest_corner<BD>(ix, sz, bc);
+  else
+    linear_corners<BD>(ix, sz, bc);
+}
+
+// All 18 coefficient channels of every valid corner with 16-byte loads (channels 0..15) and
+// one 4- (BF16) or 8-byte (float32) load for channels 16, 17. Needs coeff_stride % 8 == 0.
+template <int D>
+__device__ __forceinline__ void gather_coeff18(const __nv_bfloat16* __restrict__ grid, int stride, const Corners<D>& cn,
+                                               float* acc) {
+#pragma unroll
+  for (int v = 0; v < 18; ++v) acc[v] = 0.f;
+#pragma unroll
+  for (int k = 0; k < Corners<D>::K; ++k) {
+    if (cn.idx[k] >= 0 && cn.w[k] != 0.f) {
+      const __nv_bfloat16* p = grid + (int64_t)cn.idx[k] * stride;
+      const uint4 a = __ldg(reinterpret_cast<const uint4*>(p));
+      const uint4 b = __ldg(reinterpret_cast<const uint4*>(p + 8));
+      const uint32_t c = __ldg(reinterpret_cast<const unsigned int*>(p + 16));
+      const uint32_t w[9] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, c};
+      const float wk = cn.w[k];
+#pragma unroll
+      for (int j = 0; j < 9; ++j) {
+        acc[2 * j] += __uint_as_float(w[j] << 16) * wk;
+        acc[2 * j + 1] += __uint_as_float(w[j] & 0xffff0000u) * wk;
+      }
+    }
+  }
+}
+
+template <int D>
+__device__ __forceinline__ void gather_coeff18(const float* __restrict__ grid, int stride, const Corners<D>& cn,
+                                               float* acc) {
+#pragma unroll
+  for (int v = 0; v < 18; ++v) acc[v] = 0.f;
+#pragma unroll
+  for (int k = 0; k < Corners<D>::K; ++k) {
+    if (cn.idx[k] >= 0 && cn.w[k] != 0.f) {
+      const float* p = grid + (int64_t)cn.idx[k] * stride;
+      const float wk = cn.w[k];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const float4 t = __ldg(reinterpret_cast<const float4*>(p) + j);
+        acc[4 * j] += t.x * wk; acc[4 * j + 1] += t.y * wk; acc[4 * j + 2] += t.z * wk; acc[4 * j + 3] += t.w * wk;
+      }
+      const float2 t = __ldg(reinterpret_cast<const float2*>(p + 16));
+      acc[16] += t.x * wk;
+      acc[17] += t.y * wk;
+    }
+  }
+}
+
+// Scatter 18 coefficient-channel gradients (float32 grid, stride % 4 == 0): four float4 and
+// one float2 atomic per valid corner.
+template <int D>
+__device__ __forceinline__ void scatter_coeff18(float* __restrict__ grad, int stride, const Corners<D>& cn,
+                                                const float* g) {
+#pragma unroll
+  for (int k = 0; k < Corners<D>::K; ++k) {
+    if (cn.idx[k] >= 0 && cn.w[k] != 0.f) {
+      float* p = grad + (int64_t)cn.idx[k] * stride;
+      const float wk = cn.w[k];
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+        atomicAdd(reinterpret_cast<float4*>(p) + j,
+                  make_float4(g[4 * j] * wk, g[4 * j + 1] * wk, g[4 * j + 2] * wk, g[4 * j + 3] * wk));
+      atomicAdd(reinterpret_cast<float2*>(p + 16), make_float2(g[16] * wk, g[17] * wk));
     }
   }
 }

@@ -159,12 +159,20 @@ class FactorFields(torch.nn.Module):
         """(basis, coeff, dtype code) the kernels read: float32 params or their BF16 copies."""
         if self.precision == "fp32":
             return self.basis_flat, self.coeff_flat, N.FF_F32
+        # The BF16 copies are refreshed IN PLACE whenever the float32 masters changed (their
+        # version counters move on every in-place update, e.g. an optimizer step), so captured
+        # CUDA graphs that read them stay valid.
+        if (self._bf16 is None or self._bf16[1].numel() != self.basis_flat.numel()
+                or self._bf16[2].numel() != self.coeff_flat.numel()):
+            self._bf16 = [None, torch.empty_like(self.basis_flat, dtype=torch.bfloat16),
+                          torch.empty_like(self.coeff_flat, dtype=torch.bfloat16)]
         ver = (self.basis_flat._version, self.coeff_flat._version, self.basis_flat.data_ptr(),
                self.coeff_flat.data_ptr())
-        if self._bf16 is None or self._bf16[0] != ver:
+        if self._bf16[0] != ver:
             with torch.no_grad():
-                self._bf16 = (ver, self.basis_flat.detach().to(torch.bfloat16),
-                              self.coeff_flat.detach().to(torch.bfloat16))
+                self._bf16[1].copy_(self.basis_flat.detach())
+                self._bf16[2].copy_(self.coeff_flat.detach())
+            self._bf16[0] = ver
         return self._bf16[1], self._bf16[2], N.FF_BF16
 
     def _coeff_scene(self, buf):

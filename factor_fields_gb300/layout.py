@@ -104,6 +104,8 @@ class FieldLayout:
             f.level_reso[l] = self.basis_reso[l]
             f.level_offset[l] = self.level_offset[l]
             f.level_scale[l] = float(scale[l])
+            f.level_inv_scale[l] = 1.0 / float(scale[l])
+            f.level_inv_half[l] = 2.0 / float(scale[l])
         for k in range(self.basis_dim):
             f.map_origin[k] = float(map_aabb[0, k])
         inv = 2.0 / (aabb[1] - aabb[0])  # normalize_coord (:636), float32

@@ -50,6 +50,34 @@ class FieldFitRunner:
         for p in self._params():
             p.grad.zero_()
 
+    def graph_step(self, x, y):
+        """step() replayed from a CUDA graph: the batch is copied into static buffers and the
+        captured launches (gradient zeroing, the fit kernel, the loss scale) replay with one
+        host call. The graph is captured on first use and re-captured when the batch shape or
+        a parameter buffer changes."""
+        key = (tuple(x.shape), tuple(y.shape), self.m.basis_flat.data_ptr(), self.m.coeff_flat.data_ptr(),
+               self.m.precision)
+        if getattr(self, "_graph_key", None) != key:
+            dev = self.m.basis_flat.device
+            self._xs = torch.empty(x.shape, dtype=x.dtype, device=dev)
+            self._ys = torch.empty(y.shape, dtype=y.dtype, device=dev)
+            self._xs.copy_(x)
+            self._ys.copy_(y)
+            side = torch.cuda.Stream()
+            side.wait_stream(torch.cuda.current_stream())
+            with torch.cuda.stream(side):
+                self.step(self._xs, self._ys)  # warm-up outside the capture (sets kernel attributes)
+            torch.cuda.current_stream().wait_stream(side)
+            self._graph = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(self._graph):
+                self._graph_loss = self.step(self._xs, self._ys)
+            self._graph_key = key
+        self.m._read_buffers()  # refresh the BF16 grid copies in place if the masters changed
+        self._xs.copy_(x, non_blocking=True)
+        self._ys.copy_(y, non_blocking=True)
+        self._graph.replay()
+        return self._graph_loss
+
     def step(self, x, y, kernel_events=False):
         m = self.m
         self.zero_grad()

@@ -83,6 +83,10 @@ typedef struct FFField {
   int32_t coeff_stride;              /* channels per coefficient cell (>= n_feat) */
   float coeff_origin[3];             /* aabb[0] over coord dims (:635-637) */
   float coeff_inv_size[3];           /* 2 / (aabb[1] - aabb[0]) in float32 (:636) */
+  /* Reciprocals used by the fused kernels' division-free mapping (the drop-in kernels divide
+   * exactly as the reference does): float32 nearest to 1/scale and 2/scale. */
+  float level_inv_scale[FF_MAX_LEVELS];
+  float level_inv_half[FF_MAX_LEVELS];
 } FFField;
 
 /* MLPMixer (models/FactorFields.py:113-159): Linear+ReLU per layer, no ReLU after the last.
