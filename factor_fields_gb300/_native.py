@@ -47,6 +47,13 @@ class FFMlpGrad(ctypes.Structure):
     _fields_ = [("weight", c_vp * FF_MAX_MLP_LAYERS), ("bias", c_vp * FF_MAX_MLP_LAYERS)]
 
 
+class FFRender(ctypes.Structure):
+    _fields_ = [("aabb_min", c_f32 * 3), ("aabb_max", c_f32 * 3), ("step", c_f32), ("n_samples", c_i32),
+                ("distance_scale", c_f32), ("density_shift", c_f32), ("density_act", c_i32),
+                ("weight_thres", c_f32), ("white_bg", c_i32), ("occ_bits", c_vp), ("occ_reso", c_i32 * 3),
+                ("occ_origin", c_f32 * 3), ("occ_inv", c_f32 * 3)]
+
+
 # (name, restype, argtypes) of every exported entry point.
 _P = ctypes.POINTER
 SIGNATURES = {
@@ -63,6 +70,14 @@ SIGNATURES = {
                                       _P(FFMlpGrad), c_vp]),
     "ff_field_fit_step": (c_i32, [_P(FFField), c_vp, c_vp, _P(FFMlp), c_vp, c_vp, c_i64, c_i32, c_f32, c_vp, c_vp,
                                   c_vp, _P(FFMlpGrad), c_vp]),
+    "ff_march_count": (c_i32, [_P(FFRender), c_vp, c_vp, c_i64, c_vp, c_vp, c_vp]),
+    "ff_scan_workspace_bytes": (c_i64, [c_i64]),
+    "ff_scan_counts": (c_i32, [c_vp, c_i64, c_vp, c_vp, c_i64, c_vp]),
+    "ff_march_emit": (c_i32, [_P(FFRender), c_vp, c_vp, c_i64, c_vp, c_vp, c_vp, c_vp]),
+    "ff_composite_forward": (c_i32, [_P(FFRender), c_vp, c_vp, c_i64, c_vp, c_vp, c_vp, c_i32, c_vp, c_vp, c_vp,
+                                     c_vp, c_vp]),
+    "ff_composite_backward": (c_i32, [_P(FFRender), c_vp, c_vp, c_i64, c_vp, c_vp, c_vp, c_i32, c_vp, c_vp, c_vp,
+                                      c_vp]),
 }
 
 _lib = None
@@ -115,7 +130,7 @@ def stream_ptr():
 
 
 _launches = [0]
-_NON_LAUNCHING = {"ff_abi_version", "ff_last_error", "ff_device_info", "ff_struct_size"}
+_NON_LAUNCHING = {"ff_abi_version", "ff_last_error", "ff_device_info", "ff_struct_size", "ff_scan_workspace_bytes"}
 
 
 def reset_launch_count():

@@ -102,6 +102,7 @@ int64_t ff_struct_size(int32_t which) {
     case 0: return (int64_t)sizeof(FFField);
     case 1: return (int64_t)sizeof(FFMlp);
     case 2: return (int64_t)sizeof(FFMlpGrad);
+    case 3: return (int64_t)sizeof(FFRender);
     default: return -1;
   }
 }
@@ -159,6 +160,23 @@ int ff_mlp_backward(const FFMlp* m, const float* x, int64_t n, const float* grad
                      "ff_mlp_backward launch");
 }
 
+static int validate_render(const FFRender* r, const float* rays, int64_t n) {
+  if (!r) return set_error(FF_ERR_ARG, "render descriptor is NULL");
+  if (n < 0 || (n > 0 && !rays)) return set_error(FF_ERR_ARG, "bad rays pointer or count");
+  if (r->n_samples < 1 || r->n_samples > (1 << 20)) return set_error(FF_ERR_ARG, "n_samples must be 1..2^20");
+  if (!(r->step > 0.f)) return set_error(FF_ERR_ARG, "step must be > 0");
+  if (r->density_act != 0 && r->density_act != 1) return set_error(FF_ERR_ARG, "density_act must be 0 or 1");
+  if (r->occ_bits) {
+    int64_t cells = 1;
+    for (int k = 0; k < 3; ++k) {
+      if (r->occ_reso[k] < 1) return set_error(FF_ERR_ARG, "occupancy resolution must be >= 1");
+      cells *= r->occ_reso[k];
+    }
+    if (cells > (1ll << 31)) return set_error(FF_ERR_SIZE, "occupancy volume too large");
+  }
+  return FF_OK;
+}
+
 static int validate_fused(const FFField* f, const void* basis, const void* coeff, const FFMlp* m, const float* x,
                           int64_t n) {
   int rc = validate_field(f, basis, coeff);
@@ -206,6 +224,58 @@ int ff_field_fit_step(const FFField* f, const void* basis, const void* coeff, co
   return cuda_status(launch_fused_fit(*f, basis, coeff, *m, x, target, n, loss_kind, loss_scale, loss_sum,
                                       grad_basis, grad_coeff_grid, g ? *g : none, (cudaStream_t)stream),
                      "ff_field_fit_step launch");
+}
+
+int ff_march_count(const FFRender* r, const float* rays, const float* jitter, int64_t n_rays, int32_t* counts,
+                   float* t_min, void* stream) {
+  int rc = validate_render(r, rays, n_rays);
+  if (rc) return rc;
+  if (n_rays > 0 && !counts) return set_error(FF_ERR_ARG, "counts is NULL");
+  return cuda_status(launch_march_count(*r, rays, jitter, n_rays, counts, t_min, (cudaStream_t)stream),
+                     "ff_march_count launch");
+}
+
+int64_t ff_scan_workspace_bytes(int64_t n) { return n < 0 ? -1 : scan_workspace_bytes(n); }
+
+int ff_scan_counts(const int32_t* counts, int64_t n, int64_t* offsets, void* workspace, int64_t workspace_bytes,
+                   void* stream) {
+  if (n < 0 || !offsets || (n > 0 && (!counts || !workspace))) return set_error(FF_ERR_ARG, "bad scan arguments");
+  if (workspace_bytes < scan_workspace_bytes(n)) return set_error(FF_ERR_SIZE, "scan workspace too small");
+  if (!aligned(workspace, 8) || !aligned(offsets, 8)) return set_error(FF_ERR_ALIGN, "scan buffers must be 8-byte aligned");
+  return cuda_status(launch_scan(counts, n, offsets, workspace, (cudaStream_t)stream), "ff_scan_counts launch");
+}
+
+int ff_march_emit(const FFRender* r, const float* rays, const float* jitter, int64_t n_rays, const int64_t* offsets,
+                  float* xyz, int32_t* sample_idx, void* stream) {
+  int rc = validate_render(r, rays, n_rays);
+  if (rc) return rc;
+  if (n_rays > 0 && (!offsets || !xyz || !sample_idx)) return set_error(FF_ERR_ARG, "emit outputs are NULL");
+  return cuda_status(launch_march_emit(*r, rays, jitter, n_rays, offsets, xyz, sample_idx, (cudaStream_t)stream),
+                     "ff_march_emit launch");
+}
+
+int ff_composite_forward(const FFRender* r, const float* rays, const float* jitter, int64_t n_rays,
+                         const int64_t* offsets, const int32_t* sample_idx, const float* feat, int32_t feat_stride,
+                         const int32_t* white_bg, float* rgb, float* depth, float* acc, void* stream) {
+  int rc = validate_render(r, rays, n_rays);
+  if (rc) return rc;
+  if (feat_stride < 28) return set_error(FF_ERR_UNSUPPORTED, "the SH-2 colour head needs feat_stride >= 28");
+  if (n_rays > 0 && (!offsets || !rgb)) return set_error(FF_ERR_ARG, "offsets/rgb are NULL");
+  return cuda_status(launch_composite_forward(*r, rays, jitter, n_rays, offsets, sample_idx, feat, feat_stride,
+                                              white_bg, rgb, depth, acc, (cudaStream_t)stream),
+                     "ff_composite_forward launch");
+}
+
+int ff_composite_backward(const FFRender* r, const float* rays, const float* jitter, int64_t n_rays,
+                          const int64_t* offsets, const int32_t* sample_idx, const float* feat, int32_t feat_stride,
+                          const int32_t* white_bg, const float* grad_rgb, float* grad_feat, void* stream) {
+  int rc = validate_render(r, rays, n_rays);
+  if (rc) return rc;
+  if (feat_stride < 28) return set_error(FF_ERR_UNSUPPORTED, "the SH-2 colour head needs feat_stride >= 28");
+  if (n_rays > 0 && (!offsets || !grad_rgb || !grad_feat)) return set_error(FF_ERR_ARG, "backward buffers are NULL");
+  return cuda_status(launch_composite_backward(*r, rays, jitter, n_rays, offsets, sample_idx, feat, feat_stride,
+                                               white_bg, grad_rgb, grad_feat, (cudaStream_t)stream),
+                     "ff_composite_backward launch");
 }
 
 }  // extern "C"

@@ -43,4 +43,20 @@ cudaError_t launch_fused_fit(const FFField& f, const void* basis, const void* co
                              float* loss_sum, float* grad_basis, float* grad_coeff, const FFMlpGrad& g,
                              cudaStream_t st);
 
+// render_kernels.cu
+int64_t scan_workspace_bytes(int64_t n);
+cudaError_t launch_march_count(const FFRender& r, const float* rays, const float* jitter, int64_t n, int32_t* counts,
+                               float* t_min, cudaStream_t s);
+cudaError_t launch_scan(const int32_t* counts, int64_t n, int64_t* offsets, void* workspace, cudaStream_t s);
+cudaError_t launch_march_emit(const FFRender& r, const float* rays, const float* jitter, int64_t n,
+                              const int64_t* offsets, float* xyz, int32_t* sample_idx, cudaStream_t s);
+cudaError_t launch_composite_forward(const FFRender& r, const float* rays, const float* jitter, int64_t n,
+                                     const int64_t* offsets, const int32_t* sample_idx, const float* feat,
+                                     int feat_stride, const int32_t* white_bg, float* rgb, float* depth, float* acc,
+                                     cudaStream_t s);
+cudaError_t launch_composite_backward(const FFRender& r, const float* rays, const float* jitter, int64_t n,
+                                      const int64_t* offsets, const int32_t* sample_idx, const float* feat,
+                                      int feat_stride, const int32_t* white_bg, const float* grad_rgb,
+                                      float* grad_feat, cudaStream_t s);
+
 }  // namespace ffgb

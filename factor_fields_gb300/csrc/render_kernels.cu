@@ -1,0 +1,504 @@
+// Ray marching, compaction and alpha compositing for bounded scenes.
+//
+// Replaces FactorFields.forward's sampling and compositing (models/FactorFields.py:843-898):
+//   sample_point         :586-602  slab entry t_min, z_i = t_min + step * (i + u), in-box mask
+//   AlphaGridMask        :91-110, :865-867  trilinear lookup of the 0/1 volume > 0.5
+//   boolean compaction   :863-885  xyz_sampled[ray_valid], row-major order
+//   raw2alpha + composite :82-88, :876-896  softplus density, alpha, cumprod transmittance,
+//                         weights, colour head on w > thres, acc / rgb / white bg / clamp / depth
+// with the colour head = degree-2 SH (models/sh.py:34-64) + sigmoid.
+//
+// Everything that decides WHICH sample is live (positions, in-box test, occupancy) uses
+// explicitly rounded float32 ops in the reference's order, so the live set and its order are
+// bit-identical to the reference. The occupancy volume is a bitfield: the reference's rule
+// (trilinear interpolation of 0/1 values, > 0.5) is evaluated exactly from the 8 corner bits.
+//
+// Warp per ray throughout: marching tests 32 samples per step and compacts them with a
+// ballot + popc prefix; compositing runs a 32-wide multiplicative scan per chunk with the
+// running transmittance carried between chunks; the backward runs the forward again, then a
+// reverse affine scan for sum_{k>j} dL/dw_k * alpha_k * prod_{j<m<k} (1 - alpha_m + 1e-10).
+#include "ff_common.cuh"
+#include "ff_internal.h"
+
+namespace ffgb {
+
+namespace {
+
+constexpr int kRayWarps = 8;  // warps (rays) per block
+
+struct RayGeo {
+  float o[3], d[3], t_min, u;
+};
+
+__device__ __forceinline__ RayGeo ray_setup(const FFRender& r, const float* rays, const float* jitter, int64_t ray) {
+  RayGeo g;
+  float tm = -INFINITY;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    g.o[k] = rays[ray * 6 + k];
+    g.d[k] = rays[ray * 6 + 3 + k];
+    const float vec = (g.d[k] == 0.f) ? 1e-6f : g.d[k];
+    const float ra = __fdiv_rn(__fsub_rn(r.aabb_max[k], g.o[k]), vec);
+    const float rb = __fdiv_rn(__fsub_rn(r.aabb_min[k], g.o[k]), vec);
+    tm = fmaxf(tm, fminf(ra, rb));
+  }
+  g.t_min = fminf(fmaxf(tm, 0.05f), 1e3f);
+  g.u = jitter ? jitter[ray] : 0.f;
+  return g;
+}
+
+// z of sample i: t_min + step * (i + u)  (float32, reference order)
+__device__ __forceinline__ float sample_z(const FFRender& r, const RayGeo& g, int i) {
+  const float rng = (g.u != 0.f) ? __fadd_rn((float)i, g.u) : (float)i;
+  return __fadd_rn(g.t_min, __fmul_rn(r.step, rng));
+}
+
+__device__ __forceinline__ bool occupied(const FFRender& r, const float* p) {
+  float ix[3];
+  int sz[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    sz[k] = r.occ_reso[k];
+    const float u = __fsub_rn(__fmul_rn(__fsub_rn(p[k], r.occ_origin[k]), r.occ_inv[k]), 1.f);
+    ix[k] = unnorm_align(u, sz[k]);
+  }
+  Corners<3> c;
+  linear_corners<3>(ix, sz, c);
+  float val = 0.f;
+#pragma unroll
+  for (int b = 0; b < 8; ++b) {
+    if (c.idx[b] >= 0) {
+      const uint32_t word = __ldg(r.occ_bits + (c.idx[b] >> 5));
+      if ((word >> (c.idx[b] & 31)) & 1u) val = __fadd_rn(val, c.w[b]);
+    }
+  }
+  return val > 0.5f;
+}
+
+// Sample i of the ray: live (in the box and, with a mask, occupied) and its position.
+__device__ __forceinline__ bool sample_live(const FFRender& r, const RayGeo& g, int i, float* p) {
+  const float z = sample_z(r, g, i);
+  bool in = true;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    p[k] = __fadd_rn(g.o[k], __fmul_rn(g.d[k], z));
+    in = in && !(r.aabb_min[k] > p[k] || p[k] > r.aabb_max[k]);
+  }
+  if (in && r.occ_bits) in = occupied(r, p);
+  return in;
+}
+
+__global__ void __launch_bounds__(kRayWarps * 32) march_count_kernel(const FFRender r, const float* __restrict__ rays,
+                                                                    const float* __restrict__ jitter, int64_t n_rays,
+                                                                    int32_t* __restrict__ counts,
+                                                                    float* __restrict__ t_min) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t ray = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; ray < n_rays;
+       ray += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+    const RayGeo g = ray_setup(r, rays, jitter, ray);
+    int cnt = 0;
+    for (int i0 = 0; i0 < r.n_samples; i0 += 32) {
+      const int i = i0 + lane;
+      float p[3];
+      const bool live = (i < r.n_samples) && sample_live(r, g, i, p);
+      cnt += __popc(__ballot_sync(0xffffffffu, live));
+    }
+    if (lane == 0) {
+      counts[ray] = cnt;
+      if (t_min) t_min[ray] = g.t_min;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kRayWarps * 32) march_emit_kernel(const FFRender r, const float* __restrict__ rays,
+                                                                   const float* __restrict__ jitter, int64_t n_rays,
+                                                                   const int64_t* __restrict__ offsets,
+                                                                   float* __restrict__ xyz,
+                                                                   int32_t* __restrict__ sample_idx) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t ray = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; ray < n_rays;
+       ray += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+    const RayGeo g = ray_setup(r, rays, jitter, ray);
+    int64_t pos = offsets[ray];
+    for (int i0 = 0; i0 < r.n_samples; i0 += 32) {
+      const int i = i0 + lane;
+      float p[3];
+      const bool live = (i < r.n_samples) && sample_live(r, g, i, p);
+      const uint32_t m = __ballot_sync(0xffffffffu, live);
+      if (live) {
+        const int64_t j = pos + __popc(m & ((1u << lane) - 1u));
+        xyz[j * 3 + 0] = p[0];
+        xyz[j * 3 + 1] = p[1];
+        xyz[j * 3 + 2] = p[2];
+        sample_idx[j] = i;
+      }
+      pos += __popc(m);
+    }
+  }
+}
+
+// ---- exclusive scan of per-ray counts (two levels through a caller workspace) ----------
+
+constexpr int kScanThreads = 1024;
+constexpr int kScanItems = 4;  // per thread
+constexpr int kScanBlock = kScanThreads * kScanItems;
+
+__device__ __forceinline__ int64_t block_excl_scan(int64_t v, int64_t* warp_sums, int64_t& total) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int64_t x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int64_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) warp_sums[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    int64_t s = (lane < (int)(blockDim.x >> 5)) ? warp_sums[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int64_t y = __shfl_up_sync(0xffffffffu, s, o);
+      if (lane >= o) s += y;
+    }
+    warp_sums[lane] = s;
+  }
+  __syncthreads();
+  total = warp_sums[(blockDim.x >> 5) - 1];
+  const int64_t before = warp > 0 ? warp_sums[warp - 1] : 0;
+  __syncthreads();
+  return before + x - v;
+}
+
+__global__ void __launch_bounds__(kScanThreads) scan_blocks_kernel(const int32_t* __restrict__ counts, int64_t n,
+                                                                   int64_t* __restrict__ block_sums) {
+  __shared__ int64_t ws[32];
+  const int64_t base = (int64_t)blockIdx.x * kScanBlock + threadIdx.x * kScanItems;
+  int64_t v = 0;
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k)
+    if (base + k < n) v += counts[base + k];
+  int64_t total;
+  block_excl_scan(v, ws, total);
+  if (threadIdx.x == 0) block_sums[blockIdx.x] = total;
+}
+
+// Scans the block sums in place (one block, looping over chunks of the sums array).
+__global__ void __launch_bounds__(kScanThreads) scan_sums_kernel(int64_t* __restrict__ block_sums, int64_t nb) {
+  __shared__ int64_t ws[32];
+  int64_t carry = 0;
+  for (int64_t c = 0; c < nb; c += kScanThreads) {
+    const int64_t i = c + threadIdx.x;
+    const int64_t v = i < nb ? block_sums[i] : 0;
+    int64_t total;
+    const int64_t ex = block_excl_scan(v, ws, total);
+    if (i < nb) block_sums[i] = carry + ex;
+    carry += total;
+  }
+}
+
+__global__ void __launch_bounds__(kScanThreads) scan_apply_kernel(const int32_t* __restrict__ counts, int64_t n,
+                                                                  const int64_t* __restrict__ block_prefix,
+                                                                  int64_t* __restrict__ offsets) {
+  __shared__ int64_t ws[32];
+  const int64_t base = (int64_t)blockIdx.x * kScanBlock + threadIdx.x * kScanItems;
+  int64_t vals[kScanItems];
+  int64_t v = 0;
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    vals[k] = (base + k < n) ? counts[base + k] : 0;
+    v += vals[k];
+  }
+  int64_t total;
+  int64_t run = block_prefix[blockIdx.x] + block_excl_scan(v, ws, total);
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    if (base + k < n) offsets[base + k] = run;
+    run += vals[k];
+  }
+  if (base + kScanItems >= n && base < n) offsets[n] = run;  // the thread holding the last element
+}
+
+// ---- compositing --------------------------------------------------------------------
+
+constexpr float kSH_C0 = 0.28209479177387814f;
+constexpr float kSH_C1 = 0.4886025119029199f;
+constexpr float kSH_C2_0 = 1.0925484305920792f;
+constexpr float kSH_C2_1 = -1.0925484305920792f;
+constexpr float kSH_C2_2 = 0.31539156525252005f;
+constexpr float kSH_C2_3 = -1.0925484305920792f;
+constexpr float kSH_C2_4 = 0.5462742152960396f;
+
+// The nine real SH basis values of degree <= 2 with the reference's signs (models/sh.py:49-64).
+__device__ __forceinline__ void sh2_basis(const float* d, float* y) {
+  const float x = d[0], yy_ = d[1], z = d[2];
+  const float xx = x * x, yy = yy_ * yy_, zz = z * z;
+  y[0] = kSH_C0;
+  y[1] = -kSH_C1 * yy_;
+  y[2] = kSH_C1 * z;
+  y[3] = -kSH_C1 * x;
+  y[4] = kSH_C2_0 * (x * yy_);
+  y[5] = kSH_C2_1 * (yy_ * z);
+  y[6] = kSH_C2_2 * (2.f * zz - xx - yy);
+  y[7] = kSH_C2_3 * (x * z);
+  y[8] = kSH_C2_4 * (xx - yy);
+}
+
+struct SampleVals {
+  float z, delta, f0, sigma, alpha, fac;
+};
+
+__device__ __forceinline__ SampleVals sample_vals(const FFRender& r, const RayGeo& g, int i, const float* feat_row) {
+  SampleVals s;
+  s.z = sample_z(r, g, i);
+  const float dist = (i + 1 < r.n_samples) ? __fsub_rn(sample_z(r, g, i + 1), s.z) : 0.f;  // :861
+  s.delta = __fmul_rn(dist, r.distance_scale);
+  s.f0 = feat_row[0];
+  const float x = s.f0 + r.density_shift;
+  if (r.density_act == 0)
+    s.sigma = (x > 20.f) ? x : log1pf(expf(x));  // softplus, threshold 20
+  else
+    s.sigma = fmaxf(x, 0.f);
+  s.alpha = 1.f - expf(-s.sigma * s.delta);
+  s.fac = 1.f - s.alpha + 1e-10f;
+  return s;
+}
+
+// Per-chunk exclusive transmittance: T_j = carry * prod_{lanes < j} fac; returns the chunk product.
+__device__ __forceinline__ float excl_trans(float fac, int lane, float& excl) {
+  float incl = fac;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const float v = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl *= v;
+  }
+  excl = __shfl_up_sync(0xffffffffu, incl, 1);
+  if (lane == 0) excl = 1.f;
+  return __shfl_sync(0xffffffffu, incl, 31);
+}
+
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__device__ __forceinline__ float sigmoidf(float x) { return 1.f / (1.f + expf(-x)); }
+
+// Colour of one sample: sigmoid(SH2(dir) . sh[c]) (models/sh.py:34 composed with a sigmoid).
+__device__ __forceinline__ void sample_rgb(const float* feat_row, const float* ybasis, float* rgb, float* lin) {
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const float* sh = feat_row + 1 + c * 9;
+    float v = 0.f;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) v += ybasis[k] * sh[k];
+    lin[c] = v;
+    rgb[c] = sigmoidf(v);
+  }
+}
+
+__global__ void __launch_bounds__(kRayWarps * 32) composite_forward_kernel(
+    const FFRender r, const float* __restrict__ rays, const float* __restrict__ jitter, int64_t n_rays,
+    const int64_t* __restrict__ offsets, const int32_t* __restrict__ sample_idx, const float* __restrict__ feat,
+    int feat_stride, const int32_t* __restrict__ white_bg, float* __restrict__ rgb_out, float* __restrict__ depth_out,
+    float* __restrict__ acc_out) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t ray = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; ray < n_rays;
+       ray += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+    const RayGeo g = ray_setup(r, rays, jitter, ray);
+    float yb[9];
+    sh2_basis(g.d, yb);
+    const int64_t beg = offsets[ray], end = offsets[ray + 1];
+    float T = 1.f, acc = 0.f, depth = 0.f, col[3] = {0.f, 0.f, 0.f};
+    for (int64_t c0 = beg; c0 < end; c0 += 32) {
+      const int64_t j = c0 + lane;
+      const bool active = j < end;
+      SampleVals s = {0.f, 0.f, 0.f, 0.f, 0.f, 1.f};
+      const float* row = feat + (active ? j : beg) * feat_stride;
+      if (active) s = sample_vals(r, g, sample_idx[j], row);
+      float excl;
+      const float prod = excl_trans(s.fac, lane, excl);
+      const float w = active ? s.alpha * (T * excl) : 0.f;
+      acc += w;
+      depth += w * s.z;
+      if (active && w > r.weight_thres) {
+        float c[3], lin[3];
+        sample_rgb(row, yb, c, lin);
+        col[0] += w * c[0]; col[1] += w * c[1]; col[2] += w * c[2];
+      }
+      T *= prod;
+    }
+    acc = warp_sum(acc);
+    depth = warp_sum(depth);
+    col[0] = warp_sum(col[0]); col[1] = warp_sum(col[1]); col[2] = warp_sum(col[2]);
+    if (lane == 0) {
+      const bool wb = white_bg ? (*white_bg != 0) : (r.white_bg != 0);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        float v = col[c];
+        if (wb) v = v + (1.f - acc);
+        rgb_out[ray * 3 + c] = fminf(fmaxf(v, 0.f), 1.f);
+      }
+      if (depth_out) depth_out[ray] = depth;
+      if (acc_out) acc_out[ray] = acc;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kRayWarps * 32) composite_backward_kernel(
+    const FFRender r, const float* __restrict__ rays, const float* __restrict__ jitter, int64_t n_rays,
+    const int64_t* __restrict__ offsets, const int32_t* __restrict__ sample_idx, const float* __restrict__ feat,
+    int feat_stride, const int32_t* __restrict__ white_bg, const float* __restrict__ grad_rgb,
+    float* __restrict__ grad_feat) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t ray = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; ray < n_rays;
+       ray += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+    const RayGeo g = ray_setup(r, rays, jitter, ray);
+    float yb[9];
+    sh2_basis(g.d, yb);
+    const int64_t beg = offsets[ray], end = offsets[ray + 1];
+    const bool wb = white_bg ? (*white_bg != 0) : (r.white_bg != 0);
+    // pass 1: the forward again (rgb before the clamp decides which channels pass gradient);
+    // the exclusive transmittance of each sample is parked in grad_feat[j][0]
+    float T = 1.f, acc = 0.f, col[3] = {0.f, 0.f, 0.f};
+    for (int64_t c0 = beg; c0 < end; c0 += 32) {
+      const int64_t j = c0 + lane;
+      const bool active = j < end;
+      SampleVals s = {0.f, 0.f, 0.f, 0.f, 0.f, 1.f};
+      const float* row = feat + (active ? j : beg) * feat_stride;
+      if (active) s = sample_vals(r, g, sample_idx[j], row);
+      float excl;
+      const float prod = excl_trans(s.fac, lane, excl);
+      const float Tj = T * excl;
+      const float w = active ? s.alpha * Tj : 0.f;
+      acc += w;
+      if (active) {
+        grad_feat[j * feat_stride] = Tj;
+        if (w > r.weight_thres) {
+          float c[3], lin[3];
+          sample_rgb(row, yb, c, lin);
+          col[0] += w * c[0]; col[1] += w * c[1]; col[2] += w * c[2];
+        }
+      }
+      T *= prod;
+    }
+    acc = warp_sum(acc);
+    float G[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      float v = warp_sum(col[c]);
+      if (wb) v = v + (1.f - acc);
+      G[c] = (v >= 0.f && v <= 1.f) ? grad_rgb[ray * 3 + c] : 0.f;  // clamp backward
+    }
+    // pass 2: reverse. E_j = A_j + F_j * E_{j+1} with A = dL/dw * alpha, F = fac; S_j = E_{j+1}.
+    float carry = 0.f;
+    const int64_t n = end - beg;
+    for (int64_t k0 = ((n - 1) / 32) * 32; n > 0 && k0 >= 0; k0 -= 32) {
+      const int64_t j = beg + k0 + lane;
+      const bool active = j < end;
+      SampleVals s = {0.f, 0.f, 0.f, 0.f, 0.f, 1.f};
+      const float* row = feat + (active ? j : beg) * feat_stride;
+      float Tj = 0.f, c[3] = {0.f, 0.f, 0.f}, lin[3] = {0.f, 0.f, 0.f};
+      bool app = false;
+      float w = 0.f, gw = 0.f;
+      if (active) {
+        s = sample_vals(r, g, sample_idx[j], row);
+        Tj = grad_feat[j * feat_stride];
+        w = s.alpha * Tj;
+        app = w > r.weight_thres;
+        if (app) sample_rgb(row, yb, c, lin);
+#pragma unroll
+        for (int q = 0; q < 3; ++q) gw += G[q] * (c[q] - (wb ? 1.f : 0.f));
+      }
+      // reverse inclusive affine scan over lanes l..31: (a, f) o (a', f') = (a + f a', f f')
+      float a = active ? gw * s.alpha : 0.f, f = active ? s.fac : 1.f;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const float a2 = __shfl_down_sync(0xffffffffu, a, o);
+        const float f2 = __shfl_down_sync(0xffffffffu, f, o);
+        if (lane + o < 32) {
+          a = a + f * a2;
+          f = f * f2;
+        }
+      }
+      const float e_incl = a + f * carry;                 // E_j
+      float s_next = __shfl_down_sync(0xffffffffu, e_incl, 1);  // E_{j+1}
+      if (lane == 31) s_next = carry;
+      const float new_carry = __shfl_sync(0xffffffffu, e_incl, 0);
+      if (active) {
+        const float g_alpha = Tj * (gw - s_next);
+        const float g_sigma = g_alpha * expf(-s.sigma * s.delta) * s.delta;
+        const float x = s.f0 + r.density_shift;
+        float g_f0;
+        if (r.density_act == 0)
+          g_f0 = (x > 20.f) ? g_sigma : g_sigma * sigmoidf(x);
+        else
+          g_f0 = x > 0.f ? g_sigma : 0.f;
+        float* out = grad_feat + j * feat_stride;
+        out[0] = g_f0;
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+          const float gl = app ? G[q] * w * c[q] * (1.f - c[q]) : 0.f;
+#pragma unroll
+          for (int k = 0; k < 9; ++k) out[1 + q * 9 + k] = gl * yb[k];
+        }
+      }
+      carry = new_carry;
+    }
+  }
+}
+
+int ray_blocks(int64_t n_rays) {
+  const int64_t want = ceil_div(n_rays, kRayWarps);
+  return (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)sm_count() * 16));
+}
+
+}  // namespace
+
+int64_t scan_workspace_bytes(int64_t n) { return (ceil_div(n, kScanBlock) + 1) * (int64_t)sizeof(int64_t); }
+
+cudaError_t launch_march_count(const FFRender& r, const float* rays, const float* jitter, int64_t n, int32_t* counts,
+                               float* t_min, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  march_count_kernel<<<ray_blocks(n), kRayWarps * 32, 0, s>>>(r, rays, jitter, n, counts, t_min);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_scan(const int32_t* counts, int64_t n, int64_t* offsets, void* workspace, cudaStream_t s) {
+  if (n == 0) return cudaMemsetAsync(offsets, 0, sizeof(int64_t), s);
+  const int64_t nb = ceil_div(n, kScanBlock);
+  int64_t* sums = static_cast<int64_t*>(workspace);
+  scan_blocks_kernel<<<(unsigned)nb, kScanThreads, 0, s>>>(counts, n, sums);
+  scan_sums_kernel<<<1, kScanThreads, 0, s>>>(sums, nb);
+  scan_apply_kernel<<<(unsigned)nb, kScanThreads, 0, s>>>(counts, n, sums, offsets);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_march_emit(const FFRender& r, const float* rays, const float* jitter, int64_t n,
+                              const int64_t* offsets, float* xyz, int32_t* sample_idx, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  march_emit_kernel<<<ray_blocks(n), kRayWarps * 32, 0, s>>>(r, rays, jitter, n, offsets, xyz, sample_idx);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_composite_forward(const FFRender& r, const float* rays, const float* jitter, int64_t n,
+                                     const int64_t* offsets, const int32_t* sample_idx, const float* feat,
+                                     int feat_stride, const int32_t* white_bg, float* rgb, float* depth, float* acc,
+                                     cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  composite_forward_kernel<<<ray_blocks(n), kRayWarps * 32, 0, s>>>(r, rays, jitter, n, offsets, sample_idx, feat,
+                                                                     feat_stride, white_bg, rgb, depth, acc);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_composite_backward(const FFRender& r, const float* rays, const float* jitter, int64_t n,
+                                      const int64_t* offsets, const int32_t* sample_idx, const float* feat,
+                                      int feat_stride, const int32_t* white_bg, const float* grad_rgb,
+                                      float* grad_feat, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  composite_backward_kernel<<<ray_blocks(n), kRayWarps * 32, 0, s>>>(r, rays, jitter, n, offsets, sample_idx, feat,
+                                                                      feat_stride, white_bg, grad_rgb, grad_feat);
+  return cudaGetLastError();
+}
+
+}  // namespace ffgb

@@ -115,6 +115,7 @@ class FactorFields(torch.nn.Module):
         self.n_scene = g.n_scene
         self.n_feat = g.n_feat
         self._freq_bands = g.freq_bands.to(self.device)
+        self._freq_host = tuple(float(v) for v in g.freq_bands)  # host copy: no device sync per call
         self.layout = FieldLayout(g.basis_dims, g.basis_reso, g.in_dim, g.coeff_reso, g.n_scene)
         levels = [dct_dict(int(np.power(c, 1.0 / self.in_dim) + 1), r, n_select=c, dim=self.in_dim)
                   .reshape([1, c] + [r] * self.in_dim) for c, r in zip(g.basis_dims, g.basis_reso)]
@@ -132,7 +133,9 @@ class FactorFields(torch.nn.Module):
 
     @freq_bands.setter
     def freq_bands(self, v):
-        self._freq_bands = torch.as_tensor(v, dtype=torch.float32).to(self.device)
+        t = torch.as_tensor(v, dtype=torch.float32)
+        self._freq_host = tuple(float(x) for x in t.cpu())
+        self._freq_bands = t.to(self.device)
         self._desc_cache = {}
 
     @property
@@ -146,10 +149,10 @@ class FactorFields(torch.nn.Module):
         return [self.layout.coeff_view(self.coeff_flat, s) for s in range(self.n_scene)]
 
     def descriptor(self, dtype):
-        key = (dtype, tuple(self._freq_bands.tolist()))
+        key = (dtype, self._freq_host)
         d = self._desc_cache.get(key)
         if d is None:
-            self.geom.freq_bands = self._freq_bands.cpu()
+            self.geom.freq_bands = torch.tensor(self._freq_host, dtype=torch.float32)
             d = self.layout.descriptor(self.geom, self.cfg.model.basis_mapping, self.cfg.model.basis_mode,
                                        self.cfg.model.coef_mode, dtype)
             self._desc_cache[key] = d
@@ -259,11 +262,13 @@ class FactorFields(torch.nn.Module):
         self.stepSize = step.to(self.device)
         self.nSamples = n
 
-    def forward(self, rays_chunk, white_bg=True, is_train=False, ndc_ray=False, N_samples=-1):
-        """models/FactorFields.py:843-898 (bounded scenes): (rgb_map, depth_map, coeffs)."""
+    def forward(self, rays_chunk, white_bg=True, is_train=False, ndc_ray=False, N_samples=-1, jitter=None,
+                fused=None):
+        """models/FactorFields.py:843-898 (bounded scenes): (rgb_map, depth_map, coeffs).
+        fused=None picks the fused BF16 field kernel when precision == 'bf16'."""
         from .renderer import render_forward
         return render_forward(self, rays_chunk, white_bg=white_bg, is_train=is_train, ndc_ray=ndc_ray,
-                              N_samples=N_samples)
+                              N_samples=N_samples, jitter=jitter, fused=fused)
 
     # ---- checkpoints (models/FactorFields.py:669-691) --------------------------------------
     def reference_state_dict(self):

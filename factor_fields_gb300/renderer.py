@@ -1,7 +1,19 @@
-"""Renderer surface: render_ray (renderer.py:8-27), the colour heads, the occupancy mask and
-FactorFields.forward (models/FactorFields.py:843-898) for bounded scenes."""
+"""Renderer surface: render_ray (renderer.py:8-27), the SH-2 colour head, the occupancy mask and
+FactorFields.forward (models/FactorFields.py:843-898) for bounded scenes, on the native
+march / compact / composite kernels.
+
+Per chunk of rays: ff_march_count -> ff_scan_counts -> ff_march_emit give the live samples in
+the reference's order (xyz_sampled[ray_valid]); the field + MLP head runs on them (drop-in
+float32 kernels, or the fused BF16 kernel); ff_composite_forward alpha-composites. The backward
+is ff_composite_backward followed by the field/MLP backward kernels. One host synchronisation
+per chunk reads the number of live samples (the reference synchronises on ray_valid.any()).
+"""
+import ctypes
+
 import torch
 
+from . import _native as N
+from . import functional as FN
 from .config import Cfg
 
 
@@ -17,7 +29,8 @@ class SHRender(torch.nn.Module):
 
 
 class AlphaGridMask(torch.nn.Module):
-    """models/FactorFields.py:91-110: a 0/1 occupancy volume over an aabb."""
+    """models/FactorFields.py:91-110: a 0/1 occupancy volume [D, H, W] over an aabb, kept as
+    the float volume (reference layout) and as a packed bitfield for the kernels."""
 
     def __init__(self, device, aabb, alpha_volume):
         super().__init__()
@@ -25,9 +38,25 @@ class AlphaGridMask(torch.nn.Module):
         self.aabb = aabb.to(device)
         self.aabbSize = self.aabb[1] - self.aabb[0]
         self.invgridSize = 1.0 / self.aabbSize * 2
-        self.alpha_volume = alpha_volume.view(1, 1, *alpha_volume.shape[-3:])
+        self.alpha_volume = alpha_volume.view(1, 1, *alpha_volume.shape[-3:]).to(device)
         self.gridSize = torch.tensor([alpha_volume.shape[-1], alpha_volume.shape[-2], alpha_volume.shape[-3]],
                                      dtype=torch.long, device=device)
+        self.bits = pack_bits(self.alpha_volume.reshape(-1) > 0)
+
+    def sample_alpha(self, xyz_sampled):
+        """The reference's trilinear lookup (:103-107) — used for inspection, not by the kernels."""
+        import torch.nn.functional as F
+        pts = (xyz_sampled - self.aabb[0]) * self.invgridSize - 1
+        return F.grid_sample(self.alpha_volume, pts.view(1, -1, 1, 1, 3), align_corners=True).view(-1)
+
+
+def pack_bits(flags):
+    """Bool vector -> int32 words, bit k of word w = flags[32 w + k]."""
+    n = flags.numel()
+    pad = (-n) % 32
+    f = torch.nn.functional.pad(flags.to(torch.int64), (0, pad)).view(-1, 32)
+    words = (f << torch.arange(32, device=f.device, dtype=torch.int64)).sum(1)
+    return words.to(torch.int32).contiguous()
 
 
 def make_render_module(cfg, in_channels):
@@ -37,5 +66,198 @@ def make_render_module(cfg, in_channels):
     raise NotImplementedError(f"renderer.shadingMode {shading!r} is not implemented (use 'SH')")
 
 
-def render_forward(model, rays_chunk, white_bg=True, is_train=False, ndc_ray=False, N_samples=-1):
-    raise NotImplementedError("ray rendering is not built yet")
+def render_desc(model, n_samples, white_bg):
+    """FFRender for a FactorFields model (float32 constants computed as the reference does)."""
+    r = N.FFRender()
+    aabb = model.aabb.detach().cpu()
+    for k in range(3):
+        r.aabb_min[k] = float(aabb[0, k])
+        r.aabb_max[k] = float(aabb[1, k])
+    r.step = float(model.stepSize.detach().cpu())
+    r.n_samples = int(n_samples)
+    rc = model.cfg.renderer
+    r.distance_scale = float(rc.distance_scale)
+    r.density_shift = float(rc.density_shift)
+    act = rc.fea2denseAct or "softplus"
+    if act not in ("softplus", "relu"):
+        raise NotImplementedError(f"fea2denseAct {act!r}")
+    r.density_act = 0 if act == "softplus" else 1
+    r.weight_thres = float(rc.rayMarch_weight_thres)
+    r.white_bg = 1 if white_bg else 0
+    mask = model.alphaMask
+    if mask is not None:
+        r.occ_bits = mask.bits.data_ptr()
+        vol = mask.alpha_volume
+        r.occ_reso[0], r.occ_reso[1], r.occ_reso[2] = vol.shape[-1], vol.shape[-2], vol.shape[-3]
+        a0 = mask.aabb.detach().cpu()
+        inv = mask.invgridSize.detach().cpu()
+        for k in range(3):
+            r.occ_origin[k] = float(a0[0, k])
+            r.occ_inv[k] = float(inv[k])
+    return r
+
+
+def march(model, rays, jitter, rdesc):
+    """Live samples of a chunk: (offsets [R+1] int64, xyz [M, 3], sample_idx [M] int32)."""
+    n = rays.shape[0]
+    dev = rays.device
+    st = N.stream_ptr()
+    counts = torch.empty(n, dtype=torch.int32, device=dev)
+    N.call("ff_march_count", ctypes.byref(rdesc), N.ptr(rays), N.ptr(jitter), n, N.ptr(counts), None, st)
+    offsets = torch.empty(n + 1, dtype=torch.int64, device=dev)
+    wsb = N.lib().ff_scan_workspace_bytes(n)
+    ws = torch.empty(max(wsb, 8), dtype=torch.uint8, device=dev)
+    N.call("ff_scan_counts", N.ptr(counts), n, N.ptr(offsets), N.ptr(ws), wsb, st)
+    m = int(offsets[-1].item())
+    xyz = torch.empty(m, 3, device=dev)
+    sidx = torch.empty(m, dtype=torch.int32, device=dev)
+    N.call("ff_march_emit", ctypes.byref(rdesc), N.ptr(rays), N.ptr(jitter), n, N.ptr(offsets), N.ptr(xyz),
+           N.ptr(sidx), st)
+    return offsets, xyz, sidx
+
+
+class RenderFunction(torch.autograd.Function):
+    """rgb, depth = render(rays) with gradients to the grids and the MLP head.
+
+    apply(rays, jitter, basis_param, coeff_param, w0, b0, w1, ctx_obj) where ctx_obj carries the
+    model, its read buffers, descriptors and the path (fused or drop-in)."""
+
+    @staticmethod
+    def forward(ctx, rays, jitter, basis_param, coeff_param, w0, b0, w1, job):
+        m, rdesc = job["model"], job["rdesc"]
+        offsets, xyz, sidx = march(m, rays, jitter, rdesc)
+        feat = field_eval(m, job, xyz)
+        n = rays.shape[0]
+        rgb = torch.empty(n, 3, device=rays.device)
+        depth = torch.empty(n, device=rays.device)
+        N.call("ff_composite_forward", ctypes.byref(rdesc), N.ptr(rays), N.ptr(jitter), n, N.ptr(offsets),
+               N.ptr(sidx), N.ptr(feat), feat.shape[1], None, N.ptr(rgb), N.ptr(depth), None, N.stream_ptr())
+        ctx.save_for_backward(rays, offsets, xyz, sidx, feat)
+        ctx.jitter, ctx.job = jitter, job
+        ctx.mark_non_differentiable(depth)
+        job["xyz"] = xyz
+        return rgb, depth
+
+    @staticmethod
+    def backward(ctx, g_rgb, g_depth):
+        rays, offsets, xyz, sidx, feat = ctx.saved_tensors
+        job = ctx.job
+        m, rdesc = job["model"], job["rdesc"]
+        n = rays.shape[0]
+        g_feat = torch.empty_like(feat)
+        N.call("ff_composite_backward", ctypes.byref(rdesc), N.ptr(rays), N.ptr(ctx.jitter), n, N.ptr(offsets),
+               N.ptr(sidx), N.ptr(feat), feat.shape[1], None, N.ptr(g_rgb.contiguous()), N.ptr(g_feat),
+               N.stream_ptr())
+        grads = field_grad(m, job, xyz, g_feat)
+        return (None, None) + grads + (None,)
+
+
+def field_eval(m, job, xyz):
+    """MLP output [M, out_dim] of the field at xyz (fused BF16 path or drop-in float32 path)."""
+    n = xyz.shape[0]
+    out_dim = m.linear_mat.out_dim
+    out = torch.empty(n, out_dim, device=xyz.device)
+    if n == 0:
+        return out
+    st = N.stream_ptr()
+    lm = m.linear_mat
+    ws, bs = lm.weights()
+    mlp = FN.mlp_struct(ws, bs, lm.in_dim, lm.hidden_dim, lm.out_dim)
+    if job["fused"]:
+        N.call("ff_field_mlp_forward", ctypes.byref(job["fdesc"]), N.ptr(job["basis_r"]), N.ptr(job["coeff_r"]),
+               ctypes.byref(mlp), N.ptr(xyz), n, N.ptr(out), st)
+    else:
+        feats = torch.empty(n, m.n_feat, device=xyz.device)
+        N.call("ff_field_forward", ctypes.byref(job["fdesc"]), N.ptr(job["basis_r"]), N.ptr(job["coeff_r"]),
+               N.ptr(xyz), n, N.ptr(feats), None, None, st)
+        N.call("ff_mlp_forward", ctypes.byref(mlp), N.ptr(feats), n, N.ptr(out), st)
+        job["feats"] = feats
+    return out
+
+
+def field_grad(m, job, xyz, g_out):
+    """(grad_basis, grad_coeff, grad_w0, grad_b0, grad_w1) for dL/dout = g_out at xyz."""
+    lm = m.linear_mat
+    ws, bs = lm.weights()
+    gb = torch.zeros_like(m.basis_flat)
+    gc = torch.zeros_like(job["coeff_param"])
+    gw = [torch.zeros_like(w) for w in ws]
+    gbias = [torch.zeros_like(b) if b is not None else None for b in bs]
+    n = xyz.shape[0]
+    if n:
+        st = N.stream_ptr()
+        mlp = FN.mlp_struct(ws, bs, lm.in_dim, lm.hidden_dim, lm.out_dim)
+        g = N.FFMlpGrad()
+        for i in range(len(ws)):
+            g.weight[i] = gw[i].data_ptr()
+            g.bias[i] = gbias[i].data_ptr() if gbias[i] is not None else None
+        if job["fused"]:
+            N.call("ff_field_mlp_backward", ctypes.byref(job["fdesc"]), N.ptr(job["basis_r"]),
+                   N.ptr(job["coeff_r"]), ctypes.byref(mlp), N.ptr(xyz), n, N.ptr(g_out), N.ptr(gb), N.ptr(gc),
+                   ctypes.byref(g), st)
+        else:
+            feats = job["feats"]
+            g_feats = torch.empty_like(feats)
+            N.call("ff_mlp_backward", ctypes.byref(mlp), N.ptr(feats), n, N.ptr(g_out), N.ptr(g_feats),
+                   ctypes.byref(g), st)
+            N.call("ff_field_backward", ctypes.byref(job["fdesc"]), N.ptr(job["basis_r"]), N.ptr(job["coeff_r"]),
+                   N.ptr(xyz), n, N.ptr(g_feats), None, None, N.ptr(gb), N.ptr(gc), st)
+    return (gb, gc, gw[0], gbias[0], gw[1] if len(gw) > 1 else None)
+
+
+def render_forward(model, rays_chunk, white_bg=True, is_train=False, ndc_ray=False, N_samples=-1, fused=None,
+                   jitter=None):
+    """FactorFields.forward (models/FactorFields.py:843-898), bounded scenes, SH-2 colour head:
+    returns (rgb_map [R, 3], depth_map [R], coeffs).
+
+    jitter: optional per-ray sample offsets [R] in [0, 1) (the reference draws them with
+    torch.rand_like when is_train); given explicitly they make sampling reproducible."""
+    if ndc_ray:
+        raise NotImplementedError("NDC rays (sample_point_ndc) are not on this path")
+    if not isinstance(model.renderModule, SHRender) or model.linear_mat.out_dim < 28:
+        raise NotImplementedError("rendering needs the SH-2 colour head with out_dim = 28")
+    lm = model.linear_mat
+    if lm.num_layers != 2:
+        raise NotImplementedError("rendering needs an MLPMixer with num_layers = 2")
+    rays = rays_chunk.to(model.device, torch.float32).contiguous()
+    n_samples = N_samples if N_samples > 0 else model.nSamples
+    if jitter is not None:
+        jitter = jitter.to(rays.device, torch.float32).reshape(-1).contiguous()
+    elif is_train:
+        jitter = torch.rand(rays.shape[0], device=rays.device)
+    wb = bool(white_bg or (is_train and torch.rand((1,)) < 0.5))  # :890
+    if fused is None:
+        fused = model.precision == "bf16"
+    basis_r, coeff_r, dt = model._read_buffers()
+    coeff_param = model.coeff_flat
+    if model.n_scene > 1:
+        coeff_param = model._coeff_scene(model.coeff_flat)
+        coeff_r = model._coeff_scene(coeff_r)
+    job = {"model": model, "rdesc": render_desc(model, n_samples, wb), "fdesc": model.descriptor(dt),
+           "basis_r": basis_r, "coeff_r": coeff_r, "coeff_param": coeff_param, "fused": fused}
+    l0, l1 = lm.backbone
+    rgb, depth = RenderFunction.apply(rays, jitter, model.basis_flat, coeff_param, l0.weight, l0.bias, l1.weight, job)
+    coeffs = torch.zeros((1, model.n_feat), device=rays.device)
+    if getattr(model, "return_coeffs", False) and job["xyz"].shape[0]:
+        with torch.no_grad():
+            coeffs = model.get_coeff(job["xyz"])
+    return rgb, depth, coeffs
+
+
+def render_ray(rays, factor_fields, chunk=4096, N_samples=-1, ndc_ray=False, white_bg=True, is_train=False,
+               device="cuda"):
+    """renderer.py:8-27: render rays in chunks; returns (rgb, depth) or, when training,
+    (rgb, depth, coeffs)."""
+    rgbs, depths, coeffs = [], [], []
+    n = rays.shape[0]
+    for c in range(n // chunk + int(n % chunk > 0)):
+        rc = rays[c * chunk:(c + 1) * chunk].to(device)
+        rgb, depth, coeff = factor_fields(rc, is_train=is_train, white_bg=white_bg, ndc_ray=ndc_ray,
+                                          N_samples=N_samples)
+        rgbs.append(rgb)
+        depths.append(depth)
+        if is_train:
+            coeffs.append(coeff)
+    if is_train:
+        return torch.cat(rgbs), torch.cat(depths), torch.cat(coeffs)
+    return torch.cat(rgbs), torch.cat(depths)

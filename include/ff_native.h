@@ -109,7 +109,7 @@ typedef struct FFMlpGrad {
 /* ---- library ------------------------------------------------------------------------- */
 FF_API int ff_abi_version(void);
 FF_API const char* ff_last_error(void);
-/* sizeof of the ABI structs, for binding checks: which = 0 FFField, 1 FFMlp, 2 FFMlpGrad. */
+/* sizeof of the ABI structs, for binding checks: 0 FFField, 1 FFMlp, 2 FFMlpGrad, 3 FFRender. */
 FF_API int64_t ff_struct_size(int32_t which);
 /* Number of SMs of the current device and the compute capability (major*10+minor). */
 FF_API int ff_device_info(int32_t* sm_count, int32_t* cc);
@@ -166,6 +166,61 @@ FF_API int ff_field_fit_step(const FFField* f, const void* basis, const void* co
                              const float* x, const float* target, int64_t n, int32_t loss_kind,
                              float loss_scale, float* loss_sum, float* grad_basis, float* grad_coeff_grid,
                              const FFMlpGrad* g, void* stream);
+
+/* ---- rendering (bounded scenes): march, compact, composite ------------------------------ */
+
+/* Renderer constants (models/FactorFields.py:586-602, :693-699, :843-898; configs/nerf.yaml
+ * renderer keys). rays are [n_rays, 6] float32 (origin, direction). */
+typedef struct FFRender {
+  float aabb_min[3];
+  float aabb_max[3];
+  float step;             /* stepSize, float32 as the reference computes it (:697) */
+  int32_t n_samples;      /* samples per ray (N_samples > 0, else nSamples) */
+  float distance_scale;   /* renderer.distance_scale (25) */
+  float density_shift;    /* renderer.density_shift (-10) */
+  int32_t density_act;    /* 0 softplus, 1 relu (renderer.fea2denseAct) */
+  float weight_thres;     /* renderer.rayMarch_weight_thres (1e-3) */
+  int32_t white_bg;       /* add (1 - acc) to rgb (:890-891) */
+  /* occupancy (AlphaGridMask, :91-110): NULL = no mask. Bit (z*H + y)*W + x of the 0/1 volume
+   * [D][H][W]; a sample is live when the trilinear interpolation of the bits is > 0.5. */
+  const uint32_t* occ_bits;
+  int32_t occ_reso[3];    /* x (W), y (H), z (D) */
+  float occ_origin[3];    /* mask aabb[0] */
+  float occ_inv[3];       /* invgridSize = 1.0 / aabbSize * 2, float32 */
+} FFRender;
+
+/* Live samples per ray: in the aabb (sample_point, :586-602) and occupied (:865-867).
+ * jitter: [n_rays] per-ray offset u added to the sample index when training (:595), or NULL.
+ * counts [n_rays] int32; t_min [n_rays] float32 (optional). */
+FF_API int ff_march_count(const FFRender* r, const float* rays, const float* jitter, int64_t n_rays,
+                          int32_t* counts, float* t_min, void* stream);
+
+/* Exclusive scan: offsets[i] = sum(counts[:i]), offsets[n] = total. Uses a caller workspace of
+ * ff_scan_workspace_bytes(n) bytes (per-block partial sums). */
+FF_API int64_t ff_scan_workspace_bytes(int64_t n);
+FF_API int ff_scan_counts(const int32_t* counts, int64_t n, int64_t* offsets, void* workspace,
+                          int64_t workspace_bytes, void* stream);
+
+/* Writes the live samples in ray-major order (= xyz_sampled[ray_valid] of :874): xyz [M, 3]
+ * float32 and sample_idx [M] int32 (index along the ray), using the scanned offsets. */
+FF_API int ff_march_emit(const FFRender* r, const float* rays, const float* jitter, int64_t n_rays,
+                         const int64_t* offsets, float* xyz, int32_t* sample_idx, void* stream);
+
+/* raw2alpha + colour + compositing (:82-88, :876-896) with the SH-2 colour head: feat [M,
+ * feat_stride] holds the MLP output per live sample (channel 0 density feature, 1..27 the SH
+ * coefficients as [3][9]). rgb [n_rays, 3], depth [n_rays], acc [n_rays] (optional).
+ * white_bg: optional device int overriding r->white_bg. */
+FF_API int ff_composite_forward(const FFRender* r, const float* rays, const float* jitter, int64_t n_rays,
+                                const int64_t* offsets, const int32_t* sample_idx, const float* feat,
+                                int32_t feat_stride, const int32_t* white_bg, float* rgb, float* depth,
+                                float* acc, void* stream);
+
+/* Backward of ff_composite_forward for dL/drgb [n_rays, 3]: writes dL/dfeat [M, feat_stride]
+ * (channels 0..27; overwritten, not accumulated). Depth carries no gradient (:895). */
+FF_API int ff_composite_backward(const FFRender* r, const float* rays, const float* jitter, int64_t n_rays,
+                                 const int64_t* offsets, const int32_t* sample_idx, const float* feat,
+                                 int32_t feat_stride, const int32_t* white_bg, const float* grad_rgb,
+                                 float* grad_feat, void* stream);
 
 #ifdef __cplusplus
 }
