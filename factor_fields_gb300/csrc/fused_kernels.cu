@@ -112,6 +112,12 @@ __device__ __forceinline__ float bf_hi(uint32_t v) { return __uint_as_float(v & 
 __device__ __forceinline__ uint32_t lds32(const __nv_bfloat16* p) { return *reinterpret_cast<const uint32_t*>(p); }
 __device__ __forceinline__ void sts32(__nv_bfloat16* p, uint32_t v) { *reinterpret_cast<uint32_t*>(p) = v; }
 
+// Two float32 values as a BF16 pair hi + lo: hi = bf16(v), lo = bf16(v - hi).
+__device__ __forceinline__ void split_pair(float a, float b, uint32_t& hi, uint32_t& lo) {
+  hi = pack_bf16(a, b);
+  lo = pack_bf16(a - bf_lo(hi), b - bf_hi(hi));
+}
+
 // A-fragment register pair (hi, lo) for two consecutive float32 features of the X tile;
 // columns at or past LD_XF read as zero.
 __device__ __forceinline__ void x_pair(const float* xf, int row, int col, uint32_t& hi, uint32_t& lo) {
@@ -364,9 +370,12 @@ __global__ void __launch_bounds__(kThreads, 3) fused_field_mlp_kernel(const Fuse
             sts32(dw + r1 * ld_do<OUTT>() + c0, pack_bf16(dc[nt][2], dc[nt][3]));
           }
         }
-        // ---------------- dH = (dO W1) * [H > 0] ----------------
-        uint32_t dha[4][4];
+        // ---------------- dH = (dO W1) * [H > 0], dX = dH W0 ----------------
+        // dO and dH enter their GEMMs as BF16 pairs hi + lo (two MMAs each), so the gradients
+        // keep ~16 mantissa bits through the sums over outputs and hidden units.
         __nv_bfloat16* dhw = s.dh + warp * 32 * LD_H;
+#pragma unroll
+        for (int nt = 0; nt < kNtIn; ++nt) dx[mt][nt][0] = dx[mt][nt][1] = dx[mt][nt][2] = dx[mt][nt][3] = 0.f;
 #pragma unroll
         for (int half = 0; half < 2; ++half) {
           float dh[4][4];
@@ -374,19 +383,21 @@ __global__ void __launch_bounds__(kThreads, 3) fused_field_mlp_kernel(const Fuse
           for (int q = 0; q < 4; ++q) dh[q][0] = dh[q][1] = dh[q][2] = dh[q][3] = 0.f;
 #pragma unroll
           for (int ks = 0; ks < (OUTT + 1) / 2; ++ks) {
-            uint32_t af[4];
-            af[0] = pack_bf16(dc[2 * ks][0], dc[2 * ks][1]);
-            af[1] = pack_bf16(dc[2 * ks][2], dc[2 * ks][3]);
+            uint32_t af[4], al[4];
+            split_pair(dc[2 * ks][0], dc[2 * ks][1], af[0], al[0]);
+            split_pair(dc[2 * ks][2], dc[2 * ks][3], af[1], al[1]);
             if (2 * ks + 1 < OUTT) {
-              af[2] = pack_bf16(dc[2 * ks + 1][0], dc[2 * ks + 1][1]);
-              af[3] = pack_bf16(dc[2 * ks + 1][2], dc[2 * ks + 1][3]);
+              split_pair(dc[2 * ks + 1][0], dc[2 * ks + 1][1], af[2], al[2]);
+              split_pair(dc[2 * ks + 1][2], dc[2 * ks + 1][3], af[3], al[3]);
             } else {
-              af[2] = af[3] = 0u;
+              af[2] = af[3] = al[2] = al[3] = 0u;
             }
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
               const __nv_bfloat16* wp = s.w1t + ((4 * half + q) * 8 + g) * LD_W1T + 16 * ks + 2 * t;
-              mma_bf16(dh[q], af, lds32(wp), lds32(wp + 8));
+              const uint32_t b0 = lds32(wp), b1 = lds32(wp + 8);
+              mma_bf16(dh[q], al, b0, b1);
+              mma_bf16(dh[q], af, b0, b1);
             }
           }
 #pragma unroll
@@ -400,26 +411,23 @@ __global__ void __launch_bounds__(kThreads, 3) fused_field_mlp_kernel(const Fuse
           }
 #pragma unroll
           for (int kk = 0; kk < 2; ++kk) {
-            uint32_t* d = dha[2 * half + kk];
-            d[0] = pack_bf16(dh[2 * kk][0], dh[2 * kk][1]);
-            d[1] = pack_bf16(dh[2 * kk][2], dh[2 * kk][3]);
-            d[2] = pack_bf16(dh[2 * kk + 1][0], dh[2 * kk + 1][1]);
-            d[3] = pack_bf16(dh[2 * kk + 1][2], dh[2 * kk + 1][3]);
+            uint32_t d[4], dl[4];
+            split_pair(dh[2 * kk][0], dh[2 * kk][1], d[0], dl[0]);
+            split_pair(dh[2 * kk][2], dh[2 * kk][3], d[1], dl[1]);
+            split_pair(dh[2 * kk + 1][0], dh[2 * kk + 1][1], d[2], dl[2]);
+            split_pair(dh[2 * kk + 1][2], dh[2 * kk + 1][3], d[3], dl[3]);
             const int ks = 2 * half + kk;
             __nv_bfloat16* p0 = dhw + r0 * LD_H + 16 * ks + 2 * t;
             __nv_bfloat16* p1 = dhw + r1 * LD_H + 16 * ks + 2 * t;
             sts32(p0, d[0]); sts32(p1, d[1]); sts32(p0 + 8, d[2]); sts32(p1 + 8, d[3]);
-          }
-        }
-        // ---------------- dX = dH W0 ----------------
+            // dX += dH[:, 16 ks .. 16 ks + 15] W0[16 ks .. 16 ks + 15, :]
 #pragma unroll
-        for (int nt = 0; nt < kNtIn; ++nt) dx[mt][nt][0] = dx[mt][nt][1] = dx[mt][nt][2] = dx[mt][nt][3] = 0.f;
-#pragma unroll
-        for (int ks = 0; ks < 4; ++ks) {
-#pragma unroll
-          for (int nt = 0; nt < kNtIn; ++nt) {
-            const __nv_bfloat16* wp = s.w0t + (nt * 8 + g) * LD_W0T + 16 * ks + 2 * t;
-            mma_bf16(dx[mt][nt], dha[ks], lds32(wp), lds32(wp + 8));
+            for (int nt = 0; nt < kNtIn; ++nt) {
+              const __nv_bfloat16* wp = s.w0t + (nt * 8 + g) * LD_W0T + 16 * ks + 2 * t;
+              const uint32_t b0 = lds32(wp), b1 = lds32(wp + 8);
+              mma_bf16(dx[mt][nt], dl, b0, b1);
+              mma_bf16(dx[mt][nt], d, b0, b1);
+            }
           }
         }
       }
