@@ -73,6 +73,8 @@ SIGNATURES = {
     "ff_march_count": (c_i32, [_P(FFRender), c_vp, c_vp, c_i64, c_vp, c_vp, c_vp]),
     "ff_scan_workspace_bytes": (c_i64, [c_i64]),
     "ff_scan_counts": (c_i32, [c_vp, c_i64, c_vp, c_vp, c_i64, c_vp]),
+    "ff_scan_noalloc_max_counts": (c_i64, []),
+    "ff_scan_counts_noalloc": (c_i32, [c_vp, c_i64, c_vp, c_vp]),
     "ff_march_emit": (c_i32, [_P(FFRender), c_vp, c_vp, c_i64, c_vp, c_vp, c_vp, c_vp]),
     "ff_composite_forward": (c_i32, [_P(FFRender), c_vp, c_vp, c_i64, c_vp, c_vp, c_vp, c_i32, c_vp, c_vp, c_vp,
                                      c_vp, c_vp]),
@@ -130,7 +132,8 @@ def stream_ptr():
 
 
 _launches = [0]
-_NON_LAUNCHING = {"ff_abi_version", "ff_last_error", "ff_device_info", "ff_struct_size", "ff_scan_workspace_bytes"}
+_NON_LAUNCHING = {"ff_abi_version", "ff_last_error", "ff_device_info", "ff_struct_size", "ff_scan_workspace_bytes",
+                  "ff_scan_noalloc_max_counts"}
 
 
 def reset_launch_count():

@@ -245,6 +245,18 @@ int ff_scan_counts(const int32_t* counts, int64_t n, int64_t* offsets, void* wor
   return cuda_status(launch_scan(counts, n, offsets, workspace, (cudaStream_t)stream), "ff_scan_counts launch");
 }
 
+int64_t ff_scan_noalloc_max_counts(void) { return scan_noalloc_max_counts(); }
+
+int ff_scan_counts_noalloc(const int32_t* counts, int64_t n, int64_t* offsets, void* stream) {
+  if (n < 0 || !offsets || (n > 0 && !counts)) return set_error(FF_ERR_ARG, "bad scan arguments");
+  if (n > scan_noalloc_max_counts())
+    return set_error(FF_ERR_SIZE, "ff_scan_counts_noalloc: " + std::to_string(n) + " counts exceed its fixed scratch (" +
+                                      std::to_string(scan_noalloc_max_counts()) +
+                                      " counts); use ff_scan_counts with a workspace");
+  if (!aligned(offsets, 8)) return set_error(FF_ERR_ALIGN, "offsets must be 8-byte aligned");
+  return cuda_status(launch_scan_noalloc(counts, n, offsets, (cudaStream_t)stream), "ff_scan_counts_noalloc");
+}
+
 int ff_march_emit(const FFRender* r, const float* rays, const float* jitter, int64_t n_rays, const int64_t* offsets,
                   float* xyz, int32_t* sample_idx, void* stream) {
   int rc = validate_render(r, rays, n_rays);

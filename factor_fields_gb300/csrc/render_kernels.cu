@@ -17,6 +17,8 @@
 // ballot + popc prefix; compositing runs a 32-wide multiplicative scan per chunk with the
 // running transmittance carried between chunks; the backward runs the forward again, then a
 // reverse affine scan for sum_{k>j} dL/dw_k * alpha_k * prod_{j<m<k} (1 - alpha_m + 1e-10).
+#include <mutex>
+
 #include "ff_common.cuh"
 #include "ff_internal.h"
 
@@ -456,6 +458,44 @@ int ray_blocks(int64_t n_rays) {
 }  // namespace
 
 int64_t scan_workspace_bytes(int64_t n) { return (ceil_div(n, kScanBlock) + 1) * (int64_t)sizeof(int64_t); }
+
+// ---- the scan without a caller workspace ------------------------------------------------
+// Some callers cannot allocate device memory at all (a render loop replayed inside a captured
+// CUDA graph, where cudaMalloc is not permitted, or a host engine that owns every device
+// buffer and hands this library only its inputs and outputs). For them the per-block partial
+// sums live in this fixed file-scope device array instead of a workspace. Every process that
+// loads the library holds these 32 KiB on each GPU it uses until it exits; all calls share
+// them, so calls that overlap on the GPU (different streams, no ordering) race on the array.
+// Nothing in it needs to start at zero: the first kernel of the scan writes every partial sum
+// it later reads.
+constexpr int64_t kNoAllocScanBlocks = 4096;
+static __device__ __align__(256) int64_t g_scan_scratch[kNoAllocScanBlocks];
+
+int64_t scan_noalloc_max_counts() { return kNoAllocScanBlocks * kScanBlock; }
+
+cudaError_t launch_scan_noalloc(const int32_t* counts, int64_t n, int64_t* offsets, cudaStream_t s) {
+  // Host code cannot use g_scan_scratch directly (its name is a host-side stand-in); the
+  // device address is looked up once per device, with that device current, on the first call.
+  static std::mutex mu;
+  static void* addr[64] = {nullptr};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  void* p = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    if (!addr[dev]) {
+      e = cudaGetSymbolAddress(&addr[dev], g_scan_scratch);
+      if (e != cudaSuccess) {
+        addr[dev] = nullptr;
+        return e;
+      }
+    }
+    p = addr[dev];
+  }
+  return launch_scan(counts, n, offsets, p, s);
+}
 
 cudaError_t launch_march_count(const FFRender& r, const float* rays, const float* jitter, int64_t n, int32_t* counts,
                                float* t_min, cudaStream_t s) {

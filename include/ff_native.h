@@ -201,6 +201,18 @@ FF_API int64_t ff_scan_workspace_bytes(int64_t n);
 FF_API int ff_scan_counts(const int32_t* counts, int64_t n, int64_t* offsets, void* workspace,
                           int64_t workspace_bytes, void* stream);
 
+/* ff_scan_counts for callers that cannot allocate device memory — e.g. a render loop replayed
+ * inside a captured CUDA graph (cudaMalloc is not permitted during capture) or a host engine
+ * that owns every device buffer and passes this library only inputs and outputs. It has no
+ * counterpart in the reference. Instead of a workspace it uses a fixed scratch array inside
+ * the library (32 KiB per GPU, held until the process exits), so it takes at most
+ * ff_scan_noalloc_max_counts() = 16,777,216 counts and returns FF_ERR_SIZE beyond that.
+ * The first call on a device looks up the array's device address; make that first call
+ * before any stream capture. All calls share the array: calls that overlap on the GPU race.
+ * It allocates nothing (no cudaMalloc / cudaFree, no allocating library routine). */
+FF_API int64_t ff_scan_noalloc_max_counts(void);
+FF_API int ff_scan_counts_noalloc(const int32_t* counts, int64_t n, int64_t* offsets, void* stream);
+
 /* Writes the live samples in ray-major order (= xyz_sampled[ray_valid] of :874): xyz [M, 3]
  * float32 and sample_idx [M] int32 (index along the ray), using the scanned offsets. */
 FF_API int ff_march_emit(const FFRender* r, const float* rays, const float* jitter, int64_t n_rays,
