@@ -252,7 +252,11 @@ __global__ void __launch_bounds__(kThreads, 3) fused_field_mlp_kernel(const Fuse
     for (int mt = 0; mt < 2; ++mt) {
       const int r0 = 16 * mt + g, r1 = r0 + 8;
       // ---------------- layer 0: H = relu(X W0^T + b0), X = hi + lo ----------------
-      uint32_t ha[4][4];  // relu(H) as BF16 A fragments over the 64 hidden units
+      uint32_t ha[4][4];  // relu(H) as BF16 A fragments over the 64 hidden units (hi part)
+      // layer 1 (O = H W1^T) accumulates per half of the hidden units, H as hi + lo
+      float oc[OUTT][4];
+#pragma unroll
+      for (int nt = 0; nt < OUTT; ++nt) oc[nt][0] = oc[nt][1] = oc[nt][2] = oc[nt][3] = 0.f;
 #pragma unroll
       for (int half = 0; half < 2; ++half) {  // hidden units [32*half, 32*half + 32)
         float hc[4][4];
@@ -281,11 +285,20 @@ __global__ void __launch_bounds__(kThreads, 3) fused_field_mlp_kernel(const Fuse
         for (int kk = 0; kk < 2; ++kk) {
           const float* c0 = hc[2 * kk];
           const float* c1 = hc[2 * kk + 1];
-          uint32_t* hk = ha[2 * half + kk];
-          hk[0] = pack_bf16(fmaxf(c0[0], 0.f), fmaxf(c0[1], 0.f));
-          hk[1] = pack_bf16(fmaxf(c0[2], 0.f), fmaxf(c0[3], 0.f));
-          hk[2] = pack_bf16(fmaxf(c1[0], 0.f), fmaxf(c1[1], 0.f));
-          hk[3] = pack_bf16(fmaxf(c1[2], 0.f), fmaxf(c1[3], 0.f));
+          const int ks = 2 * half + kk;
+          uint32_t* hk = ha[ks];
+          uint32_t hl[4];
+          split_pair(fmaxf(c0[0], 0.f), fmaxf(c0[1], 0.f), hk[0], hl[0]);
+          split_pair(fmaxf(c0[2], 0.f), fmaxf(c0[3], 0.f), hk[1], hl[1]);
+          split_pair(fmaxf(c1[0], 0.f), fmaxf(c1[1], 0.f), hk[2], hl[2]);
+          split_pair(fmaxf(c1[2], 0.f), fmaxf(c1[3], 0.f), hk[3], hl[3]);
+#pragma unroll
+          for (int nt = 0; nt < OUTT; ++nt) {
+            const __nv_bfloat16* wp = s.w1 + (nt * 8 + g) * LD_W1 + 16 * ks + 2 * t;
+            const uint32_t b0 = lds32(wp), b1 = lds32(wp + 8);
+            mma_bf16(oc[nt], hl, b0, b1);
+            mma_bf16(oc[nt], hk, b0, b1);
+          }
         }
       }
       if constexpr (MODE != kFwd && OUTT > 1) {
@@ -295,18 +308,6 @@ __global__ void __launch_bounds__(kThreads, 3) fused_field_mlp_kernel(const Fuse
           __nv_bfloat16* p0 = hw + r0 * LD_H + 16 * ks + 2 * t;
           __nv_bfloat16* p1 = hw + r1 * LD_H + 16 * ks + 2 * t;
           sts32(p0, ha[ks][0]); sts32(p1, ha[ks][1]); sts32(p0 + 8, ha[ks][2]); sts32(p1 + 8, ha[ks][3]);
-        }
-      }
-      // ---------------- layer 1: O = H W1^T ----------------
-      float oc[OUTT][4];
-#pragma unroll
-      for (int nt = 0; nt < OUTT; ++nt) oc[nt][0] = oc[nt][1] = oc[nt][2] = oc[nt][3] = 0.f;
-#pragma unroll
-      for (int ks = 0; ks < 4; ++ks) {
-#pragma unroll
-        for (int nt = 0; nt < OUTT; ++nt) {
-          const __nv_bfloat16* wp = s.w1 + (nt * 8 + g) * LD_W1 + 16 * ks + 2 * t;
-          mma_bf16(oc[nt], ha[ks], lds32(wp), lds32(wp + 8));
         }
       }
       const int64_t row0 = base + warp * 32 + r0, row1 = row0 + 8;
