@@ -270,6 +270,77 @@ class FactorFields(torch.nn.Module):
         return render_forward(self, rays_chunk, white_bg=white_bg, is_train=is_train, ndc_ray=ndc_ray,
                               N_samples=N_samples, jitter=jitter, fused=fused)
 
+    # ---- occupancy maintenance (models/FactorFields.py:710-793) ----------------------------
+    @torch.no_grad()
+    def density(self, xyz, chunk=1 << 20):
+        """basis2density(linear_mat(get_coding(xyz))[:, 0]) (:639-643, :721-723), chunked."""
+        out = torch.empty(xyz.shape[0], device=xyz.device)
+        for s in range(0, xyz.shape[0], chunk):
+            x = xyz[s:s + chunk].contiguous()
+            if self.precision == "bf16":
+                f0 = self.field_mlp(x)[:, 0]
+            else:
+                f0 = self.linear_mat(self.get_coding(x)[0])[:, 0]
+            out[s:s + chunk] = self.basis2density(f0)
+        return out
+
+    @torch.no_grad()
+    def compute_alpha(self, xyz_locs, length=1):
+        """:710-727: alpha = 1 - exp(-sigma * length), zero where the current mask is empty."""
+        sigma = torch.zeros(xyz_locs.shape[0], device=xyz_locs.device)
+        if self.alphaMask is not None:
+            keep = self.alphaMask.sample_alpha(xyz_locs) > 0
+        else:
+            keep = torch.ones_like(sigma, dtype=torch.bool)
+        if keep.any():
+            sigma[keep] = self.density(xyz_locs[keep])
+        return 1 - torch.exp(-sigma * length)
+
+    @torch.no_grad()
+    def getDenseAlpha(self, gridSize=None, times=16, seed=None):
+        """:729-755: alpha on the voxel centres of an (X, Y, Z) grid over inward_aabb, averaged
+        over `times` passes jittered by up to 0.6 voxel; returns (alpha [Z, Y, X], xyz [Z, Y, X, 3])."""
+        grid = self.gridSize.tolist() if gridSize is None else list(gridSize)
+        a0, a1 = self.inward_aabb[0], self.inward_aabb[1]
+        units = (a1 - a0) / (torch.tensor(grid, device=self.device) - 1)
+        half = 1.0 / (torch.tensor(grid, dtype=torch.float32) - 1) * 0.5
+        step = torch.mean(units)
+        axes = [torch.linspace(float(half[k]), float(1 - half[k]), grid[k]) for k in range(3)]
+        samples = torch.stack(torch.meshgrid(*axes, indexing="ij"), -1).to(self.device)
+        dense_xyz = (a0 * (1 - samples) + a1 * samples).transpose(0, 2).contiguous()
+        gen = torch.Generator(device=self.device)
+        if seed is not None:
+            gen.manual_seed(seed)
+        alpha = torch.zeros(dense_xyz.shape[:-1], device=self.device)
+        length = float(step) * float(self.cfg.renderer.distance_scale)
+        flat = dense_xyz.view(-1, 3)
+        for _ in range(times):
+            shift = 0.0
+            if times > 1:
+                shift = (torch.rand(flat.shape, device=self.device, generator=gen) * 2 - 1) * (units / 2 * 1.2)
+            alpha += self.compute_alpha(flat + shift, length).view(alpha.shape)
+        return alpha / times, dense_xyz
+
+    @torch.no_grad()
+    def updateAlphaMask(self, gridSize=(200, 200, 200), is_update_alphaMask=False, times=16, seed=None):
+        """:757-793: dense alpha -> 3x3x3 max-pool -> threshold -> AlphaGridMask (bitfield), and
+        the padded bounding box of the occupied voxels. skimage's remove_small_objects (:774) is
+        not applied (a floater filter the benchmark scenes do not need)."""
+        from .renderer import AlphaGridMask
+        alpha, dense_xyz = self.getDenseAlpha(gridSize, times=times, seed=seed)
+        alpha = alpha.clamp(0, 1)[None, None]
+        alpha = F.max_pool3d(alpha, kernel_size=3, padding=1, stride=1).view(list(gridSize)[::-1])
+        thres = float(self.cfg.renderer.alphaMask_thres) if is_update_alphaMask else 0.08
+        occ = (alpha >= thres).float()
+        if is_update_alphaMask:
+            self.alphaMask = AlphaGridMask(self.device, self.inward_aabb, occ)
+        valid = dense_xyz[occ > 0.5]
+        if valid.shape[0] == 0:
+            return self.aabb.clone()
+        lo, hi = valid.amin(0), valid.amax(0)
+        pad = (hi - lo) / 20
+        return torch.stack((lo - pad, hi + pad))
+
     # ---- checkpoints (models/FactorFields.py:669-691) --------------------------------------
     def reference_state_dict(self):
         """state_dict with the reference's keys and layouts (basises.l, coeffs.s as [1,C,...])."""

@@ -8,6 +8,53 @@ from . import _native as N
 from . import functional as FN
 
 
+class RadianceFieldTrainer:
+    """The per-scene radiance-field training loop (train_per_scene.py:147-175): render a batch of
+    rays, MSE against the targets, backward, Adam with the reference's parameter groups
+    (get_optparam_groups, lr_small / lr_large) and exponential lr decay to `decay_ratio` over
+    n_iters (train_per_scene.py:118-125, 171-172)."""
+
+    def __init__(self, model, n_samples=1024, lr_small=1e-3, lr_large=2e-2, n_iters=1000, decay_ratio=0.1,
+                 white_bg=True, sampler=None):
+        self.m, self.n_samples, self.white_bg = model, n_samples, white_bg
+        self.opt = torch.optim.Adam(model.get_optparam_groups(lr_small, lr_large), betas=(0.9, 0.99))
+        self.lr_factor = decay_ratio ** (1.0 / max(n_iters, 1))
+        self.sampler = sampler  # None: the plain uniform sampler; else a ProposalSampler
+
+    def render(self, rays, is_train):
+        if self.sampler is not None:
+            return self.sampler.render(rays, is_train=is_train, white_bg=self.white_bg)
+        rgb, depth, _ = self.m(rays, white_bg=self.white_bg, is_train=is_train, N_samples=self.n_samples)
+        return rgb, depth
+
+    def step(self, rays, rgb_gt, optimize=True):
+        rgb, _ = self.render(rays, is_train=True)
+        loss = torch.mean((rgb - rgb_gt) ** 2)
+        self.opt.zero_grad(set_to_none=False)
+        if self.sampler is not None:
+            self.sampler.zero_grad()
+        loss.backward()
+        if self.sampler is not None:
+            self.sampler.backward()
+        if optimize:
+            self.opt.step()
+            for g in self.opt.param_groups:
+                g["lr"] = g["lr"] * self.lr_factor
+            if self.sampler is not None:
+                self.sampler.step()
+        return loss.detach()
+
+    @torch.no_grad()
+    def psnr(self, rays, rgb_gt, chunk=16384):
+        """Mean-squared-error PSNR (renderer.py:60) of the rendered rays against the targets."""
+        err = 0.0
+        for s in range(0, rays.shape[0], chunk):
+            rgb, _ = self.render(rays[s:s + chunk], is_train=False)
+            err += float(((rgb - rgb_gt[s:s + chunk]) ** 2).sum())
+        mse = err / (rays.shape[0] * 3)
+        return -10.0 * torch.log10(torch.tensor(mse)).item()
+
+
 class FieldFitRunner:
     """One fwd+bwd regression step of a FactorFields model on (points, targets).
 

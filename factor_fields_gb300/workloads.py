@@ -165,5 +165,99 @@ def sdf_batch(seed, n, scene=None):
     return p, scene.sdf(p).astype(np.float32)[:, None]
 
 
+# ---------------------------------------------------------------------------------------
+# radiance-field scene (cfg2, cfg3)
+# ---------------------------------------------------------------------------------------
+
+class BlobScene:
+    """32 Gaussian density blobs in [-1.5, 1.5]^3: sigma(x) = sum_b p_b exp(-|x - c_b|^2 / (2 s_b^2))
+    with peaks p_b ~ U[5, 50], widths s_b ~ U[0.05, 0.3]; the colour at x is the density-weighted
+    mean of the blobs' RGB albedos (view independent). Ground truth is rendered by FP64
+    quadrature (render_gt) against a white background."""
+
+    def __init__(self, seed=0, n_blobs=32):
+        rng = np.random.default_rng(seed)
+        self.centers = rng.uniform(-1.0, 1.0, (n_blobs, 3))
+        self.peaks = rng.uniform(5.0, 50.0, n_blobs)
+        self.widths = rng.uniform(0.05, 0.3, n_blobs)
+        self.albedo = rng.uniform(0.05, 0.95, (n_blobs, 3))
+        self.aabb = np.array([[-1.5] * 3, [1.5] * 3])
+
+    def cameras(self, n_views=100, radius=4.0, seed=1):
+        """c2w [n, 3, 4] (OpenCV axes: x right, y down, z forward) on the upper hemisphere,
+        looking at the origin."""
+        rng = np.random.default_rng(seed)
+        th = rng.uniform(0, 2 * np.pi, n_views)
+        ph = np.arccos(rng.uniform(0.1, 0.95, n_views))
+        eye = np.stack([np.sin(ph) * np.cos(th), np.sin(ph) * np.sin(th), np.cos(ph)], 1) * radius
+        out = np.zeros((n_views, 3, 4))
+        for i, e in enumerate(eye):
+            fwd = -e / np.linalg.norm(e)
+            right = np.cross(fwd, np.array([0.0, 0.0, 1.0]))
+            right /= np.linalg.norm(right)
+            down = np.cross(fwd, right)
+            out[i, :, 0], out[i, :, 1], out[i, :, 2], out[i, :, 3] = right, down, fwd, e
+        return out
+
+    @staticmethod
+    def pixel_rays(c2w, px, py, width=400, height=400, focal=555.0):
+        """Rays through pixel centres (get_ray_directions + get_rays, dataLoader/ray_utils.py:27-90,
+        directions normalised as dataLoader/blender.py:55): [n, 6] float64."""
+        d = np.stack([(px + 0.5 - width / 2) / focal, (py + 0.5 - height / 2) / focal, np.ones_like(px, float)], -1)
+        d /= np.linalg.norm(d, axis=-1, keepdims=True)
+        rd = np.einsum("nij,nj->ni", c2w[:, :3, :3], d)
+        return np.concatenate([c2w[:, :3, 3], rd], -1)
+
+    def ray_pool(self, n, seed, views=None, n_views=100, width=400, height=400):
+        """n random camera rays (random view and pixel) from the scene's views."""
+        rng = np.random.default_rng(seed)
+        cams = self.cameras(n_views)
+        v = rng.integers(0, n_views, n) if views is None else rng.choice(views, n)
+        px, py = rng.integers(0, width, n), rng.integers(0, height, n)
+        return self.pixel_rays(cams[v], px, py, width, height)
+
+    def render_gt(self, rays, n_steps=1024, chunk=2048, device="cuda"):
+        """FP64 quadrature of the emission-absorption integral along each ray through the box,
+        white background: rgb [n, 3] float32 (midpoint rule, n_steps steps between box entry
+        and exit; alpha_i = 1 - exp(-sigma_i dt))."""
+        dev = torch.device(device)
+        c = torch.tensor(self.centers, dtype=torch.float64, device=dev)
+        p = torch.tensor(self.peaks, dtype=torch.float64, device=dev)
+        inv2s2 = torch.tensor(1.0 / (2 * self.widths ** 2), dtype=torch.float64, device=dev)
+        alb = torch.tensor(self.albedo, dtype=torch.float64, device=dev)
+        lo = torch.tensor(self.aabb[0], dtype=torch.float64, device=dev)
+        hi = torch.tensor(self.aabb[1], dtype=torch.float64, device=dev)
+        out = []
+        rays_t = torch.as_tensor(rays, dtype=torch.float64)
+        for s in range(0, rays_t.shape[0], chunk):
+            r = rays_t[s:s + chunk].to(dev)
+            o, d = r[:, :3], r[:, 3:6]
+            dd = torch.where(d == 0, torch.full_like(d, 1e-12), d)
+            ta, tb = (lo - o) / dd, (hi - o) / dd
+            t0 = torch.minimum(ta, tb).amax(-1).clamp(min=0.0)
+            t1 = torch.maximum(ta, tb).amin(-1)
+            t1 = torch.maximum(t1, t0)
+            dt = (t1 - t0) / n_steps
+            rgb = torch.zeros(r.shape[0], 3, dtype=torch.float64, device=dev)
+            trans = torch.ones(r.shape[0], dtype=torch.float64, device=dev)
+            blk = 128
+            for b0 in range(0, n_steps, blk):
+                steps = torch.arange(b0, min(b0 + blk, n_steps), dtype=torch.float64, device=dev) + 0.5
+                ts = t0[:, None] + steps[None] * dt[:, None]                       # [n, blk]
+                x = o[:, None, :] + d[:, None, :] * ts[..., None]                   # [n, blk, 3]
+                g = torch.exp(-((x[:, :, None, :] - c) ** 2).sum(-1) * inv2s2) * p  # [n, blk, blobs]
+                sig = g.sum(-1)
+                col = (g @ alb) / sig.clamp(min=1e-300)[..., None]
+                keep = torch.exp(-sig * dt[:, None])                                # 1 - alpha
+                incl = torch.cumprod(keep, dim=1)
+                excl = torch.cat([torch.ones_like(incl[:, :1]), incl[:, :-1]], 1)
+                w = trans[:, None] * excl * (1.0 - keep)
+                rgb += (w[..., None] * col).sum(1)
+                trans = trans * incl[:, -1]
+            rgb += trans[:, None]  # white background
+            out.append(rgb.float())
+        return torch.cat(out).cpu()
+
+
 def to_device(arrs, device):
     return [torch.from_numpy(np.ascontiguousarray(a)).to(device) for a in arrs]
