@@ -54,6 +54,12 @@ class FFRender(ctypes.Structure):
                 ("occ_origin", c_f32 * 3), ("occ_inv", c_f32 * 3)]
 
 
+class FFProposal(ctypes.Structure):
+    _fields_ = [("aabb_min", c_f32 * 3), ("aabb_max", c_f32 * 3), ("inv_cell", c_f32 * 3), ("reso", c_i32),
+                ("param_dtype", c_i32), ("n_bins", c_i32), ("n_fine", c_i32), ("density_shift", c_f32),
+                ("distance_scale", c_f32), ("uniform_mix", c_f32)]
+
+
 # (name, restype, argtypes) of every exported entry point.
 _P = ctypes.POINTER
 SIGNATURES = {
@@ -80,6 +86,12 @@ SIGNATURES = {
                                      c_vp, c_vp]),
     "ff_composite_backward": (c_i32, [_P(FFRender), c_vp, c_vp, c_i64, c_vp, c_vp, c_vp, c_i32, c_vp, c_vp, c_vp,
                                       c_vp]),
+    "ff_composite_forward_zd": (c_i32, [_P(FFRender), c_vp, c_i64, c_vp, c_vp, c_vp, c_i32, c_vp, c_vp, c_vp, c_vp]),
+    "ff_composite_backward_zd": (c_i32, [_P(FFRender), c_vp, c_i64, c_vp, c_vp, c_vp, c_i32, c_vp, c_vp, c_vp]),
+    "ff_proposal_encode": (c_i32, [_P(FFProposal), c_vp, c_vp, c_i64, c_vp, c_vp]),
+    "ff_proposal_resample": (c_i32, [_P(FFProposal), c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
+    "ff_proposal_loss": (c_i32, [_P(FFProposal), c_vp, c_i64, c_vp, c_vp, c_vp, c_f32, c_vp, c_vp, c_vp]),
+    "ff_proposal_scatter": (c_i32, [_P(FFProposal), c_vp, c_i64, c_vp, c_vp, c_vp]),
 }
 
 _lib = None

@@ -103,6 +103,7 @@ int64_t ff_struct_size(int32_t which) {
     case 1: return (int64_t)sizeof(FFMlp);
     case 2: return (int64_t)sizeof(FFMlpGrad);
     case 3: return (int64_t)sizeof(FFRender);
+    case 4: return (int64_t)sizeof(FFProposal);
     default: return -1;
   }
 }
@@ -274,7 +275,7 @@ int ff_composite_forward(const FFRender* r, const float* rays, const float* jitt
   if (feat_stride < 28) return set_error(FF_ERR_UNSUPPORTED, "the SH-2 colour head needs feat_stride >= 28");
   if (n_rays > 0 && (!offsets || !rgb)) return set_error(FF_ERR_ARG, "offsets/rgb are NULL");
   return cuda_status(launch_composite_forward(*r, rays, jitter, n_rays, offsets, sample_idx, feat, feat_stride,
-                                              white_bg, rgb, depth, acc, (cudaStream_t)stream),
+                                              white_bg, rgb, depth, acc, nullptr, nullptr, (cudaStream_t)stream),
                      "ff_composite_forward launch");
 }
 
@@ -286,8 +287,85 @@ int ff_composite_backward(const FFRender* r, const float* rays, const float* jit
   if (feat_stride < 28) return set_error(FF_ERR_UNSUPPORTED, "the SH-2 colour head needs feat_stride >= 28");
   if (n_rays > 0 && (!offsets || !grad_rgb || !grad_feat)) return set_error(FF_ERR_ARG, "backward buffers are NULL");
   return cuda_status(launch_composite_backward(*r, rays, jitter, n_rays, offsets, sample_idx, feat, feat_stride,
-                                               white_bg, grad_rgb, grad_feat, (cudaStream_t)stream),
+                                               white_bg, grad_rgb, grad_feat, nullptr, (cudaStream_t)stream),
                      "ff_composite_backward launch");
+}
+
+int ff_composite_forward_zd(const FFRender* r, const float* rays, int64_t n_rays, const int64_t* offsets,
+                            const float* zd, const float* feat, int32_t feat_stride, float* rgb, float* depth,
+                            float* w_out, void* stream) {
+  int rc = validate_render(r, rays, n_rays);
+  if (rc) return rc;
+  if (feat_stride < 28) return set_error(FF_ERR_UNSUPPORTED, "the SH-2 colour head needs feat_stride >= 28");
+  if (n_rays > 0 && (!offsets || !rgb || !zd)) return set_error(FF_ERR_ARG, "offsets/zd/rgb are NULL");
+  return cuda_status(launch_composite_forward(*r, rays, nullptr, n_rays, offsets, nullptr, feat, feat_stride, nullptr,
+                                              rgb, depth, nullptr, zd, w_out, (cudaStream_t)stream),
+                     "ff_composite_forward_zd launch");
+}
+
+int ff_composite_backward_zd(const FFRender* r, const float* rays, int64_t n_rays, const int64_t* offsets,
+                             const float* zd, const float* feat, int32_t feat_stride, const float* grad_rgb,
+                             float* grad_feat, void* stream) {
+  int rc = validate_render(r, rays, n_rays);
+  if (rc) return rc;
+  if (feat_stride < 28) return set_error(FF_ERR_UNSUPPORTED, "the SH-2 colour head needs feat_stride >= 28");
+  if (n_rays > 0 && (!offsets || !grad_rgb || !grad_feat || !zd)) return set_error(FF_ERR_ARG, "buffers are NULL");
+  return cuda_status(launch_composite_backward(*r, rays, nullptr, n_rays, offsets, nullptr, feat, feat_stride,
+                                               nullptr, grad_rgb, grad_feat, zd, (cudaStream_t)stream),
+                     "ff_composite_backward_zd launch");
+}
+
+static int validate_proposal(const FFProposal* p, const float* rays, int64_t n) {
+  if (!p) return set_error(FF_ERR_ARG, "proposal descriptor is NULL");
+  if (n < 0 || (n > 0 && !rays)) return set_error(FF_ERR_ARG, "bad rays pointer or count");
+  if (p->reso < 2 || (int64_t)p->reso * p->reso * p->reso > (1ll << 30)) return set_error(FF_ERR_ARG, "bad proposal reso");
+  if (p->n_bins < 32 || p->n_bins > 128 || p->n_bins % 32)
+    return set_error(FF_ERR_UNSUPPORTED, "n_bins must be 32, 64, 96 or 128");
+  if (p->n_fine < 1 || p->n_fine > 128) return set_error(FF_ERR_UNSUPPORTED, "n_fine must be 1..128");
+  if (p->param_dtype != FF_F32 && p->param_dtype != FF_BF16) return set_error(FF_ERR_ARG, "bad param_dtype");
+  return FF_OK;
+}
+
+int ff_proposal_encode(const FFProposal* p, const void* grid, const float* rays, int64_t n_rays, float* feat,
+                       void* stream) {
+  int rc = validate_proposal(p, rays, n_rays);
+  if (rc) return rc;
+  if (n_rays > 0 && (!grid || !feat)) return set_error(FF_ERR_ARG, "grid/feat are NULL");
+  if (!aligned(grid, 16) || !aligned(feat, 16)) return set_error(FF_ERR_ALIGN, "grid/feat must be 16-byte aligned");
+  return cuda_status(launch_proposal_encode(*p, grid, rays, n_rays, feat, (cudaStream_t)stream),
+                     "ff_proposal_encode launch");
+}
+
+int ff_proposal_resample(const FFProposal* p, const float* rays, int64_t n_rays, const float* o_prop,
+                         const float* jitter, const float* u, float* w_prop, float* xyz, float* zd, int32_t* bin_of,
+                         void* stream) {
+  int rc = validate_proposal(p, rays, n_rays);
+  if (rc) return rc;
+  if (n_rays > 0 && (!o_prop || !w_prop || !xyz || !zd || !bin_of)) return set_error(FF_ERR_ARG, "buffers are NULL");
+  return cuda_status(launch_proposal_resample(*p, rays, n_rays, o_prop, jitter, u, w_prop, xyz, zd, bin_of,
+                                              (cudaStream_t)stream),
+                     "ff_proposal_resample launch");
+}
+
+int ff_proposal_loss(const FFProposal* p, const float* rays, int64_t n_rays, const float* o_prop,
+                     const float* w_field, const int32_t* bin_of, float loss_scale, float* loss_sum, float* grad_o,
+                     void* stream) {
+  int rc = validate_proposal(p, rays, n_rays);
+  if (rc) return rc;
+  if (n_rays > 0 && (!o_prop || !w_field || !bin_of || !grad_o)) return set_error(FF_ERR_ARG, "buffers are NULL");
+  return cuda_status(launch_proposal_loss(*p, rays, n_rays, o_prop, w_field, bin_of, loss_scale, loss_sum, grad_o,
+                                          (cudaStream_t)stream),
+                     "ff_proposal_loss launch");
+}
+
+int ff_proposal_scatter(const FFProposal* p, const float* rays, int64_t n_rays, const float* grad_feat,
+                        float* grad_grid, void* stream) {
+  int rc = validate_proposal(p, rays, n_rays);
+  if (rc) return rc;
+  if (n_rays > 0 && (!grad_feat || !grad_grid)) return set_error(FF_ERR_ARG, "buffers are NULL");
+  if (!aligned(grad_grid, 16) || !aligned(grad_feat, 16)) return set_error(FF_ERR_ALIGN, "buffers must be 16-byte aligned");
+  return cuda_status(launch_proposal_scatter(*p, rays, n_rays, grad_feat, grad_grid, (cudaStream_t)stream),
+                     "ff_proposal_scatter launch");
 }
 
 }  // extern "C"

@@ -55,10 +55,22 @@ cudaError_t launch_march_emit(const FFRender& r, const float* rays, const float*
 cudaError_t launch_composite_forward(const FFRender& r, const float* rays, const float* jitter, int64_t n,
                                      const int64_t* offsets, const int32_t* sample_idx, const float* feat,
                                      int feat_stride, const int32_t* white_bg, float* rgb, float* depth, float* acc,
-                                     cudaStream_t s);
+                                     const float* zd, float* w_out, cudaStream_t s);
 cudaError_t launch_composite_backward(const FFRender& r, const float* rays, const float* jitter, int64_t n,
                                       const int64_t* offsets, const int32_t* sample_idx, const float* feat,
                                       int feat_stride, const int32_t* white_bg, const float* grad_rgb,
-                                      float* grad_feat, cudaStream_t s);
+                                      float* grad_feat, const float* zd, cudaStream_t s);
+
+// proposal_kernels.cu
+cudaError_t launch_proposal_encode(const FFProposal& p, const void* grid, const float* rays, int64_t n, float* feat,
+                                   cudaStream_t s);
+cudaError_t launch_proposal_scatter(const FFProposal& p, const float* rays, int64_t n, const float* grad_feat,
+                                    float* grad_grid, cudaStream_t s);
+cudaError_t launch_proposal_resample(const FFProposal& p, const float* rays, int64_t n, const float* o_prop,
+                                     const float* jitter, const float* u, float* w_prop, float* xyz, float* zd,
+                                     int32_t* bin_of, cudaStream_t s);
+cudaError_t launch_proposal_loss(const FFProposal& p, const float* rays, int64_t n, const float* o_prop,
+                                 const float* w_field, const int32_t* bin_of, float loss_scale, float* loss_sum,
+                                 float* grad_o, cudaStream_t s);
 
 }  // namespace ffgb

@@ -249,10 +249,18 @@ struct SampleVals {
   float z, delta, f0, sigma, alpha, fac;
 };
 
-__device__ __forceinline__ SampleVals sample_vals(const FFRender& r, const RayGeo& g, int i, const float* feat_row) {
+// zd (optional): explicit (z, dist) of the sample, for samplers other than the uniform one.
+__device__ __forceinline__ SampleVals sample_vals(const FFRender& r, const RayGeo& g, int i, const float* feat_row,
+                                                  const float* zd = nullptr) {
   SampleVals s;
-  s.z = sample_z(r, g, i);
-  const float dist = (i + 1 < r.n_samples) ? __fsub_rn(sample_z(r, g, i + 1), s.z) : 0.f;  // :861
+  float dist;
+  if (zd) {
+    s.z = zd[0];
+    dist = zd[1];
+  } else {
+    s.z = sample_z(r, g, i);
+    dist = (i + 1 < r.n_samples) ? __fsub_rn(sample_z(r, g, i + 1), s.z) : 0.f;  // :861
+  }
   s.delta = __fmul_rn(dist, r.distance_scale);
   s.f0 = feat_row[0];
   const float x = s.f0 + r.density_shift;
@@ -303,7 +311,7 @@ __global__ void __launch_bounds__(kRayWarps * 32) composite_forward_kernel(
     const FFRender r, const float* __restrict__ rays, const float* __restrict__ jitter, int64_t n_rays,
     const int64_t* __restrict__ offsets, const int32_t* __restrict__ sample_idx, const float* __restrict__ feat,
     int feat_stride, const int32_t* __restrict__ white_bg, float* __restrict__ rgb_out, float* __restrict__ depth_out,
-    float* __restrict__ acc_out) {
+    float* __restrict__ acc_out, const float* __restrict__ zd, float* __restrict__ w_out) {
   const int lane = threadIdx.x & 31;
   for (int64_t ray = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; ray < n_rays;
        ray += ((int64_t)gridDim.x * blockDim.x) >> 5) {
@@ -317,10 +325,11 @@ __global__ void __launch_bounds__(kRayWarps * 32) composite_forward_kernel(
       const bool active = j < end;
       SampleVals s = {0.f, 0.f, 0.f, 0.f, 0.f, 1.f};
       const float* row = feat + (active ? j : beg) * feat_stride;
-      if (active) s = sample_vals(r, g, sample_idx[j], row);
+      if (active) s = sample_vals(r, g, zd ? 0 : sample_idx[j], row, zd ? zd + 2 * j : nullptr);
       float excl;
       const float prod = excl_trans(s.fac, lane, excl);
       const float w = active ? s.alpha * (T * excl) : 0.f;
+      if (active && w_out) w_out[j] = w;
       acc += w;
       depth += w * s.z;
       if (active && w > r.weight_thres) {
@@ -351,7 +360,7 @@ __global__ void __launch_bounds__(kRayWarps * 32) composite_backward_kernel(
     const FFRender r, const float* __restrict__ rays, const float* __restrict__ jitter, int64_t n_rays,
     const int64_t* __restrict__ offsets, const int32_t* __restrict__ sample_idx, const float* __restrict__ feat,
     int feat_stride, const int32_t* __restrict__ white_bg, const float* __restrict__ grad_rgb,
-    float* __restrict__ grad_feat) {
+    float* __restrict__ grad_feat, const float* __restrict__ zd) {
   const int lane = threadIdx.x & 31;
   for (int64_t ray = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; ray < n_rays;
        ray += ((int64_t)gridDim.x * blockDim.x) >> 5) {
@@ -368,7 +377,7 @@ __global__ void __launch_bounds__(kRayWarps * 32) composite_backward_kernel(
       const bool active = j < end;
       SampleVals s = {0.f, 0.f, 0.f, 0.f, 0.f, 1.f};
       const float* row = feat + (active ? j : beg) * feat_stride;
-      if (active) s = sample_vals(r, g, sample_idx[j], row);
+      if (active) s = sample_vals(r, g, zd ? 0 : sample_idx[j], row, zd ? zd + 2 * j : nullptr);
       float excl;
       const float prod = excl_trans(s.fac, lane, excl);
       const float Tj = T * excl;
@@ -404,7 +413,7 @@ __global__ void __launch_bounds__(kRayWarps * 32) composite_backward_kernel(
       bool app = false;
       float w = 0.f, gw = 0.f;
       if (active) {
-        s = sample_vals(r, g, sample_idx[j], row);
+        s = sample_vals(r, g, zd ? 0 : sample_idx[j], row, zd ? zd + 2 * j : nullptr);
         Tj = grad_feat[j * feat_stride];
         w = s.alpha * Tj;
         app = w > r.weight_thres;
@@ -524,20 +533,20 @@ cudaError_t launch_march_emit(const FFRender& r, const float* rays, const float*
 cudaError_t launch_composite_forward(const FFRender& r, const float* rays, const float* jitter, int64_t n,
                                      const int64_t* offsets, const int32_t* sample_idx, const float* feat,
                                      int feat_stride, const int32_t* white_bg, float* rgb, float* depth, float* acc,
-                                     cudaStream_t s) {
+                                     const float* zd, float* w_out, cudaStream_t s) {
   if (n == 0) return cudaSuccess;
   composite_forward_kernel<<<ray_blocks(n), kRayWarps * 32, 0, s>>>(r, rays, jitter, n, offsets, sample_idx, feat,
-                                                                     feat_stride, white_bg, rgb, depth, acc);
+                                                                     feat_stride, white_bg, rgb, depth, acc, zd, w_out);
   return cudaGetLastError();
 }
 
 cudaError_t launch_composite_backward(const FFRender& r, const float* rays, const float* jitter, int64_t n,
                                       const int64_t* offsets, const int32_t* sample_idx, const float* feat,
                                       int feat_stride, const int32_t* white_bg, const float* grad_rgb,
-                                      float* grad_feat, cudaStream_t s) {
+                                      float* grad_feat, const float* zd, cudaStream_t s) {
   if (n == 0) return cudaSuccess;
   composite_backward_kernel<<<ray_blocks(n), kRayWarps * 32, 0, s>>>(r, rays, jitter, n, offsets, sample_idx, feat,
-                                                                      feat_stride, white_bg, grad_rgb, grad_feat);
+                                                                      feat_stride, white_bg, grad_rgb, grad_feat, zd);
   return cudaGetLastError();
 }
 

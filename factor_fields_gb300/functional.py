@@ -99,7 +99,8 @@ class MLPFunction(torch.autograd.Function):
             g.weight[i] = gw[i].data_ptr() if gw[i] is not None else None
             g.bias[i] = gbias[i].data_ptr() if gbias[i] is not None else None
         gx = torch.empty_like(x) if ctx.needs_input_grad[0] else None
-        N.call("ff_mlp_backward", ctypes.byref(m), N.ptr(x), x.shape[0], N.ptr(g_out.contiguous()), N.ptr(gx),
+        g_out = g_out.contiguous()  # a named tensor stays alive until the launch is enqueued
+        N.call("ff_mlp_backward", ctypes.byref(m), N.ptr(x), x.shape[0], N.ptr(g_out), N.ptr(gx),
                ctypes.byref(g), N.stream_ptr())
         return (gx, None, None, *gw, *gbias)
 
@@ -131,8 +132,9 @@ class FusedFieldMLP(torch.autograd.Function):
         gw0, gb0, gw1 = torch.zeros_like(w0), torch.zeros_like(b0), torch.zeros_like(w1)
         g = N.FFMlpGrad()
         g.weight[0], g.bias[0], g.weight[1] = gw0.data_ptr(), gb0.data_ptr(), gw1.data_ptr()
+        g_out = g_out.contiguous()
         N.call("ff_field_mlp_backward", ctypes.byref(ctx.desc), N.ptr(basis_read), N.ptr(coeff_read),
-               ctypes.byref(m), N.ptr(x), x.shape[0], N.ptr(g_out.contiguous()), N.ptr(gb), N.ptr(gc),
+               ctypes.byref(m), N.ptr(x), x.shape[0], N.ptr(g_out), N.ptr(gb), N.ptr(gc),
                ctypes.byref(g), N.stream_ptr())
         return None, gb, gc, gw0, gb0, gw1, None, None, None, None
 

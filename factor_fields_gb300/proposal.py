@@ -1,0 +1,176 @@
+"""The learned proposal sampler (benchmark configuration 3).
+
+A coarse 64^3 x 8 grid (trilinear, BF16 storage) and an 8 -> 64 -> 1 MLP predict a density
+along each ray at 64 coarse bin centres; their compositing weights form a per-ray histogram
+from which n_fine (48) samples are drawn by inverse CDF (the reference's sample_pdf semantics,
+dataLoader/ray_utils.py:132-174). The field is evaluated only at those samples and composited
+with the sample spacing. The proposal is trained online, by its own optimizer, with a loss that
+makes its weight on each coarse bin upper-bound the field's weight mass in that bin.
+
+`learned=False` keeps everything but replaces the network by a flat histogram: n_fine
+stratified uniform samples over the ray's segment in the box — the same sample budget without
+the proposal, used to show what the network gains.
+
+Kernels: ff_proposal_encode / _resample / _loss / _scatter (csrc/proposal_kernels.cu), the
+float32 MLP kernels for the proposal head, the field kernels, ff_composite_*_zd.
+"""
+import ctypes
+
+import torch
+
+from . import _native as N
+from . import functional as FN
+from .field import MLPMixer
+from .renderer import field_eval, field_grad, render_desc
+
+
+class ProposalRenderFunction(torch.autograd.Function):
+    """rgb, depth of the resampled rays, differentiable in the field's parameters."""
+
+    @staticmethod
+    def forward(ctx, rays, basis_param, coeff_param, w0, b0, w1, job):
+        sam, m = job["sampler"], job["model"]
+        n = rays.shape[0]
+        nb, nf = sam.n_bins, sam.n_fine
+        dev = rays.device
+        st = N.stream_ptr()
+        feat_p = torch.empty(n * nb, 8, device=dev)
+        if sam.learned:
+            N.call("ff_proposal_encode", ctypes.byref(sam.desc), N.ptr(sam.grid_read()), N.ptr(rays), n,
+                   N.ptr(feat_p), st)
+            o_p = torch.empty(n * nb, 1, device=dev)
+            N.call("ff_mlp_forward", ctypes.byref(sam.mlp_struct()), N.ptr(feat_p), n * nb, N.ptr(o_p), st)
+        else:
+            o_p = torch.full((n * nb, 1), -60.0, device=dev)  # zero density: a flat histogram
+        w_p = torch.empty(n * nb, device=dev)
+        xyz = torch.empty(n * nf, 3, device=dev)
+        zd = torch.empty(n * nf, 2, device=dev)
+        bin_of = torch.empty(n * nf, dtype=torch.int32, device=dev)
+        N.call("ff_proposal_resample", ctypes.byref(sam.desc), N.ptr(rays), n, N.ptr(o_p), N.ptr(job["jitter"]),
+               None, N.ptr(w_p), N.ptr(xyz), N.ptr(zd), N.ptr(bin_of), st)
+        feat = field_eval(m, job, xyz)
+        offsets = torch.arange(n + 1, device=dev, dtype=torch.int64) * nf
+        rgb = torch.empty(n, 3, device=dev)
+        depth = torch.empty(n, device=dev)
+        w_f = torch.empty(n * nf, device=dev)
+        N.call("ff_composite_forward_zd", ctypes.byref(job["rdesc"]), N.ptr(rays), n, N.ptr(offsets), N.ptr(zd),
+               N.ptr(feat), feat.shape[1], N.ptr(rgb), N.ptr(depth), N.ptr(w_f), st)
+        ctx.save_for_backward(rays, offsets, xyz, zd, feat)
+        ctx.job = job
+        ctx.mark_non_differentiable(depth)
+        job.update(feat_p=feat_p, o_p=o_p, w_p=w_p, w_f=w_f, bin_of=bin_of, rays=rays)
+        return rgb, depth
+
+    @staticmethod
+    def backward(ctx, g_rgb, g_depth):
+        rays, offsets, xyz, zd, feat = ctx.saved_tensors
+        job = ctx.job
+        g_feat = torch.empty_like(feat)
+        g_rgb = g_rgb.contiguous()
+        N.call("ff_composite_backward_zd", ctypes.byref(job["rdesc"]), N.ptr(rays), rays.shape[0], N.ptr(offsets),
+               N.ptr(zd), N.ptr(feat), feat.shape[1], N.ptr(g_rgb), N.ptr(g_feat), N.stream_ptr())
+        grads = field_grad(job["model"], job, xyz, g_feat)
+        return (None,) + grads + (None,)
+
+
+class ProposalSampler:
+    def __init__(self, model, reso=64, n_bins=64, n_fine=48, hidden=64, lr_grid=2e-2, lr_mlp=1e-3,
+                 density_shift=-4.0, precision="bf16", learned=True, seed=0, uniform_mix=0.0):
+        self.m, self.learned = model, learned
+        self.reso, self.n_bins, self.n_fine, self.precision = reso, n_bins, n_fine, precision
+        dev = model.device
+        gen = torch.Generator().manual_seed(seed)
+        self.grid = torch.nn.Parameter(((torch.rand(reso ** 3 * 8, generator=gen) * 2 - 1) * 0.05).to(dev))
+        self.mlp = MLPMixer(8, 1, num_layers=2, hidden_dim=hidden).to(dev)
+        with torch.no_grad():
+            for lin in self.mlp.backbone:
+                bound = 1.0 / lin.in_features ** 0.5
+                lin.weight.copy_(((torch.rand(lin.weight.shape, generator=gen) * 2 - 1) * bound).to(dev))
+                if lin.bias is not None:
+                    lin.bias.zero_()
+        self.params = [self.grid] + list(self.mlp.parameters())
+        for p in self.params:
+            p.grad = torch.zeros_like(p)
+        self.opt = torch.optim.Adam([{"params": [self.grid], "lr": lr_grid},
+                                     {"params": list(self.mlp.parameters()), "lr": lr_mlp}], betas=(0.9, 0.99))
+        d = N.FFProposal()
+        aabb = model.aabb.detach().cpu()
+        for k in range(3):
+            d.aabb_min[k] = float(aabb[0, k])
+            d.aabb_max[k] = float(aabb[1, k])
+            d.inv_cell[k] = float((reso - 1) / (aabb[1, k] - aabb[0, k]))
+        d.reso, d.n_bins, d.n_fine = reso, n_bins, n_fine
+        d.param_dtype = N.FF_BF16 if precision == "bf16" else N.FF_F32
+        d.density_shift = density_shift
+        d.distance_scale = float(model.cfg.renderer.distance_scale)
+        d.uniform_mix = float(uniform_mix)
+        self.desc = d
+        self.loss_buf = torch.zeros(1, device=dev)
+        self._bf16 = None
+        self._job = None
+
+    def grid_read(self):
+        if self.precision != "bf16":
+            return self.grid
+        ver = (self.grid._version, self.grid.data_ptr())
+        if self._bf16 is None:
+            self._bf16 = [None, torch.empty_like(self.grid, dtype=torch.bfloat16)]
+        if self._bf16[0] != ver:
+            with torch.no_grad():
+                self._bf16[1].copy_(self.grid.detach())
+            self._bf16[0] = ver
+        return self._bf16[1]
+
+    def mlp_struct(self):
+        ws, bs = self.mlp.weights()
+        return FN.mlp_struct(ws, bs, 8, self.mlp.hidden_dim, 1)
+
+    def render(self, rays, is_train=False, white_bg=True, fused=None, jitter=None):
+        """(rgb [R, 3], depth [R]) of rays rendered with n_fine resampled samples each."""
+        m = self.m
+        rays = rays.to(m.device, torch.float32).contiguous()
+        if jitter is None and is_train:
+            jitter = torch.rand(rays.shape[0], device=rays.device)
+        if fused is None:
+            fused = m.precision == "bf16"
+        basis_r, coeff_r, dt = m._read_buffers()
+        job = {"model": m, "sampler": self, "rdesc": render_desc(m, self.n_fine, white_bg),
+               "fdesc": m.descriptor(dt), "basis_r": basis_r, "coeff_r": coeff_r, "coeff_param": m.coeff_flat,
+               "fused": fused, "jitter": jitter}
+        l0, l1 = m.linear_mat.backbone
+        rgb, depth = ProposalRenderFunction.apply(rays, m.basis_flat, m.coeff_flat, l0.weight, l0.bias, l1.weight, job)
+        self._job = job
+        return rgb, depth
+
+    def zero_grad(self):
+        for p in self.params:
+            p.grad.zero_()
+
+    def backward(self):
+        """Proposal loss of the last render against the field's weights; gradients into the
+        proposal grid and MLP. Returns the loss (0-d device tensor)."""
+        job = self._job
+        if job is None or not self.learned:
+            return self.loss_buf[0]
+        rays = job["rays"]
+        n, nb = rays.shape[0], self.n_bins
+        st = N.stream_ptr()
+        g_o = torch.empty(n * nb, 1, device=rays.device)
+        self.loss_buf.zero_()
+        N.call("ff_proposal_loss", ctypes.byref(self.desc), N.ptr(rays), n, N.ptr(job["o_p"]), N.ptr(job["w_f"]),
+               N.ptr(job["bin_of"]), 1.0 / max(n, 1), N.ptr(self.loss_buf), N.ptr(g_o), st)
+        g = N.FFMlpGrad()
+        ws, bs = self.mlp.weights()
+        for i, (w, b) in enumerate(zip(ws, bs)):
+            g.weight[i] = w.grad.data_ptr()
+            g.bias[i] = b.grad.data_ptr() if b is not None else None
+        g_feat = torch.empty_like(job["feat_p"])
+        N.call("ff_mlp_backward", ctypes.byref(self.mlp_struct()), N.ptr(job["feat_p"]), n * nb, N.ptr(g_o),
+               N.ptr(g_feat), ctypes.byref(g), st)
+        N.call("ff_proposal_scatter", ctypes.byref(self.desc), N.ptr(rays), n, N.ptr(g_feat), N.ptr(self.grid.grad),
+               st)
+        return self.loss_buf[0]
+
+    def step(self):
+        if self.learned:
+            self.opt.step()

@@ -145,8 +145,9 @@ class RenderFunction(torch.autograd.Function):
         m, rdesc = job["model"], job["rdesc"]
         n = rays.shape[0]
         g_feat = torch.empty_like(feat)
+        g_rgb = g_rgb.contiguous()
         N.call("ff_composite_backward", ctypes.byref(rdesc), N.ptr(rays), N.ptr(ctx.jitter), n, N.ptr(offsets),
-               N.ptr(sidx), N.ptr(feat), feat.shape[1], None, N.ptr(g_rgb.contiguous()), N.ptr(g_feat),
+               N.ptr(sidx), N.ptr(feat), feat.shape[1], None, N.ptr(g_rgb), N.ptr(g_feat),
                N.stream_ptr())
         grads = field_grad(m, job, xyz, g_feat)
         return (None, None) + grads + (None,)

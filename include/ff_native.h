@@ -109,7 +109,8 @@ typedef struct FFMlpGrad {
 /* ---- library ------------------------------------------------------------------------- */
 FF_API int ff_abi_version(void);
 FF_API const char* ff_last_error(void);
-/* sizeof of the ABI structs, for binding checks: 0 FFField, 1 FFMlp, 2 FFMlpGrad, 3 FFRender. */
+/* sizeof of the ABI structs, for binding checks: 0 FFField, 1 FFMlp, 2 FFMlpGrad, 3 FFRender,
+ * 4 FFProposal. */
 FF_API int64_t ff_struct_size(int32_t which);
 /* Number of SMs of the current device and the compute capability (major*10+minor). */
 FF_API int ff_device_info(int32_t* sm_count, int32_t* cc);
@@ -233,6 +234,53 @@ FF_API int ff_composite_backward(const FFRender* r, const float* rays, const flo
                                  const int64_t* offsets, const int32_t* sample_idx, const float* feat,
                                  int32_t feat_stride, const int32_t* white_bg, const float* grad_rgb,
                                  float* grad_feat, void* stream);
+
+/* Compositing with explicit per-sample (z, dist) pairs zd [M, 2] instead of the uniform
+ * sampler's positions (for resampled rays; dist already excludes distance_scale). w_out
+ * (optional) receives each sample's compositing weight. Otherwise as ff_composite_*. */
+FF_API int ff_composite_forward_zd(const FFRender* r, const float* rays, int64_t n_rays, const int64_t* offsets,
+                                   const float* zd, const float* feat, int32_t feat_stride, float* rgb,
+                                   float* depth, float* w_out, void* stream);
+FF_API int ff_composite_backward_zd(const FFRender* r, const float* rays, int64_t n_rays, const int64_t* offsets,
+                                    const float* zd, const float* feat, int32_t feat_stride,
+                                    const float* grad_rgb, float* grad_feat, void* stream);
+
+/* ---- learned proposal sampler (no counterpart in the reference; resampling follows
+ * sample_pdf, dataLoader/ray_utils.py:132-174) ------------------------------------------- */
+
+typedef struct FFProposal {
+  float aabb_min[3];
+  float aabb_max[3];
+  float inv_cell[3];      /* (reso - 1) / (aabb_max - aabb_min): align-corners grid mapping */
+  int32_t reso;           /* grid cells per axis; the grid is [reso^3][8] channels-last */
+  int32_t param_dtype;    /* FF_F32 or FF_BF16 storage of the grid */
+  int32_t n_bins;         /* coarse bins per ray: 32, 64, 96 or 128 */
+  int32_t n_fine;         /* resampled samples per ray: 1..128 */
+  float density_shift;    /* proposal density = softplus(o + density_shift) */
+  float distance_scale;   /* alpha = 1 - exp(-density * bin_len * distance_scale) */
+  float uniform_mix;      /* resampling pdf = (1 - mix) * sample_pdf's pdf + mix / n_bins (0 = exact) */
+} FFProposal;
+
+/* Grid features at the coarse bin centres: feat [n_rays * n_bins, 8] float32. */
+FF_API int ff_proposal_encode(const FFProposal* p, const void* grid, const float* rays, int64_t n_rays,
+                              float* feat, void* stream);
+/* From the proposal MLP's outputs o_prop [n_rays * n_bins]: proposal weights w_prop
+ * [n_rays * n_bins], and n_fine samples per ray by inverse CDF: xyz [n_rays * n_fine, 3],
+ * zd [n_rays * n_fine, 2] (z, dist to the next sample / the segment end), bin_of [.] int32.
+ * u: optional [n_rays * n_fine] uniforms; else u_i = (i + jitter[ray]) / n_fine (jitter
+ * optional, 0.5 when NULL). */
+FF_API int ff_proposal_resample(const FFProposal* p, const float* rays, int64_t n_rays, const float* o_prop,
+                                const float* jitter, const float* u, float* w_prop, float* xyz, float* zd,
+                                int32_t* bin_of, void* stream);
+/* Proposal loss sum_k max(0, m_k - w_k)^2 / (w_k + 1e-5) per ray, m_k = field weight mass in
+ * bin k (w_field [n_rays * n_fine], bin_of from resample), scaled by loss_scale; loss_sum
+ * (optional) accumulates the loss, grad_o [n_rays * n_bins] receives dL/do_prop. */
+FF_API int ff_proposal_loss(const FFProposal* p, const float* rays, int64_t n_rays, const float* o_prop,
+                            const float* w_field, const int32_t* bin_of, float loss_scale, float* loss_sum,
+                            float* grad_o, void* stream);
+/* Scatter dL/dfeat [n_rays * n_bins, 8] into the float32 grid gradient [reso^3][8] (+=). */
+FF_API int ff_proposal_scatter(const FFProposal* p, const float* rays, int64_t n_rays, const float* grad_feat,
+                               float* grad_grid, void* stream);
 
 #ifdef __cplusplus
 }

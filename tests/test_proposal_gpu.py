@@ -1,0 +1,163 @@
+"""GPU parity of the proposal-sampler kernels against the oracle.
+
+The proposal network has no reference implementation (parity unpinned for the network); the
+pieces with reference semantics are pinned: resampling = sample_pdf (dataLoader/ray_utils.py:
+132-174, itself pinned to golden vectors), compositing weights = raw2alpha (:82-88), the grid
+lookup = trilinear grid_sample. The loss gradient is checked against FP64 central differences."""
+import ctypes
+
+import numpy as np
+import pytest
+import torch
+
+from gpu_util import need_gpu, rel_err
+from oracle import ff_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(autouse=True)
+def _gpu():
+    need_gpu()
+
+
+def make_sampler(reso=12, n_bins=64, n_fine=48, precision="fp32", learned=True):
+    from factor_fields_gb300 import FactorFields
+    from factor_fields_gb300 import workloads as W
+    from factor_fields_gb300.proposal import ProposalSampler
+    torch.manual_seed(0)
+    m = FactorFields(W.field_cfg("cfg2"), device="cuda", precision="bf16")
+    return m, ProposalSampler(m, reso=reso, n_bins=n_bins, n_fine=n_fine, precision=precision, learned=learned)
+
+
+def rays_np(n, seed=0):
+    from factor_fields_gb300 import workloads as W
+    return W.BlobScene(0).ray_pool(n, seed).astype(np.float32)
+
+
+def test_encode_and_scatter_match_trilinear_grid_sample():
+    from factor_fields_gb300 import _native as N
+    m, s = make_sampler(reso=12)
+    with torch.no_grad():
+        s.grid.copy_(torch.randn(s.grid.shape, generator=torch.Generator().manual_seed(1)).cuda())
+    rays = rays_np(64)
+    rt = torch.from_numpy(rays).cuda()
+    n, nb = rays.shape[0], s.n_bins
+    feat = torch.empty(n * nb, 8, device="cuda")
+    N.call("ff_proposal_encode", ctypes.byref(s.desc), N.ptr(s.grid), N.ptr(rt), n, N.ptr(feat), N.stream_ptr())
+    # positions of the bin centres and the reference trilinear lookup (align_corners over the aabb)
+    aabb = np.array([[-1.5] * 3, [1.5] * 3])
+    t_in, t_out = O.proposal_segments(rays, aabb)
+    seg = (t_out - t_in) / nb
+    t = t_in[:, None] + (np.arange(nb)[None] + 0.5) * seg[:, None]
+    x = rays[:, None, :3].astype(np.float64) + rays[:, None, 3:6] * t[..., None]
+    coords = ((x - aabb[0]) / (aabb[1] - aabb[0]) * 2 - 1).reshape(-1, 3).astype(np.float32)
+    grid = s.grid.detach().cpu().numpy().reshape(12, 12, 12, 8).transpose(3, 0, 1, 2)  # [C, D, H, W]
+    ref = O.grid_sample_fwd(grid, coords, True, "zeros", "bilinear")
+    assert rel_err(feat, ref) < 1e-4
+    gfeat = torch.randn(n * nb, 8, generator=torch.Generator().manual_seed(2)).cuda()
+    ggrid = torch.zeros_like(s.grid)
+    N.call("ff_proposal_scatter", ctypes.byref(s.desc), N.ptr(rt), n, N.ptr(gfeat), N.ptr(ggrid), N.stream_ptr())
+    refg = O.grid_sample_bwd(grid.shape, coords, gfeat.cpu().numpy(), True, "zeros", "bilinear")
+    assert rel_err(ggrid.view(12, 12, 12, 8).permute(3, 0, 1, 2), refg) < 1e-4
+
+
+def test_resample_is_sample_pdf():
+    from factor_fields_gb300 import _native as N
+    m, s = make_sampler()
+    rays = rays_np(256, 3)
+    rt = torch.from_numpy(rays).cuda()
+    n, nb, nf = rays.shape[0], s.n_bins, s.n_fine
+    rng = np.random.default_rng(4)
+    o_p = (rng.standard_normal((n, nb)) * 3).astype(np.float32)
+    o_p[:8] = -60  # flat histograms
+    u = np.sort(rng.uniform(0, 1, (n, nf)).astype(np.float32), axis=1)
+    w_p = torch.empty(n * nb, device="cuda")
+    xyz = torch.empty(n * nf, 3, device="cuda")
+    zd = torch.empty(n * nf, 2, device="cuda")
+    bin_of = torch.empty(n * nf, dtype=torch.int32, device="cuda")
+    o_t, u_t = torch.from_numpy(o_p).cuda(), torch.from_numpy(u).cuda()  # keep alive across the call
+    N.call("ff_proposal_resample", ctypes.byref(s.desc), N.ptr(rt), n, N.ptr(o_t), None, N.ptr(u_t), N.ptr(w_p),
+           N.ptr(xyz), N.ptr(zd), N.ptr(bin_of), N.stream_ptr())
+    aabb = np.array([[-1.5] * 3, [1.5] * 3])
+    t_in, t_out = O.proposal_segments(rays, aabb)
+    seg = (t_out - t_in) / nb
+    w_ref = O.proposal_weights(o_p, seg, s.desc.density_shift, s.desc.distance_scale)
+    assert rel_err(w_p.view(n, nb), w_ref) < 1e-4
+    edges = (t_in[:, None] + np.arange(nb + 1)[None] * seg[:, None]).astype(np.float32)
+    ref_t = O.sample_pdf(edges, w_p.view(n, nb).cpu().numpy(), u)
+    got_t = zd.view(n, nf, 2)[..., 0].cpu().numpy()
+    # exclude samples whose u sits within rounding distance of a cdf knot (bin choice ambiguous)
+    w64 = w_p.view(n, nb).cpu().numpy().astype(np.float64) + 1e-5
+    cdf = np.concatenate([np.zeros((n, 1)), np.cumsum(w64 / w64.sum(1, keepdims=True), 1)], 1)
+    ok = np.min(np.abs(u[:, :, None] - cdf[:, None, :]), -1) > 1e-5
+    assert ok.mean() > 0.95
+    assert np.max(np.abs(got_t - ref_t)[ok]) <= 1e-4 * np.max(np.abs(ref_t))
+    # samples are sorted, inside their segment, dists consistent, positions on the ray
+    assert np.all(np.diff(got_t, axis=1) >= -1e-6)
+    dist = zd.view(n, nf, 2)[..., 1].cpu().numpy()
+    assert np.allclose(dist[:, :-1], np.diff(got_t, axis=1), atol=1e-5)
+    p = xyz.view(n, nf, 3).cpu().numpy()
+    assert np.allclose(p, rays[:, None, :3] + rays[:, None, 3:6] * got_t[..., None], atol=1e-4)
+    b = bin_of.view(n, nf).cpu().numpy()
+    assert np.all((b >= 0) & (b < nb))
+
+
+def test_proposal_loss_gradient_matches_finite_differences():
+    from factor_fields_gb300 import _native as N
+    m, s = make_sampler()
+    rays = rays_np(32, 5)
+    rt = torch.from_numpy(rays).cuda()
+    n, nb, nf = rays.shape[0], s.n_bins, s.n_fine
+    rng = np.random.default_rng(6)
+    o_p = (rng.standard_normal((n, nb)) * 2 - 1).astype(np.float32)
+    w_f = rng.uniform(0, 0.08, (n, nf)).astype(np.float32)
+    bin_of = rng.integers(0, nb, (n, nf)).astype(np.int32)
+    g_o = torch.empty(n * nb, device="cuda")
+    loss = torch.zeros(1, device="cuda")
+    o_t, wf_t, b_t = (torch.from_numpy(a).cuda() for a in (o_p, w_f, bin_of))  # alive across the call
+    N.call("ff_proposal_loss", ctypes.byref(s.desc), N.ptr(rt), n, N.ptr(o_t), N.ptr(wf_t), N.ptr(b_t), 1.0 / n,
+           N.ptr(loss), N.ptr(g_o), N.stream_ptr())
+    t_in, t_out = O.proposal_segments(rays, np.array([[-1.5] * 3, [1.5] * 3]))
+    ref_loss, ref_g = O.proposal_loss(o_p, (t_out - t_in) / nb, s.desc.density_shift, s.desc.distance_scale, w_f,
+                                      bin_of, 1.0 / n)
+    assert abs(float(loss) - ref_loss) <= 1e-4 * abs(ref_loss)
+    assert rel_err(g_o.view(n, nb), ref_g) < 1e-3
+
+
+def test_proposal_matches_plain_sampler_with_far_fewer_samples():
+    """What the trained proposal network gains over the method without it (the reference's
+    plain uniform sampler, up to 1024 samples per ray with occupancy pruning): after the same
+    training, rendering with 48 proposal samples per ray is at least as accurate (PSNR within
+    0.1 dB, against the FP64 ground truth) while the field is evaluated at several times
+    fewer samples per ray."""
+    from factor_fields_gb300 import FactorFields
+    from factor_fields_gb300 import workloads as W
+    from factor_fields_gb300.proposal import ProposalSampler
+    from factor_fields_gb300.renderer import march, render_desc
+    from factor_fields_gb300.train import RadianceFieldTrainer
+    scene = W.BlobScene(0)
+    pool = torch.from_numpy(scene.ray_pool(1 << 16, 5)).float()
+    gt = scene.render_gt(pool.double().numpy(), n_steps=512).cuda()
+    test = torch.from_numpy(scene.ray_pool(1 << 12, 6, views=[0, 1])).float()
+    gtt = scene.render_gt(test.double().numpy(), n_steps=512).cuda()
+    pool, test = pool.cuda(), test.cuda()
+    iters = 600
+    res = {}
+    for kind in ("plain", "proposal"):
+        torch.manual_seed(0)
+        m = FactorFields(W.field_cfg("cfg2"), device="cuda", precision="bf16")
+        sampler = ProposalSampler(m) if kind == "proposal" else None
+        tr = RadianceFieldTrainer(m, n_samples=1024, n_iters=iters, sampler=sampler)
+        g = torch.Generator(device="cuda").manual_seed(0)
+        for it in range(iters):
+            idx = torch.randint(0, pool.shape[0], (4096,), device="cuda", generator=g)
+            tr.step(pool[idx], gt[idx])
+            if kind == "plain" and it == 300:
+                m.updateAlphaMask((128, 128, 128), is_update_alphaMask=True, times=1)
+        res[kind] = tr.psnr(test, gtt)
+        if kind == "plain":
+            offsets, _, _ = march(m, test, None, render_desc(m, 1024, True))
+            res["plain_samples"] = float(offsets[-1]) / test.shape[0]
+    assert res["proposal"] >= res["plain"] - 0.1, res
+    assert res["plain_samples"] >= 3 * 48, res
