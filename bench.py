@@ -229,6 +229,72 @@ def run_native(args, ws, rank, local):
     return res
 
 
+def run_radiance(args, dev):
+    """Configurations 2 and 3 on the synthetic blob scene: rays/s of one fwd+bwd training step
+    (plain sampler: 4,096 rays x up to 1,024 samples with 128^3 occupancy-bitfield pruning;
+    proposal sampler: 8,192 rays x 48 resampled samples), and PSNR / depth error against the
+    FP64 quadrature ground truth after equal training (iters x 4,096 rays, Adam)."""
+    from factor_fields_gb300 import FactorFields
+    from factor_fields_gb300 import workloads as W
+    from factor_fields_gb300.proposal import ProposalSampler
+    from factor_fields_gb300.renderer import march, render_desc
+    from factor_fields_gb300.train import RadianceFieldTrainer
+    scene = W.BlobScene(0)
+    pool = torch.from_numpy(scene.ray_pool(1 << 18, 5)).float()
+    gt = scene.render_gt(pool.double().numpy(), n_steps=512).to(dev)
+    test = torch.from_numpy(scene.ray_pool(1 << 14, 6, views=[0, 1, 2])).float()
+    gtt, gtd = scene.render_gt(test.double().numpy(), n_steps=512, with_depth=True)
+    pool, test, gtt, gtd = pool.to(dev), test.to(dev), gtt.to(dev), gtd.to(dev)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
+    iters = args.render_iters
+    out = {}
+    for kind, batch in (("cfg2_plain", 4096), ("cfg3_proposal", 8192)):
+        torch.manual_seed(0)
+        m = FactorFields(W.field_cfg("cfg2"), device=dev, precision="bf16")
+        sampler = ProposalSampler(m) if kind == "cfg3_proposal" else None
+        tr = RadianceFieldTrainer(m, n_samples=1024, n_iters=iters, sampler=sampler)
+        g = torch.Generator(device=dev).manual_seed(0)
+        for it in range(iters):
+            idx = torch.randint(0, pool.shape[0], (4096,), device=dev, generator=g)
+            tr.step(pool[idx], gt[idx])
+            if sampler is None and it in (iters // 5, iters // 2):
+                m.updateAlphaMask((128, 128, 128), is_update_alphaMask=True, times=1)
+        psnr = tr.psnr(test, gtt)
+        with torch.no_grad():
+            dep = torch.cat([tr.render(test[s:s + 16384], is_train=False)[1] for s in range(0, test.shape[0], 16384)])
+        depth_err = float((dep - gtd).abs().mean())
+        # timed fwd+bwd steps at the configuration's batch (no optimizer step)
+        for _ in range(args.warmup):
+            idx = torch.randint(0, pool.shape[0], (batch,), device=dev, generator=g)
+            tr.step(pool[idx], gt[idx], optimize=False)
+        times = []
+        for _ in range(args.steps):
+            idx = torch.randint(0, pool.shape[0], (batch,), device=dev, generator=g)
+            rb, gb = pool[idx], gt[idx]
+            flush.zero_()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            tr.step(rb, gb, optimize=False)
+            e1.record()
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1))
+        ms = float(np.mean(times))
+        rec = {"rays_per_s": batch / (ms / 1e3), "ms_per_step": ms, "rays_per_step": batch,
+               "psnr_db": psnr, "depth_mae": depth_err, "train_steps": iters, "train_rays_per_step": 4096}
+        if sampler is None:
+            offs, _, _ = march(m, test, None, render_desc(m, 1024, True))
+            rec["live_samples_per_ray"] = float(offs[-1]) / test.shape[0]
+            rec["max_samples_per_ray"] = 1024
+        else:
+            rec["samples_per_ray"] = sampler.n_fine
+        out[kind] = rec
+    out["proposal_rays_per_s_vs_plain"] = out["cfg3_proposal"]["rays_per_s"] / out["cfg2_plain"]["rays_per_s"]
+    out["proposal_psnr_minus_plain_db"] = out["cfg3_proposal"]["psnr_db"] - out["cfg2_plain"]["psnr_db"]
+    out["scene"] = "seeded 32 Gaussian density blobs in [-1.5,1.5]^3, 100 views 400x400 focal 555, white bg"
+    return out
+
+
 def run_cpu_baseline(n_points, steps, warmup=1):
     """The reference's CPU op sequence on a bounded sample of the workload: samples/s."""
     from factor_fields_gb300 import workloads as W
@@ -271,6 +337,8 @@ def main():
     ap.add_argument("--impl", default="native", choices=["native", "reference"])
     ap.add_argument("--cpu-points", type=int, default=32768)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-render", action="store_true", help="skip the radiance-field configurations")
+    ap.add_argument("--render-iters", type=int, default=1500)
     args = ap.parse_args()
     ws, rank, local = dist_env()
     if args.impl == "reference":
@@ -288,6 +356,8 @@ def main():
     if ws > 1:
         torch.distributed.init_process_group("nccl", device_id=torch.device("cuda", local))
     res = run_native(args, ws, rank, local)
+    if not args.no_render:
+        res["radiance_field"] = run_radiance(args, torch.device("cuda", local))
     if rank == 0:
         if not args.no_cpu_baseline:
             res["cpu_baseline"] = run_cpu_baseline(args.cpu_points, 3)

@@ -332,11 +332,13 @@ class FactorFields(torch.nn.Module):
         alpha = F.max_pool3d(alpha, kernel_size=3, padding=1, stride=1).view(list(gridSize)[::-1])
         thres = float(self.cfg.renderer.alphaMask_thres) if is_update_alphaMask else 0.08
         occ = (alpha >= thres).float()
-        if is_update_alphaMask:
-            self.alphaMask = AlphaGridMask(self.device, self.inward_aabb, occ)
         valid = dense_xyz[occ > 0.5]
         if valid.shape[0] == 0:
+            # nothing occupied yet (an untrained field): keep the current mask — an empty mask
+            # would leave no live samples and so no gradients (the reference fails here on amin)
             return self.aabb.clone()
+        if is_update_alphaMask:
+            self.alphaMask = AlphaGridMask(self.device, self.inward_aabb, occ)
         lo, hi = valid.amin(0), valid.amax(0)
         pad = (hi - lo) / 20
         return torch.stack((lo - pad, hi + pad))

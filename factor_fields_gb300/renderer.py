@@ -111,8 +111,9 @@ def march(model, rays, jitter, rdesc):
     m = int(offsets[-1].item())
     xyz = torch.empty(m, 3, device=dev)
     sidx = torch.empty(m, dtype=torch.int32, device=dev)
-    N.call("ff_march_emit", ctypes.byref(rdesc), N.ptr(rays), N.ptr(jitter), n, N.ptr(offsets), N.ptr(xyz),
-           N.ptr(sidx), st)
+    if m > 0:
+        N.call("ff_march_emit", ctypes.byref(rdesc), N.ptr(rays), N.ptr(jitter), n, N.ptr(offsets), N.ptr(xyz),
+               N.ptr(sidx), st)
     return offsets, xyz, sidx
 
 

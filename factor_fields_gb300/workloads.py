@@ -216,10 +216,11 @@ class BlobScene:
         px, py = rng.integers(0, width, n), rng.integers(0, height, n)
         return self.pixel_rays(cams[v], px, py, width, height)
 
-    def render_gt(self, rays, n_steps=1024, chunk=2048, device="cuda"):
+    def render_gt(self, rays, n_steps=1024, chunk=2048, device="cuda", with_depth=False):
         """FP64 quadrature of the emission-absorption integral along each ray through the box,
         white background: rgb [n, 3] float32 (midpoint rule, n_steps steps between box entry
-        and exit; alpha_i = 1 - exp(-sigma_i dt))."""
+        and exit; alpha_i = 1 - exp(-sigma_i dt)); with_depth also returns the expected depth
+        sum_i w_i t_i [n] (the quantity depth_map is, models/FactorFields.py:895-896)."""
         dev = torch.device(device)
         c = torch.tensor(self.centers, dtype=torch.float64, device=dev)
         p = torch.tensor(self.peaks, dtype=torch.float64, device=dev)
@@ -227,7 +228,7 @@ class BlobScene:
         alb = torch.tensor(self.albedo, dtype=torch.float64, device=dev)
         lo = torch.tensor(self.aabb[0], dtype=torch.float64, device=dev)
         hi = torch.tensor(self.aabb[1], dtype=torch.float64, device=dev)
-        out = []
+        out, depths = [], []
         rays_t = torch.as_tensor(rays, dtype=torch.float64)
         for s in range(0, rays_t.shape[0], chunk):
             r = rays_t[s:s + chunk].to(dev)
@@ -239,6 +240,7 @@ class BlobScene:
             t1 = torch.maximum(t1, t0)
             dt = (t1 - t0) / n_steps
             rgb = torch.zeros(r.shape[0], 3, dtype=torch.float64, device=dev)
+            depth = torch.zeros(r.shape[0], dtype=torch.float64, device=dev)
             trans = torch.ones(r.shape[0], dtype=torch.float64, device=dev)
             blk = 128
             for b0 in range(0, n_steps, blk):
@@ -253,9 +255,13 @@ class BlobScene:
                 excl = torch.cat([torch.ones_like(incl[:, :1]), incl[:, :-1]], 1)
                 w = trans[:, None] * excl * (1.0 - keep)
                 rgb += (w[..., None] * col).sum(1)
+                depth += (w * ts).sum(1)
                 trans = trans * incl[:, -1]
             rgb += trans[:, None]  # white background
             out.append(rgb.float())
+            depths.append(depth.float())
+        if with_depth:
+            return torch.cat(out).cpu(), torch.cat(depths).cpu()
         return torch.cat(out).cpu()
 
 
