@@ -263,10 +263,14 @@ def run_radiance(args, dev):
         with torch.no_grad():
             dep = torch.cat([tr.render(test[s:s + 16384], is_train=False)[1] for s in range(0, test.shape[0], 16384)])
         depth_err = float((dep - gtd).abs().mean())
-        # timed fwd+bwd steps at the configuration's batch (no optimizer step)
+        # timed fwd+bwd steps at the configuration's batch (no optimizer step). The proposal
+        # path has a fixed sample count and replays from a CUDA graph; the plain sampler's
+        # live-sample count is data dependent (one host read per step, as in the reference).
+        run = (lambda r, t: tr.graph_step(r, t)) if sampler is not None else \
+            (lambda r, t: tr.step(r, t, optimize=False))
         for _ in range(args.warmup):
             idx = torch.randint(0, pool.shape[0], (batch,), device=dev, generator=g)
-            tr.step(pool[idx], gt[idx], optimize=False)
+            run(pool[idx], gt[idx])
         times = []
         for _ in range(args.steps):
             idx = torch.randint(0, pool.shape[0], (batch,), device=dev, generator=g)
@@ -275,7 +279,7 @@ def run_radiance(args, dev):
             torch.cuda.synchronize()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record()
-            tr.step(rb, gb, optimize=False)
+            run(rb, gb)
             e1.record()
             torch.cuda.synchronize()
             times.append(e0.elapsed_time(e1))

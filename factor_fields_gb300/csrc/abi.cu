@@ -368,4 +368,38 @@ int ff_proposal_scatter(const FFProposal* p, const float* rays, int64_t n_rays, 
                      "ff_proposal_scatter launch");
 }
 
+static int validate_head(const FFProposal* p, const void* grid, const FFMlp* m, const float* rays, int64_t n) {
+  int rc = validate_proposal(p, rays, n);
+  if (rc) return rc;
+  if (!m) return set_error(FF_ERR_ARG, "mlp is NULL");
+  if (m->n_layers != 2 || m->in_dim != 8 || m->hidden_dim != 64 || m->out_dim != 1)
+    return set_error(FF_ERR_UNSUPPORTED, "the proposal head is an 8 -> 64 -> 1 MLP");
+  if (m->bias[1]) return set_error(FF_ERR_UNSUPPORTED, "the proposal head's last layer has no bias");
+  if (n > 0 && (!grid || !m->weight[0] || !m->weight[1])) return set_error(FF_ERR_ARG, "grid/weights are NULL");
+  if (!aligned(grid, 16)) return set_error(FF_ERR_ALIGN, "grid must be 16-byte aligned");
+  return FF_OK;
+}
+
+int ff_proposal_head_forward(const FFProposal* p, const void* grid, const FFMlp* m, const float* rays,
+                             int64_t n_rays, float* o_prop, void* stream) {
+  int rc = validate_head(p, grid, m, rays, n_rays);
+  if (rc) return rc;
+  if (n_rays > 0 && !o_prop) return set_error(FF_ERR_ARG, "o_prop is NULL");
+  return cuda_status(launch_proposal_head_forward(*p, grid, *m, rays, n_rays, o_prop, (cudaStream_t)stream),
+                     "ff_proposal_head_forward launch");
+}
+
+int ff_proposal_head_backward(const FFProposal* p, const void* grid, const FFMlp* m, const float* rays,
+                              int64_t n_rays, const float* grad_o, float* grad_grid, const FFMlpGrad* g,
+                              void* stream) {
+  int rc = validate_head(p, grid, m, rays, n_rays);
+  if (rc) return rc;
+  if (n_rays > 0 && (!grad_o || !grad_grid)) return set_error(FF_ERR_ARG, "grad_o/grad_grid are NULL");
+  if (!aligned(grad_grid, 16)) return set_error(FF_ERR_ALIGN, "grad_grid must be 16-byte aligned");
+  FFMlpGrad none = {};
+  return cuda_status(launch_proposal_head_backward(*p, grid, *m, rays, n_rays, grad_o, grad_grid, g ? *g : none,
+                                                   (cudaStream_t)stream),
+                     "ff_proposal_head_backward launch");
+}
+
 }  // extern "C"

@@ -62,6 +62,11 @@ cudaError_t launch_composite_backward(const FFRender& r, const float* rays, cons
                                       float* grad_feat, const float* zd, cudaStream_t s);
 
 // proposal_kernels.cu
+cudaError_t launch_proposal_head_forward(const FFProposal& p, const void* grid, const FFMlp& m, const float* rays,
+                                         int64_t n, float* o_out, cudaStream_t s);
+cudaError_t launch_proposal_head_backward(const FFProposal& p, const void* grid, const FFMlp& m, const float* rays,
+                                          int64_t n, const float* g_o, float* grad_grid, const FFMlpGrad& gr,
+                                          cudaStream_t s);
 cudaError_t launch_proposal_encode(const FFProposal& p, const void* grid, const float* rays, int64_t n, float* feat,
                                    cudaStream_t s);
 cudaError_t launch_proposal_scatter(const FFProposal& p, const float* rays, int64_t n, const float* grad_feat,

@@ -19,6 +19,7 @@
 // bin masses, loss, reverse scan to dL/do), scatter (thread per coarse sample).
 #include "ff_common.cuh"
 #include "ff_internal.h"
+#include "mma_util.cuh"
 
 namespace ffgb {
 
@@ -341,7 +342,313 @@ int grid_blocks(int64_t total, int threads) {
   return (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(total, threads), (int64_t)sm_count() * 16));
 }
 
+// ---- the proposal head on tensor cores: encode + 8 -> 64 (ReLU) -> 1 ---------------------
+// Thread per coarse sample for the position and the 8-channel gather; 32 samples per warp for
+// the MLP (mma.sync m16n8k16 BF16, FP32 accumulation). Layer 0 runs in split BF16 (features and
+// W0 as hi + lo pairs, the lo * lo term dropped) so that the ReLU mask is the float32 one;
+// dX = dH W0 takes dH as hi + lo and W0 as BF16.
+// Backward: dH = g_o * w1 * [H > 0], dX = dH W0 (tensor cores), dW1 in registers, dW0 and the
+// bias gradient (constant-1 feature column) by a block-wide MMA over the block's 128 samples,
+// the grid gradient scattered with float4 atomics.
+constexpr int kHW = 4;            // warps per block
+constexpr int kHT = kHW * 32;     // samples per block iteration
+constexpr int HLD_X = 12;         // float32 feature tile [32][12]: 8 features, 1.0, 0, 0, 0
+constexpr int HLD_H = 72;         // BF16 dH tile [32][72]
+constexpr int HLD_W0 = 24;        // W0 [64][16 + pad] BF16 (inputs 8..15 zero)
+constexpr int HLD_W0T = 72;       // W0^T [8][64 + pad]
+
+struct HeadSmem {
+  __nv_bfloat16 *w0, *w0l, *w0t;
+  float *b0, *w1, *x;
+  __nv_bfloat16* dh;
+};
+
+template <int MODE>
+__host__ __device__ constexpr int64_t head_smem_bytes() {
+  return 2 * 64 * HLD_W0 * 2 + 8 * HLD_W0T * 2 + 64 * 4 + 64 * 4 + (int64_t)kHW * 32 * HLD_X * 4 +
+         (MODE ? (int64_t)kHW * 32 * HLD_H * 2 : 0);
+}
+
+__device__ __forceinline__ void head_pair(const float* xf, int row, int col, uint32_t& hi, uint32_t& lo) {
+  if (col < HLD_X) {
+    const float2 v = *reinterpret_cast<const float2*>(xf + row * HLD_X + col);
+    split_pair(v.x, v.y, hi, lo);
+  } else {
+    hi = lo = 0u;
+  }
+}
+
+template <int MODE, typename T>
+__global__ void __launch_bounds__(kHT) proposal_head_kernel(const FFProposal p, const T* __restrict__ grid,
+                                                             const float* __restrict__ rays, int64_t n_rays,
+                                                             const FFMlp m, float* __restrict__ o_out,
+                                                             const float* __restrict__ g_o,
+                                                             float* __restrict__ grad_grid, const FFMlpGrad gr) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, g = lane >> 2, t = lane & 3;
+  HeadSmem s;
+  {
+    unsigned char* q = smem_raw;
+    s.w0 = (__nv_bfloat16*)q; q += 64 * HLD_W0 * 2;
+    s.w0l = (__nv_bfloat16*)q; q += 64 * HLD_W0 * 2;
+    s.w0t = (__nv_bfloat16*)q; q += 8 * HLD_W0T * 2;
+    s.b0 = (float*)q; q += 64 * 4;
+    s.w1 = (float*)q; q += 64 * 4;
+    s.x = (float*)q; q += kHW * 32 * HLD_X * 4;
+    s.dh = MODE ? (__nv_bfloat16*)q : nullptr;
+  }
+  for (int e = tid; e < 64 * 16; e += kHT) {
+    const int j = e >> 4, k = e & 15;
+    const float w = k < 8 ? m.weight[0][j * 8 + k] : 0.f;
+    const __nv_bfloat16 v = __float2bfloat16_rn(w);
+    s.w0[j * HLD_W0 + k] = v;
+    s.w0l[j * HLD_W0 + k] = __float2bfloat16_rn(w - __bfloat162float(v));
+    if (k < 8) s.w0t[k * HLD_W0T + j] = v;
+  }
+  for (int j = tid; j < 64; j += kHT) {
+    s.b0[j] = m.bias[0] ? m.bias[0][j] : 0.f;
+    s.w1[j] = m.weight[1][j];
+  }
+  __syncthreads();
+  float* xf = s.x + warp * 32 * HLD_X;
+  const int64_t total = n_rays * p.n_bins;
+  float acc_w0[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
+  float acc_w1[8][2];
+#pragma unroll
+  for (int nt = 0; nt < 8; ++nt) acc_w1[nt][0] = acc_w1[nt][1] = 0.f;
+
+  for (int64_t base = (int64_t)blockIdx.x * kHT; base < total; base += (int64_t)gridDim.x * kHT) {
+    const int64_t e = base + warp * 32 + lane;
+    const bool valid = e < total;
+    float pos[3] = {0.f, 0.f, 0.f};
+    float feat[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    if (valid) {
+      const int64_t ray = e / p.n_bins;
+      const int k = (int)(e % p.n_bins);
+      const Segment sg = segment(p, rays, ray);
+      const float tt = sg.t_in + ((float)k + 0.5f) * sg.len;
+#pragma unroll
+      for (int q = 0; q < 3; ++q) pos[q] = sg.o[q] + sg.d[q] * tt;
+      Corners<3> c;
+      grid_corners(p, pos, c);
+#pragma unroll
+      for (int b = 0; b < 8; ++b) {
+        if (c.idx[b] >= 0 && c.w[b] != 0.f) {
+          float v[8];
+          load8<T>(grid + (int64_t)c.idx[b] * 8, v);
+#pragma unroll
+          for (int q = 0; q < 8; ++q) feat[q] += v[q] * c.w[b];
+        }
+      }
+    }
+    {
+      float4* xr = reinterpret_cast<float4*>(xf + lane * HLD_X);
+      xr[0] = make_float4(feat[0], feat[1], feat[2], feat[3]);
+      xr[1] = make_float4(feat[4], feat[5], feat[6], feat[7]);
+      xr[2] = make_float4(valid ? 1.f : 0.f, 0.f, 0.f, 0.f);
+    }
+    __syncwarp();
+    float dx[2][4];
+#pragma unroll
+    for (int mt = 0; mt < 2; ++mt) {
+      const int r0 = 16 * mt + g, r1 = r0 + 8;
+      float hc[8][4];
+#pragma unroll
+      for (int nt = 0; nt < 8; ++nt) {
+        const float bl = s.b0[nt * 8 + 2 * t], bh = s.b0[nt * 8 + 2 * t + 1];
+        hc[nt][0] = bl; hc[nt][1] = bh; hc[nt][2] = bl; hc[nt][3] = bh;
+      }
+      {
+        uint32_t ah[4], al[4];
+        head_pair(xf, r0, 2 * t, ah[0], al[0]);
+        head_pair(xf, r1, 2 * t, ah[1], al[1]);
+        head_pair(xf, r0, 2 * t + 8, ah[2], al[2]);
+        head_pair(xf, r1, 2 * t + 8, ah[3], al[3]);
+#pragma unroll
+        for (int nt = 0; nt < 8; ++nt) {
+          const __nv_bfloat16* wp = s.w0 + (nt * 8 + g) * HLD_W0 + 2 * t;
+          const __nv_bfloat16* wl = s.w0l + (nt * 8 + g) * HLD_W0 + 2 * t;
+          const uint32_t b0 = lds32(wp), b1 = lds32(wp + 8);
+          mma_bf16(hc[nt], ah, lds32(wl), lds32(wl + 8));
+          mma_bf16(hc[nt], al, b0, b1);
+          mma_bf16(hc[nt], ah, b0, b1);
+        }
+      }
+      // o = relu(H) . w1 (rows r0 / r1): lane partial sums, then the quad
+      float o0 = 0.f, o1 = 0.f;
+#pragma unroll
+      for (int nt = 0; nt < 8; ++nt) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) hc[nt][q] = fmaxf(hc[nt][q], 0.f);
+        const float wa = s.w1[nt * 8 + 2 * t], wb = s.w1[nt * 8 + 2 * t + 1];
+        o0 += hc[nt][0] * wa + hc[nt][1] * wb;
+        o1 += hc[nt][2] * wa + hc[nt][3] * wb;
+      }
+      o0 += __shfl_xor_sync(0xffffffffu, o0, 1);
+      o0 += __shfl_xor_sync(0xffffffffu, o0, 2);
+      o1 += __shfl_xor_sync(0xffffffffu, o1, 1);
+      o1 += __shfl_xor_sync(0xffffffffu, o1, 2);
+      const int64_t row0 = base + warp * 32 + r0, row1 = row0 + 8;
+      if constexpr (MODE == 0) {
+        if (t == 0) {
+          if (row0 < total) o_out[row0] = o0;
+          if (row1 < total) o_out[row1] = o1;
+        }
+      } else {
+        const float go0 = row0 < total ? g_o[row0] : 0.f;
+        const float go1 = row1 < total ? g_o[row1] : 0.f;
+        __nv_bfloat16* dhw = s.dh + warp * 32 * HLD_H;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) dx[mt][q] = 0.f;
+#pragma unroll
+        for (int ks = 0; ks < 4; ++ks) {
+          float dh[2][4];
+#pragma unroll
+          for (int hh = 0; hh < 2; ++hh) {
+            const int nt = 2 * ks + hh;
+            const float wa = s.w1[nt * 8 + 2 * t], wb = s.w1[nt * 8 + 2 * t + 1];
+            acc_w1[nt][0] += hc[nt][0] * go0 + hc[nt][2] * go1;
+            acc_w1[nt][1] += hc[nt][1] * go0 + hc[nt][3] * go1;
+            dh[hh][0] = hc[nt][0] > 0.f ? go0 * wa : 0.f;
+            dh[hh][1] = hc[nt][1] > 0.f ? go0 * wb : 0.f;
+            dh[hh][2] = hc[nt][2] > 0.f ? go1 * wa : 0.f;
+            dh[hh][3] = hc[nt][3] > 0.f ? go1 * wb : 0.f;
+          }
+          uint32_t d[4], dl[4];
+          split_pair(dh[0][0], dh[0][1], d[0], dl[0]);
+          split_pair(dh[0][2], dh[0][3], d[1], dl[1]);
+          split_pair(dh[1][0], dh[1][1], d[2], dl[2]);
+          split_pair(dh[1][2], dh[1][3], d[3], dl[3]);
+          __nv_bfloat16* p0 = dhw + r0 * HLD_H + 16 * ks + 2 * t;
+          __nv_bfloat16* p1 = dhw + r1 * HLD_H + 16 * ks + 2 * t;
+          sts32(p0, d[0]); sts32(p1, d[1]); sts32(p0 + 8, d[2]); sts32(p1 + 8, d[3]);
+          const __nv_bfloat16* wp = s.w0t + g * HLD_W0T + 16 * ks + 2 * t;
+          const uint32_t b0 = lds32(wp), b1 = lds32(wp + 8);
+          mma_bf16(dx[mt], dl, b0, b1);
+          mma_bf16(dx[mt], d, b0, b1);
+        }
+      }
+    }
+    if constexpr (MODE == 0) {
+      __syncwarp();
+    } else {
+      __syncthreads();  // all warps' X and dH tiles complete
+      // dW0 (+ bias in column 8): this warp's hidden rows [16 warp, +16) over the block's samples
+#pragma unroll 2
+      for (int kk = 0; kk < 8; ++kk) {
+        const int src = kk >> 1, h16 = (kk & 1) * 16;
+        const __nv_bfloat16* dhs = s.dh + src * 32 * HLD_H;
+        const float* xs = s.x + src * 32 * HLD_X;
+        uint32_t af[4];
+        ldsm_x4_t(af, dhs + (h16 + (lane & 7) + (lane >> 4) * 8) * HLD_H + 16 * warp + ((lane >> 3) & 1) * 8);
+#pragma unroll
+        for (int nt = 0; nt < 2; ++nt) {
+          const int col = nt * 8 + g;
+          uint32_t b0 = 0u, b1 = 0u;
+          if (col < HLD_X) {
+            b0 = pack_bf16(xs[(h16 + 2 * t) * HLD_X + col], xs[(h16 + 2 * t + 1) * HLD_X + col]);
+            b1 = pack_bf16(xs[(h16 + 2 * t + 8) * HLD_X + col], xs[(h16 + 2 * t + 9) * HLD_X + col]);
+          }
+          mma_bf16(acc_w0[nt], af, b0, b1);
+        }
+      }
+      __syncthreads();  // tiles consumed: X tile can hold dX
+#pragma unroll
+      for (int mt = 0; mt < 2; ++mt) {
+        *reinterpret_cast<float2*>(xf + (16 * mt + g) * HLD_X + 2 * t) = make_float2(dx[mt][0], dx[mt][1]);
+        *reinterpret_cast<float2*>(xf + (16 * mt + g + 8) * HLD_X + 2 * t) = make_float2(dx[mt][2], dx[mt][3]);
+      }
+      __syncwarp();
+      if (valid) {
+        const float4 g0 = reinterpret_cast<const float4*>(xf + lane * HLD_X)[0];
+        const float4 g1 = reinterpret_cast<const float4*>(xf + lane * HLD_X)[1];
+        Corners<3> c;
+        grid_corners(p, pos, c);
+#pragma unroll
+        for (int b = 0; b < 8; ++b) {
+          if (c.idx[b] >= 0 && c.w[b] != 0.f) {
+            const float w = c.w[b];
+            float4* dst = reinterpret_cast<float4*>(grad_grid + (int64_t)c.idx[b] * 8);
+            atomicAdd(dst, make_float4(g0.x * w, g0.y * w, g0.z * w, g0.w * w));
+            atomicAdd(dst + 1, make_float4(g1.x * w, g1.y * w, g1.z * w, g1.w * w));
+          }
+        }
+      }
+      __syncwarp();
+    }
+  }
+  if constexpr (MODE == 1) {
+#pragma unroll
+    for (int nt = 0; nt < 2; ++nt) {
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int row = 16 * warp + g + (q >= 2 ? 8 : 0);
+        const int col = nt * 8 + 2 * t + (q & 1);
+        if (col < 8) {
+          if (gr.weight[0]) atomicAdd(gr.weight[0] + row * 8 + col, acc_w0[nt][q]);
+        } else if (col == 8) {
+          if (gr.bias[0]) atomicAdd(gr.bias[0] + row, acc_w0[nt][q]);
+        }
+      }
+    }
+#pragma unroll
+    for (int nt = 0; nt < 8; ++nt) {
+#pragma unroll
+      for (int j = 0; j < 2; ++j) {
+        float v = acc_w1[nt][j];
+        v += __shfl_xor_sync(0xffffffffu, v, 4);
+        v += __shfl_xor_sync(0xffffffffu, v, 8);
+        v += __shfl_xor_sync(0xffffffffu, v, 16);
+        if (g == 0 && gr.weight[1]) atomicAdd(gr.weight[1] + nt * 8 + 2 * t + j, v);
+      }
+    }
+  }
+}
+
+// Blocks of `kern` resident per SM (at least 1): the persistent grid is sm_count() times this.
+template <typename K>
+int resident_blocks(K kern, int threads, int64_t smem) {
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, (size_t)smem) != cudaSuccess) {
+    (void)cudaGetLastError();
+    per_sm = 1;
+  }
+  return std::max(per_sm, 1);
+}
+
+template <int MODE>
+cudaError_t launch_head(const FFProposal& p, const void* grid, const float* rays, int64_t n, const FFMlp& m,
+                        float* o_out, const float* g_o, float* grad_grid, const FFMlpGrad& gr, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  constexpr int64_t smem = head_smem_bytes<MODE>();
+  const int64_t tiles = ceil_div(n * p.n_bins, kHT);
+  if (p.param_dtype == FF_BF16) {
+    static const int per_sm = resident_blocks(proposal_head_kernel<MODE, __nv_bfloat16>, kHT, smem);
+    const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>(tiles, (int64_t)sm_count() * per_sm));
+    proposal_head_kernel<MODE, __nv_bfloat16><<<blocks, kHT, smem, st>>>(p, (const __nv_bfloat16*)grid, rays, n, m,
+                                                                         o_out, g_o, grad_grid, gr);
+  } else {
+    static const int per_sm = resident_blocks(proposal_head_kernel<MODE, float>, kHT, smem);
+    const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>(tiles, (int64_t)sm_count() * per_sm));
+    proposal_head_kernel<MODE, float><<<blocks, kHT, smem, st>>>(p, (const float*)grid, rays, n, m, o_out, g_o,
+                                                                 grad_grid, gr);
+  }
+  return cudaGetLastError();
+}
+
 }  // namespace
+
+cudaError_t launch_proposal_head_forward(const FFProposal& p, const void* grid, const FFMlp& m, const float* rays,
+                                         int64_t n, float* o_out, cudaStream_t s) {
+  FFMlpGrad none = {};
+  return launch_head<0>(p, grid, rays, n, m, o_out, nullptr, nullptr, none, s);
+}
+
+cudaError_t launch_proposal_head_backward(const FFProposal& p, const void* grid, const FFMlp& m, const float* rays,
+                                          int64_t n, const float* g_o, float* grad_grid, const FFMlpGrad& gr,
+                                          cudaStream_t s) {
+  return launch_head<1>(p, grid, rays, n, m, nullptr, g_o, grad_grid, gr, s);
+}
 
 cudaError_t launch_proposal_encode(const FFProposal& p, const void* grid, const float* rays, int64_t n, float* feat,
                                    cudaStream_t s) {

@@ -11,8 +11,10 @@ makes its weight on each coarse bin upper-bound the field's weight mass in that 
 stratified uniform samples over the ray's segment in the box — the same sample budget without
 the proposal, used to show what the network gains.
 
-Kernels: ff_proposal_encode / _resample / _loss / _scatter (csrc/proposal_kernels.cu), the
-float32 MLP kernels for the proposal head, the field kernels, ff_composite_*_zd.
+Kernels: ff_proposal_head_forward / _backward (BF16: gather + MLP on tensor cores in one
+launch each way) or ff_proposal_encode + the float32 MLP kernels + ff_proposal_scatter (FP32),
+ff_proposal_resample / _loss (csrc/proposal_kernels.cu), the field kernels,
+ff_composite_*_zd.
 """
 import ctypes
 
@@ -34,8 +36,13 @@ class ProposalRenderFunction(torch.autograd.Function):
         nb, nf = sam.n_bins, sam.n_fine
         dev = rays.device
         st = N.stream_ptr()
-        feat_p = torch.empty(n * nb, 8, device=dev)
-        if sam.learned:
+        feat_p = None
+        if sam.learned and sam.fused_head:
+            o_p = torch.empty(n * nb, 1, device=dev)
+            N.call("ff_proposal_head_forward", ctypes.byref(sam.desc), N.ptr(sam.grid_read()),
+                   ctypes.byref(sam.mlp_struct()), N.ptr(rays), n, N.ptr(o_p), st)
+        elif sam.learned:
+            feat_p = torch.empty(n * nb, 8, device=dev)
             N.call("ff_proposal_encode", ctypes.byref(sam.desc), N.ptr(sam.grid_read()), N.ptr(rays), n,
                    N.ptr(feat_p), st)
             o_p = torch.empty(n * nb, 1, device=dev)
@@ -78,6 +85,9 @@ class ProposalSampler:
                  density_shift=-4.0, precision="bf16", learned=True, seed=0, uniform_mix=0.0):
         self.m, self.learned = model, learned
         self.reso, self.n_bins, self.n_fine, self.precision = reso, n_bins, n_fine, precision
+        # BF16: the head (encode + MLP, and its backward + scatter) is one tensor-core launch;
+        # FP32: ff_proposal_encode + the float32 MLP kernels + ff_proposal_scatter
+        self.fused_head = precision == "bf16"
         dev = model.device
         gen = torch.Generator().manual_seed(seed)
         self.grid = torch.nn.Parameter(((torch.rand(reso ** 3 * 8, generator=gen) * 2 - 1) * 0.05).to(dev))
@@ -134,7 +144,10 @@ class ProposalSampler:
         if fused is None:
             fused = m.precision == "bf16"
         basis_r, coeff_r, dt = m._read_buffers()
-        job = {"model": m, "sampler": self, "rdesc": render_desc(m, self.n_fine, white_bg),
+        key = (bool(white_bg), id(m.alphaMask))
+        if getattr(self, "_rdesc_key", None) != key:  # host-side cache: no device reads per call
+            self._rdesc, self._rdesc_key = render_desc(m, self.n_fine, white_bg), key
+        job = {"model": m, "sampler": self, "rdesc": self._rdesc,
                "fdesc": m.descriptor(dt), "basis_r": basis_r, "coeff_r": coeff_r, "coeff_param": m.coeff_flat,
                "fused": fused, "jitter": jitter}
         l0, l1 = m.linear_mat.backbone
@@ -164,6 +177,11 @@ class ProposalSampler:
         for i, (w, b) in enumerate(zip(ws, bs)):
             g.weight[i] = w.grad.data_ptr()
             g.bias[i] = b.grad.data_ptr() if b is not None else None
+        if self.fused_head:
+            N.call("ff_proposal_head_backward", ctypes.byref(self.desc), N.ptr(self.grid_read()),
+                   ctypes.byref(self.mlp_struct()), N.ptr(rays), n, N.ptr(g_o), N.ptr(self.grid.grad),
+                   ctypes.byref(g), st)
+            return self.loss_buf[0]
         g_feat = torch.empty_like(job["feat_p"])
         N.call("ff_mlp_backward", ctypes.byref(self.mlp_struct()), N.ptr(job["feat_p"]), n * nb, N.ptr(g_o),
                N.ptr(g_feat), ctypes.byref(g), st)

@@ -20,10 +20,12 @@ class RadianceFieldTrainer:
         self.opt = torch.optim.Adam(model.get_optparam_groups(lr_small, lr_large), betas=(0.9, 0.99))
         self.lr_factor = decay_ratio ** (1.0 / max(n_iters, 1))
         self.sampler = sampler  # None: the plain uniform sampler; else a ProposalSampler
+        self.jitter = None  # proposal sampler: fixed per-ray stratification jitter [R]; None: random per step
 
     def render(self, rays, is_train):
         if self.sampler is not None:
-            return self.sampler.render(rays, is_train=is_train, white_bg=self.white_bg)
+            return self.sampler.render(rays, is_train=is_train, white_bg=self.white_bg,
+                                       jitter=self.jitter if is_train else None)
         rgb, depth, _ = self.m(rays, white_bg=self.white_bg, is_train=is_train, N_samples=self.n_samples)
         return rgb, depth
 
@@ -43,6 +45,37 @@ class RadianceFieldTrainer:
             if self.sampler is not None:
                 self.sampler.step()
         return loss.detach()
+
+    def graph_step(self, rays, rgb_gt):
+        """step(optimize=False) replayed from a CUDA graph (fixed-size sampling only: the
+        proposal sampler). The batch is copied into static buffers; the capture covers the
+        gradient zeroing, rendering, loss, the field backward and the proposal loss/backward.
+        Re-captured when the batch shape changes."""
+        if self.sampler is None:
+            raise ValueError("the plain sampler's live-sample count varies per batch: use step()")
+        key = (tuple(rays.shape), tuple(rgb_gt.shape))
+        if getattr(self, "_gkey", None) != key:
+            dev = self.m.basis_flat.device
+            self._gr = torch.empty(rays.shape, dtype=torch.float32, device=dev)
+            self._gg = torch.empty(rgb_gt.shape, dtype=torch.float32, device=dev)
+            self._gr.copy_(rays)
+            self._gg.copy_(rgb_gt)
+            side = torch.cuda.Stream()
+            side.wait_stream(torch.cuda.current_stream())
+            with torch.cuda.stream(side):
+                for _ in range(2):
+                    self.step(self._gr, self._gg, optimize=False)
+            torch.cuda.current_stream().wait_stream(side)
+            self._graph = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(self._graph):
+                self._gloss = self.step(self._gr, self._gg, optimize=False)
+            self._gkey = key
+        self.m._read_buffers()
+        self.sampler.grid_read()
+        self._gr.copy_(rays, non_blocking=True)
+        self._gg.copy_(rgb_gt, non_blocking=True)
+        self._graph.replay()
+        return self._gloss
 
     @torch.no_grad()
     def psnr(self, rays, rgb_gt, chunk=16384):

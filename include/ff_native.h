@@ -281,6 +281,18 @@ FF_API int ff_proposal_loss(const FFProposal* p, const float* rays, int64_t n_ra
 /* Scatter dL/dfeat [n_rays * n_bins, 8] into the float32 grid gradient [reso^3][8] (+=). */
 FF_API int ff_proposal_scatter(const FFProposal* p, const float* rays, int64_t n_rays, const float* grad_feat,
                                float* grad_grid, void* stream);
+/* The proposal head fused on tensor cores: bin-centre positions, the grid gather and the
+ * 8 -> 64 (ReLU) -> 1 MLP m (n_layers 2, in_dim 8, hidden_dim 64, out_dim 1, no bias on the
+ * last layer) in one launch, o_prop [n_rays * n_bins] out. Equals ff_proposal_encode followed
+ * by ff_mlp_forward up to split-BF16 rounding (first layer: features and weights as hi + lo). */
+FF_API int ff_proposal_head_forward(const FFProposal* p, const void* grid, const FFMlp* m, const float* rays,
+                                    int64_t n_rays, float* o_prop, void* stream);
+/* Backward of ff_proposal_head_forward for grad_o [n_rays * n_bins]: the grid gradient
+ * (float32 [reso^3][8], +=) and the MLP gradients g (+=; NULL entries skipped) in one launch.
+ * Equals ff_mlp_backward followed by ff_proposal_scatter up to BF16 rounding. */
+FF_API int ff_proposal_head_backward(const FFProposal* p, const void* grid, const FFMlp* m, const float* rays,
+                                     int64_t n_rays, const float* grad_o, float* grad_grid, const FFMlpGrad* g,
+                                     void* stream);
 
 #ifdef __cplusplus
 }

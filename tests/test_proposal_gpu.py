@@ -62,6 +62,60 @@ def test_encode_and_scatter_match_trilinear_grid_sample():
     assert rel_err(ggrid.view(12, 12, 12, 8).permute(3, 0, 1, 2), refg) < 1e-4
 
 
+@pytest.mark.parametrize("precision,n_rays,n_bins", [("bf16", 61, 64), ("fp32", 33, 96), ("bf16", 1, 32)])
+def test_fused_head_matches_encode_mlp_scatter(precision, n_rays, n_bins):
+    """ff_proposal_head_forward / _backward against the unfused composition: the grid lookup
+    (ff_proposal_encode, pinned to trilinear grid_sample above), the MLP and its gradients in
+    FP64, and the grid scatter of the FP64 feature gradient. Ragged sample counts (61 * 64,
+    1 * 32 are not multiples of the 128-sample tile). BF16 tolerance: the first layer runs in
+    split BF16 (hi + lo features and weights), dX takes BF16 W0, dW0 BF16 dH and features."""
+    from factor_fields_gb300 import _native as N
+    m, s = make_sampler(reso=12, n_bins=n_bins, precision=precision)
+    gen = torch.Generator().manual_seed(7)
+    with torch.no_grad():
+        s.grid.copy_(torch.randn(s.grid.shape, generator=gen).cuda() * 0.5)
+        l0, l1 = s.mlp.backbone
+        l0.bias.copy_(torch.randn(64, generator=gen).cuda() * 0.2)
+    st = N.stream_ptr()
+    rt = torch.from_numpy(rays_np(n_rays, 9)).cuda()
+    n, nb = n_rays, n_bins
+    grid_r = s.grid_read()
+    o = torch.empty(n * nb, 1, device="cuda")
+    N.call("ff_proposal_head_forward", ctypes.byref(s.desc), N.ptr(grid_r), ctypes.byref(s.mlp_struct()), N.ptr(rt),
+           n, N.ptr(o), st)
+    feat = torch.empty(n * nb, 8, device="cuda")
+    N.call("ff_proposal_encode", ctypes.byref(s.desc), N.ptr(grid_r), N.ptr(rt), n, N.ptr(feat), st)
+    x = feat.double().cpu().requires_grad_(True)
+    w0 = l0.weight.detach().double().cpu().requires_grad_(True)
+    b0 = l0.bias.detach().double().cpu().requires_grad_(True)
+    w1 = l1.weight.detach().double().cpu().requires_grad_(True)
+    ref = torch.relu(x @ w0.T + b0) @ w1.T
+    assert rel_err(o, ref.detach().numpy()) < 1e-3
+    # samples with a hidden pre-activation within 1e-4 of 0 get no gradient: there the ReLU mask
+    # of any float32 evaluation may differ from FP64's (a discrete jump, not a rounding error)
+    pre = (x @ w0.T + b0).detach()
+    g_o = torch.randn(n * nb, 1, generator=gen)
+    g_o[(pre.abs() < 1e-4).any(1)] = 0
+    ref.backward(g_o.double())
+    s.zero_grad()
+    g = N.FFMlpGrad()
+    g.weight[0], g.bias[0], g.weight[1] = l0.weight.grad.data_ptr(), l0.bias.grad.data_ptr(), l1.weight.grad.data_ptr()
+    g_o_d = g_o.cuda()
+    N.call("ff_proposal_head_backward", ctypes.byref(s.desc), N.ptr(grid_r), ctypes.byref(s.mlp_struct()), N.ptr(rt),
+           n, N.ptr(g_o_d), N.ptr(s.grid.grad), ctypes.byref(g), st)
+    gx = x.grad.float().cuda().contiguous()
+    ref_grid = torch.zeros_like(s.grid)
+    N.call("ff_proposal_scatter", ctypes.byref(s.desc), N.ptr(rt), n, N.ptr(gx), N.ptr(ref_grid), st)
+    torch.cuda.synchronize()
+    assert rel_err(s.grid.grad, ref_grid.cpu().numpy()) < 1e-2
+    assert rel_err(l0.weight.grad, w0.grad.numpy()) < 1e-2
+    assert rel_err(l0.bias.grad, b0.grad.numpy()) < 1e-2
+    assert rel_err(l1.weight.grad, w1.grad.numpy()) < 1e-3
+    # no rays: nothing launched, success
+    N.call("ff_proposal_head_forward", ctypes.byref(s.desc), N.ptr(grid_r), ctypes.byref(s.mlp_struct()), N.ptr(rt),
+           0, None, st)
+
+
 def test_resample_is_sample_pdf():
     from factor_fields_gb300 import _native as N
     m, s = make_sampler()
@@ -169,3 +223,34 @@ def test_proposal_matches_plain_sampler_with_far_fewer_samples():
             res["plain_samples"] = float(offsets[-1]) / test.shape[0]
     assert res["proposal"] >= res["plain"] - 0.1, res
     assert res["plain_samples"] >= 2 * 48, res  # ~127 live samples per ray after occupancy pruning
+
+
+def test_trainer_graph_step_matches_eager_step():
+    """RadianceFieldTrainer.graph_step (the step captured in a CUDA graph and replayed) gives the
+    eager step's loss and gradients on the same batch (fixed jitter), and picks up parameter
+    updates made between replays (the BF16 read copies are refreshed in place)."""
+    from factor_fields_gb300 import FactorFields
+    from factor_fields_gb300 import workloads as W
+    from factor_fields_gb300.proposal import ProposalSampler
+    from factor_fields_gb300.train import RadianceFieldTrainer
+    scene = W.BlobScene(0)
+    rays = torch.from_numpy(scene.ray_pool(2048, 11)).float()
+    gt = scene.render_gt(rays.double().numpy(), n_steps=256).cuda().float()
+    rays = rays.cuda()
+    torch.manual_seed(0)
+    m = FactorFields(W.field_cfg("cfg2"), device="cuda", precision="bf16")
+    tr = RadianceFieldTrainer(m, sampler=ProposalSampler(m), n_iters=100)
+    for _ in range(30):
+        tr.step(rays, gt)
+    tr.jitter = torch.rand(rays.shape[0], device="cuda", generator=torch.Generator(device="cuda").manual_seed(3))
+    params = [m.basis_flat, m.coeff_flat] + list(m.linear_mat.parameters()) + tr.sampler.params
+    for rep in range(2):
+        loss_e = float(tr.step(rays, gt, optimize=False))
+        grads_e = [p.grad.clone() for p in params]
+        loss_g = float(tr.graph_step(rays, gt))
+        torch.cuda.synchronize()
+        assert abs(loss_g - loss_e) <= 1e-5 * abs(loss_e)
+        for p, ge in zip(params, grads_e):
+            assert rel_err(p.grad, ge) < 1e-3
+        tr.opt.step()  # parameters change between replays
+        tr.sampler.step()
