@@ -76,6 +76,9 @@ SIGNATURES = {
                                       _P(FFMlpGrad), c_vp]),
     "ff_field_fit_step": (c_i32, [_P(FFField), c_vp, c_vp, _P(FFMlp), c_vp, c_vp, c_i64, c_i32, c_f32, c_vp, c_vp,
                                   c_vp, _P(FFMlpGrad), c_vp]),
+    "ff_field_fit_binned_workspace_bytes": (c_i64, [_P(FFField), c_i64, c_i32]),
+    "ff_field_fit_step_binned": (c_i32, [_P(FFField), c_vp, c_vp, _P(FFMlp), c_vp, c_vp, c_i64, c_i32, c_f32, c_vp,
+                                         c_vp, c_vp, _P(FFMlpGrad), c_vp, c_i64, c_vp]),
     "ff_march_count": (c_i32, [_P(FFRender), c_vp, c_vp, c_i64, c_vp, c_vp, c_vp]),
     "ff_scan_workspace_bytes": (c_i64, [c_i64]),
     "ff_scan_counts": (c_i32, [c_vp, c_i64, c_vp, c_vp, c_i64, c_vp]),
@@ -148,7 +151,13 @@ def stream_ptr():
 
 _launches = [0]
 _NON_LAUNCHING = {"ff_abi_version", "ff_last_error", "ff_device_info", "ff_struct_size", "ff_scan_workspace_bytes",
+                  "ff_field_fit_binned_workspace_bytes",
                   "ff_scan_noalloc_max_counts"}
+
+
+# entry points that enqueue more than one kernel of this library
+_KERNELS_PER_CALL = {"ff_scan_counts": 3, "ff_scan_counts_noalloc": 3,
+                     "ff_field_fit_step_binned": 6}  # bin, 3 scan kernels, permute, fit
 
 
 def reset_launch_count():
@@ -156,7 +165,7 @@ def reset_launch_count():
 
 
 def launch_count():
-    """Entry-point calls that enqueue kernels since the last reset (each enqueues one kernel)."""
+    """Kernels of this library enqueued through call() since the last reset."""
     return _launches[0]
 
 
@@ -164,4 +173,4 @@ def call(name, *args):
     rc = getattr(lib(), name)(*args)
     check(rc, name)
     if name not in _NON_LAUNCHING:
-        _launches[0] += 1
+        _launches[0] += _KERNELS_PER_CALL.get(name, 1)

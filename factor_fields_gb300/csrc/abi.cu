@@ -227,6 +227,35 @@ int ff_field_fit_step(const FFField* f, const void* basis, const void* coeff, co
                      "ff_field_fit_step launch");
 }
 
+int64_t ff_field_fit_binned_workspace_bytes(const FFField* f, int64_t n, int32_t out_dim) {
+  if (!f || n < 0 || out_dim < 1 || f->coord_dim < 2 || f->coord_dim > 3) return FF_ERR_ARG;
+  const int64_t keys = fit_bin_keys(*f);
+  if (keys < 1 || keys > (int64_t(1) << 30)) return FF_ERR_UNSUPPORTED;
+  return fit_bin_workspace_bytes(*f, n, out_dim);
+}
+
+int ff_field_fit_step_binned(const FFField* f, const void* basis, const void* coeff, const FFMlp* m, const float* x,
+                             const float* target, int64_t n, int32_t loss_kind, float loss_scale, float* loss_sum,
+                             float* grad_basis, float* grad_coeff_grid, const FFMlpGrad* g, void* workspace,
+                             int64_t workspace_bytes, void* stream) {
+  int rc = validate_fused(f, basis, coeff, m, x, n);
+  if (rc) return rc;
+  if (n > 0 && !target) return set_error(FF_ERR_ARG, "target is NULL");
+  if (loss_kind != FF_LOSS_L1 && loss_kind != FF_LOSS_MSE) return set_error(FF_ERR_ARG, "loss_kind must be L1 or MSE");
+  if (!grad_basis || !grad_coeff_grid || !aligned(grad_basis, 16) || !aligned(grad_coeff_grid, 16))
+    return set_error(FF_ERR_ARG, "grid gradient buffers must be non-NULL and 16-byte aligned");
+  const int64_t need = ff_field_fit_binned_workspace_bytes(f, n, m->out_dim);
+  if (need < 0) return set_error((int)need, "coefficient grid too large to bin by cell");
+  if (n > 0 && (!workspace || workspace_bytes < need))
+    return set_error(FF_ERR_SIZE, "workspace smaller than ff_field_fit_binned_workspace_bytes");
+  if (!aligned(workspace, 256)) return set_error(FF_ERR_ALIGN, "workspace must be 256-byte aligned");
+  FFMlpGrad none = {};
+  return cuda_status(launch_fused_fit_binned(*f, basis, coeff, *m, x, target, n, loss_kind, loss_scale, loss_sum,
+                                             grad_basis, grad_coeff_grid, g ? *g : none, workspace,
+                                             (cudaStream_t)stream),
+                     "ff_field_fit_step_binned launch");
+}
+
 int ff_march_count(const FFRender* r, const float* rays, const float* jitter, int64_t n_rays, int32_t* counts,
                    float* t_min, void* stream) {
   int rc = validate_render(r, rays, n_rays);

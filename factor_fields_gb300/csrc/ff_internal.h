@@ -43,6 +43,17 @@ cudaError_t launch_fused_fit(const FFField& f, const void* basis, const void* co
                              float* loss_sum, float* grad_basis, float* grad_coeff, const FFMlpGrad& g,
                              cudaStream_t st);
 
+cudaError_t launch_fused_fit_binned(const FFField& f, const void* basis, const void* coeff, const FFMlp& m,
+                                    const float* x, const float* target, int64_t n, int loss_kind, float loss_scale,
+                                    float* loss_sum, float* grad_basis, float* grad_coeff, const FFMlpGrad& g,
+                                    void* workspace, cudaStream_t st);
+
+// fit_bin_kernels.cu
+int64_t fit_bin_keys(const FFField& f);
+int64_t fit_bin_workspace_bytes(const FFField& f, int64_t n, int out_dim);
+cudaError_t launch_fit_bin(const FFField& f, const float* x, const float* target, int out_dim, int64_t n,
+                           void* workspace, const float** xs_out, const float** ts_out, cudaStream_t st);
+
 // render_kernels.cu
 int64_t scan_workspace_bytes(int64_t n);
 cudaError_t launch_march_count(const FFRender& r, const float* rays, const float* jitter, int64_t n, int32_t* counts,

@@ -1,0 +1,31 @@
+// Fused field + MLP head: the fit step on a batch binned by coefficient cell
+// (ff_field_fit_step_binned): binning (fit_bin_kernels.cu), then the kFitBinned kernel.
+#include "fused_impl.cuh"
+
+namespace ffgb {
+
+cudaError_t launch_fused_fit_binned(const FFField& f, const void* basis, const void* coeff, const FFMlp& m,
+                                    const float* x, const float* target, int64_t n, int loss_kind, float loss_scale,
+                                    float* loss_sum, float* grad_basis, float* grad_coeff, const FFMlpGrad& g,
+                                    void* workspace, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  const float *xs = nullptr, *ts = nullptr;
+  cudaError_t e = launch_fit_bin(f, x, target, m.out_dim, n, workspace, &xs, &ts, st);
+  if (e != cudaSuccess) return e;
+  if (f.param_dtype != FF_BF16)  // float32 grids: the per-point fit on the binned batch
+    return launch_fused_fit(f, basis, coeff, m, xs, ts, n, loss_kind, loss_scale, loss_sum, grad_basis, grad_coeff, g,
+                            st);
+  FusedArgs a = make_args(f, basis, coeff, m, xs, n);
+  a.target = ts;
+  a.loss_kind = loss_kind;
+  a.loss_scale = loss_scale;
+  a.loss_sum = loss_sum;
+  a.grad_basis = grad_basis;
+  a.grad_coeff = grad_coeff;
+  a.grad_w0 = g.weight[0];
+  a.grad_b0 = g.bias[0];
+  a.grad_w1 = g.weight[1];
+  return dispatch_bf16<kFitBinned>(a, st);
+}
+
+}  // namespace ffgb

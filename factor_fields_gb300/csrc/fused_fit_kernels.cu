@@ -1,0 +1,23 @@
+// Fused field + MLP head: the fit step (ff_field_fit_step).
+#include "fused_impl.cuh"
+
+namespace ffgb {
+
+cudaError_t launch_fused_fit(const FFField& f, const void* basis, const void* coeff, const FFMlp& m, const float* x,
+                             const float* target, int64_t n, int loss_kind, float loss_scale, float* loss_sum,
+                             float* grad_basis, float* grad_coeff, const FFMlpGrad& g, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  FusedArgs a = make_args(f, basis, coeff, m, x, n);
+  a.target = target;
+  a.loss_kind = loss_kind;
+  a.loss_scale = loss_scale;
+  a.loss_sum = loss_sum;
+  a.grad_basis = grad_basis;
+  a.grad_coeff = grad_coeff;
+  a.grad_w0 = g.weight[0];
+  a.grad_b0 = g.bias[0];
+  a.grad_w1 = g.weight[1];
+  return dispatch<kFit>(a, st);
+}
+
+}  // namespace ffgb

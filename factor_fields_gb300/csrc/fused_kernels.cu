@@ -1,569 +1,7 @@
-// Fused field + MLP head: the "faster form" beside the drop-in kernels.
-//
-// One persistent launch per batch does, for every point, what the reference spreads over
-// 6+1 grid_sample launches, a product, two nn.Linear layers, the loss and their backward
-// (models/FactorFields.py:11-33, 425-527, 113-159 and autograd):
-//
-//   gather   division-free per-level mapping, bi/trilinear basis gathers (one vector load per
-//            corner and level) and the 18-channel coefficient gather (16-byte loads), in a
-//            thread-per-point layout; basis * coeff -> a float32 feature tile in shared memory
-//   forward  H = relu(X W0^T + b0), O = H W1^T on tensor cores: mma.sync m16n8k16 BF16 with
-//            FP32 accumulation, 32 points per warp. X enters layer 0 as a BF16 pair hi + lo
-//            (two MMAs) so H and the ReLU mask keep ~16 mantissa bits of the float32 features.
-//   loss     FIT: dO = d(mean L1 or MSE)/dO against the targets; BWD: dO given
-//   backward dH = (dO W1) * [H > 0], dX = dH W0 on tensor cores. Weight gradients are reduced
-//            block-wide: after a barrier each warp computes its 16-row slice of
-//            dW0 = dH^T [X | 1] over the block's 128 points (ldmatrix.trans operands), keeping
-//            the slice in registers for the whole launch; the constant-1 column yields the
-//            bias gradient. dW1 comes from registers when out_dim == 1, else from a second
-//            block-wide MMA over H^T dO. One global atomic per weight entry per block at exit.
-//   scatter dL/dbasis = dX * coeff, dL/dcoeff = dX * basis with float4 / float2 atomics into
-//            the float32 gradient grids (interpolation weights recomputed, never stored).
-//
-// Level structure is compile-time: basis_dims = [4, 4, 4, 2, 2, 2] (sum 18), which keeps each
-// point's 18 basis and 18 coefficient values in registers between the gather and the scatter.
-// MLP: in 18 -> 64 (bias, ReLU) -> out <= 32 (no bias): MLPMixer with num_layers = 2.
-#include <utility>
-
-#include "ff_common.cuh"
-#include "ff_internal.h"
-#include "mma_util.cuh"
+// Fused field + MLP head: support check and the forward (ff_field_mlp_forward).
+#include "fused_impl.cuh"
 
 namespace ffgb {
-
-namespace {
-
-constexpr int kWarps = 4;
-constexpr int kThreads = kWarps * 32;
-constexpr int kTile = kThreads;  // points per block iteration
-constexpr int kHid = 64;
-constexpr int kF = 18;    // sum(basis_dims)
-constexpr int kNtIn = 3;  // n-tiles of 8 covering the 18 input features (+ the constant-1 column)
-constexpr int kLevelC[6] = {4, 4, 4, 2, 2, 2};
-constexpr int kLevelOff[6] = {0, 4, 8, 12, 14, 16};
-
-// Shared-memory row strides (elements).
-constexpr int LD_XF = 20;   // float32 feature tile [32 pts][20]: 18 features, 1.0, 0
-constexpr int LD_H = 72;    // BF16 H / dH tiles [32 pts][64]
-constexpr int LD_W0 = 40;   // W0 [64 hidden][32 in] BF16
-constexpr int LD_W0T = 72;  // W0^T [32 in][64 hidden]
-constexpr int LD_W1 = 72;   // W1 [32 out][64 hidden]
-constexpr int LD_W1T = 40;  // W1^T [64 hidden][32 out]
-
-template <int OUTT>
-constexpr int ld_do() { return OUTT == 2 ? 24 : 40; }
-
-enum { kFwd = 0, kBwd = 1, kFit = 2 };
-
-struct FusedArgs {
-  FFField f;
-  const void* basis;
-  const void* coeff;
-  const float* w0;  // [64, 18]
-  const float* b0;  // [64]
-  const float* w1;  // [out, 64]
-  int out_dim;
-  const float* x;
-  int64_t n;
-  float* out;             // kFwd: [n, out]
-  const float* grad_out;  // kBwd: [n, out]
-  const float* target;    // kFit: [n, out]
-  int loss_kind;
-  float loss_scale;
-  float* loss_sum;
-  float* grad_basis;
-  float* grad_coeff;
-  float* grad_w0;
-  float* grad_b0;
-  float* grad_w1;
-};
-
-// A-fragment register pair (hi, lo) for two consecutive float32 features of the X tile;
-// columns at or past LD_XF read as zero.
-__device__ __forceinline__ void x_pair(const float* xf, int row, int col, uint32_t& hi, uint32_t& lo) {
-  if (col < LD_XF) {
-    const float2 v = *reinterpret_cast<const float2*>(xf + row * LD_XF + col);
-    hi = pack_bf16(v.x, v.y);
-    lo = pack_bf16(v.x - bf_lo(hi), v.y - bf_hi(hi));
-  } else {
-    hi = lo = 0u;
-  }
-}
-
-template <typename Fn, int... Ls>
-__device__ __forceinline__ void for_levels(std::integer_sequence<int, Ls...>, Fn&& fn) {
-  (fn(std::integral_constant<int, Ls>{}), ...);
-}
-
-// ---- shared memory layout -----------------------------------------------------------------
-
-struct Smem {
-  __nv_bfloat16 *w0, *w0t, *w1, *w1t;
-  float* b0;
-  float* xf;            // [kWarps][32][LD_XF]
-  __nv_bfloat16* dh;    // [kWarps][32][LD_H]
-  __nv_bfloat16* h;     // [kWarps][32][LD_H]        (out_dim > 8)
-  __nv_bfloat16* dout;  // [kWarps][32][ld_do]       (out_dim > 8)
-};
-
-template <int MODE, int OUTT>
-__host__ __device__ constexpr int64_t smem_bytes() {
-  int64_t b = 64 * LD_W0 * 2 + 32 * LD_W0T * 2 + 32 * LD_W1 * 2 + 64 * LD_W1T * 2 + 64 * 4;
-  b += (int64_t)kWarps * 32 * LD_XF * 4;
-  if (MODE != kFwd) b += (int64_t)kWarps * 32 * LD_H * 2;
-  if (MODE != kFwd && OUTT > 1) b += (int64_t)kWarps * 32 * (LD_H + ld_do<OUTT>()) * 2;
-  return b;
-}
-
-template <int MODE, int OUTT>
-__device__ __forceinline__ Smem carve(unsigned char* base) {
-  Smem s;
-  unsigned char* p = base;
-  auto take = [&](int64_t bytes) { unsigned char* r = p; p += (bytes + 15) & ~int64_t(15); return r; };
-  s.w0 = (__nv_bfloat16*)take(64 * LD_W0 * 2);
-  s.w0t = (__nv_bfloat16*)take(32 * LD_W0T * 2);
-  s.w1 = (__nv_bfloat16*)take(32 * LD_W1 * 2);
-  s.w1t = (__nv_bfloat16*)take(64 * LD_W1T * 2);
-  s.b0 = (float*)take(64 * 4);
-  s.xf = (float*)take((int64_t)kWarps * 32 * LD_XF * 4);
-  s.dh = s.h = s.dout = nullptr;
-  if (MODE != kFwd) s.dh = (__nv_bfloat16*)take((int64_t)kWarps * 32 * LD_H * 2);
-  if (MODE != kFwd && OUTT > 1) {
-    s.h = (__nv_bfloat16*)take((int64_t)kWarps * 32 * LD_H * 2);
-    s.dout = (__nv_bfloat16*)take((int64_t)kWarps * 32 * ld_do<OUTT>() * 2);
-  }
-  return s;
-}
-
-// ---- the kernel -------------------------------------------------------------------------
-
-template <int MODE, int BD, int CD, int OUTT, typename T>
-__global__ void __launch_bounds__(kThreads, 3) fused_field_mlp_kernel(const FusedArgs a) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, g = lane >> 2, t = lane & 3;
-  const Smem s = carve<MODE, OUTT>(smem_raw);
-  const FFField& f = a.f;
-  const int out = a.out_dim;
-  const T* basis = static_cast<const T*>(a.basis);
-  const T* coeff = static_cast<const T*>(a.coeff);
-  float* xf = s.xf + warp * 32 * LD_XF;  // this warp's feature tile
-
-  // stage the MLP weights as BF16 in both orientations
-  for (int e = tid; e < 64 * 32; e += kThreads) {
-    const int j = e >> 5, k = e & 31;
-    const __nv_bfloat16 v = __float2bfloat16_rn(k < kF ? a.w0[j * kF + k] : 0.f);
-    s.w0[j * LD_W0 + k] = v;
-    s.w0t[k * LD_W0T + j] = v;
-  }
-  for (int e = tid; e < 32 * 64; e += kThreads) {
-    const int o = e >> 6, hh = e & 63;
-    const __nv_bfloat16 v = __float2bfloat16_rn(o < out ? a.w1[o * kHid + hh] : 0.f);
-    s.w1[o * LD_W1 + hh] = v;
-    s.w1t[hh * LD_W1T + o] = v;
-  }
-  for (int j = tid; j < 64; j += kThreads) s.b0[j] = a.b0[j];
-  __syncthreads();
-
-  float loss_acc = 0.f;
-  float acc_w0[kNtIn][4];                        // dW0 slice: hidden rows [16*warp, +16), cols 0..23
-  float acc_w1[OUTT == 1 ? 8 : 1][2];            // out_dim <= 8: per-lane H * dO partial sums
-  float acc_w1t[OUTT > 1 ? OUTT : 1][4];         // out_dim > 8: dW1^T slice
-#pragma unroll
-  for (int nt = 0; nt < kNtIn; ++nt) acc_w0[nt][0] = acc_w0[nt][1] = acc_w0[nt][2] = acc_w0[nt][3] = 0.f;
-#pragma unroll
-  for (int nt = 0; nt < (OUTT == 1 ? 8 : 1); ++nt) acc_w1[nt][0] = acc_w1[nt][1] = 0.f;
-#pragma unroll
-  for (int nt = 0; nt < (OUTT > 1 ? OUTT : 1); ++nt) acc_w1t[nt][0] = acc_w1t[nt][1] = acc_w1t[nt][2] = acc_w1t[nt][3] = 0.f;
-
-  for (int64_t base = (int64_t)blockIdx.x * kTile; base < a.n; base += (int64_t)gridDim.x * kTile) {
-    const int64_t i = base + warp * 32 + lane;
-    const bool valid = i < a.n;
-    float bv[kF], cv[kF];
-    float p[CD];
-    // ---------------- gather ----------------
-    if (valid) {
-#pragma unroll
-      for (int k = 0; k < CD; ++k) p[k] = a.x[i * CD + k];
-      Corners<CD> cc;
-      coeff_corners<CD>(f, p, cc);
-      gather_coeff18<CD>(coeff, f.coeff_stride, cc, cv);
-      for_levels(std::make_integer_sequence<int, 6>{}, [&](auto lc) {
-        constexpr int l = decltype(lc)::value;
-        Corners<BD> bc;
-        basis_corners_fast<BD>(f, l, p, bc);
-        constexpr int C = kLevelC[l], OFF = kLevelOff[l];
-        gather<C, BD>(basis + f.level_offset[l], f.level_stride[l], 0, bc, bv + OFF);
-      });
-    } else {
-#pragma unroll
-      for (int k = 0; k < kF; ++k) bv[k] = cv[k] = 0.f;
-    }
-    {
-      float* xr = xf + lane * LD_XF;
-#pragma unroll
-      for (int k = 0; k < kF; k += 2)
-        *reinterpret_cast<float2*>(xr + k) = make_float2(bv[k] * cv[k], bv[k + 1] * cv[k + 1]);
-      *reinterpret_cast<float2*>(xr + kF) = make_float2(valid ? 1.f : 0.f, 0.f);
-    }
-    __syncwarp();
-
-    float dx[2][kNtIn][4];
-#pragma unroll
-    for (int mt = 0; mt < 2; ++mt) {
-      const int r0 = 16 * mt + g, r1 = r0 + 8;
-      // ---------------- layer 0: H = relu(X W0^T + b0), X = hi + lo ----------------
-      uint32_t ha[4][4];  // relu(H) as BF16 A fragments over the 64 hidden units (hi part)
-      // layer 1 (O = H W1^T) accumulates per half of the hidden units, H as hi + lo
-      float oc[OUTT][4];
-#pragma unroll
-      for (int nt = 0; nt < OUTT; ++nt) oc[nt][0] = oc[nt][1] = oc[nt][2] = oc[nt][3] = 0.f;
-#pragma unroll
-      for (int half = 0; half < 2; ++half) {  // hidden units [32*half, 32*half + 32)
-        float hc[4][4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const int nt = 4 * half + q;
-          const float bl = s.b0[nt * 8 + 2 * t], bh = s.b0[nt * 8 + 2 * t + 1];
-          hc[q][0] = bl; hc[q][1] = bh; hc[q][2] = bl; hc[q][3] = bh;
-        }
-#pragma unroll
-        for (int ks = 0; ks < 2; ++ks) {
-          uint32_t ah[4], al[4];
-          x_pair(xf, r0, 16 * ks + 2 * t, ah[0], al[0]);
-          x_pair(xf, r1, 16 * ks + 2 * t, ah[1], al[1]);
-          x_pair(xf, r0, 16 * ks + 2 * t + 8, ah[2], al[2]);
-          x_pair(xf, r1, 16 * ks + 2 * t + 8, ah[3], al[3]);
-#pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            const __nv_bfloat16* wp = s.w0 + ((4 * half + q) * 8 + g) * LD_W0 + 16 * ks + 2 * t;
-            const uint32_t b0 = lds32(wp), b1 = lds32(wp + 8);
-            mma_bf16(hc[q], al, b0, b1);
-            mma_bf16(hc[q], ah, b0, b1);
-          }
-        }
-#pragma unroll
-        for (int kk = 0; kk < 2; ++kk) {
-          const float* c0 = hc[2 * kk];
-          const float* c1 = hc[2 * kk + 1];
-          const int ks = 2 * half + kk;
-          uint32_t* hk = ha[ks];
-          uint32_t hl[4];
-          split_pair(fmaxf(c0[0], 0.f), fmaxf(c0[1], 0.f), hk[0], hl[0]);
-          split_pair(fmaxf(c0[2], 0.f), fmaxf(c0[3], 0.f), hk[1], hl[1]);
-          split_pair(fmaxf(c1[0], 0.f), fmaxf(c1[1], 0.f), hk[2], hl[2]);
-          split_pair(fmaxf(c1[2], 0.f), fmaxf(c1[3], 0.f), hk[3], hl[3]);
-#pragma unroll
-          for (int nt = 0; nt < OUTT; ++nt) {
-            const __nv_bfloat16* wp = s.w1 + (nt * 8 + g) * LD_W1 + 16 * ks + 2 * t;
-            const uint32_t b0 = lds32(wp), b1 = lds32(wp + 8);
-            mma_bf16(oc[nt], hl, b0, b1);
-            mma_bf16(oc[nt], hk, b0, b1);
-          }
-        }
-      }
-      if constexpr (MODE != kFwd && OUTT > 1) {
-        __nv_bfloat16* hw = s.h + warp * 32 * LD_H;
-#pragma unroll
-        for (int ks = 0; ks < 4; ++ks) {
-          __nv_bfloat16* p0 = hw + r0 * LD_H + 16 * ks + 2 * t;
-          __nv_bfloat16* p1 = hw + r1 * LD_H + 16 * ks + 2 * t;
-          sts32(p0, ha[ks][0]); sts32(p1, ha[ks][1]); sts32(p0 + 8, ha[ks][2]); sts32(p1 + 8, ha[ks][3]);
-        }
-      }
-      const int64_t row0 = base + warp * 32 + r0, row1 = row0 + 8;
-      if constexpr (MODE == kFwd) {
-#pragma unroll
-        for (int nt = 0; nt < OUTT; ++nt) {
-          const int c0 = nt * 8 + 2 * t;
-#pragma unroll
-          for (int j = 0; j < 2; ++j) {
-            if (c0 + j < out) {
-              if (row0 < a.n) a.out[row0 * out + c0 + j] = oc[nt][j];
-              if (row1 < a.n) a.out[row1 * out + c0 + j] = oc[nt][2 + j];
-            }
-          }
-        }
-      } else {
-        // ---------------- dO ----------------
-        float dc[OUTT][4];
-#pragma unroll
-        for (int nt = 0; nt < OUTT; ++nt) {
-          const int c0 = nt * 8 + 2 * t;
-#pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            const int64_t row = (q < 2) ? row0 : row1;
-            const int col = c0 + (q & 1);
-            float d = 0.f;
-            if (row < a.n && col < out) {
-              if constexpr (MODE == kFit) {
-                const float err = oc[nt][q] - a.target[row * out + col];
-                if (a.loss_kind == FF_LOSS_L1) {
-                  loss_acc += fabsf(err);
-                  d = (err > 0.f ? 1.f : (err < 0.f ? -1.f : 0.f)) * a.loss_scale;
-                } else {
-                  loss_acc += err * err;
-                  d = 2.f * err * a.loss_scale;
-                }
-              } else {
-                d = a.grad_out[row * out + col];
-              }
-            }
-            dc[nt][q] = d;
-          }
-        }
-        if constexpr (OUTT == 1) {
-          // out_dim == 1: dW1[0][j] = sum over points of H[pt][j] * dO[pt]. dO of rows r0 / r1
-          // sits in the quad's t == 0 lane; each lane accumulates its 16 hidden columns.
-          const float d0 = __shfl_sync(0xffffffffu, dc[0][0], lane & ~3);
-          const float d1 = __shfl_sync(0xffffffffu, dc[0][2], lane & ~3);
-#pragma unroll
-          for (int nt = 0; nt < 8; ++nt) {
-            const uint32_t h0 = ha[nt >> 1][(nt & 1) * 2], h1 = ha[nt >> 1][(nt & 1) * 2 + 1];
-            acc_w1[nt][0] += bf_lo(h0) * d0 + bf_lo(h1) * d1;
-            acc_w1[nt][1] += bf_hi(h0) * d0 + bf_hi(h1) * d1;
-          }
-        } else {
-          __nv_bfloat16* dw = s.dout + warp * 32 * ld_do<OUTT>();
-#pragma unroll
-          for (int nt = 0; nt < OUTT; ++nt) {
-            const int c0 = nt * 8 + 2 * t;
-            sts32(dw + r0 * ld_do<OUTT>() + c0, pack_bf16(dc[nt][0], dc[nt][1]));
-            sts32(dw + r1 * ld_do<OUTT>() + c0, pack_bf16(dc[nt][2], dc[nt][3]));
-          }
-        }
-        // ---------------- dH = (dO W1) * [H > 0], dX = dH W0 ----------------
-        // dO and dH enter their GEMMs as BF16 pairs hi + lo (two MMAs each), so the gradients
-        // keep ~16 mantissa bits through the sums over outputs and hidden units.
-        __nv_bfloat16* dhw = s.dh + warp * 32 * LD_H;
-#pragma unroll
-        for (int nt = 0; nt < kNtIn; ++nt) dx[mt][nt][0] = dx[mt][nt][1] = dx[mt][nt][2] = dx[mt][nt][3] = 0.f;
-#pragma unroll
-        for (int half = 0; half < 2; ++half) {
-          float dh[4][4];
-#pragma unroll
-          for (int q = 0; q < 4; ++q) dh[q][0] = dh[q][1] = dh[q][2] = dh[q][3] = 0.f;
-#pragma unroll
-          for (int ks = 0; ks < (OUTT + 1) / 2; ++ks) {
-            uint32_t af[4], al[4];
-            split_pair(dc[2 * ks][0], dc[2 * ks][1], af[0], al[0]);
-            split_pair(dc[2 * ks][2], dc[2 * ks][3], af[1], al[1]);
-            if (2 * ks + 1 < OUTT) {
-              split_pair(dc[2 * ks + 1][0], dc[2 * ks + 1][1], af[2], al[2]);
-              split_pair(dc[2 * ks + 1][2], dc[2 * ks + 1][3], af[3], al[3]);
-            } else {
-              af[2] = af[3] = al[2] = al[3] = 0u;
-            }
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-              const __nv_bfloat16* wp = s.w1t + ((4 * half + q) * 8 + g) * LD_W1T + 16 * ks + 2 * t;
-              const uint32_t b0 = lds32(wp), b1 = lds32(wp + 8);
-              mma_bf16(dh[q], al, b0, b1);
-              mma_bf16(dh[q], af, b0, b1);
-            }
-          }
-#pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            const int nt = 4 * half + q;
-            const uint32_t h0 = ha[nt >> 1][(nt & 1) * 2], h1 = ha[nt >> 1][(nt & 1) * 2 + 1];
-            if (!(bf_lo(h0) > 0.f)) dh[q][0] = 0.f;
-            if (!(bf_hi(h0) > 0.f)) dh[q][1] = 0.f;
-            if (!(bf_lo(h1) > 0.f)) dh[q][2] = 0.f;
-            if (!(bf_hi(h1) > 0.f)) dh[q][3] = 0.f;
-          }
-#pragma unroll
-          for (int kk = 0; kk < 2; ++kk) {
-            uint32_t d[4], dl[4];
-            split_pair(dh[2 * kk][0], dh[2 * kk][1], d[0], dl[0]);
-            split_pair(dh[2 * kk][2], dh[2 * kk][3], d[1], dl[1]);
-            split_pair(dh[2 * kk + 1][0], dh[2 * kk + 1][1], d[2], dl[2]);
-            split_pair(dh[2 * kk + 1][2], dh[2 * kk + 1][3], d[3], dl[3]);
-            const int ks = 2 * half + kk;
-            __nv_bfloat16* p0 = dhw + r0 * LD_H + 16 * ks + 2 * t;
-            __nv_bfloat16* p1 = dhw + r1 * LD_H + 16 * ks + 2 * t;
-            sts32(p0, d[0]); sts32(p1, d[1]); sts32(p0 + 8, d[2]); sts32(p1 + 8, d[3]);
-            // dX += dH[:, 16 ks .. 16 ks + 15] W0[16 ks .. 16 ks + 15, :]
-#pragma unroll
-            for (int nt = 0; nt < kNtIn; ++nt) {
-              const __nv_bfloat16* wp = s.w0t + (nt * 8 + g) * LD_W0T + 16 * ks + 2 * t;
-              const uint32_t b0 = lds32(wp), b1 = lds32(wp + 8);
-              mma_bf16(dx[mt][nt], dl, b0, b1);
-              mma_bf16(dx[mt][nt], d, b0, b1);
-            }
-          }
-        }
-      }
-    }
-    if constexpr (MODE == kFwd) {
-      __syncwarp();
-      continue;
-    } else {
-      __syncthreads();  // every warp's X and dH (and H, dO) tiles are complete
-      // ---------------- block-wide weight gradients ----------------
-      // dW0[16*warp + .., 0..23] += dH^T [X | 1] over the block's 128 points: 8 k-steps of 16.
-#pragma unroll 2
-      for (int kk = 0; kk < 8; ++kk) {
-        const int src = kk >> 1, h16 = (kk & 1) * 16;
-        const __nv_bfloat16* dhs = s.dh + src * 32 * LD_H;
-        const float* xs = s.xf + src * 32 * LD_XF;
-        uint32_t af[4];
-        ldsm_x4_t(af, dhs + (h16 + (lane & 7) + (lane >> 4) * 8) * LD_H + 16 * warp + ((lane >> 3) & 1) * 8);
-#pragma unroll
-        for (int nt = 0; nt < kNtIn; ++nt) {
-          const int col = nt * 8 + g;
-          uint32_t b0 = 0u, b1 = 0u;
-          if (col < LD_XF) {
-            b0 = pack_bf16(xs[(h16 + 2 * t) * LD_XF + col], xs[(h16 + 2 * t + 1) * LD_XF + col]);
-            b1 = pack_bf16(xs[(h16 + 2 * t + 8) * LD_XF + col], xs[(h16 + 2 * t + 9) * LD_XF + col]);
-          }
-          mma_bf16(acc_w0[nt], af, b0, b1);
-        }
-        if constexpr (OUTT > 1) {
-          const __nv_bfloat16* hs = s.h + src * 32 * LD_H;
-          const __nv_bfloat16* ds = s.dout + src * 32 * ld_do<OUTT>();
-          uint32_t ah[4];
-          ldsm_x4_t(ah, hs + (h16 + (lane & 7) + (lane >> 4) * 8) * LD_H + 16 * warp + ((lane >> 3) & 1) * 8);
-#pragma unroll
-          for (int nt = 0; nt < OUTT; ++nt) {
-            uint32_t bf[2];
-            ldsm_x2_t(bf, ds + (h16 + (lane & 7) + ((lane >> 3) & 1) * 8) * ld_do<OUTT>() + nt * 8);
-            mma_bf16(acc_w1t[nt], ah, bf[0], bf[1]);
-          }
-        }
-      }
-      __syncthreads();  // tiles consumed: the feature tile can now hold dX
-#pragma unroll
-      for (int mt = 0; mt < 2; ++mt) {
-#pragma unroll
-        for (int nt = 0; nt < kNtIn; ++nt) {
-          const int c0 = nt * 8 + 2 * t;
-          if (c0 < kF) {
-            *reinterpret_cast<float2*>(xf + (16 * mt + g) * LD_XF + c0) = make_float2(dx[mt][nt][0], dx[mt][nt][1]);
-            *reinterpret_cast<float2*>(xf + (16 * mt + g + 8) * LD_XF + c0) = make_float2(dx[mt][nt][2], dx[mt][nt][3]);
-          }
-        }
-      }
-      __syncwarp();
-      // ---------------- scatter dL/dbasis = dX * coeff, dL/dcoeff = dX * basis ----------------
-      if (valid) {
-        float gc[kF];
-        const float* xr = xf + lane * LD_XF;
-#pragma unroll
-        for (int k = 0; k < kF; ++k) {
-          const float gx = xr[k];
-          gc[k] = gx * bv[k];
-          bv[k] = gx * cv[k];  // bv now holds dL/dbasis
-        }
-        Corners<CD> cc;
-        coeff_corners<CD>(f, p, cc);
-        scatter_coeff18<CD>(a.grad_coeff, f.coeff_stride, cc, gc);
-        for_levels(std::make_integer_sequence<int, 6>{}, [&](auto lc) {
-          constexpr int l = decltype(lc)::value;
-          Corners<BD> bc;
-          basis_corners_fast<BD>(f, l, p, bc);
-          constexpr int C = kLevelC[l], OFF = kLevelOff[l];
-          scatter<C, BD>(a.grad_basis + f.level_offset[l], f.level_stride[l], 0, bc, bv + OFF);
-        });
-      }
-      __syncwarp();
-    }
-  }
-
-  if constexpr (MODE != kFwd) {
-    if constexpr (MODE == kFit) {
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) loss_acc += __shfl_xor_sync(0xffffffffu, loss_acc, o);
-      if (lane == 0 && a.loss_sum) atomicAdd(a.loss_sum, loss_acc);
-    }
-    // dW0 slice (rows 16*warp + g, + 8; cols 8*nt + 2t, + 1): features -> grad_w0, column 18 -> grad_b0
-#pragma unroll
-    for (int nt = 0; nt < kNtIn; ++nt) {
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const int row = 16 * warp + g + (q >= 2 ? 8 : 0);
-        const int col = nt * 8 + 2 * t + (q & 1);
-        if (col < kF) {
-          if (a.grad_w0) atomicAdd(a.grad_w0 + row * kF + col, acc_w0[nt][q]);
-        } else if (col == kF) {
-          if (a.grad_b0) atomicAdd(a.grad_b0 + row, acc_w0[nt][q]);
-        }
-      }
-    }
-    if constexpr (OUTT == 1) {
-      // out_dim <= 8 with one n-tile: column 0 accumulated in registers (out_dim == 1)
-#pragma unroll
-      for (int nt = 0; nt < 8; ++nt) {
-#pragma unroll
-        for (int j = 0; j < 2; ++j) {
-          float v = acc_w1[nt][j];
-          v += __shfl_xor_sync(0xffffffffu, v, 4);
-          v += __shfl_xor_sync(0xffffffffu, v, 8);
-          v += __shfl_xor_sync(0xffffffffu, v, 16);
-          if (g == 0 && a.grad_w1) atomicAdd(a.grad_w1 + nt * 8 + 2 * t + j, v);
-        }
-      }
-    } else {
-#pragma unroll
-      for (int nt = 0; nt < OUTT; ++nt) {
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const int hid = 16 * warp + g + (q >= 2 ? 8 : 0);
-          const int o = nt * 8 + 2 * t + (q & 1);
-          if (o < out && a.grad_w1) atomicAdd(a.grad_w1 + o * kHid + hid, acc_w1t[nt][q]);
-        }
-      }
-    }
-  }
-}
-
-template <int MODE, int BD, int CD, int OUTT, typename T>
-cudaError_t launch_one(const FusedArgs& a, cudaStream_t st) {
-  constexpr int64_t smem = smem_bytes<MODE, OUTT>();
-  auto kern = fused_field_mlp_kernel<MODE, BD, CD, OUTT, T>;
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
-  int per_sm = 1;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, smem);
-  if (e != cudaSuccess || per_sm < 1) per_sm = 1;
-  const int64_t tiles = ceil_div(a.n, kTile);
-  const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>(tiles, (int64_t)sm_count() * per_sm));
-  kern<<<blocks, kThreads, smem, st>>>(a);
-  return cudaGetLastError();
-}
-
-template <int MODE, int OUTT, typename T>
-cudaError_t dispatch_dims(const FusedArgs& a, cudaStream_t st) {
-  const FFField& f = a.f;
-  if (f.basis_dim == 2 && f.coord_dim == 2) return launch_one<MODE, 2, 2, OUTT, T>(a, st);
-  if (f.basis_dim == 3 && f.coord_dim == 3) return launch_one<MODE, 3, 3, OUTT, T>(a, st);
-  if (f.basis_dim == 2 && f.coord_dim == 3) return launch_one<MODE, 2, 3, OUTT, T>(a, st);
-  return cudaErrorInvalidValue;
-}
-
-template <int MODE>
-cudaError_t dispatch(const FusedArgs& a, cudaStream_t st) {
-  const bool bf = a.f.param_dtype == FF_BF16;
-  const int o = a.out_dim;
-  if (o == 1) return bf ? dispatch_dims<MODE, 1, __nv_bfloat16>(a, st) : dispatch_dims<MODE, 1, float>(a, st);
-  if (o <= 16) return bf ? dispatch_dims<MODE, 2, __nv_bfloat16>(a, st) : dispatch_dims<MODE, 2, float>(a, st);
-  return bf ? dispatch_dims<MODE, 4, __nv_bfloat16>(a, st) : dispatch_dims<MODE, 4, float>(a, st);
-}
-
-FusedArgs make_args(const FFField& f, const void* basis, const void* coeff, const FFMlp& m, const float* x,
-                    int64_t n) {
-  FusedArgs a = {};
-  a.f = f;
-  a.basis = basis;
-  a.coeff = coeff;
-  a.w0 = m.weight[0];
-  a.b0 = m.bias[0];
-  a.w1 = m.weight[1];
-  a.out_dim = m.out_dim;
-  a.x = x;
-  a.n = n;
-  return a;
-}
-
-}  // namespace
 
 const char* fused_unsupported(const FFField& f, const FFMlp& m) {
   if (f.n_levels != 6) return "the fused path needs 6 basis levels with basis_dims [4,4,4,2,2,2]";
@@ -584,37 +22,6 @@ cudaError_t launch_fused_forward(const FFField& f, const void* basis, const void
   FusedArgs a = make_args(f, basis, coeff, m, x, n);
   a.out = out;
   return dispatch<kFwd>(a, st);
-}
-
-cudaError_t launch_fused_backward(const FFField& f, const void* basis, const void* coeff, const FFMlp& m,
-                                  const float* x, int64_t n, const float* grad_out, float* grad_basis,
-                                  float* grad_coeff, const FFMlpGrad& g, cudaStream_t st) {
-  if (n == 0) return cudaSuccess;
-  FusedArgs a = make_args(f, basis, coeff, m, x, n);
-  a.grad_out = grad_out;
-  a.grad_basis = grad_basis;
-  a.grad_coeff = grad_coeff;
-  a.grad_w0 = g.weight[0];
-  a.grad_b0 = g.bias[0];
-  a.grad_w1 = g.weight[1];
-  return dispatch<kBwd>(a, st);
-}
-
-cudaError_t launch_fused_fit(const FFField& f, const void* basis, const void* coeff, const FFMlp& m, const float* x,
-                             const float* target, int64_t n, int loss_kind, float loss_scale, float* loss_sum,
-                             float* grad_basis, float* grad_coeff, const FFMlpGrad& g, cudaStream_t st) {
-  if (n == 0) return cudaSuccess;
-  FusedArgs a = make_args(f, basis, coeff, m, x, n);
-  a.target = target;
-  a.loss_kind = loss_kind;
-  a.loss_scale = loss_scale;
-  a.loss_sum = loss_sum;
-  a.grad_basis = grad_basis;
-  a.grad_coeff = grad_coeff;
-  a.grad_w0 = g.weight[0];
-  a.grad_b0 = g.bias[0];
-  a.grad_w1 = g.weight[1];
-  return dispatch<kFit>(a, st);
 }
 
 }  // namespace ffgb

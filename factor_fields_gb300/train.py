@@ -92,16 +92,27 @@ class FieldFitRunner:
     """One fwd+bwd regression step of a FactorFields model on (points, targets).
 
     fused=True: ONE ff_field_fit_step launch (gathers, BF16 tensor-core MLP, loss, backward,
-    scatter) after zeroing the gradient buffers. fused=False: the drop-in kernels launched one
-    after the other (field fwd, MLP fwd, MLP bwd, field bwd) with the loss in PyTorch.
-    Gradients land in the model's .grad buffers; step() returns the mean loss as a 0-d device
-    tensor (no host synchronisation)."""
+    scatter) after zeroing the gradient buffers; binned=True (the default with fused) runs
+    ff_field_fit_step_binned instead: the batch is binned by coefficient cell first so that the
+    coefficient gradients of points sharing a cell are summed on chip. fused=False: the drop-in
+    kernels launched one after the other (field fwd, MLP fwd, MLP bwd, field bwd) with the loss
+    in PyTorch. Gradients land in the model's .grad buffers; step() returns the mean loss as a
+    0-d device tensor (no host synchronisation)."""
 
-    def __init__(self, model, loss="l1", fused=True):
+    def __init__(self, model, loss="l1", fused=True, binned=None):
         if loss not in N.FF_LOSS:
             raise ValueError("loss must be 'l1' or 'mse'")
         self.m, self.loss, self.fused = model, loss, fused
-        if fused:
+        self.binned = fused if binned is None else bool(binned)
+        if self.binned and not fused:
+            raise ValueError("binned=True needs fused=True")
+        self._ws = None
+        if fused and self.binned:
+            self.path_name = ("fused, binned: ff_field_fit_step_binned per step (bin by coefficient cell, scan, "
+                              "permute, one fit launch; + gradient zeroing)")
+            self.dominant_kernel = "ff_field_fit_step_binned"
+            self.gathers_per_point = 1
+        elif fused:
             self.path_name = "fused: one ff_field_fit_step launch per step (+ gradient zeroing)"
             self.dominant_kernel = "ff_field_fit_step"
             self.gathers_per_point = 1
@@ -135,8 +146,11 @@ class FieldFitRunner:
         captured launches (gradient zeroing, the fit kernel, the loss scale) replay with one
         host call. The graph is captured on first use and re-captured when the batch shape or
         a parameter buffer changes."""
+        ws = 0
+        if self.fused and self.binned:  # the captured launches keep the workspace address
+            ws = self._workspace(self.m.descriptor(self.m._read_buffers()[2]), x.shape[0]).data_ptr()
         key = (tuple(x.shape), tuple(y.shape), self.m.basis_flat.data_ptr(), self.m.coeff_flat.data_ptr(),
-               self.m.precision)
+               self.m.precision, ws)
         if getattr(self, "_graph_key", None) != key:
             dev = self.m.basis_flat.device
             self._xs = torch.empty(x.shape, dtype=x.dtype, device=dev)
@@ -158,6 +172,15 @@ class FieldFitRunner:
         self._graph.replay()
         return self._graph_loss
 
+    def _workspace(self, desc, n):
+        """Device workspace of ff_field_fit_step_binned for n points, kept across steps."""
+        need = int(N.lib().ff_field_fit_binned_workspace_bytes(ctypes.byref(desc), n, self.m.linear_mat.out_dim))
+        if need < 0:
+            N.check(need, "ff_field_fit_binned_workspace_bytes")
+        if self._ws is None or self._ws.numel() < need:
+            self._ws = torch.empty(need, dtype=torch.uint8, device=self.m.basis_flat.device)
+        return self._ws
+
     def step(self, x, y, kernel_events=False):
         m = self.m
         self.zero_grad()
@@ -173,14 +196,20 @@ class FieldFitRunner:
             ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
         if self.fused:
             self.loss_buf.zero_()
+            if self.binned:
+                ws = self._workspace(desc, n)
             if ev:
                 ev[0].record()
-            N.call("ff_field_fit_step", ctypes.byref(desc), N.ptr(basis_r), N.ptr(coeff_r), ctypes.byref(mlp),
-                   N.ptr(x), N.ptr(y), n, N.FF_LOSS[self.loss], 1.0 / (n * m.linear_mat.out_dim),
-                   N.ptr(self.loss_buf), N.ptr(m.basis_flat.grad), N.ptr(m.coeff_flat.grad), ctypes.byref(g), st)
+            common = (ctypes.byref(desc), N.ptr(basis_r), N.ptr(coeff_r), ctypes.byref(mlp), N.ptr(x), N.ptr(y), n,
+                      N.FF_LOSS[self.loss], 1.0 / max(n * m.linear_mat.out_dim, 1), N.ptr(self.loss_buf),
+                      N.ptr(m.basis_flat.grad), N.ptr(m.coeff_flat.grad), ctypes.byref(g))
+            if self.binned:
+                N.call("ff_field_fit_step_binned", *common, N.ptr(ws), ws.numel(), st)
+            else:
+                N.call("ff_field_fit_step", *common, st)
             if ev:
                 ev[1].record()
-            loss = self.loss_buf[0] / (n * m.linear_mat.out_dim)
+            loss = self.loss_buf[0] / max(n * m.linear_mat.out_dim, 1)
             return ev if kernel_events else loss
         feats = torch.empty(n, m.n_feat, device=x.device)
         N.call("ff_field_forward", ctypes.byref(desc), N.ptr(basis_r), N.ptr(coeff_r), N.ptr(x), n, N.ptr(feats),

@@ -168,6 +168,18 @@ FF_API int ff_field_fit_step(const FFField* f, const void* basis, const void* co
                              float loss_scale, float* loss_sum, float* grad_basis, float* grad_coeff_grid,
                              const FFMlpGrad* g, void* stream);
 
+/* ff_field_fit_step on the batch binned by coefficient cell first (a counting sort inside the
+ * call: bin, scan, permute), so that points sharing coefficient corners sit in the same warp and
+ * their coefficient gradients are summed on chip before the atomics. Same loss and gradients
+ * as ff_field_fit_step up to float32 summation order. workspace: device memory of at least
+ * ff_field_fit_binned_workspace_bytes(f, n, out_dim) bytes, 256-byte aligned, not shared with
+ * a call in flight. */
+FF_API int64_t ff_field_fit_binned_workspace_bytes(const FFField* f, int64_t n, int32_t out_dim);
+FF_API int ff_field_fit_step_binned(const FFField* f, const void* basis, const void* coeff, const FFMlp* m,
+                                    const float* x, const float* target, int64_t n, int32_t loss_kind,
+                                    float loss_scale, float* loss_sum, float* grad_basis, float* grad_coeff_grid,
+                                    const FFMlpGrad* g, void* workspace, int64_t workspace_bytes, void* stream);
+
 /* ---- rendering (bounded scenes): march, compact, composite ------------------------------ */
 
 /* Renderer constants (models/FactorFields.py:586-602, :693-699, :843-898; configs/nerf.yaml

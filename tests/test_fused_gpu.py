@@ -84,9 +84,10 @@ def test_field_mlp_fwd_bwd_golden(case, precision):
     check_grads(m, ref)
 
 
+@pytest.mark.parametrize("binned", [False, True])
 @pytest.mark.parametrize("loss", ["l1", "mse"])
 @pytest.mark.parametrize("key", ["cfg0", "cfg1", "cfg2", "cfg4"])
-def test_fit_step_full_size(key, loss):
+def test_fit_step_full_size(key, loss, binned):
     from factor_fields_gb300 import FactorFields
     from factor_fields_gb300 import workloads as W
     from factor_fields_gb300.train import FieldFitRunner
@@ -118,7 +119,7 @@ def test_fit_step_full_size(key, loss):
         g_out = 2 * err / err.size
         loss_ref = (err * err).mean()
     _, ref = oracle_fwd_bwd(m, x, g_out)
-    runner = FieldFitRunner(m, loss=loss, fused=True)
+    runner = FieldFitRunner(m, loss=loss, fused=True, binned=binned)
     lv = runner.step(torch.from_numpy(x).cuda(), torch.from_numpy(y).cuda())
     torch.cuda.synchronize()
     assert abs(float(lv) - loss_ref) <= FWD_TOL * abs(loss_ref)
@@ -186,3 +187,47 @@ def test_graph_step_matches_step_and_tracks_updates():
         for a, b in zip(g_eager, r._params()):
             assert torch.allclose(a, b.grad, rtol=1e-5, atol=1e-9)
         opt.step()
+
+
+@pytest.mark.parametrize("precision", ["bf16", "fp32"])
+def test_binned_fit_matches_unbinned_on_clustered_points(precision):
+    """ff_field_fit_step_binned against ff_field_fit_step on a batch where many points share a
+    coefficient cell: segments of a whole warp (and longer, crossing warps and blocks), short
+    segments, isolated points and a ragged tail (n % 128 != 0). Same loss and gradients up to
+    float32 summation order."""
+    from factor_fields_gb300 import FactorFields
+    from factor_fields_gb300 import workloads as W
+    from factor_fields_gb300.train import FieldFitRunner
+    torch.manual_seed(0)
+    m = FactorFields(W.field_cfg("cfg1"), device="cuda", precision=precision)
+    rng = np.random.default_rng(5)
+    n_uniform, cells, per_cell = 3001, 12, 333
+    xu = rng.uniform(-1, 1, (n_uniform, 3))
+    centers = rng.integers(0, 32, (cells, 3))
+    # points strictly inside coefficient cell c (cell width 2/32, texel centres at (i + 0.5) / 16 - 1)
+    xc = (centers[:, None, :] + 0.5 + rng.uniform(0.05, 0.95, (cells, per_cell, 3))) / 16.0 - 1.0
+    x = np.concatenate([xu, xc.reshape(-1, 3)]).astype(np.float32)
+    x = x[rng.permutation(x.shape[0])]
+    y = rng.normal(0, 0.5, (x.shape[0], 1)).astype(np.float32)
+    xt, yt = torch.from_numpy(x).cuda(), torch.from_numpy(y).cuda()
+    res = []
+    for binned in (False, True):
+        r = FieldFitRunner(m, loss="mse", fused=True, binned=binned)
+        loss = float(r.step(xt, yt))
+        ws, bs = m.linear_mat.weights()
+        res.append((loss, [t.grad.clone() for t in [m.basis_flat, m.coeff_flat] + ws + [bs[0]]]))
+    (l0, g0), (l1, g1) = res
+    assert abs(l1 - l0) <= 1e-5 * abs(l0)
+    for name, a, b in zip(["basis", "coeff", "w0", "w1", "b0"], g1, g0):
+        assert rel_err(a, b) < 1e-4, name
+
+
+def test_binned_fit_empty_batch():
+    from factor_fields_gb300 import FactorFields
+    from factor_fields_gb300 import workloads as W
+    from factor_fields_gb300.train import FieldFitRunner
+    m = FactorFields(W.field_cfg("cfg1"), device="cuda", precision="bf16")
+    r = FieldFitRunner(m, loss="l1", fused=True, binned=True)
+    r.step(torch.empty(0, 3, device="cuda"), torch.empty(0, 1, device="cuda"))
+    torch.cuda.synchronize()
+    assert float(m.coeff_flat.grad.abs().sum()) == 0.0
