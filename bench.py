@@ -132,8 +132,14 @@ def run_native(args, ws, rank, local):
     def timed(step_fn, k, with_kernel_events):
         times, ktimes = [], []
         for i in range(k):
-            flush_l2(flush)
-            torch.cuda.synchronize()
+            if with_kernel_events and ws == 1:
+                # no host sync after the flush: the GPU is still writing the 256 MB while the
+                # host enqueues the step, so the kernel events see device time, not enqueue gaps
+                torch.cuda.synchronize()
+                flush_l2(flush)
+            else:
+                flush_l2(flush)
+                torch.cuda.synchronize()
             if ws > 1:
                 torch.distributed.barrier()
             s0 = torch.cuda.Event(enable_timing=True)

@@ -79,6 +79,7 @@ SIGNATURES = {
     "ff_field_fit_binned_workspace_bytes": (c_i64, [_P(FFField), c_i64, c_i32]),
     "ff_field_fit_step_binned": (c_i32, [_P(FFField), c_vp, c_vp, _P(FFMlp), c_vp, c_vp, c_i64, c_i32, c_f32, c_vp,
                                          c_vp, c_vp, _P(FFMlpGrad), c_vp, c_i64, c_vp]),
+    "ff_zero_f32": (c_i32, [c_vp, c_vp, c_i32, c_vp]),
     "ff_march_count": (c_i32, [_P(FFRender), c_vp, c_vp, c_i64, c_vp, c_vp, c_vp]),
     "ff_scan_workspace_bytes": (c_i64, [c_i64]),
     "ff_scan_counts": (c_i32, [c_vp, c_i64, c_vp, c_vp, c_i64, c_vp]),
@@ -156,8 +157,7 @@ _NON_LAUNCHING = {"ff_abi_version", "ff_last_error", "ff_device_info", "ff_struc
 
 
 # entry points that enqueue more than one kernel of this library
-_KERNELS_PER_CALL = {"ff_scan_counts": 3, "ff_scan_counts_noalloc": 3,
-                     "ff_field_fit_step_binned": 6}  # bin, 3 scan kernels, permute, fit
+_KERNELS_PER_CALL = {"ff_scan_counts": 3, "ff_scan_counts_noalloc": 3}
 
 
 def reset_launch_count():
@@ -169,8 +169,10 @@ def launch_count():
     return _launches[0]
 
 
-def call(name, *args):
+def call(name, *args, kernels=None):
+    """Call an entry point and raise on a non-zero return code. kernels: how many kernels the
+    call enqueues when that depends on its arguments (else _KERNELS_PER_CALL, default 1)."""
     rc = getattr(lib(), name)(*args)
     check(rc, name)
     if name not in _NON_LAUNCHING:
-        _launches[0] += _KERNELS_PER_CALL.get(name, 1)
+        _launches[0] += kernels if kernels is not None else _KERNELS_PER_CALL.get(name, 1)

@@ -256,6 +256,13 @@ int ff_field_fit_step_binned(const FFField* f, const void* basis, const void* co
                      "ff_field_fit_step_binned launch");
 }
 
+int ff_zero_f32(float* const* ptrs, const int64_t* counts, int32_t n_buffers, void* stream) {
+  if (n_buffers < 0 || (n_buffers > 0 && (!ptrs || !counts))) return set_error(FF_ERR_ARG, "bad buffer list");
+  for (int b = 0; b < n_buffers; ++b)
+    if (counts[b] < 0 || (counts[b] > 0 && !ptrs[b])) return set_error(FF_ERR_ARG, "NULL buffer or negative count");
+  return cuda_status(launch_zero_buffers(ptrs, counts, n_buffers, (cudaStream_t)stream), "ff_zero_f32 launch");
+}
+
 int ff_march_count(const FFRender* r, const float* rays, const float* jitter, int64_t n_rays, int32_t* counts,
                    float* t_min, void* stream) {
   int rc = validate_render(r, rays, n_rays);

@@ -43,6 +43,11 @@ cudaError_t launch_fused_fit(const FFField& f, const void* basis, const void* co
                              float* loss_sum, float* grad_basis, float* grad_coeff, const FFMlpGrad& g,
                              cudaStream_t st);
 
+// launch_fused_fit on point rows x_stride / t_stride floats apart (binned, packed batches)
+cudaError_t launch_fused_fit_rows(const FFField& f, const void* basis, const void* coeff, const FFMlp& m,
+                                  const float* x, int64_t x_stride, const float* target, int64_t t_stride, int64_t n,
+                                  int loss_kind, float loss_scale, float* loss_sum, float* grad_basis,
+                                  float* grad_coeff, const FFMlpGrad& g, cudaStream_t st);
 cudaError_t launch_fused_fit_binned(const FFField& f, const void* basis, const void* coeff, const FFMlp& m,
                                     const float* x, const float* target, int64_t n, int loss_kind, float loss_scale,
                                     float* loss_sum, float* grad_basis, float* grad_coeff, const FFMlpGrad& g,
@@ -51,8 +56,15 @@ cudaError_t launch_fused_fit_binned(const FFField& f, const void* basis, const v
 // fit_bin_kernels.cu
 int64_t fit_bin_keys(const FFField& f);
 int64_t fit_bin_workspace_bytes(const FFField& f, int64_t n, int out_dim);
+// Bins the batch; *rows_out: per binned point its coordinates then its targets, *stride_out
+// floats per row (coord_dim + out_dim rounded up to a multiple of 4).
 cudaError_t launch_fit_bin(const FFField& f, const float* x, const float* target, int out_dim, int64_t n,
-                           void* workspace, const float** xs_out, const float** ts_out, cudaStream_t st);
+                           void* workspace, const float** rows_out, int64_t* stride_out, cudaStream_t st);
+int fit_bin_kernel_launches(const FFField& f);  // kernels launch_fit_bin enqueues
+
+// util_kernels.cu
+constexpr int kMaxZeroBuffers = 8;  // buffers per zeroing launch (more: several launches)
+cudaError_t launch_zero_buffers(float* const* ptrs, const int64_t* counts, int n_buffers, cudaStream_t st);
 
 // render_kernels.cu
 int64_t scan_workspace_bytes(int64_t n);

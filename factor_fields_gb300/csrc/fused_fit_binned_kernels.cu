@@ -9,14 +9,17 @@ cudaError_t launch_fused_fit_binned(const FFField& f, const void* basis, const v
                                     float* loss_sum, float* grad_basis, float* grad_coeff, const FFMlpGrad& g,
                                     void* workspace, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
-  const float *xs = nullptr, *ts = nullptr;
-  cudaError_t e = launch_fit_bin(f, x, target, m.out_dim, n, workspace, &xs, &ts, st);
+  const float* rows = nullptr;
+  int64_t stride = 0;
+  cudaError_t e = launch_fit_bin(f, x, target, m.out_dim, n, workspace, &rows, &stride, st);
   if (e != cudaSuccess) return e;
-  if (f.param_dtype != FF_BF16)  // float32 grids: the per-point fit on the binned batch
-    return launch_fused_fit(f, basis, coeff, m, xs, ts, n, loss_kind, loss_scale, loss_sum, grad_basis, grad_coeff, g,
-                            st);
-  FusedArgs a = make_args(f, basis, coeff, m, xs, n);
-  a.target = ts;
+  if (f.param_dtype != FF_BF16)  // float32 grids: the per-point fit on the binned rows
+    return launch_fused_fit_rows(f, basis, coeff, m, rows, stride, rows + f.coord_dim, stride, n, loss_kind,
+                                 loss_scale, loss_sum, grad_basis, grad_coeff, g, st);
+  FusedArgs a = make_args(f, basis, coeff, m, rows, n);
+  a.x_stride = stride;  // packed rows: coordinates, then the targets
+  a.target = rows + f.coord_dim;
+  a.t_stride = stride;
   a.loss_kind = loss_kind;
   a.loss_scale = loss_scale;
   a.loss_sum = loss_sum;

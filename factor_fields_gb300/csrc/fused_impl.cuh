@@ -73,10 +73,12 @@ struct FusedArgs {
   const float* w1;  // [out, 64]
   int out_dim;
   const float* x;
+  int64_t x_stride;  // floats between consecutive points' coordinates (coord_dim, or the packed row)
   int64_t n;
   float* out;             // kFwd: [n, out]
   const float* grad_out;  // kBwd: [n, out]
-  const float* target;    // kFit: [n, out]
+  const float* target;    // kFit: [n, out] rows t_stride floats apart
+  int64_t t_stride;
   int loss_kind;
   float loss_scale;
   float* loss_sum;
@@ -256,7 +258,7 @@ __global__ void __launch_bounds__(kThreads, 3) fused_field_mlp_kernel(const Fuse
     // ---------------- gather ----------------
     if (valid) {
 #pragma unroll
-      for (int k = 0; k < CD; ++k) p[k] = a.x[i * CD + k];
+      for (int k = 0; k < CD; ++k) p[k] = a.x[i * a.x_stride + k];
       Corners<CD> cc;
       coeff_corners<CD>(f, p, cc);
       gather_coeff18<CD>(coeff, f.coeff_stride, cc, cv);
@@ -369,7 +371,7 @@ __global__ void __launch_bounds__(kThreads, 3) fused_field_mlp_kernel(const Fuse
             float d = 0.f;
             if (row < a.n && col < out) {
               if constexpr (is_fit<MODE>()) {
-                const float err = oc[nt][q] - a.target[row * out + col];
+                const float err = oc[nt][q] - a.target[row * a.t_stride + col];
                 if (a.loss_kind == FF_LOSS_L1) {
                   loss_acc += fabsf(err);
                   d = (err > 0.f ? 1.f : (err < 0.f ? -1.f : 0.f)) * a.loss_scale;
@@ -622,11 +624,22 @@ template <int MODE, int BD, int CD, int OUTT, typename T>
 cudaError_t launch_one(const FusedArgs& a, cudaStream_t st) {
   constexpr int64_t smem = smem_bytes<MODE, OUTT>();
   auto kern = fused_field_mlp_kernel<MODE, BD, CD, OUTT, T>;
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  // the shared-memory opt-in and the occupancy query, once per process and device
+  static int per_sm_cache[64] = {0};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
-  int per_sm = 1;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, smem);
-  if (e != cudaSuccess || per_sm < 1) per_sm = 1;
+  int per_sm = (dev >= 0 && dev < 64) ? per_sm_cache[dev] : 0;
+  if (per_sm == 0) {
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, smem);
+    if (e != cudaSuccess || per_sm < 1) {
+      (void)cudaGetLastError();
+      per_sm = 1;
+    }
+    if (dev >= 0 && dev < 64) per_sm_cache[dev] = per_sm;
+  }
   const int64_t tiles = ceil_div(a.n, kTile);
   const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>(tiles, (int64_t)sm_count() * per_sm));
   kern<<<blocks, kThreads, smem, st>>>(a);
@@ -671,6 +684,8 @@ inline FusedArgs make_args(const FFField& f, const void* basis, const void* coef
   a.w1 = m.weight[1];
   a.out_dim = m.out_dim;
   a.x = x;
+  a.x_stride = f.coord_dim;
+  a.t_stride = m.out_dim;
   a.n = n;
   return a;
 }

@@ -138,8 +138,18 @@ class FieldFitRunner:
         return g
 
     def zero_grad(self):
-        for p in self._params():
-            p.grad.zero_()
+        """Zero the parameters' gradients and the loss accumulator in one ff_zero_f32 launch."""
+        bufs = [p.grad for p in self._params()] + [self.loss_buf]
+        key = tuple(b.data_ptr() for b in bufs)
+        if getattr(self, "_zero_key", None) != key:
+            for b in bufs:
+                if b.dtype != torch.float32 or not b.is_contiguous():
+                    raise ValueError("gradient buffers must be contiguous float32")
+            self._zero_ptrs = (ctypes.c_void_p * len(bufs))(*key)
+            self._zero_counts = (ctypes.c_int64 * len(bufs))(*[b.numel() for b in bufs])
+            self._zero_key = key
+        N.call("ff_zero_f32", self._zero_ptrs, self._zero_counts, len(bufs), N.stream_ptr(),
+               kernels=-(-len(bufs) // 8))
 
     def graph_step(self, x, y):
         """step() replayed from a CUDA graph: the batch is copied into static buffers and the
@@ -195,7 +205,6 @@ class FieldFitRunner:
         if kernel_events:
             ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
         if self.fused:
-            self.loss_buf.zero_()
             if self.binned:
                 ws = self._workspace(desc, n)
             if ev:
@@ -204,7 +213,11 @@ class FieldFitRunner:
                       N.FF_LOSS[self.loss], 1.0 / max(n * m.linear_mat.out_dim, 1), N.ptr(self.loss_buf),
                       N.ptr(m.basis_flat.grad), N.ptr(m.coeff_flat.grad), ctypes.byref(g))
             if self.binned:
-                N.call("ff_field_fit_step_binned", *common, N.ptr(ws), ws.numel(), st)
+                keys = 1
+                for d in range(desc.coord_dim):
+                    keys *= int(desc.coeff_reso[d])
+                N.call("ff_field_fit_step_binned", *common, N.ptr(ws), ws.numel(), st,
+                       kernels=4 if keys <= (1 << 15) else 6)  # bin, scan (1 or 3), permute, fit
             else:
                 N.call("ff_field_fit_step", *common, st)
             if ev:

@@ -180,6 +180,11 @@ FF_API int ff_field_fit_step_binned(const FFField* f, const void* basis, const v
                                     float loss_scale, float* loss_sum, float* grad_basis, float* grad_coeff_grid,
                                     const FFMlpGrad* g, void* workspace, int64_t workspace_bytes, void* stream);
 
+/* Zero n_buffers float32 device buffers (ptrs[b], counts[b] elements; the two arrays are host
+ * memory, read during the call) in one launch per 8 buffers: a training step's gradient
+ * zeroing (optimizer.zero_grad) and loss accumulator reset without one fill per tensor. */
+FF_API int ff_zero_f32(float* const* ptrs, const int64_t* counts, int32_t n_buffers, void* stream);
+
 /* ---- rendering (bounded scenes): march, compact, composite ------------------------------ */
 
 /* Renderer constants (models/FactorFields.py:586-602, :693-699, :843-898; configs/nerf.yaml
