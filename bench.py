@@ -102,6 +102,12 @@ def make_model(precision):
     return m
 
 
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one full-size launch of the fit
+# kernel from the ncu captures summarised in profiles/fused_fit_kernel_cfg1_ncu.md.
+NCU_TRAFFIC = {"ff_field_fit_step_binned": 69.623552e6 + 1.303296e6,
+               "ff_field_fit_step": 69.626112e6 + 1.560832e6}
+
+
 def bytes_per_point(m, gathers, param_bytes):
     """Algorithmic bytes per point: `gathers` passes over K corners x (sum C + C_coeff)
     channels at param_bytes, one float32 scatter of the same, coords (12 B) + target (4 B)."""
@@ -226,7 +232,10 @@ def run_native(args, ws, rank, local):
         "fp32_dropin": {"value": pts / (ms_drop / 1e3), "unit": "samples/s",
                         "ms_per_step": ms_drop / args.steps},
         "roofline": {"bound": "hbm", "kernel": runner.dominant_kernel, "achieved": achieved, "peak": peak,
-                     "unit": "GB/s", "frac": (achieved / peak) if achieved else None, "traffic": None,
+                     "unit": "GB/s", "frac": (achieved / peak) if achieved else None,
+                     "traffic": NCU_TRAFFIC.get(runner.dominant_kernel),
+                     "traffic_source": "ncu dram read+write of the fit kernel, one 262,144-point launch "
+                                       "(profiles/fused_fit_kernel_cfg1_ncu.md)",
                      "bytes_per_point": bpp, "kernel_ms": kern_ms,
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if "hbm_gbs" in peaks else "fallback"},
         "gpu_launches": launches,
