@@ -21,6 +21,7 @@ FF_MAP = {"sawtooth": 0, "triangle": 1}
 FF_INTERP = {"bilinear": 0, "linear": 0, "trilinear": 0, "nearest": 1}
 FF_F32, FF_BF16 = 0, 1
 FF_LOSS = {"l1": 0, "mse": 1}
+FF_FIT_ZERO_GRADS = 1
 
 c_i32, c_i64, c_f32, c_vp = ctypes.c_int32, ctypes.c_int64, ctypes.c_float, ctypes.c_void_p
 
@@ -78,7 +79,7 @@ SIGNATURES = {
                                   c_vp, _P(FFMlpGrad), c_vp]),
     "ff_field_fit_binned_workspace_bytes": (c_i64, [_P(FFField), c_i64, c_i32]),
     "ff_field_fit_step_binned": (c_i32, [_P(FFField), c_vp, c_vp, _P(FFMlp), c_vp, c_vp, c_i64, c_i32, c_f32, c_vp,
-                                         c_vp, c_vp, _P(FFMlpGrad), c_vp, c_i64, c_vp]),
+                                         c_vp, c_vp, _P(FFMlpGrad), c_i32, c_vp, c_i64, c_vp]),
     "ff_zero_f32": (c_i32, [c_vp, c_vp, c_i32, c_vp]),
     "ff_march_count": (c_i32, [_P(FFRender), c_vp, c_vp, c_i64, c_vp, c_vp, c_vp]),
     "ff_scan_workspace_bytes": (c_i64, [c_i64]),

@@ -236,8 +236,8 @@ int64_t ff_field_fit_binned_workspace_bytes(const FFField* f, int64_t n, int32_t
 
 int ff_field_fit_step_binned(const FFField* f, const void* basis, const void* coeff, const FFMlp* m, const float* x,
                              const float* target, int64_t n, int32_t loss_kind, float loss_scale, float* loss_sum,
-                             float* grad_basis, float* grad_coeff_grid, const FFMlpGrad* g, void* workspace,
-                             int64_t workspace_bytes, void* stream) {
+                             float* grad_basis, float* grad_coeff_grid, const FFMlpGrad* g, int32_t flags,
+                             void* workspace, int64_t workspace_bytes, void* stream) {
   int rc = validate_fused(f, basis, coeff, m, x, n);
   if (rc) return rc;
   if (n > 0 && !target) return set_error(FF_ERR_ARG, "target is NULL");
@@ -249,10 +249,12 @@ int ff_field_fit_step_binned(const FFField* f, const void* basis, const void* co
   if (n > 0 && (!workspace || workspace_bytes < need))
     return set_error(FF_ERR_SIZE, "workspace smaller than ff_field_fit_binned_workspace_bytes");
   if (!aligned(workspace, 256)) return set_error(FF_ERR_ALIGN, "workspace must be 256-byte aligned");
+  if (flags & ~FF_FIT_ZERO_GRADS) return set_error(FF_ERR_ARG, "unknown flags");
+  if (!workspace) return set_error(FF_ERR_ARG, "workspace is NULL");
   FFMlpGrad none = {};
   return cuda_status(launch_fused_fit_binned(*f, basis, coeff, *m, x, target, n, loss_kind, loss_scale, loss_sum,
                                              grad_basis, grad_coeff_grid, g ? *g : none, workspace,
-                                             (cudaStream_t)stream),
+                                             (flags & FF_FIT_ZERO_GRADS) != 0, (cudaStream_t)stream),
                      "ff_field_fit_step_binned launch");
 }
 

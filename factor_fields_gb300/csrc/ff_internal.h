@@ -51,16 +51,25 @@ cudaError_t launch_fused_fit_rows(const FFField& f, const void* basis, const voi
 cudaError_t launch_fused_fit_binned(const FFField& f, const void* basis, const void* coeff, const FFMlp& m,
                                     const float* x, const float* target, int64_t n, int loss_kind, float loss_scale,
                                     float* loss_sum, float* grad_basis, float* grad_coeff, const FFMlpGrad& g,
-                                    void* workspace, cudaStream_t st);
+                                    void* workspace, bool zero_grads, cudaStream_t st);
 
 // fit_bin_kernels.cu
 int64_t fit_bin_keys(const FFField& f);
 int64_t fit_bin_workspace_bytes(const FFField& f, int64_t n, int out_dim);
-// Bins the batch; *rows_out: per binned point its coordinates then its targets, *stride_out
-// floats per row (coord_dim + out_dim rounded up to a multiple of 4).
+// Gradient buffers the binning pass zeroes (NULL entries skipped): the grid gradients (16-byte
+// aligned, sizes from the descriptor) and up to 4 small float buffers with explicit sizes.
+struct FitZero {
+  float* grad_basis;
+  float* grad_coeff;
+  float* other[4];
+  int64_t other_n[4];
+};
+int64_t field_basis_elems(const FFField& f);  // elements of the flat basis buffer
+// Bins the batch (3 kernels: bin, alloc, permute); *rows_out: per binned point its coordinates
+// then its targets, *stride_out floats per row (coord_dim + out_dim rounded up to 4).
 cudaError_t launch_fit_bin(const FFField& f, const float* x, const float* target, int out_dim, int64_t n,
-                           void* workspace, const float** rows_out, int64_t* stride_out, cudaStream_t st);
-int fit_bin_kernel_launches(const FFField& f);  // kernels launch_fit_bin enqueues
+                           void* workspace, const FitZero* zero, const float** rows_out, int64_t* stride_out,
+                           cudaStream_t st);
 
 // util_kernels.cu
 constexpr int kMaxZeroBuffers = 8;  // buffers per zeroing launch (more: several launches)

@@ -8,10 +8,14 @@
 // a cell is the order in which the atomics hand out ranks; results do not depend on it (the
 // gradients are sums).
 //
-//   bin      (key[i], rank[i] = atomicAdd(count[key], 1))        thread per point
-//   scan     offsets = exclusive prefix sum of count             one block up to 2^15 keys, else
-//                                                                the two-level scan (render_kernels.cu)
-//   permute  row[offsets[key] + rank] = (x[i], target[i], 0 pad)  one 16-byte-multiple row per point
+//   bin      (key[i], rank[i] = atomicAdd(count[key], 1))          thread per point; optionally
+//                                                                  also zeroes the step's gradients
+//   alloc    start[key] = atomicAdd(cursor, count[key])           warp per 32 keys, one atomic per
+//                                                                  warp: every key gets a contiguous
+//                                                                  range; the order of the ranges is
+//                                                                  whatever the atomics hand out
+//   permute  row[start[key] + rank] = (x[i], target[i], 0 pad)    one 16-byte-multiple row per point
+// Only contiguity matters (segments are found from the keys of adjacent lanes), so no scan.
 #include "ff_common.cuh"
 #include "ff_internal.h"
 
@@ -20,14 +24,22 @@ namespace ffgb {
 namespace {
 
 constexpr int kBinThreads = 256;
-constexpr int kScanThreads1 = 1024;
-constexpr int64_t kOneBlockKeys = kScanThreads1 * 32;  // scan in a single block up to this many keys
+
+// Buffers the bin kernel zeroes before the fit accumulates into them (FF_FIT_ZERO_GRADS).
+struct ZeroSet {
+  float* vec4[2];  // 16-byte aligned: grid gradients
+  int64_t n4[2];   // float4 counts
+  float* flt[6];   // MLP gradients, loss accumulator, the grid gradients' last (n % 4) elements
+  int64_t n[6];
+};
 
 template <int CD>
 __global__ void __launch_bounds__(kBinThreads) fit_bin_kernel(const FFField f, const float* __restrict__ x,
                                                               int64_t n, int32_t n_keys, int32_t* __restrict__ count,
-                                                              int2* __restrict__ key_rank) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+                                                              int2* __restrict__ key_rank,
+                                                              const __grid_constant__ ZeroSet zs) {
+  const int64_t t0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = t0; i < n; i += stride) {
     float p[CD];
 #pragma unroll
     for (int k = 0; k < CD; ++k) p[k] = x[i * CD + k];
@@ -37,48 +49,37 @@ __global__ void __launch_bounds__(kBinThreads) fit_bin_kernel(const FFField f, c
     if (k < 0 || k >= n_keys) k = 0;  // non-finite coordinates: any bin will do
     key_rank[i] = make_int2(k, atomicAdd(count + k, 1));
   }
+#pragma unroll
+  for (int b = 0; b < 2; ++b) {
+    float4* q = reinterpret_cast<float4*>(zs.vec4[b]);
+    for (int64_t i = t0; i < zs.n4[b]; i += stride) q[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+#pragma unroll
+  for (int b = 0; b < 6; ++b)
+    for (int64_t i = t0; i < zs.n[b]; i += stride) zs.flt[b][i] = 0.f;
 }
 
-// Exclusive prefix sum of n <= kOneBlockKeys counts in one block. Warp w owns the 32 x 32 counts
-// [1024 w, 1024 (w + 1)); lane l holds counts 1024 w + 32 k + l (k < 32) in registers, loaded in
-// one coalesced round. The warps' totals are scanned in shared memory; each warp then scans its
-// counts 32 at a time (warp shuffle scan, carry from the previous 32).
-__global__ void __launch_bounds__(kScanThreads1) fit_scan_one_block_kernel(const int32_t* __restrict__ count,
-                                                                           int64_t n, int64_t* __restrict__ offsets) {
-  constexpr int kWarps = kScanThreads1 / 32;
-  __shared__ int64_t chunk_start[kWarps + 1];
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  int32_t v[32];
-  int32_t s = 0;
-#pragma unroll
-  for (int k = 0; k < 32; ++k) {
-    const int64_t i = (int64_t)warp * 1024 + k * 32 + lane;
-    v[k] = i < n ? count[i] : 0;
-    s += v[k];
-  }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-  if (lane == 0) chunk_start[warp + 1] = s;
-  __syncthreads();
-  if (tid == 0) {
-    chunk_start[0] = 0;
-    for (int w = 1; w <= kWarps; ++w) chunk_start[w] += chunk_start[w - 1];
-  }
-  __syncthreads();
-  int64_t carry = chunk_start[warp];
-#pragma unroll
-  for (int k = 0; k < 32; ++k) {
-    const int64_t i = (int64_t)warp * 1024 + k * 32 + lane;
-    int32_t incl = v[k];
+// Warp per 32 keys: a contiguous range of count[key] rows for every key, one atomic per warp.
+__global__ void __launch_bounds__(kBinThreads) fit_alloc_kernel(const int32_t* __restrict__ count, int64_t n_keys,
+                                                                int64_t* __restrict__ cursor,
+                                                                int64_t* __restrict__ start) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; w * 32 < n_keys; w += warps) {
+    const int64_t k = w * 32 + lane;
+    const int32_t c = k < n_keys ? count[k] : 0;
+    int32_t incl = c;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
       const int32_t u = __shfl_up_sync(0xffffffffu, incl, o);
       if (lane >= o) incl += u;
     }
-    if (i < n) offsets[i] = carry + incl - v[k];
-    carry += __shfl_sync(0xffffffffu, incl, 31);
+    int64_t base = 0;
+    if (lane == 31 && incl > 0) base = atomicAdd(reinterpret_cast<unsigned long long*>(cursor),
+                                                 (unsigned long long)incl);
+    base = __shfl_sync(0xffffffffu, base, 31);
+    if (k < n_keys) start[k] = base + incl - c;
   }
-  if (tid == 0) offsets[n] = chunk_start[kWarps];
 }
 
 // One row of `stride` floats per binned point: coordinates, targets, zero padding.
@@ -86,11 +87,11 @@ template <int CD>
 __global__ void __launch_bounds__(kBinThreads) fit_permute_kernel(const float* __restrict__ x,
                                                                   const float* __restrict__ target, int out_dim,
                                                                   int64_t n, const int2* __restrict__ key_rank,
-                                                                  const int64_t* __restrict__ offsets, int stride,
+                                                                  const int64_t* __restrict__ start, int stride,
                                                                   float* __restrict__ rows) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const int2 kr = key_rank[i];
-    float4* dst = reinterpret_cast<float4*>(rows + (offsets[kr.x] + kr.y) * stride);
+    float4* dst = reinterpret_cast<float4*>(rows + (start[kr.x] + kr.y) * stride);
     if (CD == 3 && out_dim == 1) {
       dst[0] = make_float4(x[i * 3], x[i * 3 + 1], x[i * 3 + 2], target[i]);
     } else {
@@ -123,47 +124,70 @@ int64_t fit_bin_keys(const FFField& f) {
   return k;
 }
 
+int64_t field_basis_elems(const FFField& f) {
+  int64_t most = 0;
+  for (int l = 0; l < f.n_levels; ++l) {
+    int64_t cells = 1;
+    for (int d = 0; d < f.basis_dim; ++d) cells *= f.level_reso[l];
+    most = std::max(most, f.level_offset[l] + cells * f.level_stride[l]);
+  }
+  return most;
+}
+
 int64_t fit_bin_workspace_bytes(const FFField& f, int64_t n, int out_dim) {
   const int64_t keys = fit_bin_keys(f);
-  return align_up(keys * 4) + align_up(n * 8) + align_up((keys + 1) * 8) + align_up(scan_workspace_bytes(keys)) +
-         align_up(n * row_stride(f, out_dim) * 4);
+  return align_up(keys * 4 + 16) + align_up(n * 8) + align_up(keys * 8) + align_up(n * row_stride(f, out_dim) * 4);
 }
 
 cudaError_t launch_fit_bin(const FFField& f, const float* x, const float* target, int out_dim, int64_t n,
-                           void* workspace, const float** rows_out, int64_t* stride_out, cudaStream_t st) {
+                           void* workspace, const FitZero* zero, const float** rows_out, int64_t* stride_out,
+                           cudaStream_t st) {
   const int64_t keys = fit_bin_keys(f);
   const int stride = row_stride(f, out_dim);
   unsigned char* w = static_cast<unsigned char*>(workspace);
-  int32_t* count = reinterpret_cast<int32_t*>(w); w += align_up(keys * 4);
+  int32_t* count = reinterpret_cast<int32_t*>(w);
+  int64_t* cursor = reinterpret_cast<int64_t*>(w + ((keys * 4 + 7) & ~int64_t(7)));
+  w += align_up(keys * 4 + 16);
   int2* key_rank = reinterpret_cast<int2*>(w); w += align_up(n * 8);
-  int64_t* offsets = reinterpret_cast<int64_t*>(w); w += align_up((keys + 1) * 8);
-  void* scan_ws = w; w += align_up(scan_workspace_bytes(keys));
+  int64_t* start = reinterpret_cast<int64_t*>(w); w += align_up(keys * 8);
   float* rows = reinterpret_cast<float*>(w);
   *rows_out = rows;
   *stride_out = stride;
-  cudaError_t e = cudaMemsetAsync(count, 0, keys * 4, st);
+  cudaError_t e = cudaMemsetAsync(count, 0, ((keys * 4 + 7) & ~int64_t(7)) + 8, st);
   if (e != cudaSuccess) return e;
-  const int blocks = bin_blocks(n);
+  ZeroSet zs = {};
+  if (zero) {
+    float* grids[2] = {zero->grad_basis, zero->grad_coeff};
+    const int64_t elems[2] = {field_basis_elems(f), keys * f.coeff_stride};
+    for (int b = 0; b < 2; ++b) {
+      if (!grids[b]) continue;
+      zs.vec4[b] = grids[b];
+      zs.n4[b] = elems[b] / 4;
+      zs.flt[4 + b] = grids[b] + zs.n4[b] * 4;
+      zs.n[4 + b] = elems[b] % 4;
+    }
+    for (int b = 0; b < 4; ++b) {
+      zs.flt[b] = zero->other[b];
+      zs.n[b] = zero->other[b] ? zero->other_n[b] : 0;
+    }
+  }
+  const int blocks = bin_blocks(std::max<int64_t>(n, zs.n4[0]));
   if (f.coord_dim == 3)
-    fit_bin_kernel<3><<<blocks, kBinThreads, 0, st>>>(f, x, n, (int32_t)keys, count, key_rank);
+    fit_bin_kernel<3><<<blocks, kBinThreads, 0, st>>>(f, x, n, (int32_t)keys, count, key_rank, zs);
   else
-    fit_bin_kernel<2><<<blocks, kBinThreads, 0, st>>>(f, x, n, (int32_t)keys, count, key_rank);
+    fit_bin_kernel<2><<<blocks, kBinThreads, 0, st>>>(f, x, n, (int32_t)keys, count, key_rank, zs);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  if (keys <= kOneBlockKeys) {
-    fit_scan_one_block_kernel<<<1, kScanThreads1, 0, st>>>(count, keys, offsets);
-    e = cudaGetLastError();
-  } else {
-    e = launch_scan(count, keys, offsets, scan_ws, st);
-  }
+  const int ablocks = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(keys, kBinThreads), (int64_t)sm_count() * 8));
+  fit_alloc_kernel<<<ablocks, kBinThreads, 0, st>>>(count, keys, cursor, start);
+  e = cudaGetLastError();
   if (e != cudaSuccess) return e;
+  const int pblocks = bin_blocks(n);
   if (f.coord_dim == 3)
-    fit_permute_kernel<3><<<blocks, kBinThreads, 0, st>>>(x, target, out_dim, n, key_rank, offsets, stride, rows);
+    fit_permute_kernel<3><<<pblocks, kBinThreads, 0, st>>>(x, target, out_dim, n, key_rank, start, stride, rows);
   else
-    fit_permute_kernel<2><<<blocks, kBinThreads, 0, st>>>(x, target, out_dim, n, key_rank, offsets, stride, rows);
+    fit_permute_kernel<2><<<pblocks, kBinThreads, 0, st>>>(x, target, out_dim, n, key_rank, start, stride, rows);
   return cudaGetLastError();
 }
-
-int fit_bin_kernel_launches(const FFField& f) { return fit_bin_keys(f) <= kOneBlockKeys ? 3 : 5; }
 
 }  // namespace ffgb

@@ -7,11 +7,29 @@ namespace ffgb {
 cudaError_t launch_fused_fit_binned(const FFField& f, const void* basis, const void* coeff, const FFMlp& m,
                                     const float* x, const float* target, int64_t n, int loss_kind, float loss_scale,
                                     float* loss_sum, float* grad_basis, float* grad_coeff, const FFMlpGrad& g,
-                                    void* workspace, cudaStream_t st) {
-  if (n == 0) return cudaSuccess;
+                                    void* workspace, bool zero_grads, cudaStream_t st) {
+  FitZero z = {};
+  if (zero_grads) {
+    z.grad_basis = grad_basis;
+    z.grad_coeff = grad_coeff;
+    z.other[0] = g.weight[0];
+    z.other_n[0] = (int64_t)m.hidden_dim * m.in_dim;
+    z.other[1] = g.bias[0];
+    z.other_n[1] = m.hidden_dim;
+    z.other[2] = g.weight[1];
+    z.other_n[2] = (int64_t)m.out_dim * m.hidden_dim;
+    z.other[3] = loss_sum;
+    z.other_n[3] = 1;
+  }
+  if (n == 0) {  // nothing to bin or fit; the zeroing still happens
+    if (!zero_grads) return cudaSuccess;
+    const float* rows = nullptr;
+    int64_t stride = 0;
+    return launch_fit_bin(f, x, target, m.out_dim, 0, workspace, &z, &rows, &stride, st);
+  }
   const float* rows = nullptr;
   int64_t stride = 0;
-  cudaError_t e = launch_fit_bin(f, x, target, m.out_dim, n, workspace, &rows, &stride, st);
+  cudaError_t e = launch_fit_bin(f, x, target, m.out_dim, n, workspace, zero_grads ? &z : nullptr, &rows, &stride, st);
   if (e != cudaSuccess) return e;
   if (f.param_dtype != FF_BF16)  // float32 grids: the per-point fit on the binned rows
     return launch_fused_fit_rows(f, basis, coeff, m, rows, stride, rows + f.coord_dim, stride, n, loss_kind,

@@ -108,8 +108,8 @@ class FieldFitRunner:
             raise ValueError("binned=True needs fused=True")
         self._ws = None
         if fused and self.binned:
-            self.path_name = ("fused, binned: ff_field_fit_step_binned per step (bin by coefficient cell, scan, "
-                              "permute, one fit launch; + gradient zeroing)")
+            self.path_name = ("fused, binned: one ff_field_fit_step_binned call per step (bin by coefficient cell "
+                              "with the gradient zeroing, allocate cell ranges, permute, fit)")
             self.dominant_kernel = "ff_field_fit_step_binned"
             self.gathers_per_point = 1
         elif fused:
@@ -193,7 +193,8 @@ class FieldFitRunner:
 
     def step(self, x, y, kernel_events=False):
         m = self.m
-        self.zero_grad()
+        if not (self.fused and self.binned):  # the binned call zeroes them in its binning pass
+            self.zero_grad()
         basis_r, coeff_r, dt = m._read_buffers()
         desc = m.descriptor(dt)
         n = x.shape[0]
@@ -212,12 +213,9 @@ class FieldFitRunner:
             common = (ctypes.byref(desc), N.ptr(basis_r), N.ptr(coeff_r), ctypes.byref(mlp), N.ptr(x), N.ptr(y), n,
                       N.FF_LOSS[self.loss], 1.0 / max(n * m.linear_mat.out_dim, 1), N.ptr(self.loss_buf),
                       N.ptr(m.basis_flat.grad), N.ptr(m.coeff_flat.grad), ctypes.byref(g))
-            if self.binned:
-                keys = 1
-                for d in range(desc.coord_dim):
-                    keys *= int(desc.coeff_reso[d])
-                N.call("ff_field_fit_step_binned", *common, N.ptr(ws), ws.numel(), st,
-                       kernels=4 if keys <= (1 << 15) else 6)  # bin, scan (1 or 3), permute, fit
+            if self.binned:  # kernels: bin (+ gradient zeroing), alloc, permute, fit
+                N.call("ff_field_fit_step_binned", *common, N.FF_FIT_ZERO_GRADS, N.ptr(ws), ws.numel(), st,
+                       kernels=4)
             else:
                 N.call("ff_field_fit_step", *common, st)
             if ev:

@@ -49,6 +49,8 @@ enum { FF_MAP_SAWTOOTH = 0, FF_MAP_TRIANGLE = 1 };
 enum { FF_INTERP_LINEAR = 0, FF_INTERP_NEAREST = 1 };
 enum { FF_F32 = 0, FF_BF16 = 1 };
 enum { FF_LOSS_L1 = 0, FF_LOSS_MSE = 1 };
+/* ff_field_fit_step_binned flags */
+enum { FF_FIT_ZERO_GRADS = 1 };
 
 /*
  * Description of one grid/grid factor field (models/FactorFields.py:262-309 setup_params,
@@ -168,17 +170,21 @@ FF_API int ff_field_fit_step(const FFField* f, const void* basis, const void* co
                              float loss_scale, float* loss_sum, float* grad_basis, float* grad_coeff_grid,
                              const FFMlpGrad* g, void* stream);
 
-/* ff_field_fit_step on the batch binned by coefficient cell first (a counting sort inside the
- * call: bin, scan, permute), so that points sharing coefficient corners sit in the same warp and
- * their coefficient gradients are summed on chip before the atomics. Same loss and gradients
- * as ff_field_fit_step up to float32 summation order. workspace: device memory of at least
- * ff_field_fit_binned_workspace_bytes(f, n, out_dim) bytes, 256-byte aligned, not shared with
- * a call in flight. */
+/* ff_field_fit_step on the batch binned by coefficient cell first (inside the call: bin with
+ * atomic ranks, a contiguous row range per cell, permute), so that points sharing coefficient
+ * corners sit in the same warp and their coefficient gradients are summed on chip before the
+ * atomics. Same loss and gradients as ff_field_fit_step up to float32 summation order.
+ * flags: FF_FIT_ZERO_GRADS zeroes grad_basis (the whole flat basis), grad_coeff_grid (this
+ * coefficient grid), the MLP gradients in g and *loss_sum first, in the binning pass (the step's
+ * zero_grad without a launch of its own); otherwise they are accumulated into (+=).
+ * workspace: device memory of at least ff_field_fit_binned_workspace_bytes(f, n, out_dim)
+ * bytes, 256-byte aligned, not shared with a call in flight. */
 FF_API int64_t ff_field_fit_binned_workspace_bytes(const FFField* f, int64_t n, int32_t out_dim);
 FF_API int ff_field_fit_step_binned(const FFField* f, const void* basis, const void* coeff, const FFMlp* m,
                                     const float* x, const float* target, int64_t n, int32_t loss_kind,
                                     float loss_scale, float* loss_sum, float* grad_basis, float* grad_coeff_grid,
-                                    const FFMlpGrad* g, void* workspace, int64_t workspace_bytes, void* stream);
+                                    const FFMlpGrad* g, int32_t flags, void* workspace, int64_t workspace_bytes,
+                                    void* stream);
 
 /* Zero n_buffers float32 device buffers (ptrs[b], counts[b] elements; the two arrays are host
  * memory, read during the call) in one launch per 8 buffers: a training step's gradient
