@@ -62,7 +62,8 @@ static int validate_field(const FFField* f, const void* basis, const void* coeff
     if (f->level_scale[l] <= 0.f) return set_error(FF_ERR_ARG, "level_scale must be > 0");
     int64_t cells = 1;
     for (int k = 0; k < f->basis_dim; ++k) cells *= f->level_reso[l];
-    if (cells > (1ll << 31) / 8) return set_error(FF_ERR_SIZE, "basis level too large");
+    if (cells > (1ll << 31) / 8 || cells * f->level_stride[l] >= (1ll << 31))  // 32-bit corner offsets
+      return set_error(FF_ERR_SIZE, "basis level too large");
     sum += c;
   }
   if (sum != f->n_feat) return set_error(FF_ERR_ARG, "n_feat != sum(level_channels)");
@@ -72,7 +73,8 @@ static int validate_field(const FFField* f, const void* basis, const void* coeff
     if (f->coeff_reso[k] < 1) return set_error(FF_ERR_ARG, "coeff_reso must be >= 1");
     cells *= f->coeff_reso[k];
   }
-  if (cells > (1ll << 31) / 8) return set_error(FF_ERR_SIZE, "coefficient grid too large");
+  if (cells > (1ll << 31) / 8 || cells * f->coeff_stride >= (1ll << 31))
+    return set_error(FF_ERR_SIZE, "coefficient grid too large");
   (void)es;
   return FF_OK;
 }

@@ -116,29 +116,38 @@ struct Corners {
 // the product is formed x*y*z in that order like ATen.
 template <int D>
 __device__ __forceinline__ void linear_corners(const float* ix, const int* size, Corners<D>& c) {
-  int lo[D];
+  static_assert(D == 2 || D == 3, "bi- or trilinear corners");
+  int lo[D], step[D];
   float wl[D], wh[D];
+  bool ok_lo[D], ok_hi[D];  // the low / high corner along axis k is inside the grid
+  int base = 0;
 #pragma unroll
   for (int k = 0; k < D; ++k) {
     const float f = floorf(ix[k]);
     lo[k] = (int)f;
     wl[k] = __fsub_rn(__fadd_rn(f, 1.f), ix[k]);
     wh[k] = __fsub_rn(ix[k], f);
+    ok_lo[k] = lo[k] >= 0 && lo[k] < size[k];
+    ok_hi[k] = lo[k] >= -1 && lo[k] + 1 < size[k];
+    step[k] = k == 0 ? 1 : step[k - 1] * size[k - 1];
+    base += lo[k] * step[k];
   }
+  // weight products in the order x * y (* z), shared by the corners that differ only in z
+  float wxy[4];
+#pragma unroll
+  for (int b = 0; b < 4; ++b) wxy[b] = __fmul_rn((b & 1) ? wh[0] : wl[0], ((b >> 1) & 1) ? wh[1] : wl[1]);
 #pragma unroll
   for (int b = 0; b < (1 << D); ++b) {
-    float w;
-    int flat = 0;
+    int flat = base;
     bool ok = true;
 #pragma unroll
-    for (int k = D - 1; k >= 0; --k) {
-      const int ck = lo[k] + ((b >> k) & 1);
-      ok = ok && (ck >= 0) && (ck < size[k]);
-      flat = flat * size[k] + ck;
+    for (int k = 0; k < D; ++k) {
+      const bool hi = (b >> k) & 1;
+      if (hi) flat += step[k];
+      ok = ok && (hi ? ok_hi[k] : ok_lo[k]);
     }
-    w = (b & 1) ? wh[0] : wl[0];
-#pragma unroll
-    for (int k = 1; k < D; ++k) w = __fmul_rn(w, ((b >> k) & 1) ? wh[k] : wl[k]);
+    float w = wxy[b & 3];
+    if (D == 3) w = __fmul_rn(w, ((b >> 2) & 1) ? wh[D - 1] : wl[D - 1]);
     c.idx[b] = ok ? flat : -1;
     c.w[b] = ok ? w : 0.f;
   }
@@ -242,9 +251,10 @@ __device__ __forceinline__ void basis_corners(const FFField& f, int l, const flo
     linear_corners<BD>(ix, sz, bc);
 }
 
-// Gather V channels at channel offset c of every valid corner (ATen corner order).
+// Gather V channels at channel offset c of every valid corner (ATen corner order). Offsets are
+// 32-bit: every grid (one basis level, one coefficient volume) has fewer than 2^31 elements.
 template <int V, int D, typename T>
-__device__ __forceinline__ void gather(const T* __restrict__ grid, int64_t stride, int c, const Corners<D>& cn,
+__device__ __forceinline__ void gather(const T* __restrict__ grid, int stride, int c, const Corners<D>& cn,
                                        float* acc) {
 #pragma unroll
   for (int v = 0; v < V; ++v) acc[v] = 0.f;
@@ -252,7 +262,7 @@ __device__ __forceinline__ void gather(const T* __restrict__ grid, int64_t strid
   for (int k = 0; k < Corners<D>::K; ++k) {
     if (cn.idx[k] >= 0 && cn.w[k] != 0.f) {
       float t[V];
-      load_vec<V>(grid + (int64_t)cn.idx[k] * stride + c, t);
+      load_vec<V>(grid + (cn.idx[k] * stride + c), t);
 #pragma unroll
       for (int v = 0; v < V; ++v) acc[v] += t[v] * cn.w[k];
     }
@@ -260,7 +270,7 @@ __device__ __forceinline__ void gather(const T* __restrict__ grid, int64_t strid
 }
 
 template <int V, int D>
-__device__ __forceinline__ void scatter(float* __restrict__ grad, int64_t stride, int c, const Corners<D>& cn,
+__device__ __forceinline__ void scatter(float* __restrict__ grad, int stride, int c, const Corners<D>& cn,
                                         const float* g) {
 #pragma unroll
   for (int k = 0; k < Corners<D>::K; ++k) {
@@ -268,7 +278,7 @@ __device__ __forceinline__ void scatter(float* __restrict__ grad, int64_t stride
       float t[V];
 #pragma unroll
       for (int v = 0; v < V; ++v) t[v] = g[v] * cn.w[k];
-      atomic_add_vec<V>(grad + (int64_t)cn.idx[k] * stride + c, t);
+      atomic_add_vec<V>(grad + (cn.idx[k] * stride + c), t);
     }
   }
 }
