@@ -110,10 +110,13 @@ NCU_TRAFFIC = {"ff_field_fit_step_binned": 69.623552e6 + 1.303296e6,
 
 def bytes_per_point(m, gathers, param_bytes):
     """Algorithmic bytes per point: `gathers` passes over K corners x (sum C + C_coeff)
-    channels at param_bytes, one float32 scatter of the same, coords (12 B) + target (4 B)."""
+    channels at param_bytes, one float32 scatter of the same, coords + targets (4 B each).
+    The fwd+bwd algorithm gathers twice (the backward re-reads the grid values it multiplies
+    by): 2 G + S + IO = 2,320 B for the 3-D BF16 point; the fused kernel keeps the values in
+    registers and reads them once (1 G + S + IO = 1,744 B)."""
     k = 2 ** m.in_dim
     ch = m.n_feat * 2
-    return gathers * k * ch * param_bytes + k * ch * 4 + 12 + 4
+    return gathers * k * ch * param_bytes + k * ch * 4 + 4 * m.in_dim + 4 * m.linear_mat.out_dim
 
 
 def run_native(args, ws, rank, local):
@@ -211,7 +214,9 @@ def run_native(args, ws, rank, local):
     pts = n * args.steps * ws
     value = pts / (ms / 1e3)
     kern_ms = float(np.mean(k_fast)) if k_fast else None
-    bpp = bytes_per_point(m, runner.gathers_per_point, 2 if m.precision == "bf16" else 4)
+    pb = 2 if m.precision == "bf16" else 4
+    bpp = bytes_per_point(m, 2, pb)  # the fwd+bwd algorithm's bytes
+    bpp_read_once = bytes_per_point(m, 1, pb)  # what the fused kernel reads and writes
     peaks = {}
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -236,7 +241,9 @@ def run_native(args, ws, rank, local):
                      "traffic": NCU_TRAFFIC.get(runner.dominant_kernel),
                      "traffic_source": "ncu dram read+write of the fit kernel, one 262,144-point launch "
                                        "(profiles/fused_fit_kernel_cfg1_ncu.md)",
-                     "bytes_per_point": bpp, "kernel_ms": kern_ms,
+                     "bytes_per_point": bpp, "bytes_per_point_read_once": bpp_read_once,
+                     "frac_read_once": (achieved * bpp_read_once / bpp / peak) if achieved else None,
+                     "kernel_ms": kern_ms,
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if "hbm_gbs" in peaks else "fallback"},
         "gpu_launches": launches,
         "clocks": ck,

@@ -16,7 +16,7 @@ LIB_PATH = os.path.join(_PKG, "libffgb.so")
 
 FF_MAX_LEVELS = 8
 FF_MAX_MLP_LAYERS = 4
-FF_OK, FF_ERR_ARG, FF_ERR_UNSUPPORTED, FF_ERR_ALIGN, FF_ERR_CUDA, FF_ERR_SIZE = 0, -1, -2, -3, -4, -5
+FF_OK, FF_ERR_ARG, FF_ERR_UNSUPPORTED, FF_ERR_ALIGN, FF_ERR_CUDA, FF_ERR_SIZE, FF_ERR_LIMIT = 0, -1, -2, -3, -4, -5, -6
 FF_MAP = {"sawtooth": 0, "triangle": 1}
 FF_INTERP = {"bilinear": 0, "linear": 0, "trilinear": 0, "nearest": 1}
 FF_F32, FF_BF16 = 0, 1
@@ -81,6 +81,8 @@ SIGNATURES = {
     "ff_field_fit_step_binned": (c_i32, [_P(FFField), c_vp, c_vp, _P(FFMlp), c_vp, c_vp, c_i64, c_i32, c_f32, c_vp,
                                          c_vp, c_vp, _P(FFMlpGrad), c_i32, c_vp, c_i64, c_vp]),
     "ff_zero_f32": (c_i32, [c_vp, c_vp, c_i32, c_vp]),
+    "ff_occupancy_workspace_bytes": (c_i64, [c_i32, c_i32, c_i32]),
+    "ff_occupancy_mask": (c_i32, [c_vp, c_i32, c_i32, c_i32, c_f32, c_i32, c_vp, c_vp, c_vp, c_vp, c_i64, c_vp]),
     "ff_march_count": (c_i32, [_P(FFRender), c_vp, c_vp, c_i64, c_vp, c_vp, c_vp]),
     "ff_scan_workspace_bytes": (c_i64, [c_i64]),
     "ff_scan_counts": (c_i32, [c_vp, c_i64, c_vp, c_vp, c_i64, c_vp]),
@@ -153,12 +155,13 @@ def stream_ptr():
 
 _launches = [0]
 _NON_LAUNCHING = {"ff_abi_version", "ff_last_error", "ff_device_info", "ff_struct_size", "ff_scan_workspace_bytes",
-                  "ff_field_fit_binned_workspace_bytes",
+                  "ff_field_fit_binned_workspace_bytes", "ff_occupancy_workspace_bytes",
                   "ff_scan_noalloc_max_counts"}
 
 
 # entry points that enqueue more than one kernel of this library
-_KERNELS_PER_CALL = {"ff_scan_counts": 3, "ff_scan_counts_noalloc": 3}
+_KERNELS_PER_CALL = {"ff_scan_counts": 3, "ff_scan_counts_noalloc": 3,
+                     "ff_occupancy_mask": 5}  # init, pool, unite, size, filter (3 when min_size <= 1)
 
 
 def reset_launch_count():

@@ -267,6 +267,29 @@ int ff_zero_f32(float* const* ptrs, const int64_t* counts, int32_t n_buffers, vo
   return cuda_status(launch_zero_buffers(ptrs, counts, n_buffers, (cudaStream_t)stream), "ff_zero_f32 launch");
 }
 
+int64_t ff_occupancy_workspace_bytes(int32_t depth, int32_t height, int32_t width) {
+  const int64_t v = (int64_t)depth * height * width;
+  if (depth < 1 || height < 1 || width < 1 || v >= (1ll << 31)) return FF_ERR_ARG;
+  return occupancy_workspace_bytes(v);
+}
+
+int ff_occupancy_mask(const float* alpha, int32_t depth, int32_t height, int32_t width, float threshold,
+                      int32_t min_size, int32_t* bits, float* volume, int32_t* bbox, void* workspace,
+                      int64_t workspace_bytes, void* stream) {
+  const int64_t need = ff_occupancy_workspace_bytes(depth, height, width);
+  if (need < 0) return set_error(FF_ERR_ARG, "bad occupancy volume dimensions");
+  if (!alpha || !bits || !bbox || !workspace) return set_error(FF_ERR_ARG, "alpha/bits/bbox/workspace are NULL");
+  if (workspace_bytes < need) return set_error(FF_ERR_SIZE, "workspace smaller than ff_occupancy_workspace_bytes");
+  if (!aligned(workspace, 256)) return set_error(FF_ERR_ALIGN, "workspace must be 256-byte aligned");
+  int status = 0;
+  int rc = cuda_status(launch_occupancy_mask(alpha, depth, height, width, threshold, min_size, bits, volume, bbox,
+                                             workspace, &status, (cudaStream_t)stream),
+                       "ff_occupancy_mask");
+  if (rc) return rc;
+  if (status) return set_error(FF_ERR_LIMIT, "ff_occupancy_mask: a union-find loop hit its iteration limit");
+  return FF_OK;
+}
+
 int ff_march_count(const FFRender* r, const float* rays, const float* jitter, int64_t n_rays, int32_t* counts,
                    float* t_min, void* stream) {
   int rc = validate_render(r, rays, n_rays);

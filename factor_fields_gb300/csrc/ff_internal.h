@@ -75,6 +75,12 @@ cudaError_t launch_fit_bin(const FFField& f, const float* x, const float* target
 constexpr int kMaxZeroBuffers = 8;  // buffers per zeroing launch (more: several launches)
 cudaError_t launch_zero_buffers(float* const* ptrs, const int64_t* counts, int n_buffers, cudaStream_t st);
 
+// occupancy_kernels.cu
+int64_t occupancy_workspace_bytes(int64_t voxels);
+cudaError_t launch_occupancy_mask(const float* alpha, int d, int h, int w, float threshold, int min_size,
+                                  int32_t* bits, float* vol, int32_t* bbox, void* workspace, int* status_host,
+                                  cudaStream_t st);
+
 // render_kernels.cu
 int64_t scan_workspace_bytes(int64_t n);
 cudaError_t launch_march_count(const FFRender& r, const float* rays, const float* jitter, int64_t n, int32_t* counts,

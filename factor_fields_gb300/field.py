@@ -323,23 +323,33 @@ class FactorFields(torch.nn.Module):
 
     @torch.no_grad()
     def updateAlphaMask(self, gridSize=(200, 200, 200), is_update_alphaMask=False, times=16, seed=None):
-        """:757-793: dense alpha -> 3x3x3 max-pool -> threshold -> AlphaGridMask (bitfield), and
-        the padded bounding box of the occupied voxels. skimage's remove_small_objects (:774) is
-        not applied (a floater filter the benchmark scenes do not need)."""
+        """:757-793: dense alpha -> ff_occupancy_mask (clamp, 3x3x3 max-pool, threshold, removal
+        of 6-connected components smaller than the mean grid dimension like the reference's
+        remove_small_objects, bit packing, bounding box) -> AlphaGridMask, and the padded
+        bounding box of the occupied voxels as the new aabb."""
         from .renderer import AlphaGridMask
         alpha, dense_xyz = self.getDenseAlpha(gridSize, times=times, seed=seed)
-        alpha = alpha.clamp(0, 1)[None, None]
-        alpha = F.max_pool3d(alpha, kernel_size=3, padding=1, stride=1).view(list(gridSize)[::-1])
+        d, h, w = alpha.shape
         thres = float(self.cfg.renderer.alphaMask_thres) if is_update_alphaMask else 0.08
-        occ = (alpha >= thres).float()
-        valid = dense_xyz[occ > 0.5]
-        if valid.shape[0] == 0:
-            # nothing occupied yet (an untrained field): keep the current mask — an empty mask
+        min_size = int(math.ceil(float(np.mean(alpha.shape))))  # remove_small_objects keeps size >= min_size
+        need = int(N.lib().ff_occupancy_workspace_bytes(d, h, w))
+        N.check(0 if need >= 0 else need, "ff_occupancy_workspace_bytes")
+        ws = torch.empty(need, dtype=torch.uint8, device=self.device)
+        bits = torch.empty((alpha.numel() + 31) // 32, dtype=torch.int32, device=self.device)
+        vol = torch.empty(alpha.shape, dtype=torch.float32, device=self.device)
+        bbox = torch.empty(6, dtype=torch.int32, device=self.device)
+        alpha = alpha.contiguous()
+        N.call("ff_occupancy_mask", N.ptr(alpha), d, h, w, thres, min_size, N.ptr(bits), N.ptr(vol), N.ptr(bbox),
+               N.ptr(ws), need, N.stream_ptr(), kernels=5 if min_size > 1 else 3)
+        x0, y0, z0, x1, y1, z1 = bbox.tolist()
+        if x0 > x1:
+            # nothing occupied yet (an untrained field): keep the current mask - an empty mask
             # would leave no live samples and so no gradients (the reference fails here on amin)
             return self.aabb.clone()
         if is_update_alphaMask:
-            self.alphaMask = AlphaGridMask(self.device, self.inward_aabb, occ)
-        lo, hi = valid.amin(0), valid.amax(0)
+            self.alphaMask = AlphaGridMask(self.device, self.inward_aabb, vol, bits=bits)
+        lo = torch.stack((dense_xyz[0, 0, x0, 0], dense_xyz[0, y0, 0, 1], dense_xyz[z0, 0, 0, 2]))
+        hi = torch.stack((dense_xyz[0, 0, x1, 0], dense_xyz[0, y1, 0, 1], dense_xyz[z1, 0, 0, 2]))
         pad = (hi - lo) / 20
         return torch.stack((lo - pad, hi + pad))
 

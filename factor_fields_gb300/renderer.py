@@ -32,7 +32,7 @@ class AlphaGridMask(torch.nn.Module):
     """models/FactorFields.py:91-110: a 0/1 occupancy volume [D, H, W] over an aabb, kept as
     the float volume (reference layout) and as a packed bitfield for the kernels."""
 
-    def __init__(self, device, aabb, alpha_volume):
+    def __init__(self, device, aabb, alpha_volume, bits=None):
         super().__init__()
         self.device = device
         self.aabb = aabb.to(device)
@@ -41,7 +41,8 @@ class AlphaGridMask(torch.nn.Module):
         self.alpha_volume = alpha_volume.view(1, 1, *alpha_volume.shape[-3:]).to(device)
         self.gridSize = torch.tensor([alpha_volume.shape[-1], alpha_volume.shape[-2], alpha_volume.shape[-3]],
                                      dtype=torch.long, device=device)
-        self.bits = pack_bits(self.alpha_volume.reshape(-1) > 0)
+        # bits: the packed volume when the caller has it (ff_occupancy_mask), else packed here
+        self.bits = bits.to(device) if bits is not None else pack_bits(self.alpha_volume.reshape(-1) > 0)
 
     def sample_alpha(self, xyz_sampled):
         """The reference's trilinear lookup (:103-107) — used for inspection, not by the kernels."""

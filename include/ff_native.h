@@ -42,7 +42,8 @@ enum {
   FF_ERR_UNSUPPORTED = -2, /* a shape or mode this library does not implement */
   FF_ERR_ALIGN = -3,       /* a pointer is not aligned as documented */
   FF_ERR_CUDA = -4,        /* a CUDA runtime call failed (see ff_last_error) */
-  FF_ERR_SIZE = -5         /* a size exceeds a documented maximum */
+  FF_ERR_SIZE = -5,        /* a size exceeds a documented maximum */
+  FF_ERR_LIMIT = -6        /* a bounded device loop ran out of iterations (result not valid) */
 };
 
 enum { FF_MAP_SAWTOOTH = 0, FF_MAP_TRIANGLE = 1 };
@@ -190,6 +191,20 @@ FF_API int ff_field_fit_step_binned(const FFField* f, const void* basis, const v
  * memory, read during the call) in one launch per 8 buffers: a training step's gradient
  * zeroing (optimizer.zero_grad) and loss accumulator reset without one fill per tensor. */
 FF_API int ff_zero_f32(float* const* ptrs, const int64_t* counts, int32_t n_buffers, void* stream);
+
+/* ---- occupancy-volume maintenance (updateAlphaMask, models/FactorFields.py:757-793) -------- */
+/* From the dense alpha volume [depth][height][width] (z, y, x; float32): clamp to [0, 1], 3x3x3
+ * max-pool (stride 1, padding 1), >= threshold, then drop the 6-connected components with fewer
+ * than min_size voxels (skimage remove_small_objects, connectivity=1; min_size <= 1 keeps
+ * all). Outputs: bits [ceil(V / 32)] int32 (bit k of word w = voxel 32 w + k, the layout
+ * FFRender.alpha_bits reads), volume [V] 0/1 float32 (optional), bbox [6] int32 = x, y, z
+ * minimum then maximum voxel index of the kept voxels (x_min > x_max when none is kept).
+ * Synchronises the stream before returning (it reads a status word back): not for graph
+ * capture. FF_ERR_LIMIT if a bounded union-find loop ran out (results invalid). */
+FF_API int64_t ff_occupancy_workspace_bytes(int32_t depth, int32_t height, int32_t width);
+FF_API int ff_occupancy_mask(const float* alpha, int32_t depth, int32_t height, int32_t width, float threshold,
+                             int32_t min_size, int32_t* bits, float* volume, int32_t* bbox, void* workspace,
+                             int64_t workspace_bytes, void* stream);
 
 /* ---- rendering (bounded scenes): march, compact, composite ------------------------------ */
 

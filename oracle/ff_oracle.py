@@ -379,6 +379,35 @@ def occupancy_test(alpha_volume, aabb, xyz):
     return val > f32(0.5)
 
 
+def occupancy_mask(alpha, threshold, min_size):
+    """updateAlphaMask's volume steps (models/FactorFields.py:763-774): alpha [D, H, W] clamped to
+    [0, 1], 3x3x3 max-pool (stride 1, padding 1), >= threshold, then remove_small_objects(...,
+    min_size, connectivity=1). That last function is scikit-image's (requirements.txt:8, version
+    unpinned; not installed here): it labels the True voxels into connected components with
+    the connectivity-1 structure (6 neighbours in 3-D) and clears every component with fewer
+    than min_size voxels. Restated here with scipy.ndimage.label, the labelling routine it
+    wraps; parity with scikit-image itself is unpinned. Returns (keep [D, H, W] bool, bitfield
+    words int32 [ceil(V / 32)], bbox (x_min, y_min, z_min, x_max, y_max, z_max) or None)."""
+    from scipy import ndimage
+    a = np.clip(np.asarray(alpha, f32), f32(0), f32(1))
+    pooled = ndimage.maximum_filter(a, size=3, mode="constant", cval=-np.inf)
+    occ = pooled >= f32(threshold)
+    if min_size > 1:
+        labels, _ = ndimage.label(occ, structure=ndimage.generate_binary_structure(3, 1))
+        sizes = np.bincount(labels.reshape(-1))
+        small = sizes < min_size
+        small[0] = True  # background
+        occ = ~small[labels]
+    flat = occ.reshape(-1)
+    pad = (-flat.size) % 32
+    b = np.concatenate([flat, np.zeros(pad, bool)]).reshape(-1, 32).astype(np.uint64)
+    words = (b << np.arange(32, dtype=np.uint64)).sum(1).astype(np.uint32).view(np.int32)
+    if not flat.any():
+        return occ, words, None
+    z, y, x = np.nonzero(occ)
+    return occ, words, (x.min(), y.min(), z.min(), x.max(), y.max(), z.max())
+
+
 def softplus_shift(f, shift):
     """models/FactorFields.py:639-641 with torch.nn.functional.softplus (threshold 20)."""
     x = np.asarray(f, f64) + shift

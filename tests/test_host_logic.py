@@ -102,3 +102,24 @@ def test_reference_state_dict_round_trip(tmp_path):
     m3 = FactorFields(cfg, device="cpu")
     m3.load(torch.load(str(p), weights_only=False))
     assert torch.equal(m3.coeffs[0], m.coeffs[0])
+
+
+def test_occupancy_oracle_known_answer():
+    """The oracle's remove_small_objects restatement: 6-connectivity (diagonal neighbours are
+    separate components), components below min_size removed, max-pool before the threshold."""
+    from oracle import ff_oracle as O
+    a = np.zeros((12, 12, 12), np.float32)
+    a[2, 2, 2] = 1.0                  # pooled: a 3x3x3 cube = 27 voxels
+    a[8, 8, 8] = 0.9                  # another 27-voxel cube
+    a[8, 8, 11] = 0.7                 # pooled cube clipped at the x border: 3x3x2 = 18, touching the
+    occ, _, box = O.occupancy_mask(a, 0.5, 28)  # previous one (x 9 / x 10): one 45-voxel component
+    assert occ.sum() == 45 and not occ[2, 2, 2]
+    assert box == (7, 7, 7, 11, 9, 9)
+    occ, words, _ = O.occupancy_mask(a, 0.5, 1)
+    assert occ.sum() == 27 + 45
+    c = np.zeros((10, 10, 10), np.float32)
+    c[2, 2, 2] = c[2, 5, 5] = 1.0     # pooled cubes touching only along an edge (diagonal in y-x)
+    occ, _, _ = O.occupancy_mask(c, 0.5, 28)
+    assert occ.sum() == 0             # two 27-voxel components under 6-connectivity, both < 28
+    occ, _, _ = O.occupancy_mask(c, 0.5, 27)
+    assert occ.sum() == 54
