@@ -81,6 +81,7 @@ SIGNATURES = {
     "ff_field_fit_step_binned": (c_i32, [_P(FFField), c_vp, c_vp, _P(FFMlp), c_vp, c_vp, c_i64, c_i32, c_f32, c_vp,
                                          c_vp, c_vp, _P(FFMlpGrad), c_i32, c_vp, c_i64, c_vp]),
     "ff_zero_f32": (c_i32, [c_vp, c_vp, c_i32, c_vp]),
+    "ff_filter_rays": (c_i32, [_P(FFRender), c_vp, c_i64, c_i32, c_i32, c_vp, c_vp]),
     "ff_occupancy_workspace_bytes": (c_i64, [c_i32, c_i32, c_i32]),
     "ff_occupancy_mask": (c_i32, [c_vp, c_i32, c_i32, c_i32, c_f32, c_i32, c_vp, c_vp, c_vp, c_vp, c_i64, c_vp]),
     "ff_march_count": (c_i32, [_P(FFRender), c_vp, c_vp, c_i64, c_vp, c_vp, c_vp]),

@@ -321,6 +321,17 @@ int ff_scan_counts_noalloc(const int32_t* counts, int64_t n, int64_t* offsets, v
   return cuda_status(launch_scan_noalloc(counts, n, offsets, (cudaStream_t)stream), "ff_scan_counts_noalloc");
 }
 
+int ff_filter_rays(const FFRender* r, const float* rays, int64_t n_rays, int32_t n_samples, int32_t bbox_only,
+                   uint8_t* keep, void* stream) {
+  int rc = validate_render(r, rays, n_rays);
+  if (rc) return rc;
+  if (n_rays > 0 && !keep) return set_error(FF_ERR_ARG, "keep is NULL");
+  if (!bbox_only && (n_samples < 1 || !r->occ_bits))
+    return set_error(FF_ERR_ARG, "ff_filter_rays needs n_samples >= 1 and an occupancy bitfield (or bbox_only)");
+  return cuda_status(launch_filter_rays(*r, rays, n_rays, n_samples, bbox_only, keep, (cudaStream_t)stream),
+                     "ff_filter_rays launch");
+}
+
 int ff_march_emit(const FFRender* r, const float* rays, const float* jitter, int64_t n_rays, const int64_t* offsets,
                   float* xyz, int32_t* sample_idx, void* stream) {
   int rc = validate_render(r, rays, n_rays);

@@ -88,6 +88,8 @@ cudaError_t launch_march_count(const FFRender& r, const float* rays, const float
 cudaError_t launch_scan(const int32_t* counts, int64_t n, int64_t* offsets, void* workspace, cudaStream_t s);
 int64_t scan_noalloc_max_counts();
 cudaError_t launch_scan_noalloc(const int32_t* counts, int64_t n, int64_t* offsets, cudaStream_t s);
+cudaError_t launch_filter_rays(const FFRender& r, const float* rays, int64_t n, int n_samples, int bbox_only,
+                               uint8_t* keep, cudaStream_t s);
 cudaError_t launch_march_emit(const FFRender& r, const float* rays, const float* jitter, int64_t n,
                               const int64_t* offsets, float* xyz, int32_t* sample_idx, cudaStream_t s);
 cudaError_t launch_composite_forward(const FFRender& r, const float* rays, const float* jitter, int64_t n,

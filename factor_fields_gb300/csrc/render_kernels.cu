@@ -55,7 +55,9 @@ __device__ __forceinline__ float sample_z(const FFRender& r, const RayGeo& g, in
   return __fadd_rn(g.t_min, __fmul_rn(r.step, rng));
 }
 
-__device__ __forceinline__ bool occupied(const FFRender& r, const float* p) {
+// Trilinear value of the 0/1 occupancy volume at p (AlphaGridMask.sample_alpha, :103-107):
+// float32 sum of the weights of the occupied corners in ATen's corner order, zero padding.
+__device__ __forceinline__ float occupancy_value(const FFRender& r, const float* p) {
   float ix[3];
   int sz[3];
 #pragma unroll
@@ -74,8 +76,11 @@ __device__ __forceinline__ bool occupied(const FFRender& r, const float* p) {
       if ((word >> (c.idx[b] & 31)) & 1u) val = __fadd_rn(val, c.w[b]);
     }
   }
-  return val > 0.5f;
+  return val;
 }
+
+// The march's mask test (:866): sample_alpha > 0.5.
+__device__ __forceinline__ bool occupied(const FFRender& r, const float* p) { return occupancy_value(r, p) > 0.5f; }
 
 // Sample i of the ray: live (in the box and, with a mask, occupied) and its position.
 __device__ __forceinline__ bool sample_live(const FFRender& r, const RayGeo& g, int i, float* p) {
@@ -88,6 +93,47 @@ __device__ __forceinline__ bool sample_live(const FFRender& r, const RayGeo& g, 
   }
   if (in && r.occ_bits) in = occupied(r, p);
   return in;
+}
+
+// filtering_rays (:825-841), warp per ray. bbox_only: the ray meets the aabb (t_max > t_min of
+// the slab test, no clamping). Else: some sample z_i = t_min + step * i, i < n_samples (no
+// jitter, all samples, in the box or not) has sample_alpha > 0.
+__global__ void __launch_bounds__(kRayWarps * 32) filter_rays_kernel(const FFRender r, const float* __restrict__ rays,
+                                                                    int64_t n_rays, int n_samples, int bbox_only,
+                                                                    uint8_t* __restrict__ keep) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t ray = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; ray < n_rays;
+       ray += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+    bool hit = false;
+    if (bbox_only) {
+      float tmin = -INFINITY, tmax = INFINITY;
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const float o = rays[ray * 6 + k], d = rays[ray * 6 + 3 + k];
+        const float vec = (d == 0.f) ? 1e-6f : d;
+        const float ra = __fdiv_rn(__fsub_rn(r.aabb_max[k], o), vec);
+        const float rb = __fdiv_rn(__fsub_rn(r.aabb_min[k], o), vec);
+        tmin = fmaxf(tmin, fminf(ra, rb));
+        tmax = fminf(tmax, fmaxf(ra, rb));
+      }
+      hit = tmax > tmin;
+    } else {
+      const RayGeo g = ray_setup(r, rays, nullptr, ray);
+      for (int i0 = 0; i0 < n_samples && !hit; i0 += 32) {
+        const int i = i0 + lane;
+        bool h = false;
+        if (i < n_samples) {
+          const float z = sample_z(r, g, i);
+          float p[3];
+#pragma unroll
+          for (int k = 0; k < 3; ++k) p[k] = __fadd_rn(g.o[k], __fmul_rn(g.d[k], z));
+          h = occupancy_value(r, p) > 0.f;
+        }
+        hit = __any_sync(0xffffffffu, h);
+      }
+    }
+    if (lane == 0) keep[ray] = hit ? 1 : 0;
+  }
 }
 
 __global__ void __launch_bounds__(kRayWarps * 32) march_count_kernel(const FFRender r, const float* __restrict__ rays,
@@ -520,6 +566,13 @@ cudaError_t launch_scan(const int32_t* counts, int64_t n, int64_t* offsets, void
   scan_blocks_kernel<<<(unsigned)nb, kScanThreads, 0, s>>>(counts, n, sums);
   scan_sums_kernel<<<1, kScanThreads, 0, s>>>(sums, nb);
   scan_apply_kernel<<<(unsigned)nb, kScanThreads, 0, s>>>(counts, n, sums, offsets);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_filter_rays(const FFRender& r, const float* rays, int64_t n, int n_samples, int bbox_only,
+                               uint8_t* keep, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  filter_rays_kernel<<<ray_blocks(n), kRayWarps * 32, 0, s>>>(r, rays, n, n_samples, bbox_only, keep);
   return cudaGetLastError();
 }
 

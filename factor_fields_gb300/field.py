@@ -15,6 +15,7 @@ precision='fp32' is the drop-in path (float32 storage and math, parity 1e-5 with
 reference). precision='bf16' reads BF16 copies of the grids (refreshed automatically after
 the float32 master parameters change) with float32 accumulation and float32 gradients.
 """
+import ctypes
 import math
 
 import numpy as np
@@ -352,6 +353,40 @@ class FactorFields(torch.nn.Module):
         hi = torch.stack((dense_xyz[0, 0, x1, 0], dense_xyz[0, y1, 0, 1], dense_xyz[z1, 0, 0, 2]))
         pad = (hi - lo) / 20
         return torch.stack((lo - pad, hi + pad))
+
+    @torch.no_grad()
+    def shrink(self, new_aabb):
+        """:795-809: the field is rebuilt for the new box (setup_params: coefficient / basis
+        resolutions follow the box) and re-initialised; aabb and inward_aabb become new_aabb and
+        the render parameters are recomputed. The parameters are new tensors: build a new
+        optimizer afterwards, as the reference's training loop does."""
+        new_aabb = torch.as_tensor(new_aabb, dtype=torch.float32)
+        self.cfg.dataset.aabb = new_aabb.tolist()
+        self._setup(self.cfg)
+        self.aabb = self.inward_aabb = new_aabb.to(self.device)
+        self.update_renderParams(self.gridSize.tolist())
+
+    @torch.no_grad()
+    def filtering_rays(self, all_rays, all_rgbs, N_samples=256, chunk=10240 * 5, bbox_only=False):
+        """:825-841: the rays (and their colours) that meet the box (bbox_only) or have some of
+        their N_samples un-jittered samples on an occupied voxel (ff_filter_rays), in their
+        original order. Works chunk by chunk on the GPU; returns tensors on all_rays' device."""
+        from .renderer import render_desc
+        if not bbox_only and self.alphaMask is None:
+            raise ValueError("filtering_rays needs an alpha mask (updateAlphaMask) unless bbox_only=True")
+        rays = all_rays.reshape(-1, all_rays.shape[-1])
+        rgbs = all_rgbs.reshape(-1, all_rgbs.shape[-1])
+        desc = render_desc(self, N_samples, True)
+        keep = []
+        for s in range(0, rays.shape[0], chunk):
+            r = rays[s:s + chunk].to(self.device, torch.float32).contiguous()
+            k = torch.empty(r.shape[0], dtype=torch.uint8, device=self.device)
+            N.call("ff_filter_rays", ctypes.byref(desc), N.ptr(r), r.shape[0], N_samples, int(bool(bbox_only)),
+                   N.ptr(k), N.stream_ptr())
+            keep.append(k)
+        keep = torch.cat(keep).bool() if keep else torch.zeros(0, dtype=torch.bool, device=self.device)
+        keep = keep.to(rays.device)
+        return rays[keep], rgbs[keep]
 
     # ---- checkpoints (models/FactorFields.py:669-691) --------------------------------------
     def reference_state_dict(self):

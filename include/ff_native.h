@@ -252,6 +252,12 @@ FF_API int ff_scan_counts(const int32_t* counts, int64_t n, int64_t* offsets, vo
 FF_API int64_t ff_scan_noalloc_max_counts(void);
 FF_API int ff_scan_counts_noalloc(const int32_t* counts, int64_t n, int64_t* offsets, void* stream);
 
+/* filtering_rays (models/FactorFields.py:825-841): keep[ray] = 1 if some sample
+ * z_i = t_min + step * i (i < n_samples, no jitter, inside the box or not) has a trilinear
+ * occupancy value > 0 (r->occ_bits required), or with bbox_only if the ray meets r's aabb
+ * (slab test t_max > t_min, unclamped); else 0. keep: [n_rays] uint8. */
+FF_API int ff_filter_rays(const FFRender* r, const float* rays, int64_t n_rays, int32_t n_samples, int32_t bbox_only,
+                          uint8_t* keep, void* stream);
 /* Writes the live samples in ray-major order (= xyz_sampled[ray_valid] of :874): xyz [M, 3]
  * float32 and sample_idx [M] int32 (index along the ray), using the scanned offsets. */
 FF_API int ff_march_emit(const FFRender* r, const float* rays, const float* jitter, int64_t n_rays,

@@ -363,8 +363,9 @@ def sample_point(rays_o, rays_d, aabb, step, n_samples, jitter=None):
     return xyz, z, ~outside
 
 
-def occupancy_test(alpha_volume, aabb, xyz):
-    """models/FactorFields.py:103-110 + :866 — trilinear sample of a 0/1 volume > 0.5."""
+def occupancy_test(alpha_volume, aabb, xyz, thres=0.5):
+    """models/FactorFields.py:103-110 + :866 — trilinear sample of a 0/1 volume > thres (0.5 in
+    the ray march, 0 in filtering_rays :836)."""
     aabb = np.asarray(aabb, f32)
     # AlphaGridMask.invgridSize = 1.0 / aabbSize * 2 (two roundings)
     inv = ((f32(1.0) / (aabb[1] - aabb[0]).astype(f32)).astype(f32) * f32(2)).astype(f32)
@@ -376,7 +377,7 @@ def occupancy_test(alpha_volume, aabb, xyz):
     # float32 accumulation in ATen's corner order (the test is a threshold on a float32 sum)
     for flat, w, valid in sample_corners(pts, sizes, True, "zeros", "bilinear"):
         val = (val + np.where(valid, (flatv[flat] * w).astype(f32), f32(0))).astype(f32)
-    return val > f32(0.5)
+    return val > f32(thres)
 
 
 def occupancy_mask(alpha, threshold, min_size):

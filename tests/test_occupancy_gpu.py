@@ -89,3 +89,66 @@ def test_update_alpha_mask_uses_the_native_pipeline(monkeypatch):
     lo, hi = xyz.min(0), xyz.max(0)
     pad = (hi - lo) / 20
     assert np.allclose(new_aabb.cpu().numpy(), np.stack([lo - pad, hi + pad]), rtol=0, atol=1e-6)
+
+
+def _model_with_mask(seed=4, reso=(40, 36, 44)):
+    """cfg2 model with an alpha mask from a thresholded blob volume over its aabb."""
+    from factor_fields_gb300 import FactorFields
+    from factor_fields_gb300 import workloads as W
+    from factor_fields_gb300.renderer import AlphaGridMask
+    m = FactorFields(W.field_cfg("cfg2"), device="cuda", precision="bf16")
+    vol = (blob_volume(reso, seed=seed, n_blobs=3, n_floaters=10) > 0.6).astype(np.float32)
+    m.alphaMask = AlphaGridMask(m.device, m.inward_aabb, torch.from_numpy(vol).cuda())
+    return m, vol
+
+
+@pytest.mark.parametrize("bbox_only", [False, True])
+def test_filtering_rays_matches_oracle(bbox_only):
+    """filtering_rays (models/FactorFields.py:825-841): a ray survives if any of its 256
+    un-jittered samples has trilinear occupancy > 0 (or, bbox_only, if it meets the box);
+    survivors keep their order. Rays from the blob scene's cameras plus rays that miss."""
+    from factor_fields_gb300 import workloads as W
+    m, vol = _model_with_mask()
+    rays = W.BlobScene(0).ray_pool(3000, 7).astype(np.float32)
+    rng = np.random.default_rng(8)
+    miss = np.concatenate([rng.uniform(3, 4, (500, 3)), np.tile([[1.0, 0.0, 0.0]], (500, 1))], 1).astype(np.float32)
+    rays = np.concatenate([rays, miss])[rng.permutation(3500)]
+    rgbs = rng.uniform(0, 1, (rays.shape[0], 3)).astype(np.float32)
+    kept_r, kept_c = m.filtering_rays(torch.from_numpy(rays).cuda(), torch.from_numpy(rgbs).cuda(), N_samples=256,
+                                      chunk=1024, bbox_only=bbox_only)
+    aabb = m.aabb.cpu().numpy()
+    if bbox_only:
+        o, d = rays[:, :3], rays[:, 3:6]
+        vec = np.where(d == 0, np.float32(1e-6), d)
+        ra = ((aabb[1] - o) / vec).astype(np.float32)
+        rb = ((aabb[0] - o) / vec).astype(np.float32)
+        keep = np.minimum(ra, rb).max(-1) < np.maximum(ra, rb).min(-1)
+    else:
+        xyz, _, _ = O.sample_point(rays[:, :3], rays[:, 3:6], aabb, float(m.stepSize), 256)
+        hit = O.occupancy_test(vol, m.alphaMask.aabb.cpu().numpy(), xyz.reshape(-1, 3), thres=0.0)
+        keep = hit.reshape(rays.shape[0], 256).any(-1)
+    assert 0 < keep.sum() < rays.shape[0]
+    assert np.array_equal(kept_r.cpu().numpy(), rays[keep])
+    assert np.array_equal(kept_c.cpu().numpy(), rgbs[keep])
+
+
+def test_shrink_rebuilds_the_field_for_the_new_box():
+    """shrink (models/FactorFields.py:795-809): new aabb, grids re-derived for it (setup_params)
+    and re-initialised, render step recomputed; rendering works afterwards."""
+    from factor_fields_gb300 import FactorFields
+    from factor_fields_gb300 import workloads as W
+    from factor_fields_gb300.config import FieldGeometry
+    m = FactorFields(W.field_cfg("cfg2"), device="cuda", precision="bf16")
+    new_aabb = torch.tensor([[-1.0, -0.8, -0.5], [0.9, 1.1, 0.7]])
+    m.shrink(new_aabb)
+    assert torch.equal(m.aabb.cpu(), new_aabb) and torch.equal(m.inward_aabb.cpu(), new_aabb)
+    g = FieldGeometry(m.cfg)
+    assert list(m.coeff_reso) == list(g.coeff_reso) and list(m.basis_reso) == list(g.basis_reso)
+    assert m.coeff_flat.numel() == m.layout.coeff_numel
+    assert torch.all(m.coeffs[0] == float(m.cfg.model.coef_init))
+    size = (new_aabb[1] - new_aabb[0])
+    units = size / (m.gridSize.cpu().float() - 1)
+    assert abs(float(m.stepSize) - float(units.mean() * m.cfg.renderer.step_ratio)) < 1e-6
+    rays = torch.from_numpy(W.BlobScene(0).ray_pool(256, 2)).float().cuda()
+    rgb, depth, _ = m(rays, white_bg=True, is_train=False, N_samples=256)
+    assert torch.isfinite(rgb).all() and rgb.shape == (256, 3)
