@@ -306,8 +306,24 @@ def run_radiance(args, dev):
             torch.cuda.synchronize()
             times.append(e0.elapsed_time(e1))
         ms = float(np.mean(times))
+        # a whole training step (fwd + bwd + the fused Adam update of field and proposal) at the
+        # training batch, after the measurements above
+        ttimes = []
+        for i in range(args.steps):
+            idx = torch.randint(0, pool.shape[0], (4096,), device=dev, generator=g)
+            rb, gb = pool[idx], gt[idx]
+            flush.zero_()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            tr.step(rb, gb)
+            e1.record()
+            torch.cuda.synchronize()
+            ttimes.append(e0.elapsed_time(e1))
+        tms = float(np.mean(ttimes))
         rec = {"rays_per_s": batch / (ms / 1e3), "ms_per_step": ms, "rays_per_step": batch,
-               "psnr_db": psnr, "depth_mae": depth_err, "train_steps": iters, "train_rays_per_step": 4096}
+               "psnr_db": psnr, "depth_mae": depth_err, "train_steps": iters, "train_rays_per_step": 4096,
+               "train_step_ms_with_adam": tms, "train_rays_per_s_with_adam": 4096 / (tms / 1e3)}
         if sampler is None:
             offs, _, _ = march(m, test, None, render_desc(m, 1024, True))
             rec["live_samples_per_ray"] = float(offs[-1]) / test.shape[0]

@@ -22,6 +22,7 @@ FF_INTERP = {"bilinear": 0, "linear": 0, "trilinear": 0, "nearest": 1}
 FF_F32, FF_BF16 = 0, 1
 FF_LOSS = {"l1": 0, "mse": 1}
 FF_FIT_ZERO_GRADS = 1
+FF_ADAM_ZERO_GRAD = 1
 
 c_i32, c_i64, c_f32, c_vp = ctypes.c_int32, ctypes.c_int64, ctypes.c_float, ctypes.c_void_p
 
@@ -55,6 +56,11 @@ class FFRender(ctypes.Structure):
                 ("occ_origin", c_f32 * 3), ("occ_inv", c_f32 * 3)]
 
 
+class FFAdamParam(ctypes.Structure):
+    _fields_ = [("param", c_vp), ("grad", c_vp), ("exp_avg", c_vp), ("exp_avg_sq", c_vp), ("param_bf16", c_vp),
+                ("n", c_i64), ("step", c_i64), ("lr", c_f32), ("reserved", c_f32)]
+
+
 class FFProposal(ctypes.Structure):
     _fields_ = [("aabb_min", c_f32 * 3), ("aabb_max", c_f32 * 3), ("inv_cell", c_f32 * 3), ("reso", c_i32),
                 ("param_dtype", c_i32), ("n_bins", c_i32), ("n_fine", c_i32), ("density_shift", c_f32),
@@ -81,6 +87,7 @@ SIGNATURES = {
     "ff_field_fit_step_binned": (c_i32, [_P(FFField), c_vp, c_vp, _P(FFMlp), c_vp, c_vp, c_i64, c_i32, c_f32, c_vp,
                                          c_vp, c_vp, _P(FFMlpGrad), c_i32, c_vp, c_i64, c_vp]),
     "ff_zero_f32": (c_i32, [c_vp, c_vp, c_i32, c_vp]),
+    "ff_adam_step": (c_i32, [c_vp, c_i32, c_f32, c_f32, c_f32, c_i32, c_vp]),
     "ff_filter_rays": (c_i32, [_P(FFRender), c_vp, c_i64, c_i32, c_i32, c_vp, c_vp]),
     "ff_occupancy_workspace_bytes": (c_i64, [c_i32, c_i32, c_i32]),
     "ff_occupancy_mask": (c_i32, [c_vp, c_i32, c_i32, c_i32, c_f32, c_i32, c_vp, c_vp, c_vp, c_vp, c_i64, c_vp]),

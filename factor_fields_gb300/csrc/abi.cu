@@ -106,6 +106,7 @@ int64_t ff_struct_size(int32_t which) {
     case 2: return (int64_t)sizeof(FFMlpGrad);
     case 3: return (int64_t)sizeof(FFRender);
     case 4: return (int64_t)sizeof(FFProposal);
+    case 5: return (int64_t)sizeof(FFAdamParam);
     default: return -1;
   }
 }
@@ -265,6 +266,24 @@ int ff_zero_f32(float* const* ptrs, const int64_t* counts, int32_t n_buffers, vo
   for (int b = 0; b < n_buffers; ++b)
     if (counts[b] < 0 || (counts[b] > 0 && !ptrs[b])) return set_error(FF_ERR_ARG, "NULL buffer or negative count");
   return cuda_status(launch_zero_buffers(ptrs, counts, n_buffers, (cudaStream_t)stream), "ff_zero_f32 launch");
+}
+
+int ff_adam_step(const FFAdamParam* params, int32_t n_params, float beta1, float beta2, float eps, int32_t flags,
+                 void* stream) {
+  if (n_params < 0 || (n_params > 0 && !params)) return set_error(FF_ERR_ARG, "bad parameter list");
+  if (flags & ~FF_ADAM_ZERO_GRAD) return set_error(FF_ERR_ARG, "unknown flags");
+  if (!(beta1 >= 0.f && beta1 < 1.f && beta2 >= 0.f && beta2 < 1.f && eps >= 0.f))
+    return set_error(FF_ERR_ARG, "betas must be in [0, 1) and eps >= 0");
+  for (int b = 0; b < n_params; ++b) {
+    const FFAdamParam& q = params[b];
+    if (q.n < 0 || (q.n > 0 && (!q.param || !q.grad || !q.exp_avg || !q.exp_avg_sq)))
+      return set_error(FF_ERR_ARG, "parameter " + std::to_string(b) + ": NULL buffer or negative size");
+    if (q.n > 0 && q.step < 1) return set_error(FF_ERR_ARG, "step must be >= 1");
+    if (q.param_bf16 && !aligned(q.param_bf16, 2)) return set_error(FF_ERR_ALIGN, "param_bf16 misaligned");
+  }
+  return cuda_status(launch_adam(params, n_params, beta1, beta2, eps, (flags & FF_ADAM_ZERO_GRAD) != 0,
+                                 (cudaStream_t)stream),
+                     "ff_adam_step launch");
 }
 
 int64_t ff_occupancy_workspace_bytes(int32_t depth, int32_t height, int32_t width) {

@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
+#include <cmath>
 #include <string>
 
 #include "../../include/ff_native.h"
@@ -74,6 +76,10 @@ cudaError_t launch_fit_bin(const FFField& f, const float* x, const float* target
 // util_kernels.cu
 constexpr int kMaxZeroBuffers = 8;  // buffers per zeroing launch (more: several launches)
 cudaError_t launch_zero_buffers(float* const* ptrs, const int64_t* counts, int n_buffers, cudaStream_t st);
+
+// optim_kernels.cu
+cudaError_t launch_adam(const FFAdamParam* prm, int n, float beta1, float beta2, float eps, bool zero_grad,
+                        cudaStream_t st);
 
 // occupancy_kernels.cu
 int64_t occupancy_workspace_bytes(int64_t voxels);

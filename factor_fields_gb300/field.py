@@ -179,6 +179,14 @@ class FactorFields(torch.nn.Module):
             self._bf16[0] = ver
         return self._bf16[1], self._bf16[2], N.FF_BF16
 
+    def bf16_shadows(self):
+        """{parameter: its BF16 read copy} for an optimizer that refreshes the copies itself
+        (FusedAdam); empty for precision='fp32'."""
+        if self.precision != "bf16":
+            return {}
+        self._read_buffers()
+        return {self.basis_flat: self._bf16[1], self.coeff_flat: self._bf16[2]}
+
     def _coeff_scene(self, buf):
         n = self.layout.coeff_scene_numel
         return buf[self.scene_idx * n:(self.scene_idx + 1) * n]

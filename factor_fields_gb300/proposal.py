@@ -82,7 +82,7 @@ class ProposalRenderFunction(torch.autograd.Function):
 
 class ProposalSampler:
     def __init__(self, model, reso=64, n_bins=64, n_fine=48, hidden=64, lr_grid=2e-2, lr_mlp=1e-3,
-                 density_shift=-4.0, precision="bf16", learned=True, seed=0, uniform_mix=0.0):
+                 density_shift=-4.0, precision="bf16", learned=True, seed=0, uniform_mix=0.0, fused_adam=True):
         self.m, self.learned = model, learned
         self.reso, self.n_bins, self.n_fine, self.precision = reso, n_bins, n_fine, precision
         # BF16: the head (encode + MLP, and its backward + scatter) is one tensor-core launch;
@@ -101,8 +101,15 @@ class ProposalSampler:
         self.params = [self.grid] + list(self.mlp.parameters())
         for p in self.params:
             p.grad = torch.zeros_like(p)
-        self.opt = torch.optim.Adam([{"params": [self.grid], "lr": lr_grid},
-                                     {"params": list(self.mlp.parameters()), "lr": lr_mlp}], betas=(0.9, 0.99))
+        self._bf16 = None
+        groups = [{"params": [self.grid], "lr": lr_grid}, {"params": list(self.mlp.parameters()), "lr": lr_mlp}]
+        self.fused_adam = fused_adam
+        if fused_adam:  # the update also writes the BF16 grid copy and zeroes the gradients
+            from .optim import FusedAdam
+            shadows = {self.grid: self.grid_read()} if precision == "bf16" else {}
+            self.opt = FusedAdam(groups, betas=(0.9, 0.99), shadows=shadows)
+        else:
+            self.opt = torch.optim.Adam(groups, betas=(0.9, 0.99))
         d = N.FFProposal()
         aabb = model.aabb.detach().cpu()
         for k in range(3):
@@ -116,7 +123,6 @@ class ProposalSampler:
         d.uniform_mix = float(uniform_mix)
         self.desc = d
         self.loss_buf = torch.zeros(1, device=dev)
-        self._bf16 = None
         self._job = None
 
     def grid_read(self):

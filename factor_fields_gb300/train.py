@@ -15,9 +15,16 @@ class RadianceFieldTrainer:
     n_iters (train_per_scene.py:118-125, 171-172)."""
 
     def __init__(self, model, n_samples=1024, lr_small=1e-3, lr_large=2e-2, n_iters=1000, decay_ratio=0.1,
-                 white_bg=True, sampler=None):
+                 white_bg=True, sampler=None, fused_adam=True):
         self.m, self.n_samples, self.white_bg = model, n_samples, white_bg
-        self.opt = torch.optim.Adam(model.get_optparam_groups(lr_small, lr_large), betas=(0.9, 0.99))
+        groups = model.get_optparam_groups(lr_small, lr_large)
+        if fused_adam:  # update + BF16 read copies + next step's zero_grad in one pass
+            from .optim import FusedAdam
+            self.opt = FusedAdam(groups, betas=(0.9, 0.99), shadows=model.bf16_shadows())
+        else:
+            self.opt = torch.optim.Adam(groups, betas=(0.9, 0.99))
+        self.fused_adam = fused_adam
+        self._grads_clean = False  # every gradient is known to be zero (a fused step zeroed them)
         self.lr_factor = decay_ratio ** (1.0 / max(n_iters, 1))
         self.sampler = sampler  # None: the plain uniform sampler; else a ProposalSampler
         self.jitter = None  # proposal sampler: fixed per-ray stratification jitter [R]; None: random per step
@@ -29,12 +36,23 @@ class RadianceFieldTrainer:
         rgb, depth, _ = self.m(rays, white_bg=self.white_bg, is_train=is_train, N_samples=self.n_samples)
         return rgb, depth
 
+    def _zero_grads(self):
+        if self.fused_adam:
+            for g in self.opt.param_groups:
+                for p in g["params"]:
+                    if p.grad is not None:
+                        p.grad.zero_()
+        else:
+            self.opt.zero_grad(set_to_none=False)
+        if self.sampler is not None:
+            self.sampler.zero_grad()
+
     def step(self, rays, rgb_gt, optimize=True):
         rgb, _ = self.render(rays, is_train=True)
         loss = torch.mean((rgb - rgb_gt) ** 2)
-        self.opt.zero_grad(set_to_none=False)
-        if self.sampler is not None:
-            self.sampler.zero_grad()
+        if not self._grads_clean:
+            self._zero_grads()
+        self._grads_clean = False
         loss.backward()
         if self.sampler is not None:
             self.sampler.backward()
@@ -44,6 +62,7 @@ class RadianceFieldTrainer:
                 g["lr"] = g["lr"] * self.lr_factor
             if self.sampler is not None:
                 self.sampler.step()
+            self._grads_clean = self.fused_adam and (self.sampler is None or self.sampler.fused_adam)
         return loss.detach()
 
     def graph_step(self, rays, rgb_gt):

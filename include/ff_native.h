@@ -113,7 +113,7 @@ typedef struct FFMlpGrad {
 FF_API int ff_abi_version(void);
 FF_API const char* ff_last_error(void);
 /* sizeof of the ABI structs, for binding checks: 0 FFField, 1 FFMlp, 2 FFMlpGrad, 3 FFRender,
- * 4 FFProposal. */
+ * 4 FFProposal, 5 FFAdamParam. */
 FF_API int64_t ff_struct_size(int32_t which);
 /* Number of SMs of the current device and the compute capability (major*10+minor). */
 FF_API int ff_device_info(int32_t* sm_count, int32_t* cc);
@@ -191,6 +191,28 @@ FF_API int ff_field_fit_step_binned(const FFField* f, const void* basis, const v
  * memory, read during the call) in one launch per 8 buffers: a training step's gradient
  * zeroing (optimizer.zero_grad) and loss accumulator reset without one fill per tensor. */
 FF_API int ff_zero_f32(float* const* ptrs, const int64_t* counts, int32_t n_buffers, void* stream);
+
+/* ---- optimizer --------------------------------------------------------------------------- */
+/* One parameter of ff_adam_step: float32 param, grad, Adam moments (exp_avg, exp_avg_sq, zeroed
+ * before the first step), optional BF16 copy of the param to refresh (NULL: none), element
+ * count, the step number t >= 1 after this update, and the learning rate. */
+typedef struct FFAdamParam {
+  float* param;
+  float* grad;
+  float* exp_avg;
+  float* exp_avg_sq;
+  void* param_bf16;
+  int64_t n;
+  int64_t step;
+  float lr;
+  float reserved;
+} FFAdamParam;
+enum { FF_ADAM_ZERO_GRAD = 1 };
+/* torch.optim.Adam's update (amsgrad=False, weight_decay=0) of n_params parameters in one
+ * launch per 8 parameters (params is host memory, read during the call): moments, param, the
+ * BF16 copy, and with FF_ADAM_ZERO_GRAD the gradient set to 0 (the next step's zero_grad). */
+FF_API int ff_adam_step(const FFAdamParam* params, int32_t n_params, float beta1, float beta2, float eps,
+                        int32_t flags, void* stream);
 
 /* ---- occupancy-volume maintenance (updateAlphaMask, models/FactorFields.py:757-793) -------- */
 /* From the dense alpha volume [depth][height][width] (z, y, x; float32): clamp to [0, 1], 3x3x3

@@ -44,5 +44,5 @@ def test_bindings_cover_header(lib):
 def test_struct_layouts_match(lib):
     from factor_fields_gb300 import _native as N
     assert lib.ff_abi_version() == 1
-    for i, st in enumerate([N.FFField, N.FFMlp, N.FFMlpGrad, N.FFRender, N.FFProposal]):
+    for i, st in enumerate([N.FFField, N.FFMlp, N.FFMlpGrad, N.FFRender, N.FFProposal, N.FFAdamParam]):
         assert lib.ff_struct_size(i) == ctypes.sizeof(st), st.__name__

@@ -1,0 +1,84 @@
+"""GPU checks of FusedAdam (ff_adam_step) against torch.optim.Adam."""
+import pytest
+import torch
+
+from gpu_util import need_gpu, rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(autouse=True)
+def _gpu():
+    need_gpu()
+
+
+def test_fused_adam_matches_torch_adam():
+    """Five steps over two parameter groups (different learning rates), sizes that are not
+    multiples of 4, one parameter that is an unaligned view; moments and parameters within
+    float32 rounding (1e-5 relative) of torch's single-tensor Adam; the BF16 copies equal the rounded
+    parameters; the gradients are zeroed."""
+    from factor_fields_gb300.optim import FusedAdam
+    gen = torch.Generator().manual_seed(0)
+    sizes = [1, 7, 1024, 4097, 100003]
+    base = torch.randn(sum(sizes) + 1, generator=gen)
+    ref = [torch.nn.Parameter(t.clone().cuda()) for t in torch.split(base[1:], sizes)]
+    holder = torch.randn(sizes[3] + 1, generator=gen).cuda()
+    ours = [torch.nn.Parameter(t.detach().clone()) for t in ref]
+    ours[3] = torch.nn.Parameter(holder[1:])  # storage offset 4 bytes: not 16-byte aligned
+    with torch.no_grad():
+        ours[3].copy_(ref[3])
+    shadows = {p: torch.empty_like(p, dtype=torch.bfloat16) for p in ours[2:]}
+    groups = lambda ps: [{"params": ps[:2], "lr": 2e-2}, {"params": ps[2:], "lr": 1e-3}]
+    opt_ref = torch.optim.Adam(groups(ref), betas=(0.9, 0.99), eps=1e-8, foreach=False)
+    opt = FusedAdam(groups(ours), betas=(0.9, 0.99), eps=1e-8, shadows=shadows)
+    for it in range(5):
+        for a, b in zip(ref, ours):
+            g = torch.randn(a.shape, generator=gen).cuda() * (0.1 + it)
+            a.grad = g.clone()
+            b.grad = g.clone()
+        opt_ref.step()
+        opt.step()
+        torch.cuda.synchronize()
+        for a, b in zip(ref, ours):
+            # float32 rounding: torch's kernels contract into FMAs, ff_adam_step rounds every
+            # operation (a few ulp per step, accumulating over the steps)
+            assert rel_err(b, a.detach()) < 1e-5
+            sa, sb = opt_ref.state[a], opt.state[b]
+            assert rel_err(sb["exp_avg"], sa["exp_avg"]) < 1e-5
+            assert rel_err(sb["exp_avg_sq"], sa["exp_avg_sq"]) < 1e-5
+            assert int(sb["step"]) == int(sa["step"]) == it + 1
+            assert float(b.grad.abs().max()) == 0.0
+        for p, s in shadows.items():
+            assert torch.equal(s, p.detach().to(torch.bfloat16))
+
+
+def test_trainer_with_fused_adam_trains_like_torch_adam():
+    """Configuration 3 for 150 steps with FusedAdam (field and proposal) and with torch's Adam:
+    the losses follow each other (float32 rounding and atomic order only) and go down."""
+    import numpy as np
+    from factor_fields_gb300 import FactorFields
+    from factor_fields_gb300 import workloads as W
+    from factor_fields_gb300.proposal import ProposalSampler
+    from factor_fields_gb300.train import RadianceFieldTrainer
+    scene = W.BlobScene(0)
+    pool = torch.from_numpy(scene.ray_pool(1 << 14, 5)).float()
+    gt = scene.render_gt(pool.double().numpy(), n_steps=256).cuda().float()
+    pool = pool.cuda()
+    losses = {}
+    for fused in (False, True):
+        torch.manual_seed(0)
+        m = FactorFields(W.field_cfg("cfg2"), device="cuda", precision="bf16")
+        tr = RadianceFieldTrainer(m, sampler=ProposalSampler(m, fused_adam=fused), n_iters=150, fused_adam=fused)
+        g = torch.Generator(device="cuda").manual_seed(0)
+        jit = torch.Generator(device="cuda").manual_seed(1)
+        ls = []
+        for it in range(150):
+            idx = torch.randint(0, pool.shape[0], (2048,), device="cuda", generator=g)
+            tr.jitter = torch.rand(2048, device="cuda", generator=jit)
+            ls.append(float(tr.step(pool[idx], gt[idx])))
+        losses[fused] = np.array(ls)
+    first, last = losses[True][:20].mean(), losses[True][-20:].mean()
+    assert last < 0.9 * first, (first, last)
+    for a, b in ((0, 20), (65, 85), (130, 150)):
+        fa, ta = losses[True][a:b].mean(), losses[False][a:b].mean()
+        assert abs(fa - ta) < 0.05 * ta, (a, fa, ta)
