@@ -268,6 +268,7 @@ def run_radiance(args, dev):
     gtt, gtd = scene.render_gt(test.double().numpy(), n_steps=512, with_depth=True)
     pool, test, gtt, gtd = pool.to(dev), test.to(dev), gtt.to(dev), gtd.to(dev)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
+    eval_ds = scene.test_dataset([7], width=400, height=400, n_steps=512)  # one full 400x400 test view
     iters = args.render_iters
     out = {}
     for kind, batch in (("cfg2_plain", 4096), ("cfg3_proposal", 8192)):
@@ -321,9 +322,15 @@ def run_radiance(args, dev):
             torch.cuda.synchronize()
             ttimes.append(e0.elapsed_time(e1))
         tms = float(np.mean(ttimes))
+        # the evaluation renderer on a whole 400x400 image (one pass, metrics on the GPU)
+        from factor_fields_gb300.renderer import evaluation
+        evaluation(eval_ds, m, N_vis=-1, N_samples=1024, white_bg=True, sampler=sampler)  # warm-up
+        e_psnr, e_extra = evaluation(eval_ds, m, N_vis=-1, N_samples=1024, white_bg=True, sampler=sampler)
         rec = {"rays_per_s": batch / (ms / 1e3), "ms_per_step": ms, "rays_per_step": batch,
                "psnr_db": psnr, "depth_mae": depth_err, "train_steps": iters, "train_rays_per_step": 4096,
-               "train_step_ms_with_adam": tms, "train_rays_per_s_with_adam": 4096 / (tms / 1e3)}
+               "train_step_ms_with_adam": tms, "train_rays_per_s_with_adam": 4096 / (tms / 1e3),
+               "eval_400x400": {"ms_per_image": e_extra["ms_per_image"][0], "psnr_db": e_psnr[0],
+                                "ssim": e_extra["ssim"][0]}}
         if sampler is None:
             offs, _, _ = march(m, test, None, render_desc(m, 1024, True))
             rec["live_samples_per_ray"] = float(offs[-1]) / test.shape[0]

@@ -88,6 +88,8 @@ SIGNATURES = {
                                          c_vp, c_vp, _P(FFMlpGrad), c_i32, c_vp, c_i64, c_vp]),
     "ff_zero_f32": (c_i32, [c_vp, c_vp, c_i32, c_vp]),
     "ff_adam_step": (c_i32, [c_vp, c_i32, c_f32, c_f32, c_f32, c_i32, c_vp]),
+    "ff_image_metrics_workspace_bytes": (c_i64, [c_i32, c_i32, c_i32]),
+    "ff_image_metrics": (c_i32, [c_vp, c_vp, c_i32, c_i32, c_i32, c_f32, c_vp, c_vp, c_i64, c_vp]),
     "ff_filter_rays": (c_i32, [_P(FFRender), c_vp, c_i64, c_i32, c_i32, c_vp, c_vp]),
     "ff_occupancy_workspace_bytes": (c_i64, [c_i32, c_i32, c_i32]),
     "ff_occupancy_mask": (c_i32, [c_vp, c_i32, c_i32, c_i32, c_f32, c_i32, c_vp, c_vp, c_vp, c_vp, c_i64, c_vp]),
@@ -164,12 +166,14 @@ def stream_ptr():
 _launches = [0]
 _NON_LAUNCHING = {"ff_abi_version", "ff_last_error", "ff_device_info", "ff_struct_size", "ff_scan_workspace_bytes",
                   "ff_field_fit_binned_workspace_bytes", "ff_occupancy_workspace_bytes",
+                  "ff_image_metrics_workspace_bytes",
                   "ff_scan_noalloc_max_counts"}
 
 
 # entry points that enqueue more than one kernel of this library
 _KERNELS_PER_CALL = {"ff_scan_counts": 3, "ff_scan_counts_noalloc": 3,
-                     "ff_occupancy_mask": 5}  # init, pool, unite, size, filter (3 when min_size <= 1)
+                     "ff_occupancy_mask": 5,  # init, pool, unite, size, filter (3 when min_size <= 1)
+                     "ff_image_metrics": 2}
 
 
 def reset_launch_count():

@@ -286,6 +286,23 @@ int ff_adam_step(const FFAdamParam* params, int32_t n_params, float beta1, float
                      "ff_adam_step launch");
 }
 
+int64_t ff_image_metrics_workspace_bytes(int32_t height, int32_t width, int32_t channels) {
+  if (height < 11 || width < 11 || channels < 1 || (int64_t)height * width * channels >= (1ll << 31)) return FF_ERR_ARG;
+  return image_metrics_workspace_bytes(height, width, channels);
+}
+
+int ff_image_metrics(const float* img0, const float* img1, int32_t height, int32_t width, int32_t channels,
+                     float max_val, double* mse_ssim, void* workspace, int64_t workspace_bytes, void* stream) {
+  const int64_t need = ff_image_metrics_workspace_bytes(height, width, channels);
+  if (need < 0) return set_error(FF_ERR_ARG, "images need height, width >= 11 and channels >= 1");
+  if (!img0 || !img1 || !mse_ssim || !workspace) return set_error(FF_ERR_ARG, "NULL argument");
+  if (workspace_bytes < need) return set_error(FF_ERR_SIZE, "workspace smaller than ff_image_metrics_workspace_bytes");
+  if (!aligned(workspace, 8)) return set_error(FF_ERR_ALIGN, "workspace must be 8-byte aligned");
+  return cuda_status(launch_image_metrics(img0, img1, height, width, channels, max_val, workspace, mse_ssim,
+                                          (cudaStream_t)stream),
+                     "ff_image_metrics");
+}
+
 int64_t ff_occupancy_workspace_bytes(int32_t depth, int32_t height, int32_t width) {
   const int64_t v = (int64_t)depth * height * width;
   if (depth < 1 || height < 1 || width < 1 || v >= (1ll << 31)) return FF_ERR_ARG;

@@ -81,6 +81,11 @@ cudaError_t launch_zero_buffers(float* const* ptrs, const int64_t* counts, int n
 cudaError_t launch_adam(const FFAdamParam* prm, int n, float beta1, float beta2, float eps, bool zero_grad,
                         cudaStream_t st);
 
+// metrics_kernels.cu
+int64_t image_metrics_workspace_bytes(int h, int w, int c);
+cudaError_t launch_image_metrics(const float* a, const float* b, int h, int w, int c, float max_val,
+                                 void* workspace, double* out_host, cudaStream_t st);
+
 // occupancy_kernels.cu
 int64_t occupancy_workspace_bytes(int64_t voxels);
 cudaError_t launch_occupancy_mask(const float* alpha, int d, int h, int w, float threshold, int min_size,

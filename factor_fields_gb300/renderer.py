@@ -9,6 +9,7 @@ is ff_composite_backward followed by the field/MLP backward kernels. One host sy
 per chunk reads the number of live samples (the reference synchronises on ray_valid.any()).
 """
 import ctypes
+import math
 
 import torch
 
@@ -264,3 +265,71 @@ def render_ray(rays, factor_fields, chunk=4096, N_samples=-1, ndc_ray=False, whi
     if is_train:
         return torch.cat(rgbs), torch.cat(depths), torch.cat(coeffs)
     return torch.cat(rgbs), torch.cat(depths)
+
+
+def image_metrics(img0, img1, max_val=1.0):
+    """(mse, ssim) of two [H, W, C] float32 device images (ff_image_metrics: the reference's
+    rgb_ssim, utils.py:110-156, and the MSE behind its PSNR, renderer.py:64)."""
+    a = img0.to(torch.float32).contiguous()
+    b = img1.to(device=a.device, dtype=torch.float32).contiguous()
+    h, w, c = a.shape
+    need = int(N.lib().ff_image_metrics_workspace_bytes(h, w, c))
+    N.check(0 if need >= 0 else need, "ff_image_metrics_workspace_bytes")
+    ws = torch.empty(need, dtype=torch.uint8, device=a.device)
+    out = (ctypes.c_double * 2)()
+    N.call("ff_image_metrics", N.ptr(a), N.ptr(b), h, w, c, float(max_val), out, N.ptr(ws), need, N.stream_ptr())
+    return float(out[0]), float(out[1])
+
+
+@torch.no_grad()
+def evaluation(test_dataset, factor_fields, renderer=None, savePath=None, N_vis=5, prtx="", N_samples=-1,
+               white_bg=False, ndc_ray=False, compute_extra_metrics=True, device="cuda", chunk=None,
+               sampler=None):
+    """renderer.py:30-98: render every (N_vis-spaced) test image and return its PSNRs.
+
+    The image's rays are rendered in one pass (chunk=None: H*W rays; the reference uses
+    chunks of 1,024), with the plain sampler through `renderer` (default render_ray) or, if
+    `sampler` is given, with the learned proposal sampler. Metrics run on the GPU
+    (ff_image_metrics): PSNR from the MSE and, with compute_extra_metrics, SSIM as the
+    reference's rgb_ssim. LPIPS is not computed: it needs the lpips package and its pretrained
+    AlexNet/VGG weights, which are not available. With savePath, each rendered image is saved
+    as <prtx><idx>.npy (uint8 [H, W, 3]) and <prtx>mean.txt holds (psnr[, ssim], n_params);
+    the reference's PNG/MP4 writers and the colour-mapped depth image are left out.
+    Returns (PSNRs, extras) with extras = {"ssim": [...], "ms_per_image": [...]}."""
+    import os
+    import time
+    renderer = renderer or render_ray
+    W, H = test_dataset.img_wh
+    all_rays, all_rgbs = test_dataset.all_rays, test_dataset.all_rgbs
+    n_img = all_rays.shape[0]
+    step = 1 if N_vis < 0 else max(n_img // N_vis, 1)
+    idxs = list(range(0, n_img, step))
+    psnrs, ssims, times = [], [], []
+    if savePath is not None:
+        os.makedirs(savePath, exist_ok=True)
+    for idx in idxs:
+        rays = all_rays[idx].reshape(-1, all_rays.shape[-1]).to(device, torch.float32)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        if sampler is not None:
+            rgb, depth = sampler.render(rays, is_train=False, white_bg=white_bg)
+        else:
+            rgb, depth = renderer(rays, factor_fields, chunk=chunk or rays.shape[0], N_samples=N_samples,
+                                  ndc_ray=ndc_ray, white_bg=white_bg, device=device)
+        rgb = rgb.clamp(0.0, 1.0).reshape(H, W, 3)
+        torch.cuda.synchronize()
+        times.append((time.perf_counter() - t0) * 1e3)
+        if all_rgbs is not None and len(all_rgbs):
+            gt = all_rgbs[idx].reshape(H, W, 3).to(device, torch.float32)
+            mse, ssim = image_metrics(rgb, gt, 1.0)
+            psnrs.append(-10.0 * math.log10(mse))
+            if compute_extra_metrics:
+                ssims.append(ssim)
+        if savePath is not None:
+            import numpy as np
+            np.save(os.path.join(savePath, f"{prtx}{idx:03d}.npy"), (rgb.cpu().numpy() * 255).astype("uint8"))
+    if savePath is not None and psnrs:
+        import numpy as np
+        vals = [float(np.mean(psnrs))] + ([float(np.mean(ssims))] if ssims else []) + [factor_fields.n_parameters()]
+        np.savetxt(os.path.join(savePath, f"{prtx}mean.txt"), np.asarray(vals))
+    return psnrs, {"ssim": ssims, "ms_per_image": times}

@@ -216,6 +216,21 @@ class BlobScene:
         px, py = rng.integers(0, width, n), rng.integers(0, height, n)
         return self.pixel_rays(cams[v], px, py, width, height)
 
+    def test_dataset(self, views, width=400, height=400, n_views=100, n_steps=512, device="cuda"):
+        """Full test images of the given views in the layout the reference's evaluation reads
+        (renderer.py:30-98): an object with img_wh, all_rays [V, H*W, 6] and all_rgbs
+        [V, H*W, 3] (float32 CPU tensors; the colours are the FP64 ground truth)."""
+        import types
+        cams = self.cameras(n_views)
+        py, px = np.meshgrid(np.arange(height), np.arange(width), indexing="ij")
+        px, py = px.reshape(-1), py.reshape(-1)
+        rays, rgbs = [], []
+        for v in views:
+            r = self.pixel_rays(np.repeat(cams[v][None], px.size, 0), px, py, width, height)
+            rays.append(torch.from_numpy(r).float())
+            rgbs.append(self.render_gt(r, n_steps=n_steps, device=device).float().cpu())
+        return types.SimpleNamespace(img_wh=(width, height), all_rays=torch.stack(rays), all_rgbs=torch.stack(rgbs))
+
     def render_gt(self, rays, n_steps=1024, chunk=2048, device="cuda", with_depth=False):
         """FP64 quadrature of the emission-absorption integral along each ray through the box,
         white background: rgb [n, 3] float32 (midpoint rule, n_steps steps between box entry

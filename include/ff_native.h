@@ -214,6 +214,14 @@ enum { FF_ADAM_ZERO_GRAD = 1 };
 FF_API int ff_adam_step(const FFAdamParam* params, int32_t n_params, float beta1, float beta2, float eps,
                         int32_t flags, void* stream);
 
+/* ---- evaluation metrics (renderer.py:30-98, utils.py:110-156) ------------------------------ */
+/* Mean squared error and SSIM of two [height][width][channels] float32 device images, SSIM as
+ * the reference's rgb_ssim (11-tap Gaussian, sigma 1.5, 'valid' window, k1 0.01, k2 0.03,
+ * max_val). mse_ssim: HOST double[2] = {mse, ssim}. Synchronises the stream. */
+FF_API int64_t ff_image_metrics_workspace_bytes(int32_t height, int32_t width, int32_t channels);
+FF_API int ff_image_metrics(const float* img0, const float* img1, int32_t height, int32_t width, int32_t channels,
+                            float max_val, double* mse_ssim, void* workspace, int64_t workspace_bytes, void* stream);
+
 /* ---- occupancy-volume maintenance (updateAlphaMask, models/FactorFields.py:757-793) -------- */
 /* From the dense alpha volume [depth][height][width] (z, y, x; float32): clamp to [0, 1], 3x3x3
  * max-pool (stride 1, padding 1), >= threshold, then drop the 6-connected components with fewer

@@ -618,3 +618,31 @@ def proposal_loss(o, seg_len, shift, distance_scale, w_field, bin_of, loss_scale
         om[:, k] -= h
         grad[:, k] = (loss_of(op) - loss_of(om)) / (2 * h)
     return base.sum(), grad
+
+
+def image_metrics(img0, img1, max_val=1.0):
+    """utils.py:110-156 (rgb_ssim) and renderer.py:64 (the MSE behind PSNR) on [H, W, C] float32
+    images: (mse, ssim). The squared and product images are float32 like the reference's tensor
+    ops; the blurs run in float64 through scipy.signal.convolve2d as the reference's do."""
+    from scipy import signal
+    a = np.asarray(img0, f32)
+    b = np.asarray(img1, f32)
+    mse = float(np.mean((a.astype(f64) - b.astype(f64)) ** 2))
+    fs, sigma = 11, 1.5
+    hw = fs // 2
+    shift = (2 * hw - fs + 1) / 2
+    filt = np.exp(-0.5 * ((np.arange(fs) - hw + shift) / sigma) ** 2)
+    filt /= np.sum(filt)
+
+    def blur(z):
+        return np.stack([signal.convolve2d(signal.convolve2d(z[..., i], filt[:, None], mode="valid"),
+                                           filt[None, :], mode="valid") for i in range(z.shape[-1])], -1)
+    mu0, mu1 = blur(a), blur(b)
+    mu00, mu11, mu01 = mu0 * mu0, mu1 * mu1, mu0 * mu1
+    s00 = np.maximum(0.0, blur((a * a).astype(f32)) - mu00)
+    s11 = np.maximum(0.0, blur((b * b).astype(f32)) - mu11)
+    s01 = blur((a * b).astype(f32)) - mu01
+    s01 = np.sign(s01) * np.minimum(np.sqrt(s00 * s11), np.abs(s01))
+    c1, c2 = (0.01 * max_val) ** 2, (0.03 * max_val) ** 2
+    ssim = np.mean(((2 * mu01 + c1) * (2 * s01 + c2)) / ((mu00 + mu11 + c1) * (s00 + s11 + c2)))
+    return mse, float(ssim)
