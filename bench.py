@@ -251,11 +251,32 @@ def run_native(args, ws, rank, local):
     return res
 
 
+def _train_radiance(kind, seed, iters, pool, gt, dev):
+    from factor_fields_gb300 import FactorFields
+    from factor_fields_gb300 import workloads as W
+    from factor_fields_gb300.proposal import ProposalSampler
+    from factor_fields_gb300.train import RadianceFieldTrainer
+    torch.manual_seed(seed)
+    m = FactorFields(W.field_cfg("cfg2"), device=dev, precision="bf16")
+    sampler = ProposalSampler(m, seed=seed) if kind == "cfg3_proposal" else None
+    tr = RadianceFieldTrainer(m, n_samples=1024, n_iters=iters, sampler=sampler)
+    g = torch.Generator(device=dev).manual_seed(seed)
+    for it in range(iters):
+        idx = torch.randint(0, pool.shape[0], (4096,), device=dev, generator=g)
+        tr.step(pool[idx], gt[idx])
+        if sampler is None and it in (iters // 5, iters // 2):
+            m.updateAlphaMask((128, 128, 128), is_update_alphaMask=True, times=1)
+    return m, sampler, tr, g
+
+
 def run_radiance(args, dev):
     """Configurations 2 and 3 on the synthetic blob scene: rays/s of one fwd+bwd training step
     (plain sampler: 4,096 rays x up to 1,024 samples with 128^3 occupancy-bitfield pruning;
-    proposal sampler: 8,192 rays x 48 resampled samples), and PSNR / depth error against the
-    FP64 quadrature ground truth after equal training (iters x 4,096 rays, Adam)."""
+    proposal sampler: 8,192 rays x 48 stratified training samples + the proposal network's
+    training), and PSNR / depth error against the FP64 quadrature ground truth after equal
+    training (iters x 4,096 rays, Adam; the proposal configuration renders with 96 samples
+    drawn from the network). The PSNR comparison is repeated on seeds 1 and 2 (training alone)
+    because single runs differ by up to ~0.5 dB, more for an unlucky seed."""
     from factor_fields_gb300 import FactorFields
     from factor_fields_gb300 import workloads as W
     from factor_fields_gb300.proposal import ProposalSampler
@@ -272,16 +293,7 @@ def run_radiance(args, dev):
     iters = args.render_iters
     out = {}
     for kind, batch in (("cfg2_plain", 4096), ("cfg3_proposal", 8192)):
-        torch.manual_seed(0)
-        m = FactorFields(W.field_cfg("cfg2"), device=dev, precision="bf16")
-        sampler = ProposalSampler(m) if kind == "cfg3_proposal" else None
-        tr = RadianceFieldTrainer(m, n_samples=1024, n_iters=iters, sampler=sampler)
-        g = torch.Generator(device=dev).manual_seed(0)
-        for it in range(iters):
-            idx = torch.randint(0, pool.shape[0], (4096,), device=dev, generator=g)
-            tr.step(pool[idx], gt[idx])
-            if sampler is None and it in (iters // 5, iters // 2):
-                m.updateAlphaMask((128, 128, 128), is_update_alphaMask=True, times=1)
+        m, sampler, tr, g = _train_radiance(kind, 0, iters, pool, gt, dev)
         psnr = tr.psnr(test, gtt)
         with torch.no_grad():
             dep = torch.cat([tr.render(test[s:s + 16384], is_train=False)[1] for s in range(0, test.shape[0], 16384)])
@@ -339,7 +351,15 @@ def run_radiance(args, dev):
             rec["samples_per_ray"] = sampler.n_fine
         out[kind] = rec
     out["proposal_rays_per_s_vs_plain"] = out["cfg3_proposal"]["rays_per_s"] / out["cfg2_plain"]["rays_per_s"]
-    out["proposal_psnr_minus_plain_db"] = out["cfg3_proposal"]["psnr_db"] - out["cfg2_plain"]["psnr_db"]
+    seeds = {0: {k: out[k]["psnr_db"] for k in ("cfg2_plain", "cfg3_proposal")}}
+    if args.psnr_seeds > 1:
+        for seed in range(1, args.psnr_seeds):
+            seeds[seed] = {k: _train_radiance(k, seed, iters, pool, gt, dev)[2].psnr(test, gtt)
+                           for k in ("cfg2_plain", "cfg3_proposal")}
+    diffs = [v["cfg3_proposal"] - v["cfg2_plain"] for v in seeds.values()]
+    out["psnr_db_by_seed"] = {str(k): v for k, v in seeds.items()}
+    out["proposal_psnr_minus_plain_db"] = float(np.mean(diffs))
+    out["proposal_psnr_minus_plain_db_by_seed"] = diffs
     out["scene"] = "seeded 32 Gaussian density blobs in [-1.5,1.5]^3, 100 views 400x400 focal 555, white bg"
     return out
 
@@ -388,6 +408,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-render", action="store_true", help="skip the radiance-field configurations")
     ap.add_argument("--render-iters", type=int, default=1500)
+    ap.add_argument("--psnr-seeds", type=int, default=3, help="training seeds of the PSNR comparison")
     args = ap.parse_args()
     ws, rank, local = dist_env()
     if args.impl == "reference":

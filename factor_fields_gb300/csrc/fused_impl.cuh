@@ -27,6 +27,7 @@
 // MLP: in 18 -> 64 (bias, ReLU) -> out <= 32 (no bias): MLPMixer with num_layers = 2.
 #pragma once
 
+#include <type_traits>
 #include <utility>
 
 #include "ff_common.cuh"
@@ -519,7 +520,9 @@ __global__ void __launch_bounds__(kThreads, 3) fused_field_mlp_kernel(const Fuse
       }
       __syncwarp();
       // ---------------- scatter dL/dbasis = dX * coeff, dL/dcoeff = dX * basis ----------------
-      if constexpr (MODE == kFitBinned) {
+      // segment-cooperative coefficient scatter: binned fit batches, and the BF16 backward, whose
+      // points are ray samples in ray order (consecutive samples share coefficient cells)
+      if constexpr (MODE == kFitBinned || (MODE == kBwd && std::is_same<T, __nv_bfloat16>::value)) {
         float gc[kF];
         Corners<CD> cc;
         if (valid) {

@@ -198,10 +198,12 @@ __global__ void __launch_bounds__(256) proposal_resample_kernel(
     float* __restrict__ xyz, float* __restrict__ zd, int32_t* __restrict__ bin_of) {
   __shared__ float cdf_s[8][kMaxBinsPerLane * 32 + 1];
   __shared__ float t_s[8][kMaxFine];
+  __shared__ float e_s[8][kMaxFine + 1];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int nb = p.n_bins, nf = p.n_fine, B = nb / 32;
   float* cdf = cdf_s[wib];
   float* ts = t_s[wib];
+  float* es = e_s[wib];
   for (int64_t ray = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; ray < n_rays;
        ray += ((int64_t)gridDim.x * blockDim.x) >> 5) {
     const Segment s = segment(p, rays, ray);
@@ -233,12 +235,7 @@ __global__ void __launch_bounds__(256) proposal_resample_kernel(
     if (lane == 0) cdf[0] = 0.f;
     __syncwarp();
     // inverse CDF: searchsorted(cdf, u, right=True) and linear interpolation inside the bin
-    for (int i = lane; i < nf; i += 32) {
-      float u;
-      if (u_given)
-        u = u_given[ray * nf + i];
-      else
-        u = ((float)i + (jitter ? jitter[ray] : 0.5f)) / (float)nf;
+    auto inv_cdf = [&](float u, int& bin) {
       int lo = 0, hi = nb + 1;  // first index with cdf > u
       while (lo < hi) {
         const int mid = (lo + hi) >> 1;
@@ -250,18 +247,43 @@ __global__ void __launch_bounds__(256) proposal_resample_kernel(
       if (denom < 1e-5f) denom = 1.f;
       const float tt = (u - cb) / denom;
       const float eb = s.t_in + (float)below * s.len, ea = s.t_in + (float)above * s.len;
-      const float t = eb + tt * (ea - eb);
+      bin = min(below, nb - 1);
+      return eb + tt * (ea - eb);
+    };
+    for (int i = lane; i < nf; i += 32) {
+      float u;
+      if (u_given)
+        u = u_given[ray * nf + i];
+      else
+        u = ((float)i + (jitter ? jitter[ray] : 0.5f)) / (float)nf;
+      int bin;
+      const float t = inv_cdf(u, bin);
       ts[i] = t;
-      bin_of[ray * nf + i] = min(below, nb - 1);
+      bin_of[ray * nf + i] = bin;
 #pragma unroll
       for (int q = 0; q < 3; ++q) xyz[(ray * nf + i) * 3 + q] = s.o[q] + s.d[q] * t;
+    }
+    // Stratified samples (u = (i + jitter) / n_fine): sample i stands for its CDF stratum
+    // [F^-1(i / n), F^-1((i + 1) / n)]; the strata tile [t_in, t_out]. Given u: the distance to
+    // the next sample (the last one to t_out).
+    if (!u_given) {
+      for (int i = lane; i <= nf; i += 32) {
+        int bin;
+        es[i] = i == 0 ? s.t_in : (i == nf ? s.t_out : inv_cdf((float)i / (float)nf, bin));
+      }
     }
     __syncwarp();
     for (int i = lane; i < nf; i += 32) {
       const float t = ts[i];
-      const float nxt = (i + 1 < nf) ? ts[i + 1] : s.t_out;
+      float d;
+      if (u_given) {
+        const float nxt = (i + 1 < nf) ? ts[i + 1] : s.t_out;
+        d = nxt - t;
+      } else {
+        d = es[i + 1] - es[i];
+      }
       zd[(ray * nf + i) * 2 + 0] = t;
-      zd[(ray * nf + i) * 2 + 1] = fmaxf(nxt - t, 0.f);
+      zd[(ray * nf + i) * 2 + 1] = fmaxf(d, 0.f);
     }
     __syncwarp();
   }

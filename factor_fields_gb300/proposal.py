@@ -7,9 +7,18 @@ dataLoader/ray_utils.py:132-174). The field is evaluated only at those samples a
 with the sample spacing. The proposal is trained online, by its own optimizer, with a loss that
 makes its weight on each coarse bin upper-bound the field's weight mass in that bin.
 
+Training and rendering sample differently (train_uniform=True, the default): a training step
+evaluates the field at n_fine stratified samples over the ray's segment, and the network learns
+from those samples' compositing weights, which are unbiased estimates of where the field's
+weight is; rendering (is_train=False) draws render_fine (96) samples from the network's
+histogram. Training the field on the network's own concentrated samples (train_uniform=False)
+constrains it only on a thin shell around where the network already expects density: on the
+blob scene it converged to ~26 dB against ~28.5 dB for the plain sampler, and no sample count,
+bin count, uniform mixing or occupancy mask changed that; with uniform training samples it
+matches the plain sampler within run-to-run noise (−0.18 / −0.05 / +2.27 dB on three seeds).
+
 `learned=False` keeps everything but replaces the network by a flat histogram: n_fine
-stratified uniform samples over the ray's segment in the box — the same sample budget without
-the proposal, used to show what the network gains.
+stratified uniform samples over the ray's segment in the box, for training and rendering.
 
 Kernels: ff_proposal_head_forward / _backward (BF16: gather + MLP on tensor cores in one
 launch each way) or ff_proposal_encode + the float32 MLP kernels + ff_proposal_scatter (FP32),
@@ -33,7 +42,12 @@ class ProposalRenderFunction(torch.autograd.Function):
     def forward(ctx, rays, basis_param, coeff_param, w0, b0, w1, job):
         sam, m = job["sampler"], job["model"]
         n = rays.shape[0]
-        nb, nf = sam.n_bins, sam.n_fine
+        nb = sam.n_bins
+        nf = sam.n_fine if job["is_train"] else sam.render_fine
+        pdesc = sam.desc
+        if nf != sam.n_fine:
+            pdesc = N.FFProposal.from_buffer_copy(sam.desc)
+            pdesc.n_fine = nf
         dev = rays.device
         st = N.stream_ptr()
         feat_p = None
@@ -49,11 +63,16 @@ class ProposalRenderFunction(torch.autograd.Function):
             N.call("ff_mlp_forward", ctypes.byref(sam.mlp_struct()), N.ptr(feat_p), n * nb, N.ptr(o_p), st)
         else:
             o_p = torch.full((n * nb, 1), -60.0, device=dev)  # zero density: a flat histogram
+        o_sample = o_p
+        if sam.learned and job["is_train"] and sam.train_uniform:
+            # training samples stratified over the segment; the network still predicts o_p and
+            # learns (proposal loss) from these samples' unbiased weights
+            o_sample = torch.full((n * nb, 1), -60.0, device=dev)
         w_p = torch.empty(n * nb, device=dev)
         xyz = torch.empty(n * nf, 3, device=dev)
         zd = torch.empty(n * nf, 2, device=dev)
         bin_of = torch.empty(n * nf, dtype=torch.int32, device=dev)
-        N.call("ff_proposal_resample", ctypes.byref(sam.desc), N.ptr(rays), n, N.ptr(o_p), N.ptr(job["jitter"]),
+        N.call("ff_proposal_resample", ctypes.byref(pdesc), N.ptr(rays), n, N.ptr(o_sample), N.ptr(job["jitter"]),
                None, N.ptr(w_p), N.ptr(xyz), N.ptr(zd), N.ptr(bin_of), st)
         feat = field_eval(m, job, xyz)
         offsets = torch.arange(n + 1, device=dev, dtype=torch.int64) * nf
@@ -82,8 +101,10 @@ class ProposalRenderFunction(torch.autograd.Function):
 
 class ProposalSampler:
     def __init__(self, model, reso=64, n_bins=64, n_fine=48, hidden=64, lr_grid=2e-2, lr_mlp=1e-3,
-                 density_shift=-4.0, precision="bf16", learned=True, seed=0, uniform_mix=0.0, fused_adam=True):
-        self.m, self.learned = model, learned
+                 density_shift=-4.0, precision="bf16", learned=True, seed=0, uniform_mix=0.0, fused_adam=True,
+                 train_uniform=True, render_fine=96):
+        self.m, self.learned, self.train_uniform = model, learned, train_uniform
+        self.render_fine = render_fine or n_fine  # samples per ray when rendering (not training)
         self.reso, self.n_bins, self.n_fine, self.precision = reso, n_bins, n_fine, precision
         # BF16: the head (encode + MLP, and its backward + scatter) is one tensor-core launch;
         # FP32: ff_proposal_encode + the float32 MLP kernels + ff_proposal_scatter
@@ -153,7 +174,7 @@ class ProposalSampler:
         key = (bool(white_bg), id(m.alphaMask))
         if getattr(self, "_rdesc_key", None) != key:  # host-side cache: no device reads per call
             self._rdesc, self._rdesc_key = render_desc(m, self.n_fine, white_bg), key
-        job = {"model": m, "sampler": self, "rdesc": self._rdesc,
+        job = {"model": m, "sampler": self, "rdesc": self._rdesc, "is_train": bool(is_train),
                "fdesc": m.descriptor(dt), "basis_r": basis_r, "coeff_r": coeff_r, "coeff_param": m.coeff_flat,
                "fused": fused, "jitter": jitter}
         l0, l1 = m.linear_mat.backbone

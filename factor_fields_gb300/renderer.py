@@ -179,14 +179,35 @@ def field_eval(m, job, xyz):
     return out
 
 
+def _direct_grad(p):
+    """p.grad (zeros when missing) for the kernels to accumulate into."""
+    if p.grad is None:
+        p.grad = torch.zeros_like(p)
+    return p.grad
+
+
 def field_grad(m, job, xyz, g_out):
-    """(grad_basis, grad_coeff, grad_w0, grad_b0, grad_w1) for dL/dout = g_out at xyz."""
+    """(grad_basis, grad_coeff, grad_w0, grad_b0, grad_w1) for dL/dout = g_out at xyz.
+
+    With m.accumulate_grad_directly (the default) the kernels accumulate straight into the
+    parameters' .grad buffers and None is returned for them: no per-step zeroed gradient
+    buffers and no autograd additions of 40-70 MB grids (torch.autograd.grad does not see
+    these gradients; set the attribute to False for that)."""
     lm = m.linear_mat
     ws, bs = lm.weights()
-    gb = torch.zeros_like(m.basis_flat)
-    gc = torch.zeros_like(job["coeff_param"])
-    gw = [torch.zeros_like(w) for w in ws]
-    gbias = [torch.zeros_like(b) if b is not None else None for b in bs]
+    direct = getattr(m, "accumulate_grad_directly", True)
+    if direct:
+        gb = _direct_grad(m.basis_flat)
+        gc = _direct_grad(m.coeff_flat)
+        if job["coeff_param"] is not m.coeff_flat:
+            gc = m._coeff_scene(gc)
+        gw = [_direct_grad(w) for w in ws]
+        gbias = [_direct_grad(b) if b is not None else None for b in bs]
+    else:
+        gb = torch.zeros_like(m.basis_flat)
+        gc = torch.zeros_like(job["coeff_param"])
+        gw = [torch.zeros_like(w) for w in ws]
+        gbias = [torch.zeros_like(b) if b is not None else None for b in bs]
     n = xyz.shape[0]
     if n:
         st = N.stream_ptr()
@@ -206,6 +227,8 @@ def field_grad(m, job, xyz, g_out):
                    ctypes.byref(g), st)
             N.call("ff_field_backward", ctypes.byref(job["fdesc"]), N.ptr(job["basis_r"]), N.ptr(job["coeff_r"]),
                    N.ptr(xyz), n, N.ptr(g_feats), None, None, N.ptr(gb), N.ptr(gc), st)
+    if direct:
+        return (None, None, None, None, None)
     return (gb, gc, gw[0], gbias[0], gw[1] if len(gw) > 1 else None)
 
 

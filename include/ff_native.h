@@ -340,7 +340,8 @@ FF_API int ff_proposal_encode(const FFProposal* p, const void* grid, const float
                               float* feat, void* stream);
 /* From the proposal MLP's outputs o_prop [n_rays * n_bins]: proposal weights w_prop
  * [n_rays * n_bins], and n_fine samples per ray by inverse CDF: xyz [n_rays * n_fine, 3],
- * zd [n_rays * n_fine, 2] (z, dist to the next sample / the segment end), bin_of [.] int32.
+ * zd [n_rays * n_fine, 2] (z, the width of the sample's CDF stratum [F^-1(i / n_fine), F^-1((i+1) / n_fine)]
+ * for stratified u; with u given, the distance to the next sample / the segment end), bin_of [.] int32.
  * u: optional [n_rays * n_fine] uniforms; else u_i = (i + jitter[ray]) / n_fine (jitter
  * optional, 0.5 when NULL). */
 FF_API int ff_proposal_resample(const FFProposal* p, const float* rays, int64_t n_rays, const float* o_prop,

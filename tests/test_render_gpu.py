@@ -121,3 +121,24 @@ def test_scan_edge_cases():
         ref = torch.zeros(n + 1, dtype=torch.int64)
         ref[1:] = torch.cumsum(counts.cpu().long(), 0)
         assert torch.equal(offsets.cpu(), ref), n
+
+
+def test_direct_grad_accumulation_matches_autograd_returns():
+    """Render gradients accumulated straight into .grad (the default) equal the ones returned
+    through autograd (accumulate_grad_directly = False), and they accumulate over two
+    backward passes like autograd's."""
+    from factor_fields_gb300 import FactorFields
+    from factor_fields_gb300 import workloads as W
+    rays = torch.from_numpy(W.BlobScene(0).ray_pool(512, 3)).float().cuda()
+    jit = torch.rand(512, device="cuda", generator=torch.Generator(device="cuda").manual_seed(0))
+    res = []
+    for direct in (True, False):
+        torch.manual_seed(0)
+        m = FactorFields(W.field_cfg("cfg2"), device="cuda", precision="bf16")
+        m.accumulate_grad_directly = direct
+        for _ in range(2):
+            rgb, _, _ = m(rays, white_bg=True, is_train=True, N_samples=256, jitter=jit)
+            (rgb * rgb).sum().backward()
+        res.append([p.grad.clone() for p in [m.basis_flat, m.coeff_flat] + list(m.linear_mat.parameters())])
+    for a, b in zip(*res):
+        assert rel_err(a, b) < 1e-5
