@@ -451,7 +451,7 @@ int ff_proposal_resample(const FFProposal* p, const float* rays, int64_t n_rays,
                          void* stream) {
   int rc = validate_proposal(p, rays, n_rays);
   if (rc) return rc;
-  if (n_rays > 0 && (!o_prop || !w_prop || !xyz || !zd || !bin_of)) return set_error(FF_ERR_ARG, "buffers are NULL");
+  if (n_rays > 0 && (!w_prop || !xyz || !zd || !bin_of)) return set_error(FF_ERR_ARG, "buffers are NULL");
   return cuda_status(launch_proposal_resample(*p, rays, n_rays, o_prop, jitter, u, w_prop, xyz, zd, bin_of,
                                               (cudaStream_t)stream),
                      "ff_proposal_resample launch");

@@ -158,7 +158,7 @@ __device__ __forceinline__ void bin_weights(const FFProposal& p, const float* o_
 #pragma unroll
   for (int b = 0; b < kMaxBinsPerLane; ++b) {
     if (b < B) {
-      const float o = o_row[lane * B + b];
+      const float o = o_row ? o_row[lane * B + b] : -60.f;  // NULL: a flat histogram
       const float x = o + p.density_shift;
       st.o[b] = o;
       st.sigma[b] = (x > 20.f) ? x : log1pf(expf(x));
@@ -208,7 +208,7 @@ __global__ void __launch_bounds__(256) proposal_resample_kernel(
        ray += ((int64_t)gridDim.x * blockDim.x) >> 5) {
     const Segment s = segment(p, rays, ray);
     BinState st;
-    bin_weights(p, o_prop + ray * nb, s.len, lane, B, st);
+    bin_weights(p, o_prop ? o_prop + ray * nb : nullptr, s.len, lane, B, st);
     // pdf = (w + 1e-5) / sum, cdf with a leading zero (sample_pdf, ray_utils.py:135-138)
     float lsum = 0.f;
 #pragma unroll

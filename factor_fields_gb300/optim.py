@@ -78,3 +78,17 @@ class FusedAdam(torch.optim.Optimizer):
         if self.fused_zero_grad:
             return
         super().zero_grad(set_to_none=set_to_none)
+
+
+def zero_grads(params):
+    """Zero the gradients of `params` (those that have one; contiguous float32) in one
+    ff_zero_f32 launch per 8 buffers instead of one fill per tensor."""
+    bufs = [p.grad for p in params if p.grad is not None]
+    if not bufs:
+        return
+    for b in bufs:
+        if b.dtype != torch.float32 or not b.is_contiguous():
+            raise ValueError("gradient buffers must be contiguous float32")
+    ptrs = (ctypes.c_void_p * len(bufs))(*[b.data_ptr() for b in bufs])
+    counts = (ctypes.c_int64 * len(bufs))(*[b.numel() for b in bufs])
+    N.call("ff_zero_f32", ptrs, counts, len(bufs), N.stream_ptr(), kernels=-(-len(bufs) // 8))

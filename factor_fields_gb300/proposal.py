@@ -62,12 +62,12 @@ class ProposalRenderFunction(torch.autograd.Function):
             o_p = torch.empty(n * nb, 1, device=dev)
             N.call("ff_mlp_forward", ctypes.byref(sam.mlp_struct()), N.ptr(feat_p), n * nb, N.ptr(o_p), st)
         else:
-            o_p = torch.full((n * nb, 1), -60.0, device=dev)  # zero density: a flat histogram
+            o_p = None  # a flat histogram
         o_sample = o_p
         if sam.learned and job["is_train"] and sam.train_uniform:
-            # training samples stratified over the segment; the network still predicts o_p and
-            # learns (proposal loss) from these samples' unbiased weights
-            o_sample = torch.full((n * nb, 1), -60.0, device=dev)
+            # training samples stratified over the segment (a flat histogram); the network still
+            # predicts o_p and learns (proposal loss) from these samples' unbiased weights
+            o_sample = None
         w_p = torch.empty(n * nb, device=dev)
         xyz = torch.empty(n * nf, 3, device=dev)
         zd = torch.empty(n * nf, 2, device=dev)
@@ -183,8 +183,8 @@ class ProposalSampler:
         return rgb, depth
 
     def zero_grad(self):
-        for p in self.params:
-            p.grad.zero_()
+        from .optim import zero_grads
+        zero_grads(self.params)
 
     def backward(self):
         """Proposal loss of the last render against the field's weights; gradients into the

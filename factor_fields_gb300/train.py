@@ -37,15 +37,12 @@ class RadianceFieldTrainer:
         return rgb, depth
 
     def _zero_grads(self):
-        if self.fused_adam:
-            for g in self.opt.param_groups:
-                for p in g["params"]:
-                    if p.grad is not None:
-                        p.grad.zero_()
-        else:
-            self.opt.zero_grad(set_to_none=False)
+        """Every gradient of the field and the sampler, in one ff_zero_f32 launch."""
+        from .optim import zero_grads
+        params = [p for g in self.opt.param_groups for p in g["params"]]
         if self.sampler is not None:
-            self.sampler.zero_grad()
+            params += self.sampler.params
+        zero_grads(params)
 
     def step(self, rays, rgb_gt, optimize=True):
         rgb, _ = self.render(rays, is_train=True)
@@ -126,6 +123,7 @@ class FieldFitRunner:
         if self.binned and not fused:
             raise ValueError("binned=True needs fused=True")
         self._ws = None
+        self._ws_gen = 0
         if fused and self.binned:
             self.path_name = ("fused, binned: one ff_field_fit_step_binned call per step (bin by coefficient cell "
                               "with the gradient zeroing, allocate cell ranges, permute, fit)")
@@ -172,14 +170,13 @@ class FieldFitRunner:
 
     def graph_step(self, x, y):
         """step() replayed from a CUDA graph: the batch is copied into static buffers and the
-        captured launches (gradient zeroing, the fit kernel, the loss scale) replay with one
-        host call. The graph is captured on first use and re-captured when the batch shape or
-        a parameter buffer changes."""
-        ws = 0
-        if self.fused and self.binned:  # the captured launches keep the workspace address
-            ws = self._workspace(self.m.descriptor(self.m._read_buffers()[2]), x.shape[0]).data_ptr()
+        captured launches (the binning with the gradient zeroing, the fit kernel, the loss
+        scale) replay with one host call. The graph is captured on first use and re-captured
+        when the batch shape, a parameter buffer or the binning workspace changes."""
+        # the captured launches keep the workspace address: a reallocation (an eager step on a
+        # larger batch) bumps _ws_gen and forces a new capture
         key = (tuple(x.shape), tuple(y.shape), self.m.basis_flat.data_ptr(), self.m.coeff_flat.data_ptr(),
-               self.m.precision, ws)
+               self.m.precision, self._ws_gen)
         if getattr(self, "_graph_key", None) != key:
             dev = self.m.basis_flat.device
             self._xs = torch.empty(x.shape, dtype=x.dtype, device=dev)
@@ -189,12 +186,12 @@ class FieldFitRunner:
             side = torch.cuda.Stream()
             side.wait_stream(torch.cuda.current_stream())
             with torch.cuda.stream(side):
-                self.step(self._xs, self._ys)  # warm-up outside the capture (sets kernel attributes)
+                self.step(self._xs, self._ys)  # warm-up outside the capture (kernel attributes, workspace)
             torch.cuda.current_stream().wait_stream(side)
             self._graph = torch.cuda.CUDAGraph()
             with torch.cuda.graph(self._graph):
                 self._graph_loss = self.step(self._xs, self._ys)
-            self._graph_key = key
+            self._graph_key = key[:-1] + (self._ws_gen,)  # the warm-up may have sized the workspace
         self.m._read_buffers()  # refresh the BF16 grid copies in place if the masters changed
         self._xs.copy_(x, non_blocking=True)
         self._ys.copy_(y, non_blocking=True)
@@ -208,6 +205,7 @@ class FieldFitRunner:
             N.check(need, "ff_field_fit_binned_workspace_bytes")
         if self._ws is None or self._ws.numel() < need:
             self._ws = torch.empty(need, dtype=torch.uint8, device=self.m.basis_flat.device)
+            self._ws_gen += 1
         return self._ws
 
     def step(self, x, y, kernel_events=False):

@@ -343,7 +343,7 @@ FF_API int ff_proposal_encode(const FFProposal* p, const void* grid, const float
  * zd [n_rays * n_fine, 2] (z, the width of the sample's CDF stratum [F^-1(i / n_fine), F^-1((i+1) / n_fine)]
  * for stratified u; with u given, the distance to the next sample / the segment end), bin_of [.] int32.
  * u: optional [n_rays * n_fine] uniforms; else u_i = (i + jitter[ray]) / n_fine (jitter
- * optional, 0.5 when NULL). */
+ * optional, 0.5 when NULL). o_prop NULL: a flat histogram (stratified samples over the segment). */
 FF_API int ff_proposal_resample(const FFProposal* p, const float* rays, int64_t n_rays, const float* o_prop,
                                 const float* jitter, const float* u, float* w_prop, float* xyz, float* zd,
                                 int32_t* bin_of, void* stream);

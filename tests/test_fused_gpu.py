@@ -167,8 +167,9 @@ def test_unsupported_shapes_fail_loudly():
 
 
 def test_graph_step_matches_step_and_tracks_updates():
-    """The CUDA-graph replay gives the eager step's loss and gradients, also after an
-    optimizer update of the float32 masters (the BF16 copies refresh in place)."""
+    """The CUDA-graph replay gives the eager step's loss and gradients, for batches from host
+    memory and from the GPU, also after optimizer updates of the float32 masters (the BF16
+    copies refresh in place)."""
     from factor_fields_gb300 import FactorFields
     from factor_fields_gb300 import workloads as W
     from factor_fields_gb300.train import FieldFitRunner
@@ -176,16 +177,22 @@ def test_graph_step_matches_step_and_tracks_updates():
     m = FactorFields(W.field_cfg("cfg1"), device="cuda", precision="bf16")
     r = FieldFitRunner(m, loss="l1")
     opt = torch.optim.Adam(m.parameters(), lr=1e-2)
-    for it in range(3):
-        xs, ys = W.sdf_batch(10 + it, 4096)
-        x, y = torch.from_numpy(xs).cuda(), torch.from_numpy(ys).cuda()
+    batches = [W.sdf_batch(10 + it, 4096) for it in range(2)]
+    dev = [(torch.from_numpy(a).cuda(), torch.from_numpy(b).cuda()) for a, b in batches]
+    for it in range(4):
+        xs, ys = batches[it % 2]
+        x, y = dev[it % 2]
         l_eager = float(r.step(x, y))
         g_eager = [p.grad.clone() for p in r._params()]
-        l_graph = float(r.graph_step(torch.from_numpy(xs), torch.from_numpy(ys)))  # from host memory
-        torch.cuda.synchronize()
-        assert abs(l_graph - l_eager) <= 1e-6 * max(1.0, abs(l_eager))
-        for a, b in zip(g_eager, r._params()):
-            assert torch.allclose(a, b.grad, rtol=1e-5, atol=1e-9)
+        for src in ("host", "device"):
+            if src == "host":
+                l_graph = float(r.graph_step(torch.from_numpy(xs), torch.from_numpy(ys)))
+            else:
+                l_graph = float(r.graph_step(x, y))
+            torch.cuda.synchronize()
+            assert abs(l_graph - l_eager) <= 1e-6 * max(1.0, abs(l_eager)), (it, src)
+            for a, b in zip(g_eager, r._params()):
+                assert torch.allclose(a, b.grad, rtol=1e-5, atol=1e-9), (it, src)
         opt.step()
 
 
