@@ -46,3 +46,41 @@ def test_struct_layouts_match(lib):
     assert lib.ff_abi_version() == 1
     for i, st in enumerate([N.FFField, N.FFMlp, N.FFMlpGrad, N.FFRender, N.FFProposal, N.FFAdamParam]):
         assert lib.ff_struct_size(i) == ctypes.sizeof(st), st.__name__
+
+
+def test_argument_validation_before_any_launch(lib):
+    """Bad arguments are rejected with the documented codes and a message, before any CUDA
+    call (so this runs without a GPU)."""
+    from factor_fields_gb300 import _native as N
+    vp = ctypes.c_void_p
+    # ff_adam_step: negative count, unknown flag, betas out of range, step < 1
+    assert lib.ff_adam_step(None, -1, 0.9, 0.99, 1e-8, 0, None) == N.FF_ERR_ARG
+    p = N.FFAdamParam()
+    p.param = p.grad = p.exp_avg = p.exp_avg_sq = 16
+    p.n, p.step, p.lr = 4, 1, 1e-3
+    arr = (N.FFAdamParam * 1)(p)
+    assert lib.ff_adam_step(ctypes.cast(arr, vp), 1, 0.9, 0.99, 1e-8, 4, None) == N.FF_ERR_ARG
+    assert lib.ff_adam_step(ctypes.cast(arr, vp), 1, 1.0, 0.99, 1e-8, 0, None) == N.FF_ERR_ARG
+    arr[0].step = 0
+    assert lib.ff_adam_step(ctypes.cast(arr, vp), 1, 0.9, 0.99, 1e-8, 0, None) == N.FF_ERR_ARG
+    assert b"step" in lib.ff_last_error()
+    # ff_zero_f32: NULL buffer with a count
+    ptrs = (vp * 1)(None)
+    counts = (ctypes.c_int64 * 1)(5)
+    assert lib.ff_zero_f32(ptrs, counts, 1, None) == N.FF_ERR_ARG
+    # ff_occupancy_mask / ff_image_metrics: bad dimensions, missing workspace
+    assert lib.ff_occupancy_workspace_bytes(0, 4, 4) < 0
+    assert lib.ff_occupancy_mask(vp(16), 4, 4, 4, 0.5, 1, vp(16), None, vp(16), None, 0, None) == N.FF_ERR_ARG
+    ws = lib.ff_occupancy_workspace_bytes(4, 4, 4)
+    assert lib.ff_occupancy_mask(vp(16), 4, 4, 4, 0.5, 1, vp(16), None, vp(16), vp(256), ws - 1, None) == N.FF_ERR_SIZE
+    assert lib.ff_image_metrics_workspace_bytes(10, 20, 3) < 0  # SSIM's window needs >= 11 pixels
+    out = (ctypes.c_double * 2)()
+    assert lib.ff_image_metrics(vp(16), vp(16), 11, 11, 3, 1.0, out, None, 0, None) == N.FF_ERR_ARG
+    # ff_field_fit_step_binned: unknown flags / too small a workspace are reported
+    assert lib.ff_field_fit_binned_workspace_bytes(None, 10, 1) < 0
+    # ff_filter_rays: needs an occupancy bitfield unless bbox_only
+    r = N.FFRender()
+    r.step, r.n_samples, r.distance_scale = 0.01, 16, 25.0
+    for k in range(3):
+        r.aabb_min[k], r.aabb_max[k] = -1.0, 1.0
+    assert lib.ff_filter_rays(ctypes.byref(r), vp(16), 4, 16, 0, vp(16), None) == N.FF_ERR_ARG
