@@ -277,11 +277,8 @@ def run_radiance(args, dev):
     training (iters x 4,096 rays, Adam; the proposal configuration renders with 96 samples
     drawn from the network). The PSNR comparison is repeated on seeds 1 and 2 (training alone)
     because single runs differ by up to ~0.5 dB, more for an unlucky seed."""
-    from factor_fields_gb300 import FactorFields
     from factor_fields_gb300 import workloads as W
-    from factor_fields_gb300.proposal import ProposalSampler
     from factor_fields_gb300.renderer import march, render_desc
-    from factor_fields_gb300.train import RadianceFieldTrainer
     scene = W.BlobScene(0)
     pool = torch.from_numpy(scene.ray_pool(1 << 18, 5)).float()
     gt = scene.render_gt(pool.double().numpy(), n_steps=512).to(dev)

@@ -50,6 +50,9 @@ constexpr int kLevelOff[6] = {0, 4, 8, 12, 14, 16};
 // Shared-memory row strides (elements).
 constexpr int LD_XF = 20;   // float32 feature tile [32 pts][20]: 18 features, 1.0, 0
 constexpr int LD_H = 72;    // BF16 H / dH tiles [32 pts][64]
+// Row strides of 40 keep the 32-bit fragment loads bank-conflict free. (With the 28-wide head
+// the backward fits 2 blocks per SM; a stride of 36 would fit 3, but measured slower: the
+// third block's shared memory is taken from the L1 that the grid gathers hit.)
 constexpr int LD_W0 = 40;   // W0 [64 hidden][32 in] BF16
 constexpr int LD_W0T = 72;  // W0^T [32 in][64 hidden]
 constexpr int LD_W1 = 72;   // W1 [32 out][64 hidden]
