@@ -119,6 +119,26 @@ def bytes_per_point(m, gathers, param_bytes):
     return gathers * k * ch * param_bytes + k * ch * 4 + 4 * m.in_dim + 4 * m.linear_mat.out_dim
 
 
+def max_over_ranks(vals):
+    """Element-wise maximum of per-rank values over the process group (each rank's timed
+    region; the slowest rank sets the job's time). Identity without a process group."""
+    import torch.distributed as dist
+    vals = [float(v) for v in vals]
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return vals
+    dev = torch.device("cuda", torch.cuda.current_device()) if dist.get_backend() == "nccl" else torch.device("cpu")
+    t = torch.tensor(vals, dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t.tolist()]
+
+
+def whole_job_rate(points_per_rank_step, steps, world_size, ms_max):
+    """Points of all ranks over the max-over-ranks time (points/s): every rank processes its
+    own batches (replicas), so the job's rate is the sum of the ranks' work over the slowest
+    rank's time."""
+    return points_per_rank_step * steps * world_size / (ms_max / 1e3)
+
+
 def run_native(args, ws, rank, local):
     from factor_fields_gb300 import _native as N
     from factor_fields_gb300 import workloads as W
@@ -207,12 +227,9 @@ def run_native(args, ws, rank, local):
     t_drop, _ = timed(dropin_step, args.steps, False)
 
     # ---- max over ranks ----
-    tot = torch.tensor([ms, float(np.sum(t_e2e)), float(np.sum(t_drop))], device=dev)
-    if ws > 1:
-        torch.distributed.all_reduce(tot, op=torch.distributed.ReduceOp.MAX)
-    ms, ms_e2e, ms_drop = [float(v) for v in tot.tolist()]
+    ms, ms_e2e, ms_drop = max_over_ranks([ms, float(np.sum(t_e2e)), float(np.sum(t_drop))])
     pts = n * args.steps * ws
-    value = pts / (ms / 1e3)
+    value = whole_job_rate(n, args.steps, ws, ms)
     kern_ms = float(np.mean(k_fast)) if k_fast else None
     pb = 2 if m.precision == "bf16" else 4
     bpp = bytes_per_point(m, 2, pb)  # the fwd+bwd algorithm's bytes
