@@ -1,6 +1,6 @@
 """CPU oracle for the Factor Fields field-evaluation and ray-rendering path.
 
-TEST INFRASTRUCTURE ONLY. This module is the checker: only tests/, the smoke check in
+TEST INFRASTRUCTURE ONLY. This module is the oracle: only tests/, the smoke check in
 __graft_entry__.py and bench.py's CPU-baseline leg may import it. The product path
 (factor_fields_gb300) never calls into it.
 

@@ -1,8 +1,8 @@
 """CPU baseline: the reference's own PyTorch op sequence for the field path, on the host cores.
 
 TEST INFRASTRUCTURE ONLY: used by bench.py (--impl reference, and the cpu_baseline leg) and
-by tests; never by the product path. The reference checkout cannot travel to the GPU machine, so
-this module restates, with the same PyTorch CPU kernels the reference calls, its field path:
+by tests; never by the product path. The reference checkout is not available where the
+benchmarks run, so this module restates, with the same PyTorch CPU kernels the reference calls, its field path:
 
   grid_mapping           models/FactorFields.py:11-22   (remainder / floor_divide / where)
   get_basis (grid)       models/FactorFields.py:479-490 (one F.grid_sample per level)

@@ -1,7 +1,7 @@
 """GPU parity of the drop-in field (get_coding / get_basis / get_coeff) and MLP head against the
 reference's golden outputs and the FP64 oracle.
 
-Tolerances (spec contract): float32 drop-in forward 1e-5 relative, gradients 1e-4;
+Tolerances: float32 drop-in forward 1e-5 relative, gradients 1e-4;
 BF16 storage forward 2e-2, gradients 3e-2. Relative = max|a-b| / max|ref|."""
 import numpy as np
 import pytest
