@@ -36,6 +36,11 @@ class RadianceFieldTrainer:
         rgb, depth, _ = self.m(rays, white_bg=self.white_bg, is_train=is_train, N_samples=self.n_samples)
         return rgb, depth
 
+    def _side_stream(self):
+        if getattr(self, "_side", None) is None:
+            self._side = torch.cuda.Stream(device=self.m.basis_flat.device)
+        return self._side
+
     def _zero_grads(self):
         """Every gradient of the field and the sampler, in one ff_zero_f32 launch."""
         from .optim import zero_grads
@@ -50,9 +55,19 @@ class RadianceFieldTrainer:
         if not self._grads_clean:
             self._zero_grads()
         self._grads_clean = False
-        loss.backward()
+        side = None
         if self.sampler is not None:
-            self.sampler.backward()
+            # the proposal's loss and backward need only the forward's outputs: they run on a
+            # second stream beside the field's backward (the field backward leaves room for them
+            # on the SMs) and are joined before the update
+            main = torch.cuda.current_stream()
+            side = self._side_stream()
+            side.wait_stream(main)
+            with torch.cuda.stream(side):
+                self.sampler.backward()
+        loss.backward()
+        if side is not None:
+            torch.cuda.current_stream().wait_stream(side)
         if optimize:
             self.opt.step()
             for g in self.opt.param_groups:
