@@ -64,7 +64,7 @@ class FFAdamParam(ctypes.Structure):
 class FFProposal(ctypes.Structure):
     _fields_ = [("aabb_min", c_f32 * 3), ("aabb_max", c_f32 * 3), ("inv_cell", c_f32 * 3), ("reso", c_i32),
                 ("param_dtype", c_i32), ("n_bins", c_i32), ("n_fine", c_i32), ("density_shift", c_f32),
-                ("distance_scale", c_f32), ("uniform_mix", c_f32)]
+                ("distance_scale", c_f32), ("uniform_mix", c_f32), ("u_stratified", c_i32)]
 
 
 # (name, restype, argtypes) of every exported entry point.

@@ -263,10 +263,11 @@ __global__ void __launch_bounds__(256) proposal_resample_kernel(
 #pragma unroll
       for (int q = 0; q < 3; ++q) xyz[(ray * nf + i) * 3 + q] = s.o[q] + s.d[q] * t;
     }
-    // Stratified samples (u = (i + jitter) / n_fine): sample i stands for its CDF stratum
-    // [F^-1(i / n), F^-1((i + 1) / n)]; the strata tile [t_in, t_out]. Given u: the distance to
-    // the next sample (the last one to t_out).
-    if (!u_given) {
+    // Stratified samples (u = (i + jitter) / n_fine, or given u with p.u_stratified): sample i
+    // stands for its CDF stratum [F^-1(i / n), F^-1((i + 1) / n)]; the strata tile
+    // [t_in, t_out]. Other given u: the distance to the next sample (the last one to t_out).
+    const bool strata = !u_given || p.u_stratified;
+    if (strata) {
       for (int i = lane; i <= nf; i += 32) {
         int bin;
         es[i] = i == 0 ? s.t_in : (i == nf ? s.t_out : inv_cdf((float)i / (float)nf, bin));
@@ -276,7 +277,7 @@ __global__ void __launch_bounds__(256) proposal_resample_kernel(
     for (int i = lane; i < nf; i += 32) {
       const float t = ts[i];
       float d;
-      if (u_given) {
+      if (!strata) {
         const float nxt = (i + 1 < nf) ? ts[i + 1] : s.t_out;
         d = nxt - t;
       } else {

@@ -8,10 +8,12 @@ with the sample spacing. The proposal is trained online, by its own optimizer, w
 makes its weight on each coarse bin upper-bound the field's weight mass in that bin.
 
 Training and rendering sample differently (train_uniform=True, the default): a training step
-evaluates the field at n_fine stratified samples over the ray's segment, and the network learns
-from those samples' compositing weights, which are unbiased estimates of where the field's
-weight is; rendering (is_train=False) draws render_fine (96) samples from the network's
-histogram. Training the field on the network's own concentrated samples (train_uniform=False)
+evaluates the field at n_fine stratified samples over the ray's segment, each jittered
+independently inside its stratum (sample_jitter=True), and the network learns from those
+samples' compositing weights, which are unbiased estimates of where the field's weight is;
+rendering (is_train=False) draws render_fine (96) samples from the network's histogram.
+Jittering all samples of a ray by one offset instead (like the reference's uniform sampler)
+trains the field on a lattice along each ray: 0.9-1.3 dB lower PSNR on the blob scene. Training the field on the network's own concentrated samples (train_uniform=False)
 constrains it only on a thin shell around where the network already expects density: on the
 blob scene it converged to ~26 dB against ~28.5 dB for the plain sampler, and no sample count,
 bin count, uniform mixing or occupancy mask changed that; with uniform training samples it
@@ -72,8 +74,15 @@ class ProposalRenderFunction(torch.autograd.Function):
         xyz = torch.empty(n * nf, 3, device=dev)
         zd = torch.empty(n * nf, 2, device=dev)
         bin_of = torch.empty(n * nf, dtype=torch.int32, device=dev)
+        u = None
+        if job["is_train"] and sam.sample_jitter:
+            # each training sample jittered independently inside its stratum
+            u = (torch.arange(nf, device=dev, dtype=torch.float32) + torch.rand(n, nf, device=dev)) / nf
+            if pdesc is sam.desc:
+                pdesc = N.FFProposal.from_buffer_copy(sam.desc)
+            pdesc.u_stratified = 1
         N.call("ff_proposal_resample", ctypes.byref(pdesc), N.ptr(rays), n, N.ptr(o_sample), N.ptr(job["jitter"]),
-               None, N.ptr(w_p), N.ptr(xyz), N.ptr(zd), N.ptr(bin_of), st)
+               N.ptr(u), N.ptr(w_p), N.ptr(xyz), N.ptr(zd), N.ptr(bin_of), st)
         feat = field_eval(m, job, xyz)
         offsets = torch.arange(n + 1, device=dev, dtype=torch.int64) * nf
         rgb = torch.empty(n, 3, device=dev)
@@ -102,9 +111,10 @@ class ProposalRenderFunction(torch.autograd.Function):
 class ProposalSampler:
     def __init__(self, model, reso=64, n_bins=64, n_fine=48, hidden=64, lr_grid=2e-2, lr_mlp=1e-3,
                  density_shift=-4.0, precision="bf16", learned=True, seed=0, uniform_mix=0.0, fused_adam=True,
-                 train_uniform=True, render_fine=96):
+                 train_uniform=True, render_fine=96, sample_jitter=True):
         self.m, self.learned, self.train_uniform = model, learned, train_uniform
         self.render_fine = render_fine or n_fine  # samples per ray when rendering (not training)
+        self.sample_jitter = sample_jitter  # training: jitter each sample in its stratum (else per ray)
         self.reso, self.n_bins, self.n_fine, self.precision = reso, n_bins, n_fine, precision
         # BF16: the head (encode + MLP, and its backward + scatter) is one tensor-core launch;
         # FP32: ff_proposal_encode + the float32 MLP kernels + ff_proposal_scatter

@@ -333,6 +333,8 @@ typedef struct FFProposal {
   float density_shift;    /* proposal density = softplus(o + density_shift) */
   float distance_scale;   /* alpha = 1 - exp(-density * bin_len * distance_scale) */
   float uniform_mix;      /* resampling pdf = (1 - mix) * sample_pdf's pdf + mix / n_bins (0 = exact) */
+  int32_t u_stratified;   /* given u: u_i lies in stratum [i / n_fine, (i + 1) / n_fine), so each
+                             sample's dist is its stratum's width (else: to the next sample) */
 } FFProposal;
 
 /* Grid features at the coarse bin centres: feat [n_rays * n_bins, 8] float32. */

@@ -191,9 +191,9 @@ def test_proposal_matches_plain_sampler_with_far_fewer_samples():
     plain uniform sampler, up to 1024 samples per ray with occupancy pruning): after the same
     training (1500 steps of 4096 rays; the field sees 48 stratified samples per ray in the
     proposal configuration against ~125 live samples in the plain one), rendering with 96
-    proposal samples per ray is as accurate against the FP64 ground truth. Runs of this
-    comparison differ by up to ~0.5 dB from the seed alone, so it is made on two seeds and a
-    10-view test set and the mean difference is held to -0.25 dB."""
+    proposal samples per ray is at least as accurate against the FP64 ground truth (within
+    0.1 dB; measured about +1 dB). Runs of this comparison differ by up to ~0.5 dB from the
+    seed alone, so it is made on two seeds and a 10-view test set (their mean)."""
     from factor_fields_gb300 import FactorFields
     from factor_fields_gb300 import workloads as W
     from factor_fields_gb300.proposal import ProposalSampler
@@ -224,7 +224,7 @@ def test_proposal_matches_plain_sampler_with_far_fewer_samples():
                 offsets, _, _ = march(m, test, None, render_desc(m, 1024, True))
                 res[(seed, "plain_samples")] = float(offsets[-1]) / test.shape[0]
         diffs.append(res[(seed, "proposal")] - res[(seed, "plain")])
-    assert sum(diffs) / len(diffs) >= -0.25, res
+    assert sum(diffs) / len(diffs) >= -0.1, res
     assert min(res[(s, "plain_samples")] for s in (1, 2)) >= 2 * 48, res  # ~125 live samples per ray
 
 
@@ -243,7 +243,8 @@ def test_trainer_graph_step_matches_eager_step():
     rays = rays.cuda()
     torch.manual_seed(0)
     m = FactorFields(W.field_cfg("cfg2"), device="cuda", precision="bf16")
-    tr = RadianceFieldTrainer(m, sampler=ProposalSampler(m), n_iters=100)
+    # per-ray jitter (fixed below) so that the eager and the replayed step draw the same samples
+    tr = RadianceFieldTrainer(m, sampler=ProposalSampler(m, sample_jitter=False), n_iters=100)
     for _ in range(30):
         tr.step(rays, gt)
     tr.jitter = torch.rand(rays.shape[0], device="cuda", generator=torch.Generator(device="cuda").manual_seed(3))
