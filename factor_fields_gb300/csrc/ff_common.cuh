@@ -153,6 +153,46 @@ __device__ __forceinline__ void linear_corners(const float* ix, const int* size,
   }
 }
 
+// Linear corners for lookups whose coordinates lie inside the grid on every axis, 0 <= ix <= size-1:
+// basis lookups (align_corners=True after grid_mapping, |loc| <= 1) and coefficient lookups
+// (border padding clamps). No corner is ever out of bounds, so there are no per-corner checks: the
+// low corner is clamped to size-2, and at ix == size-1 the high corner takes weight 1 and the low
+// one weight 0, the same nonzero terms as ATen's single in-bounds corner (an axis of size 1 aliases
+// both corners onto cell 0, the high one with weight 0). ix is clamped into the grid first, which
+// leaves in-range values unchanged and keeps any input (even NaN) inside the buffer. Weights and
+// their products are formed exactly as in linear_corners.
+template <int D>
+__device__ __forceinline__ void linear_corners_inside(const float* ix_in, const int* size, Corners<D>& c) {
+  static_assert(D == 2 || D == 3, "bi- or trilinear corners");
+  int base = 0, step[D], pitch = 1;
+  float wl[D], wh[D];
+#pragma unroll
+  for (int k = 0; k < D; ++k) {
+    const float ix = fminf(fmaxf(ix_in[k], 0.f), (float)(size[k] - 1));
+    const int lo = max(0, min((int)floorf(ix), size[k] - 2));
+    const float f = (float)lo;
+    wl[k] = __fsub_rn(__fadd_rn(f, 1.f), ix);
+    wh[k] = __fsub_rn(ix, f);
+    step[k] = size[k] > 1 ? pitch : 0;
+    base += lo * pitch;
+    pitch *= size[k];
+  }
+  float wxy[4];
+#pragma unroll
+  for (int b = 0; b < 4; ++b) wxy[b] = __fmul_rn((b & 1) ? wh[0] : wl[0], ((b >> 1) & 1) ? wh[1] : wl[1]);
+#pragma unroll
+  for (int b = 0; b < (1 << D); ++b) {
+    int flat = base;
+#pragma unroll
+    for (int k = 0; k < D; ++k)
+      if ((b >> k) & 1) flat += step[k];
+    float w = wxy[b & 3];
+    if (D == 3) w = __fmul_rn(w, ((b >> 2) & 1) ? wh[D - 1] : wl[D - 1]);
+    c.idx[b] = flat;
+    c.w[b] = w;
+  }
+}
+
 // Nearest corner (nearbyint = round half to even), stored in slot 0 with weight 1.
 template <int D>
 __device__ __forceinline__ void nearest_corner(const float* ix, const int* size, Corners<D>& c) {
@@ -220,7 +260,9 @@ __device__ __forceinline__ void atomic_add_vec(float* p, const float* v) {
 // per-point corner sets of the coefficient grid and of one basis level; gather / scatter
 // ---------------------------------------------------------------------------------------
 
-template <int CD>
+// kInside: linear corners without per-corner bounds checks (border padding keeps every lookup
+// inside the grid); the fused kernels' gathers then read every corner unconditionally.
+template <int CD, bool kInside = false>
 __device__ __forceinline__ void coeff_corners(const FFField& f, const float* p, Corners<CD>& cc) {
   float ix[CD];
   int sz[CD];
@@ -231,6 +273,8 @@ __device__ __forceinline__ void coeff_corners(const FFField& f, const float* p, 
   }
   if (f.coeff_interp == FF_INTERP_NEAREST)
     nearest_corner<CD>(ix, sz, cc);
+  else if constexpr (kInside)
+    linear_corners_inside<CD>(ix, sz, cc);
   else
     linear_corners<CD>(ix, sz, cc);
 }
@@ -283,7 +327,8 @@ __device__ __forceinline__ void scatter(float* __restrict__ grad, int stride, in
   }
 }
 
-// Basis corners with the division-free mapping (fused kernels).
+// Basis corners with the division-free mapping (fused kernels). The mapped coordinate lies in
+// [-1, 1], so every linear lookup is inside the grid (linear_corners_inside).
 template <int BD>
 __device__ __forceinline__ void basis_corners_fast(const FFField& f, int l, const float* p, Corners<BD>& bc) {
   float ix[BD];
@@ -299,19 +344,55 @@ __device__ __forceinline__ void basis_corners_fast(const FFField& f, int l, cons
   if (f.basis_interp == FF_INTERP_NEAREST)
     nearest_corner<BD>(ix, sz, bc);
   else
-    linear_corners<BD>(ix, sz, bc);
+    linear_corners_inside<BD>(ix, sz, bc);
+}
+
+// Gather / scatter over corner sets whose corners are all inside the grid (linear_corners_inside),
+// or, with all == false, over slot 0 alone (nearest_corner; the slot is inside the grid for the
+// lookups that use these helpers). No index checks: every read is unconditional.
+template <int V, int D, typename T>
+__device__ __forceinline__ void gather_inside(const T* __restrict__ grid, int stride, const Corners<D>& cn, bool all,
+                                              float* acc) {
+#pragma unroll
+  for (int v = 0; v < V; ++v) acc[v] = 0.f;
+#pragma unroll
+  for (int k = 0; k < Corners<D>::K; ++k) {
+    if (k == 0 || all) {
+      float t[V];
+      load_vec<V>(grid + cn.idx[k] * stride, t);
+#pragma unroll
+      for (int v = 0; v < V; ++v) acc[v] += t[v] * cn.w[k];
+    }
+  }
+}
+
+// Zero-weight corners (nearest's unused slots, the weight-0 corner at the grid's far edge) are
+// skipped: they would add zeros.
+template <int V, int D>
+__device__ __forceinline__ void scatter_inside(float* __restrict__ grad, int stride, const Corners<D>& cn,
+                                               const float* g) {
+#pragma unroll
+  for (int k = 0; k < Corners<D>::K; ++k) {
+    if (cn.w[k] != 0.f) {
+      float t[V];
+#pragma unroll
+      for (int v = 0; v < V; ++v) t[v] = g[v] * cn.w[k];
+      atomic_add_vec<V>(grad + cn.idx[k] * stride, t);
+    }
+  }
 }
 
 // All 18 coefficient channels of every valid corner with 16-byte loads (channels 0..15) and
 // one 4- (BF16) or 8-byte (float32) load for channels 16, 17. Needs coeff_stride % 8 == 0.
+// Corner sets as in gather_inside (all: every corner; else slot 0 only).
 template <int D>
 __device__ __forceinline__ void gather_coeff18(const __nv_bfloat16* __restrict__ grid, int stride, const Corners<D>& cn,
-                                               float* acc) {
+                                               bool all, float* acc) {
 #pragma unroll
   for (int v = 0; v < 18; ++v) acc[v] = 0.f;
 #pragma unroll
   for (int k = 0; k < Corners<D>::K; ++k) {
-    if (cn.idx[k] >= 0 && cn.w[k] != 0.f) {
+    if (k == 0 || all) {
       const __nv_bfloat16* p = grid + (int64_t)cn.idx[k] * stride;
       const uint4 a = __ldg(reinterpret_cast<const uint4*>(p));
       const uint4 b = __ldg(reinterpret_cast<const uint4*>(p + 8));
@@ -329,12 +410,12 @@ __device__ __forceinline__ void gather_coeff18(const __nv_bfloat16* __restrict__
 
 template <int D>
 __device__ __forceinline__ void gather_coeff18(const float* __restrict__ grid, int stride, const Corners<D>& cn,
-                                               float* acc) {
+                                               bool all, float* acc) {
 #pragma unroll
   for (int v = 0; v < 18; ++v) acc[v] = 0.f;
 #pragma unroll
   for (int k = 0; k < Corners<D>::K; ++k) {
-    if (cn.idx[k] >= 0 && cn.w[k] != 0.f) {
+    if (k == 0 || all) {
       const float* p = grid + (int64_t)cn.idx[k] * stride;
       const float wk = cn.w[k];
 #pragma unroll
@@ -350,13 +431,13 @@ __device__ __forceinline__ void gather_coeff18(const float* __restrict__ grid, i
 }
 
 // Scatter 18 coefficient-channel gradients (float32 grid, stride % 4 == 0): four float4 and
-// one float2 atomic per valid corner.
+// one float2 atomic per corner of nonzero weight (corner sets as in gather_inside).
 template <int D>
 __device__ __forceinline__ void scatter_coeff18(float* __restrict__ grad, int stride, const Corners<D>& cn,
                                                 const float* g) {
 #pragma unroll
   for (int k = 0; k < Corners<D>::K; ++k) {
-    if (cn.idx[k] >= 0 && cn.w[k] != 0.f) {
+    if (cn.w[k] != 0.f) {
       float* p = grad + (int64_t)cn.idx[k] * stride;
       const float wk = cn.w[k];
 #pragma unroll

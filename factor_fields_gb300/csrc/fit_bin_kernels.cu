@@ -44,7 +44,7 @@ __global__ void __launch_bounds__(kBinThreads) fit_bin_kernel(const FFField f, c
 #pragma unroll
     for (int k = 0; k < CD; ++k) p[k] = x[i * CD + k];
     Corners<CD> cc;
-    coeff_corners<CD>(f, p, cc);
+    coeff_corners<CD, true>(f, p, cc);  // the low corner as the fit kernel computes it
     int32_t k = cc.idx[0];
     if (k < 0 || k >= n_keys) k = 0;  // non-finite coordinates: any bin will do
     key_rank[i] = make_int2(k, atomicAdd(count + k, 1));

@@ -38,6 +38,7 @@ cudaError_t launch_fused_fit_binned(const FFField& f, const void* basis, const v
   a.x_stride = stride;  // packed rows: coordinates, then the targets
   a.target = rows + f.coord_dim;
   a.t_stride = stride;
+  a.packed_rows = (f.coord_dim == 3 && m.out_dim == 1 && stride == 4) ? 1 : 0;
   a.loss_kind = loss_kind;
   a.loss_scale = loss_scale;
   a.loss_sum = loss_sum;

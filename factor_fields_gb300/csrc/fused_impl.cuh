@@ -83,6 +83,7 @@ struct FusedArgs {
   const float* grad_out;  // kBwd: [n, out]
   const float* target;    // kFit: [n, out] rows t_stride floats apart
   int64_t t_stride;
+  int packed_rows;  // fits, coord_dim 3, out_dim 1: x holds 16-byte-aligned rows (x, y, z, target)
   int loss_kind;
   float loss_scale;
   float* loss_sum;
@@ -223,6 +224,8 @@ __global__ void __launch_bounds__(kThreads, 3) fused_field_mlp_kernel(const Fuse
   const Smem s = carve<MODE, OUTT>(smem_raw);
   const FFField& f = a.f;
   const int out = a.out_dim;
+  // fits of one output on packed 16-byte rows (x, y, z, target): one load per point
+  constexpr bool kPackedRow = is_fit<MODE>() && OUTT == 1 && CD == 3;
   const T* basis = static_cast<const T*>(a.basis);
   const T* coeff = static_cast<const T*>(a.coeff);
   float* xf = s.xf + warp * 32 * LD_XF;  // this warp's feature tile
@@ -260,18 +263,26 @@ __global__ void __launch_bounds__(kThreads, 3) fused_field_mlp_kernel(const Fuse
     float bv[kF], cv[kF];
     float p[CD];
     // ---------------- gather ----------------
+    float tgt = 0.f;  // packed rows: the point's target, read with its coordinates
     if (valid) {
+      if (kPackedRow && a.packed_rows) {
+        const float4 r = *reinterpret_cast<const float4*>(a.x + i * 4);
+        p[0] = r.x; p[1] = r.y; p[2] = r.z;
+        tgt = r.w;
+      } else {
 #pragma unroll
-      for (int k = 0; k < CD; ++k) p[k] = a.x[i * a.x_stride + k];
+        for (int k = 0; k < CD; ++k) p[k] = a.x[i * a.x_stride + k];
+      }
       Corners<CD> cc;
-      coeff_corners<CD>(f, p, cc);
-      gather_coeff18<CD>(coeff, f.coeff_stride, cc, cv);
+      coeff_corners<CD, true>(f, p, cc);
+      gather_coeff18<CD>(coeff, f.coeff_stride, cc, f.coeff_interp != FF_INTERP_NEAREST, cv);
+      const bool all_b = f.basis_interp != FF_INTERP_NEAREST;
       for_levels(std::make_integer_sequence<int, 6>{}, [&](auto lc) {
         constexpr int l = decltype(lc)::value;
         Corners<BD> bc;
         basis_corners_fast<BD>(f, l, p, bc);
         constexpr int C = kLevelC[l], OFF = kLevelOff[l];
-        gather<C, BD>(basis + f.level_offset[l], f.level_stride[l], 0, bc, bv + OFF);
+        gather_inside<C, BD>(basis + f.level_offset[l], f.level_stride[l], bc, all_b, bv + OFF);
       });
     } else {
 #pragma unroll
@@ -364,6 +375,11 @@ __global__ void __launch_bounds__(kThreads, 3) fused_field_mlp_kernel(const Fuse
         }
       } else {
         // ---------------- dO ----------------
+        float tr0 = 0.f, tr1 = 0.f;  // packed rows: targets of rows r0 / r1 from their point lanes
+        if constexpr (kPackedRow) {
+          tr0 = __shfl_sync(0xffffffffu, tgt, r0);
+          tr1 = __shfl_sync(0xffffffffu, tgt, r1);
+        }
         float dc[OUTT][4];
 #pragma unroll
         for (int nt = 0; nt < OUTT; ++nt) {
@@ -375,7 +391,9 @@ __global__ void __launch_bounds__(kThreads, 3) fused_field_mlp_kernel(const Fuse
             float d = 0.f;
             if (row < a.n && col < out) {
               if constexpr (is_fit<MODE>()) {
-                const float err = oc[nt][q] - a.target[row * a.t_stride + col];
+                const float tv = (kPackedRow && a.packed_rows) ? ((q < 2) ? tr0 : tr1)
+                                                               : a.target[row * a.t_stride + col];
+                const float err = oc[nt][q] - tv;
                 if (a.loss_kind == FF_LOSS_L1) {
                   loss_acc += fabsf(err);
                   d = (err > 0.f ? 1.f : (err < 0.f ? -1.f : 0.f)) * a.loss_scale;
@@ -536,13 +554,13 @@ __global__ void __launch_bounds__(kThreads, 3) fused_field_mlp_kernel(const Fuse
             gc[k] = gx * bv[k];
             bv[k] = gx * cv[k];  // bv now holds dL/dbasis
           }
-          coeff_corners<CD>(f, p, cc);
+          coeff_corners<CD, true>(f, p, cc);
           for_levels(std::make_integer_sequence<int, 6>{}, [&](auto lc) {
             constexpr int l = decltype(lc)::value;
             Corners<BD> bc;
             basis_corners_fast<BD>(f, l, p, bc);
             constexpr int C = kLevelC[l], OFF = kLevelOff[l];
-            scatter<C, BD>(a.grad_basis + f.level_offset[l], f.level_stride[l], 0, bc, bv + OFF);
+            scatter_inside<C, BD>(a.grad_basis + f.level_offset[l], f.level_stride[l], bc, bv + OFF);
           });
         } else {
 #pragma unroll
@@ -565,14 +583,14 @@ __global__ void __launch_bounds__(kThreads, 3) fused_field_mlp_kernel(const Fuse
           bv[k] = gx * cv[k];  // bv now holds dL/dbasis
         }
         Corners<CD> cc;
-        coeff_corners<CD>(f, p, cc);
+        coeff_corners<CD, true>(f, p, cc);
         scatter_coeff18<CD>(a.grad_coeff, f.coeff_stride, cc, gc);
         for_levels(std::make_integer_sequence<int, 6>{}, [&](auto lc) {
           constexpr int l = decltype(lc)::value;
           Corners<BD> bc;
           basis_corners_fast<BD>(f, l, p, bc);
           constexpr int C = kLevelC[l], OFF = kLevelOff[l];
-          scatter<C, BD>(a.grad_basis + f.level_offset[l], f.level_stride[l], 0, bc, bv + OFF);
+          scatter_inside<C, BD>(a.grad_basis + f.level_offset[l], f.level_stride[l], bc, bv + OFF);
         });
       }
       __syncwarp();
