@@ -186,6 +186,8 @@ def run_native(args, ws, rank, local):
     N.reset_launch_count()
     runner.step(*devb[0])
     per_step = N.launch_count()
+    # setup: one CUDA graph per resident batch (graph_step reads device batches in place)
+    runner.capture_graphs(devb)
     for i in range(args.warmup):
         runner.graph_step(*devb[i % nb])
     torch.cuda.synchronize()

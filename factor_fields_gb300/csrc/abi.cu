@@ -252,12 +252,13 @@ int ff_field_fit_step_binned(const FFField* f, const void* basis, const void* co
   if (n > 0 && (!workspace || workspace_bytes < need))
     return set_error(FF_ERR_SIZE, "workspace smaller than ff_field_fit_binned_workspace_bytes");
   if (!aligned(workspace, 256)) return set_error(FF_ERR_ALIGN, "workspace must be 256-byte aligned");
-  if (flags & ~FF_FIT_ZERO_GRADS) return set_error(FF_ERR_ARG, "unknown flags");
+  if (flags & ~(FF_FIT_ZERO_GRADS | FF_FIT_MEAN_LOSS)) return set_error(FF_ERR_ARG, "unknown flags");
   if (!workspace) return set_error(FF_ERR_ARG, "workspace is NULL");
   FFMlpGrad none = {};
   return cuda_status(launch_fused_fit_binned(*f, basis, coeff, *m, x, target, n, loss_kind, loss_scale, loss_sum,
                                              grad_basis, grad_coeff_grid, g ? *g : none, workspace,
-                                             (flags & FF_FIT_ZERO_GRADS) != 0, (cudaStream_t)stream),
+                                             (flags & FF_FIT_ZERO_GRADS) != 0,
+                                             (flags & FF_FIT_MEAN_LOSS) ? loss_scale : 1.f, (cudaStream_t)stream),
                      "ff_field_fit_step_binned launch");
 }
 

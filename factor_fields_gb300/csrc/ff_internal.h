@@ -49,11 +49,11 @@ cudaError_t launch_fused_fit(const FFField& f, const void* basis, const void* co
 cudaError_t launch_fused_fit_rows(const FFField& f, const void* basis, const void* coeff, const FFMlp& m,
                                   const float* x, int64_t x_stride, const float* target, int64_t t_stride, int64_t n,
                                   int loss_kind, float loss_scale, float* loss_sum, float* grad_basis,
-                                  float* grad_coeff, const FFMlpGrad& g, cudaStream_t st);
+                                  float* grad_coeff, const FFMlpGrad& g, float loss_mul, cudaStream_t st);
 cudaError_t launch_fused_fit_binned(const FFField& f, const void* basis, const void* coeff, const FFMlp& m,
                                     const float* x, const float* target, int64_t n, int loss_kind, float loss_scale,
                                     float* loss_sum, float* grad_basis, float* grad_coeff, const FFMlpGrad& g,
-                                    void* workspace, bool zero_grads, cudaStream_t st);
+                                    void* workspace, bool zero_grads, float loss_mul, cudaStream_t st);
 
 // fit_bin_kernels.cu
 int64_t fit_bin_keys(const FFField& f);

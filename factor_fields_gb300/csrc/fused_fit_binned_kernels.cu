@@ -7,7 +7,7 @@ namespace ffgb {
 cudaError_t launch_fused_fit_binned(const FFField& f, const void* basis, const void* coeff, const FFMlp& m,
                                     const float* x, const float* target, int64_t n, int loss_kind, float loss_scale,
                                     float* loss_sum, float* grad_basis, float* grad_coeff, const FFMlpGrad& g,
-                                    void* workspace, bool zero_grads, cudaStream_t st) {
+                                    void* workspace, bool zero_grads, float loss_mul, cudaStream_t st) {
   FitZero z = {};
   if (zero_grads) {
     z.grad_basis = grad_basis;
@@ -33,7 +33,7 @@ cudaError_t launch_fused_fit_binned(const FFField& f, const void* basis, const v
   if (e != cudaSuccess) return e;
   if (f.param_dtype != FF_BF16)  // float32 grids: the per-point fit on the binned rows
     return launch_fused_fit_rows(f, basis, coeff, m, rows, stride, rows + f.coord_dim, stride, n, loss_kind,
-                                 loss_scale, loss_sum, grad_basis, grad_coeff, g, st);
+                                 loss_scale, loss_sum, grad_basis, grad_coeff, g, loss_mul, st);
   FusedArgs a = make_args(f, basis, coeff, m, rows, n);
   a.x_stride = stride;  // packed rows: coordinates, then the targets
   a.target = rows + f.coord_dim;
@@ -42,6 +42,7 @@ cudaError_t launch_fused_fit_binned(const FFField& f, const void* basis, const v
   a.loss_kind = loss_kind;
   a.loss_scale = loss_scale;
   a.loss_sum = loss_sum;
+  a.loss_mul = loss_mul;
   a.grad_basis = grad_basis;
   a.grad_coeff = grad_coeff;
   a.grad_w0 = g.weight[0];

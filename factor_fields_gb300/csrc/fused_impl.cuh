@@ -87,6 +87,7 @@ struct FusedArgs {
   int loss_kind;
   float loss_scale;
   float* loss_sum;
+  float loss_mul;  // the loss accumulates loss_mul * sum (1, or loss_scale for the mean)
   float* grad_basis;
   float* grad_coeff;
   float* grad_w0;
@@ -601,7 +602,7 @@ __global__ void __launch_bounds__(kThreads, 3) fused_field_mlp_kernel(const Fuse
     if constexpr (is_fit<MODE>()) {
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) loss_acc += __shfl_xor_sync(0xffffffffu, loss_acc, o);
-      if (lane == 0 && a.loss_sum) atomicAdd(a.loss_sum, loss_acc);
+      if (lane == 0 && a.loss_sum) atomicAdd(a.loss_sum, loss_acc * a.loss_mul);
     }
     // dW0 slice (rows 16*warp + g, + 8; cols 8*nt + 2t, + 1): features -> grad_w0, column 18 -> grad_b0
 #pragma unroll
@@ -710,6 +711,7 @@ inline FusedArgs make_args(const FFField& f, const void* basis, const void* coef
   a.x = x;
   a.x_stride = f.coord_dim;
   a.t_stride = m.out_dim;
+  a.loss_mul = 1.f;
   a.n = n;
   return a;
 }

@@ -169,9 +169,9 @@ class FieldFitRunner:
             g.bias[i] = b.grad.data_ptr() if b is not None else None
         return g
 
-    def zero_grad(self):
+    def zero_grad(self, loss_buf=None):
         """Zero the parameters' gradients and the loss accumulator in one ff_zero_f32 launch."""
-        bufs = [p.grad for p in self._params()] + [self.loss_buf]
+        bufs = [p.grad for p in self._params()] + [self.loss_buf if loss_buf is None else loss_buf]
         key = tuple(b.data_ptr() for b in bufs)
         if getattr(self, "_zero_key", None) != key:
             for b in bufs:
@@ -183,35 +183,81 @@ class FieldFitRunner:
         N.call("ff_zero_f32", self._zero_ptrs, self._zero_counts, len(bufs), N.stream_ptr(),
                kernels=-(-len(bufs) // 8))
 
+    _GRAPHS_KEPT = 8  # graphs of device input pairs read in place (least recently used first out)
+
     def graph_step(self, x, y):
-        """step() replayed from a CUDA graph: the batch is copied into static buffers and the
-        captured launches (the binning with the gradient zeroing, the fit kernel, the loss
-        scale) replay with one host call. The graph is captured on first use and re-captured
-        when the batch shape, a parameter buffer or the binning workspace changes."""
-        # the captured launches keep the workspace address: a reallocation (an eager step on a
-        # larger batch) bumps _ws_gen and forces a new capture
-        key = (tuple(x.shape), tuple(y.shape), self.m.basis_flat.data_ptr(), self.m.coeff_flat.data_ptr(),
-               self.m.precision, self._ws_gen)
-        if getattr(self, "_graph_key", None) != key:
-            dev = self.m.basis_flat.device
-            self._xs = torch.empty(x.shape, dtype=x.dtype, device=dev)
-            self._ys = torch.empty(y.shape, dtype=y.dtype, device=dev)
-            self._xs.copy_(x)
-            self._ys.copy_(y)
-            side = torch.cuda.Stream()
-            side.wait_stream(torch.cuda.current_stream())
-            with torch.cuda.stream(side):
-                self.step(self._xs, self._ys)  # warm-up outside the capture (kernel attributes, workspace)
-            torch.cuda.current_stream().wait_stream(side)
-            self._graph = torch.cuda.CUDAGraph()
-            with torch.cuda.graph(self._graph):
-                self._graph_loss = self.step(self._xs, self._ys)
-            self._graph_key = key[:-1] + (self._ws_gen,)  # the warm-up may have sized the workspace
+        """step() replayed from a CUDA graph, one host call for all its launches (the binning with
+        the gradient zeroing, the fit kernel; the loss is the mean, accumulated by the kernel).
+
+        Device batches (contiguous float32 on the model's device) are read in place: a graph is
+        captured per input buffer pair and kept (up to 8), so that a ring of batches resident in
+        HBM replays without copies. Any other batch (host memory, other dtypes or strides) is
+        copied into static buffers whose graph then replays. Graphs are re-captured when the batch
+        shape, a parameter buffer or the binning workspace changes. The returned 0-d loss belongs
+        to the replayed graph: the next replay of the same graph overwrites it."""
+        from collections import OrderedDict
+        key, in_place = self._graph_key(x, y)
+        graphs = self.__dict__.setdefault("_graphs", OrderedDict())
+        ent = graphs.get(key)
+        if ent is not None and ent["ws_gen"] != self._ws_gen:  # captured with a workspace since freed
+            del graphs[key]
+            ent = None
+        if ent is None:
+            ent = self._capture(x, y, in_place)
+            graphs[key] = ent
+            for k in [k for k, e in graphs.items() if e["ws_gen"] != self._ws_gen]:
+                del graphs[k]
+            while len(graphs) > self._GRAPHS_KEPT + 1:
+                graphs.popitem(last=False)
+        graphs.move_to_end(key)
         self.m._read_buffers()  # refresh the BF16 grid copies in place if the masters changed
-        self._xs.copy_(x, non_blocking=True)
-        self._ys.copy_(y, non_blocking=True)
-        self._graph.replay()
-        return self._graph_loss
+        if not in_place:
+            ent["x"].copy_(x, non_blocking=True)
+            ent["y"].copy_(y, non_blocking=True)
+        ent["graph"].replay()
+        return ent["loss"]
+
+    def capture_graphs(self, batches):
+        """Capture (without replaying) the graphs graph_step will use for these (x, y) batches,
+        e.g. a ring of batches resident in HBM, so that no step pays for a capture."""
+        from collections import OrderedDict
+        graphs = self.__dict__.setdefault("_graphs", OrderedDict())
+        if len(batches) > self._GRAPHS_KEPT:
+            raise ValueError(f"at most {self._GRAPHS_KEPT} batches keep their graphs")
+        for x, y in batches:
+            key, in_place = self._graph_key(x, y)
+            if key not in graphs or graphs[key]["ws_gen"] != self._ws_gen:
+                graphs[key] = self._capture(x, y, in_place)
+        for k in [k for k, e in graphs.items() if e["ws_gen"] != self._ws_gen]:
+            del graphs[k]
+
+    def _graph_key(self, x, y):
+        dev = self.m.basis_flat.device
+        in_place = (x.device == dev and y.device == dev and x.dtype == torch.float32 and y.dtype == torch.float32
+                    and x.is_contiguous() and y.is_contiguous())
+        key = (tuple(x.shape), tuple(y.shape), self.m.basis_flat.data_ptr(), self.m.coeff_flat.data_ptr(),
+               self.m.precision) + ((x.data_ptr(), y.data_ptr()) if in_place else ("static",))
+        return key, in_place
+
+    def _capture(self, x, y, in_place):
+        dev = self.m.basis_flat.device
+        if in_place:
+            xs, ys = x, y
+        else:
+            xs = torch.empty(x.shape, dtype=torch.float32, device=dev)
+            ys = torch.empty(y.shape, dtype=torch.float32, device=dev)
+            xs.copy_(x)
+            ys.copy_(y)
+        loss_buf = torch.zeros(1, device=dev)
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(side):
+            self.step(xs, ys, _loss_buf=loss_buf)  # warm-up outside the capture (kernel attributes, workspace)
+        torch.cuda.current_stream().wait_stream(side)
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph):
+            loss = self.step(xs, ys, _loss_buf=loss_buf)
+        return {"graph": graph, "loss": loss, "x": xs, "y": ys, "buf": loss_buf, "ws_gen": self._ws_gen}
 
     def _workspace(self, desc, n):
         """Device workspace of ff_field_fit_step_binned for n points, kept across steps."""
@@ -223,10 +269,10 @@ class FieldFitRunner:
             self._ws_gen += 1
         return self._ws
 
-    def step(self, x, y, kernel_events=False):
+    def step(self, x, y, kernel_events=False, _loss_buf=None):
         m = self.m
         if not (self.fused and self.binned):  # the binned call zeroes them in its binning pass
-            self.zero_grad()
+            self.zero_grad(_loss_buf)
         basis_r, coeff_r, dt = m._read_buffers()
         desc = m.descriptor(dt)
         n = x.shape[0]
@@ -242,17 +288,22 @@ class FieldFitRunner:
                 ws = self._workspace(desc, n)
             if ev:
                 ev[0].record()
+            lbuf = self.loss_buf if _loss_buf is None else _loss_buf
             common = (ctypes.byref(desc), N.ptr(basis_r), N.ptr(coeff_r), ctypes.byref(mlp), N.ptr(x), N.ptr(y), n,
-                      N.FF_LOSS[self.loss], 1.0 / max(n * m.linear_mat.out_dim, 1), N.ptr(self.loss_buf),
+                      N.FF_LOSS[self.loss], 1.0 / max(n * m.linear_mat.out_dim, 1), N.ptr(lbuf),
                       N.ptr(m.basis_flat.grad), N.ptr(m.coeff_flat.grad), ctypes.byref(g))
-            if self.binned:  # kernels: bin (+ gradient zeroing), alloc, permute, fit
-                N.call("ff_field_fit_step_binned", *common, N.FF_FIT_ZERO_GRADS, N.ptr(ws), ws.numel(), st,
-                       kernels=4)
+            if self.binned:  # kernels: bin (+ gradient and loss zeroing), alloc, permute, fit (mean loss)
+                N.call("ff_field_fit_step_binned", *common, N.FF_FIT_ZERO_GRADS | N.FF_FIT_MEAN_LOSS, N.ptr(ws),
+                       ws.numel(), st, kernels=4)
             else:
                 N.call("ff_field_fit_step", *common, st)
             if ev:
                 ev[1].record()
-            loss = self.loss_buf[0] / max(n * m.linear_mat.out_dim, 1)
+            if self.binned:
+                # the kernel accumulated the mean; a captured step returns its own buffer
+                loss = lbuf[0] if _loss_buf is not None else lbuf[0].clone()
+            else:
+                loss = lbuf[0] / max(n * m.linear_mat.out_dim, 1)
             return ev if kernel_events else loss
         feats = torch.empty(n, m.n_feat, device=x.device)
         N.call("ff_field_forward", ctypes.byref(desc), N.ptr(basis_r), N.ptr(coeff_r), N.ptr(x), n, N.ptr(feats),

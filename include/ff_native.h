@@ -51,7 +51,7 @@ enum { FF_INTERP_LINEAR = 0, FF_INTERP_NEAREST = 1 };
 enum { FF_F32 = 0, FF_BF16 = 1 };
 enum { FF_LOSS_L1 = 0, FF_LOSS_MSE = 1 };
 /* ff_field_fit_step_binned flags */
-enum { FF_FIT_ZERO_GRADS = 1 };
+enum { FF_FIT_ZERO_GRADS = 1, FF_FIT_MEAN_LOSS = 2 };
 
 /*
  * Description of one grid/grid factor field (models/FactorFields.py:262-309 setup_params,
@@ -178,6 +178,8 @@ FF_API int ff_field_fit_step(const FFField* f, const void* basis, const void* co
  * flags: FF_FIT_ZERO_GRADS zeroes grad_basis (the whole flat basis), grad_coeff_grid (this
  * coefficient grid), the MLP gradients in g and *loss_sum first, in the binning pass (the step's
  * zero_grad without a launch of its own); otherwise they are accumulated into (+=).
+ * FF_FIT_MEAN_LOSS: *loss_sum accumulates loss_scale * sum of the per-element losses (with
+ * loss_scale = 1 / (n * out_dim) the mean loss itself) instead of the plain sum.
  * workspace: device memory of at least ff_field_fit_binned_workspace_bytes(f, n, out_dim)
  * bytes, 256-byte aligned, not shared with a call in flight. */
 FF_API int64_t ff_field_fit_binned_workspace_bytes(const FFField* f, int64_t n, int32_t out_dim);

@@ -194,6 +194,15 @@ def test_graph_step_matches_step_and_tracks_updates():
             for a, b in zip(g_eager, r._params()):
                 assert torch.allclose(a, b.grad, rtol=1e-5, atol=1e-9), (it, src)
         opt.step()
+    # device batches replay their own graphs (read in place, no copies): a loss returned by one
+    # graph is not overwritten by the replay of another
+    eager = [float(r.step(x, y)) for x, y in dev]
+    la = r.graph_step(*dev[0])
+    lb = r.graph_step(*dev[1])
+    torch.cuda.synchronize()
+    assert abs(float(la) - eager[0]) <= 1e-6 * max(1.0, abs(eager[0]))
+    assert abs(float(lb) - eager[1]) <= 1e-6 * max(1.0, abs(eager[1]))
+    assert len(r._graphs) == 3  # two device pairs + the static buffers of the host batches
 
 
 @pytest.mark.parametrize("precision", ["bf16", "fp32"])
