@@ -87,6 +87,10 @@ SIGNATURES = {
     "ff_field_fit_binned_workspace_bytes": (c_i64, [_P(FFField), c_i64, c_i32]),
     "ff_field_fit_step_binned": (c_i32, [_P(FFField), c_vp, c_vp, _P(FFMlp), c_vp, c_vp, c_i64, c_i32, c_f32, c_vp,
                                          c_vp, c_vp, _P(FFMlpGrad), c_i32, c_vp, c_i64, c_vp]),
+    "ff_field_fit_bin": (c_i32, [_P(FFField), _P(FFMlp), c_vp, c_vp, c_i64, c_vp, c_vp, c_vp, _P(FFMlpGrad), c_i32,
+                                 c_vp, c_i64, c_vp]),
+    "ff_field_fit_step_on_bins": (c_i32, [_P(FFField), c_vp, c_vp, _P(FFMlp), c_i64, c_i32, c_f32, c_vp, c_vp, c_vp,
+                                          _P(FFMlpGrad), c_i32, c_vp, c_i64, c_vp]),
     "ff_zero_f32": (c_i32, [c_vp, c_vp, c_i32, c_vp]),
     "ff_adam_step": (c_i32, [c_vp, c_i32, c_f32, c_f32, c_f32, c_i32, c_vp]),
     "ff_image_metrics_workspace_bytes": (c_i64, [c_i32, c_i32, c_i32]),
@@ -173,6 +177,7 @@ _NON_LAUNCHING = {"ff_abi_version", "ff_last_error", "ff_device_info", "ff_struc
 
 # entry points that enqueue more than one kernel of this library
 _KERNELS_PER_CALL = {"ff_scan_counts": 3, "ff_scan_counts_noalloc": 3,
+                     "ff_field_fit_bin": 3,  # bin (+ zeroing), alloc, permute
                      "ff_occupancy_mask": 5,  # init, pool, unite, size, filter (3 when min_size <= 1)
                      "ff_image_metrics": 2}
 

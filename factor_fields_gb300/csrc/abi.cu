@@ -37,7 +37,8 @@ static int cuda_status(cudaError_t e, const char* what) {
 static bool aligned(const void* p, int bytes) { return (reinterpret_cast<uintptr_t>(p) % bytes) == 0; }
 
 // Validates an FFField; returns FF_OK or an error code with ff_last_error set.
-static int validate_field(const FFField* f, const void* basis, const void* coeff) {
+// need_grids false: the descriptor alone (entries that touch no grid values)
+static int validate_field(const FFField* f, const void* basis, const void* coeff, bool need_grids = true) {
   if (!f) return set_error(FF_ERR_ARG, "field descriptor is NULL");
   if (!(f->basis_dim == 2 || f->basis_dim == 3)) return set_error(FF_ERR_ARG, "basis_dim must be 2 or 3");
   if (!(f->coord_dim == f->basis_dim || (f->basis_dim == 2 && f->coord_dim == 3)))
@@ -50,8 +51,9 @@ static int validate_field(const FFField* f, const void* basis, const void* coeff
     return set_error(FF_ERR_ARG, "interpolation mode must be linear or nearest");
   if (f->param_dtype != FF_F32 && f->param_dtype != FF_BF16) return set_error(FF_ERR_ARG, "param_dtype must be F32 or BF16");
   const int es = f->param_dtype == FF_F32 ? 4 : 2;
-  if (!basis || !coeff) return set_error(FF_ERR_ARG, "basis/coeff pointer is NULL");
-  if (!aligned(basis, 16) || !aligned(coeff, 16)) return set_error(FF_ERR_ALIGN, "basis/coeff must be 16-byte aligned");
+  if (need_grids && (!basis || !coeff)) return set_error(FF_ERR_ARG, "basis/coeff pointer is NULL");
+  if (need_grids && (!aligned(basis, 16) || !aligned(coeff, 16)))
+    return set_error(FF_ERR_ALIGN, "basis/coeff must be 16-byte aligned");
   int sum = 0;
   for (int l = 0; l < f->n_levels; ++l) {
     const int c = f->level_channels[l], v = f->level_vec[l];
@@ -237,29 +239,88 @@ int64_t ff_field_fit_binned_workspace_bytes(const FFField* f, int64_t n, int32_t
   return fit_bin_workspace_bytes(*f, n, out_dim);
 }
 
+// Checks shared by the binned fit entries: the binning half (x, target, zeroing targets) and the
+// fit half (loss, gradient buffers); both need a large enough, aligned workspace.
+static int validate_fit_bin(const FFField* f, const FFMlp* m, const float* x, const float* target, int64_t n,
+                            float* grad_basis, float* grad_coeff_grid, int32_t flags, const void* workspace,
+                            int64_t workspace_bytes) {
+  int rc = validate_mlp(m);
+  if (rc) return rc;
+  if (n < 0 || (n > 0 && !x)) return set_error(FF_ERR_ARG, "bad points pointer or count");
+  if (n > 0 && !target) return set_error(FF_ERR_ARG, "target is NULL");
+  if (flags & ~FF_FIT_ZERO_GRADS) return set_error(FF_ERR_ARG, "unknown flags");
+  if ((flags & FF_FIT_ZERO_GRADS) &&
+      (!grad_basis || !grad_coeff_grid || !aligned(grad_basis, 16) || !aligned(grad_coeff_grid, 16)))
+    return set_error(FF_ERR_ARG, "grid gradient buffers must be non-NULL and 16-byte aligned");
+  const int64_t need = ff_field_fit_binned_workspace_bytes(f, n, m->out_dim);
+  if (need < 0) return set_error((int)need, "coefficient grid too large to bin by cell");
+  if (!workspace) return set_error(FF_ERR_ARG, "workspace is NULL");
+  if (workspace_bytes < need) return set_error(FF_ERR_SIZE, "workspace smaller than ff_field_fit_binned_workspace_bytes");
+  if (!aligned(workspace, 256)) return set_error(FF_ERR_ALIGN, "workspace must be 256-byte aligned");
+  return FF_OK;
+}
+
+static int validate_fit_on_bins(const FFField* f, const void* basis, const void* coeff, const FFMlp* m, int64_t n,
+                                int32_t loss_kind, float* grad_basis, float* grad_coeff_grid, int32_t flags,
+                                const void* workspace, int64_t workspace_bytes) {
+  int rc = validate_fused(f, basis, coeff, m, static_cast<const float*>(workspace), n);
+  if (rc) return rc;
+  if (loss_kind != FF_LOSS_L1 && loss_kind != FF_LOSS_MSE) return set_error(FF_ERR_ARG, "loss_kind must be L1 or MSE");
+  if (!grad_basis || !grad_coeff_grid || !aligned(grad_basis, 16) || !aligned(grad_coeff_grid, 16))
+    return set_error(FF_ERR_ARG, "grid gradient buffers must be non-NULL and 16-byte aligned");
+  if (flags & ~FF_FIT_MEAN_LOSS) return set_error(FF_ERR_ARG, "unknown flags");
+  const int64_t need = ff_field_fit_binned_workspace_bytes(f, n, m->out_dim);
+  if (need < 0) return set_error((int)need, "coefficient grid too large to bin by cell");
+  if (!workspace) return set_error(FF_ERR_ARG, "workspace is NULL");
+  if (workspace_bytes < need) return set_error(FF_ERR_SIZE, "workspace smaller than ff_field_fit_binned_workspace_bytes");
+  if (!aligned(workspace, 256)) return set_error(FF_ERR_ALIGN, "workspace must be 256-byte aligned");
+  return FF_OK;
+}
+
 int ff_field_fit_step_binned(const FFField* f, const void* basis, const void* coeff, const FFMlp* m, const float* x,
                              const float* target, int64_t n, int32_t loss_kind, float loss_scale, float* loss_sum,
                              float* grad_basis, float* grad_coeff_grid, const FFMlpGrad* g, int32_t flags,
                              void* workspace, int64_t workspace_bytes, void* stream) {
-  int rc = validate_fused(f, basis, coeff, m, x, n);
-  if (rc) return rc;
-  if (n > 0 && !target) return set_error(FF_ERR_ARG, "target is NULL");
-  if (loss_kind != FF_LOSS_L1 && loss_kind != FF_LOSS_MSE) return set_error(FF_ERR_ARG, "loss_kind must be L1 or MSE");
-  if (!grad_basis || !grad_coeff_grid || !aligned(grad_basis, 16) || !aligned(grad_coeff_grid, 16))
-    return set_error(FF_ERR_ARG, "grid gradient buffers must be non-NULL and 16-byte aligned");
-  const int64_t need = ff_field_fit_binned_workspace_bytes(f, n, m->out_dim);
-  if (need < 0) return set_error((int)need, "coefficient grid too large to bin by cell");
-  if (n > 0 && (!workspace || workspace_bytes < need))
-    return set_error(FF_ERR_SIZE, "workspace smaller than ff_field_fit_binned_workspace_bytes");
-  if (!aligned(workspace, 256)) return set_error(FF_ERR_ALIGN, "workspace must be 256-byte aligned");
   if (flags & ~(FF_FIT_ZERO_GRADS | FF_FIT_MEAN_LOSS)) return set_error(FF_ERR_ARG, "unknown flags");
-  if (!workspace) return set_error(FF_ERR_ARG, "workspace is NULL");
+  int rc = validate_fit_on_bins(f, basis, coeff, m, n, loss_kind, grad_basis, grad_coeff_grid,
+                                flags & FF_FIT_MEAN_LOSS, workspace, workspace_bytes);
+  if (rc) return rc;
+  rc = validate_fit_bin(f, m, x, target, n, grad_basis, grad_coeff_grid, flags & FF_FIT_ZERO_GRADS, workspace,
+                        workspace_bytes);
+  if (rc) return rc;
   FFMlpGrad none = {};
   return cuda_status(launch_fused_fit_binned(*f, basis, coeff, *m, x, target, n, loss_kind, loss_scale, loss_sum,
                                              grad_basis, grad_coeff_grid, g ? *g : none, workspace,
                                              (flags & FF_FIT_ZERO_GRADS) != 0,
                                              (flags & FF_FIT_MEAN_LOSS) ? loss_scale : 1.f, (cudaStream_t)stream),
                      "ff_field_fit_step_binned launch");
+}
+
+int ff_field_fit_bin(const FFField* f, const FFMlp* m, const float* x, const float* target, int64_t n,
+                     float* loss_sum, float* grad_basis, float* grad_coeff_grid, const FFMlpGrad* g, int32_t flags,
+                     void* workspace, int64_t workspace_bytes, void* stream) {
+  int rc = validate_field(f, nullptr, nullptr, /*need_grids=*/false);
+  if (rc) return rc;
+  rc = validate_fit_bin(f, m, x, target, n, grad_basis, grad_coeff_grid, flags, workspace, workspace_bytes);
+  if (rc) return rc;
+  FFMlpGrad none = {};
+  return cuda_status(launch_fit_bin_phase(*f, *m, x, target, n, loss_sum, grad_basis, grad_coeff_grid, g ? *g : none,
+                                          workspace, (flags & FF_FIT_ZERO_GRADS) != 0, (cudaStream_t)stream),
+                     "ff_field_fit_bin launch");
+}
+
+int ff_field_fit_step_on_bins(const FFField* f, const void* basis, const void* coeff, const FFMlp* m, int64_t n,
+                              int32_t loss_kind, float loss_scale, float* loss_sum, float* grad_basis,
+                              float* grad_coeff_grid, const FFMlpGrad* g, int32_t flags, const void* workspace,
+                              int64_t workspace_bytes, void* stream) {
+  int rc = validate_fit_on_bins(f, basis, coeff, m, n, loss_kind, grad_basis, grad_coeff_grid, flags, workspace,
+                                workspace_bytes);
+  if (rc) return rc;
+  FFMlpGrad none = {};
+  return cuda_status(launch_fit_on_bins(*f, basis, coeff, *m, n, loss_kind, loss_scale, loss_sum, grad_basis,
+                                        grad_coeff_grid, g ? *g : none, workspace,
+                                        (flags & FF_FIT_MEAN_LOSS) ? loss_scale : 1.f, (cudaStream_t)stream),
+                     "ff_field_fit_step_on_bins launch");
 }
 
 int ff_zero_f32(float* const* ptrs, const int64_t* counts, int32_t n_buffers, void* stream) {

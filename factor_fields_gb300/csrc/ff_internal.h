@@ -54,6 +54,13 @@ cudaError_t launch_fused_fit_binned(const FFField& f, const void* basis, const v
                                     const float* x, const float* target, int64_t n, int loss_kind, float loss_scale,
                                     float* loss_sum, float* grad_basis, float* grad_coeff, const FFMlpGrad& g,
                                     void* workspace, bool zero_grads, float loss_mul, cudaStream_t st);
+// its two halves: binning (with the gradient zeroing) and the fit kernel on the binned rows
+cudaError_t launch_fit_bin_phase(const FFField& f, const FFMlp& m, const float* x, const float* target, int64_t n,
+                                 float* loss_sum, float* grad_basis, float* grad_coeff, const FFMlpGrad& g,
+                                 void* workspace, bool zero_grads, cudaStream_t st);
+cudaError_t launch_fit_on_bins(const FFField& f, const void* basis, const void* coeff, const FFMlp& m, int64_t n,
+                               int loss_kind, float loss_scale, float* loss_sum, float* grad_basis, float* grad_coeff,
+                               const FFMlpGrad& g, const void* workspace, float loss_mul, cudaStream_t st);
 
 // fit_bin_kernels.cu
 int64_t fit_bin_keys(const FFField& f);
@@ -67,11 +74,12 @@ struct FitZero {
   int64_t other_n[4];
 };
 int64_t field_basis_elems(const FFField& f);  // elements of the flat basis buffer
-// Bins the batch (3 kernels: bin, alloc, permute); *rows_out: per binned point its coordinates
-// then its targets, *stride_out floats per row (coord_dim + out_dim rounded up to 4).
+// Bins the batch (3 kernels: bin, alloc, permute) into the workspace's rows: per binned point
+// its coordinates then its targets; fit_bin_rows locates them, *stride_out floats per row
+// (coord_dim + out_dim rounded up to 4).
 cudaError_t launch_fit_bin(const FFField& f, const float* x, const float* target, int out_dim, int64_t n,
-                           void* workspace, const FitZero* zero, const float** rows_out, int64_t* stride_out,
-                           cudaStream_t st);
+                           void* workspace, const FitZero* zero, cudaStream_t st);
+const float* fit_bin_rows(const FFField& f, int64_t n, int out_dim, const void* workspace, int64_t* stride_out);
 
 // util_kernels.cu
 constexpr int kMaxZeroBuffers = 8;  // buffers per zeroing launch (more: several launches)

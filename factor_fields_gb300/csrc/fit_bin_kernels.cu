@@ -139,9 +139,16 @@ int64_t fit_bin_workspace_bytes(const FFField& f, int64_t n, int out_dim) {
   return align_up(keys * 4 + 16) + align_up(n * 8) + align_up(keys * 8) + align_up(n * row_stride(f, out_dim) * 4);
 }
 
+// Workspace layout: count[keys] + cursor | key_rank[n] | start[keys] | rows[n][stride].
+const float* fit_bin_rows(const FFField& f, int64_t n, int out_dim, const void* workspace, int64_t* stride_out) {
+  const int64_t keys = fit_bin_keys(f);
+  *stride_out = row_stride(f, out_dim);
+  return reinterpret_cast<const float*>(static_cast<const unsigned char*>(workspace) + align_up(keys * 4 + 16) +
+                                        align_up(n * 8) + align_up(keys * 8));
+}
+
 cudaError_t launch_fit_bin(const FFField& f, const float* x, const float* target, int out_dim, int64_t n,
-                           void* workspace, const FitZero* zero, const float** rows_out, int64_t* stride_out,
-                           cudaStream_t st) {
+                           void* workspace, const FitZero* zero, cudaStream_t st) {
   const int64_t keys = fit_bin_keys(f);
   const int stride = row_stride(f, out_dim);
   unsigned char* w = static_cast<unsigned char*>(workspace);
@@ -151,8 +158,6 @@ cudaError_t launch_fit_bin(const FFField& f, const float* x, const float* target
   int2* key_rank = reinterpret_cast<int2*>(w); w += align_up(n * 8);
   int64_t* start = reinterpret_cast<int64_t*>(w); w += align_up(keys * 8);
   float* rows = reinterpret_cast<float*>(w);
-  *rows_out = rows;
-  *stride_out = stride;
   cudaError_t e = cudaMemsetAsync(count, 0, ((keys * 4 + 7) & ~int64_t(7)) + 8, st);
   if (e != cudaSuccess) return e;
   ZeroSet zs = {};

@@ -1,13 +1,13 @@
 // Fused field + MLP head: the fit step on a batch binned by coefficient cell
-// (ff_field_fit_step_binned): binning (fit_bin_kernels.cu), then the kFitBinned kernel.
+// (ff_field_fit_step_binned = ff_field_fit_bin + ff_field_fit_step_on_bins): binning with the
+// gradient zeroing (fit_bin_kernels.cu), then the kFitBinned kernel on the binned rows.
 #include "fused_impl.cuh"
 
 namespace ffgb {
 
-cudaError_t launch_fused_fit_binned(const FFField& f, const void* basis, const void* coeff, const FFMlp& m,
-                                    const float* x, const float* target, int64_t n, int loss_kind, float loss_scale,
-                                    float* loss_sum, float* grad_basis, float* grad_coeff, const FFMlpGrad& g,
-                                    void* workspace, bool zero_grads, float loss_mul, cudaStream_t st) {
+cudaError_t launch_fit_bin_phase(const FFField& f, const FFMlp& m, const float* x, const float* target, int64_t n,
+                                 float* loss_sum, float* grad_basis, float* grad_coeff, const FFMlpGrad& g,
+                                 void* workspace, bool zero_grads, cudaStream_t st) {
   FitZero z = {};
   if (zero_grads) {
     z.grad_basis = grad_basis;
@@ -21,16 +21,16 @@ cudaError_t launch_fused_fit_binned(const FFField& f, const void* basis, const v
     z.other[3] = loss_sum;
     z.other_n[3] = 1;
   }
-  if (n == 0) {  // nothing to bin or fit; the zeroing still happens
-    if (!zero_grads) return cudaSuccess;
-    const float* rows = nullptr;
-    int64_t stride = 0;
-    return launch_fit_bin(f, x, target, m.out_dim, 0, workspace, &z, &rows, &stride, st);
-  }
-  const float* rows = nullptr;
+  if (n == 0 && !zero_grads) return cudaSuccess;  // nothing to bin; with n == 0 the zeroing still happens
+  return launch_fit_bin(f, x, target, m.out_dim, n, workspace, zero_grads ? &z : nullptr, st);
+}
+
+cudaError_t launch_fit_on_bins(const FFField& f, const void* basis, const void* coeff, const FFMlp& m, int64_t n,
+                               int loss_kind, float loss_scale, float* loss_sum, float* grad_basis, float* grad_coeff,
+                               const FFMlpGrad& g, const void* workspace, float loss_mul, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
   int64_t stride = 0;
-  cudaError_t e = launch_fit_bin(f, x, target, m.out_dim, n, workspace, zero_grads ? &z : nullptr, &rows, &stride, st);
-  if (e != cudaSuccess) return e;
+  const float* rows = fit_bin_rows(f, n, m.out_dim, workspace, &stride);
   if (f.param_dtype != FF_BF16)  // float32 grids: the per-point fit on the binned rows
     return launch_fused_fit_rows(f, basis, coeff, m, rows, stride, rows + f.coord_dim, stride, n, loss_kind,
                                  loss_scale, loss_sum, grad_basis, grad_coeff, g, loss_mul, st);
@@ -49,6 +49,17 @@ cudaError_t launch_fused_fit_binned(const FFField& f, const void* basis, const v
   a.grad_b0 = g.bias[0];
   a.grad_w1 = g.weight[1];
   return dispatch_bf16<kFitBinned>(a, st);
+}
+
+cudaError_t launch_fused_fit_binned(const FFField& f, const void* basis, const void* coeff, const FFMlp& m,
+                                    const float* x, const float* target, int64_t n, int loss_kind, float loss_scale,
+                                    float* loss_sum, float* grad_basis, float* grad_coeff, const FFMlpGrad& g,
+                                    void* workspace, bool zero_grads, float loss_mul, cudaStream_t st) {
+  cudaError_t e = launch_fit_bin_phase(f, m, x, target, n, loss_sum, grad_basis, grad_coeff, g, workspace, zero_grads,
+                                       st);
+  if (e != cudaSuccess) return e;
+  return launch_fit_on_bins(f, basis, coeff, m, n, loss_kind, loss_scale, loss_sum, grad_basis, grad_coeff, g,
+                            workspace, loss_mul, st);
 }
 
 }  // namespace ffgb

@@ -142,15 +142,18 @@ class FieldFitRunner:
         if fused and self.binned:
             self.path_name = ("fused, binned: one ff_field_fit_step_binned call per step (bin by coefficient cell "
                               "with the gradient zeroing, allocate cell ranges, permute, fit)")
-            self.dominant_kernel = "ff_field_fit_step_binned"
+            self.dominant_kernel = "fused_field_mlp_kernel<3,3,3,1,bf16> (binned fit)"
+            self.dominant_call = "ff_field_fit_step_binned"
             self.gathers_per_point = 1
         elif fused:
             self.path_name = "fused: one ff_field_fit_step launch per step (+ gradient zeroing)"
-            self.dominant_kernel = "ff_field_fit_step"
+            self.dominant_kernel = "fused_field_mlp_kernel<2,3,3,1,bf16> (fit)"
+            self.dominant_call = "ff_field_fit_step"
             self.gathers_per_point = 1
         else:
             self.path_name = "explicit drop-in kernels (field fwd, MLP fwd, MLP bwd, field bwd)"
             self.dominant_kernel = "ff_field_backward"
+            self.dominant_call = "ff_field_backward"
             self.gathers_per_point = 2
         for p in self._params():
             if p.grad is None:
@@ -280,31 +283,43 @@ class FieldFitRunner:
         mlp = FN.mlp_struct(ws, bs, m.linear_mat.in_dim, m.linear_mat.hidden_dim, m.linear_mat.out_dim)
         st = N.stream_ptr()
         g = self._grad_struct()
-        ev = None
-        if kernel_events:
-            ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+        # kernel_events: CUDA events around the dominant kernel alone ("kernel": the fit kernel,
+        # the binned call issued as its two halves; the drop-in path's field backward) and
+        # around the whole call ("call"); kernel_events="call": one combined call, its events only
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)] if kernel_events else None
+        split = bool(kernel_events) and kernel_events != "call"
         if self.fused:
             if self.binned:
                 ws = self._workspace(desc, n)
             if ev:
                 ev[0].record()
             lbuf = self.loss_buf if _loss_buf is None else _loss_buf
-            common = (ctypes.byref(desc), N.ptr(basis_r), N.ptr(coeff_r), ctypes.byref(mlp), N.ptr(x), N.ptr(y), n,
-                      N.FF_LOSS[self.loss], 1.0 / max(n * m.linear_mat.out_dim, 1), N.ptr(lbuf),
-                      N.ptr(m.basis_flat.grad), N.ptr(m.coeff_flat.grad), ctypes.byref(g))
-            if self.binned:  # kernels: bin (+ gradient and loss zeroing), alloc, permute, fit (mean loss)
-                N.call("ff_field_fit_step_binned", *common, N.FF_FIT_ZERO_GRADS | N.FF_FIT_MEAN_LOSS, N.ptr(ws),
-                       ws.numel(), st, kernels=4)
-            else:
-                N.call("ff_field_fit_step", *common, st)
-            if ev:
+            scale = 1.0 / max(n * m.linear_mat.out_dim, 1)
+            gb, gc = N.ptr(m.basis_flat.grad), N.ptr(m.coeff_flat.grad)
+            if self.binned and split:  # the same launches as one ff_field_fit_step_binned call, in two calls
+                N.call("ff_field_fit_bin", ctypes.byref(desc), ctypes.byref(mlp), N.ptr(x), N.ptr(y), n, N.ptr(lbuf),
+                       gb, gc, ctypes.byref(g), N.FF_FIT_ZERO_GRADS, N.ptr(ws), ws.numel(), st)
                 ev[1].record()
+                N.call("ff_field_fit_step_on_bins", ctypes.byref(desc), N.ptr(basis_r), N.ptr(coeff_r),
+                       ctypes.byref(mlp), n, N.FF_LOSS[self.loss], scale, N.ptr(lbuf), gb, gc, ctypes.byref(g),
+                       N.FF_FIT_MEAN_LOSS, N.ptr(ws), ws.numel(), st)
+            else:
+                if ev:
+                    ev[1].record()
+                common = (ctypes.byref(desc), N.ptr(basis_r), N.ptr(coeff_r), ctypes.byref(mlp), N.ptr(x), N.ptr(y),
+                          n, N.FF_LOSS[self.loss], scale, N.ptr(lbuf), gb, gc, ctypes.byref(g))
+                if self.binned:  # kernels: bin (+ gradient and loss zeroing), alloc, permute, fit (mean loss)
+                    N.call("ff_field_fit_step_binned", *common, N.FF_FIT_ZERO_GRADS | N.FF_FIT_MEAN_LOSS,
+                           N.ptr(ws), ws.numel(), st, kernels=4)
+                else:
+                    N.call("ff_field_fit_step", *common, st)
+            if ev:
+                ev[2].record()
+                return {"call": (ev[0], ev[2]), "kernel": (ev[1], ev[2]) if split else None}
             if self.binned:
                 # the kernel accumulated the mean; a captured step returns its own buffer
-                loss = lbuf[0] if _loss_buf is not None else lbuf[0].clone()
-            else:
-                loss = lbuf[0] / max(n * m.linear_mat.out_dim, 1)
-            return ev if kernel_events else loss
+                return lbuf[0] if _loss_buf is not None else lbuf[0].clone()
+            return lbuf[0] / max(n * m.linear_mat.out_dim, 1)
         feats = torch.empty(n, m.n_feat, device=x.device)
         N.call("ff_field_forward", ctypes.byref(desc), N.ptr(basis_r), N.ptr(coeff_r), N.ptr(x), n, N.ptr(feats),
                None, None, st)
@@ -325,5 +340,5 @@ class FieldFitRunner:
                None, None, N.ptr(m.basis_flat.grad), N.ptr(m.coeff_flat.grad), st)
         if ev:
             ev[1].record()
-            return ev
+            return {"call": (ev[0], ev[1]), "kernel": (ev[0], ev[1])}
         return loss

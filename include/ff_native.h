@@ -189,6 +189,21 @@ FF_API int ff_field_fit_step_binned(const FFField* f, const void* basis, const v
                                     const FFMlpGrad* g, int32_t flags, void* workspace, int64_t workspace_bytes,
                                     void* stream);
 
+/* The two halves of ff_field_fit_step_binned, one call each (the same launches in the same
+ * order), for callers that time the fit kernel apart from the binning or bin a batch once for
+ * several steps. ff_field_fit_bin: bins (x, target) into the workspace; flags: FF_FIT_ZERO_GRADS
+ * (grad_basis, grad_coeff_grid, g and loss_sum are touched only by that zeroing; the grids' values
+ * are not read, so f alone describes them). ff_field_fit_step_on_bins: the fit on the rows that the
+ * last ff_field_fit_bin call on this workspace wrote for the same f, n and m->out_dim, in stream
+ * order; flags: FF_FIT_MEAN_LOSS. */
+FF_API int ff_field_fit_bin(const FFField* f, const FFMlp* m, const float* x, const float* target, int64_t n,
+                            float* loss_sum, float* grad_basis, float* grad_coeff_grid, const FFMlpGrad* g,
+                            int32_t flags, void* workspace, int64_t workspace_bytes, void* stream);
+FF_API int ff_field_fit_step_on_bins(const FFField* f, const void* basis, const void* coeff, const FFMlp* m,
+                                     int64_t n, int32_t loss_kind, float loss_scale, float* loss_sum,
+                                     float* grad_basis, float* grad_coeff_grid, const FFMlpGrad* g, int32_t flags,
+                                     const void* workspace, int64_t workspace_bytes, void* stream);
+
 /* Zero n_buffers float32 device buffers (ptrs[b], counts[b] elements; the two arrays are host
  * memory, read during the call) in one launch per 8 buffers: a training step's gradient
  * zeroing (optimizer.zero_grad) and loss accumulator reset without one fill per tensor. */

@@ -84,3 +84,34 @@ def test_argument_validation_before_any_launch(lib):
     for k in range(3):
         r.aabb_min[k], r.aabb_max[k] = -1.0, 1.0
     assert lib.ff_filter_rays(ctypes.byref(r), vp(16), 4, 16, 0, vp(16), None) == N.FF_ERR_ARG
+
+
+def test_binned_fit_halves_validate_their_flags(lib):
+    """ff_field_fit_bin takes FF_FIT_ZERO_GRADS only, ff_field_fit_step_on_bins FF_FIT_MEAN_LOSS
+    only; both reject a missing or short workspace (all before any launch)."""
+    from factor_fields_gb300 import FactorFields
+    from factor_fields_gb300 import functional as FN
+    from factor_fields_gb300 import workloads as W
+    from factor_fields_gb300 import _native as N
+    m = FactorFields(W.field_cfg("cfg1"), device="cpu", precision="bf16")
+    desc = m.descriptor(N.FF_BF16)
+    ws_, bs_ = m.linear_mat.weights()
+    mlp = FN.mlp_struct(ws_, bs_, m.linear_mat.in_dim, m.linear_mat.hidden_dim, m.linear_mat.out_dim)
+    g = N.FFMlpGrad()
+    vp = ctypes.c_void_p
+    n = 1024
+    need = lib.ff_field_fit_binned_workspace_bytes(ctypes.byref(desc), n, 1)
+    assert need > 0
+    ws = vp(256)
+    args_bin = (ctypes.byref(desc), ctypes.byref(mlp), vp(16), vp(16), n, vp(16), vp(16), vp(16), ctypes.byref(g))
+    assert lib.ff_field_fit_bin(*args_bin, N.FF_FIT_MEAN_LOSS, ws, need, None) == N.FF_ERR_ARG
+    assert lib.ff_field_fit_bin(*args_bin, N.FF_FIT_ZERO_GRADS, None, need, None) == N.FF_ERR_ARG
+    assert lib.ff_field_fit_bin(*args_bin, N.FF_FIT_ZERO_GRADS, ws, need - 1, None) == N.FF_ERR_SIZE
+    args_fit = (ctypes.byref(desc), vp(16), vp(16), ctypes.byref(mlp), n, N.FF_LOSS["l1"], 1.0 / n, vp(16), vp(16),
+                vp(16), ctypes.byref(g))
+    assert lib.ff_field_fit_step_on_bins(*args_fit, N.FF_FIT_ZERO_GRADS, ws, need, None) == N.FF_ERR_ARG
+    assert lib.ff_field_fit_step_on_bins(*args_fit, N.FF_FIT_MEAN_LOSS, ws, need - 1, None) == N.FF_ERR_SIZE
+    assert lib.ff_field_fit_step_on_bins(*args_fit, N.FF_FIT_MEAN_LOSS, vp(128), need, None) == N.FF_ERR_ALIGN
+    assert lib.ff_field_fit_step_binned(ctypes.byref(desc), vp(16), vp(16), ctypes.byref(mlp), vp(16), vp(16), n,
+                                        N.FF_LOSS["l1"], 1.0 / n, vp(16), vp(16), vp(16), ctypes.byref(g), 4, ws, need,
+                                        None) == N.FF_ERR_ARG

@@ -252,3 +252,25 @@ def test_binned_fit_empty_batch():
     for p in r._params():
         assert float(p.grad.abs().sum()) == 0.0
     assert float(loss) == 0.0
+
+
+def test_binned_fit_in_two_calls_matches_one_call():
+    """ff_field_fit_bin + ff_field_fit_step_on_bins (the split the bench times the fit kernel
+    through) give the combined call's mean loss and gradients."""
+    from factor_fields_gb300 import FactorFields
+    from factor_fields_gb300 import workloads as W
+    from factor_fields_gb300.train import FieldFitRunner
+    torch.manual_seed(0)
+    m = FactorFields(W.field_cfg("cfg1"), device="cuda", precision="bf16")
+    r = FieldFitRunner(m, loss="l1")
+    xs, ys = W.sdf_batch(3, 8192)
+    x, y = torch.from_numpy(xs).cuda(), torch.from_numpy(ys).cuda()
+    l_one = float(r.step(x, y))
+    g_one = [p.grad.clone() for p in r._params()]
+    ev = r.step(x, y, kernel_events=True)
+    torch.cuda.synchronize()
+    assert ev["kernel"][0].elapsed_time(ev["kernel"][1]) > 0
+    assert ev["call"][0].elapsed_time(ev["call"][1]) >= ev["kernel"][0].elapsed_time(ev["kernel"][1])
+    assert abs(float(r.loss_buf[0]) - l_one) <= 1e-6 * max(1.0, abs(l_one))
+    for a, b in zip(g_one, r._params()):
+        assert torch.allclose(a, b.grad, rtol=1e-5, atol=1e-9)
