@@ -367,17 +367,35 @@ __device__ __forceinline__ void gather_inside(const T* __restrict__ grid, int st
 }
 
 // Zero-weight corners (nearest's unused slots, the weight-0 corner at the grid's far edge) are
-// skipped: they would add zeros.
+// skipped: they would add zeros. Two channels per corner, packed (stride 2, 16-byte-aligned
+// level): the x-adjacent corners k, k + 1 of a lookup are neighbouring 8-byte entries, and when
+// the low one has an even index they share one 16-byte chunk: one float4 atomic covers both.
 template <int V, int D>
 __device__ __forceinline__ void scatter_inside(float* __restrict__ grad, int stride, const Corners<D>& cn,
                                                const float* g) {
+  if constexpr (V == 2) {
+    const bool packed = stride == 2 && (reinterpret_cast<uintptr_t>(grad) & 15) == 0;
 #pragma unroll
-  for (int k = 0; k < Corners<D>::K; ++k) {
-    if (cn.w[k] != 0.f) {
-      float t[V];
+    for (int k = 0; k < Corners<D>::K; k += 2) {
+      const int i0 = cn.idx[k];
+      const float w0 = cn.w[k], w1 = cn.w[k + 1];
+      if (packed && (i0 & 1) == 0 && cn.idx[k + 1] == i0 + 1) {
+        atomicAdd(reinterpret_cast<float4*>(grad + i0 * 2), make_float4(g[0] * w0, g[1] * w0, g[0] * w1, g[1] * w1));
+      } else {
+        if (w0 != 0.f) atomicAdd(reinterpret_cast<float2*>(grad + i0 * stride), make_float2(g[0] * w0, g[1] * w0));
+        if (w1 != 0.f)
+          atomicAdd(reinterpret_cast<float2*>(grad + cn.idx[k + 1] * stride), make_float2(g[0] * w1, g[1] * w1));
+      }
+    }
+  } else {
 #pragma unroll
-      for (int v = 0; v < V; ++v) t[v] = g[v] * cn.w[k];
-      atomic_add_vec<V>(grad + cn.idx[k] * stride, t);
+    for (int k = 0; k < Corners<D>::K; ++k) {
+      if (cn.w[k] != 0.f) {
+        float t[V];
+#pragma unroll
+        for (int v = 0; v < V; ++v) t[v] = g[v] * cn.w[k];
+        atomic_add_vec<V>(grad + cn.idx[k] * stride, t);
+      }
     }
   }
 }
