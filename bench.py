@@ -153,7 +153,7 @@ def run_native(args, ws, rank, local):
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MB > L2
 
     res = {}
-    # ---- fast path: fused BF16 (falls back to the float32 drop-in step only if absent) ----
+    # ---- fast path: the fused BF16 fit step (binned), replayed from CUDA graphs ----
     m = make_model("bf16")
     runner = T.FieldFitRunner(m, loss="l1")
     stream = torch.cuda.current_stream()
