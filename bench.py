@@ -299,7 +299,7 @@ def run_radiance(args, dev):
     (plain sampler: 4,096 rays x up to 1,024 samples with 128^3 occupancy-bitfield pruning;
     proposal sampler: 8,192 rays x 48 stratified training samples + the proposal network's
     training), and PSNR / depth error against the FP64 quadrature ground truth after equal
-    training (iters x 4,096 rays, Adam; the proposal configuration renders with 96 samples
+    training (iters x 4,096 rays, Adam; the proposal configuration renders with 48 samples
     drawn from the network). The PSNR comparison is repeated on seeds 1 and 2 (training alone)
     because single runs differ by up to ~0.5 dB, more for an unlucky seed."""
     from factor_fields_gb300 import workloads as W
@@ -364,7 +364,8 @@ def run_radiance(args, dev):
                "psnr_db": psnr, "depth_mae": depth_err, "train_steps": iters, "train_rays_per_step": 4096,
                "train_step_ms_with_adam": tms, "train_rays_per_s_with_adam": 4096 / (tms / 1e3),
                "eval_400x400": {"ms_per_image": e_extra["ms_per_image"][0], "psnr_db": e_psnr[0],
-                                "ssim": e_extra["ssim"][0]}}
+                                "ssim": e_extra["ssim"][0],
+                                "rays_per_s": 400 * 400 / (e_extra["ms_per_image"][0] / 1e3)}}
         if sampler is None:
             offs, _, _ = march(m, test, None, render_desc(m, 1024, True))
             rec["live_samples_per_ray"] = float(offs[-1]) / test.shape[0]
@@ -373,6 +374,10 @@ def run_radiance(args, dev):
             rec["samples_per_ray"] = sampler.n_fine
         out[kind] = rec
     out["proposal_rays_per_s_vs_plain"] = out["cfg3_proposal"]["rays_per_s"] / out["cfg2_plain"]["rays_per_s"]
+    # rendering alone (the evaluation renderer, no backward): 48 proposal samples per ray
+    # against the plain sampler's ~125 live samples after occupancy pruning
+    out["proposal_eval_rays_per_s_vs_plain"] = (out["cfg3_proposal"]["eval_400x400"]["rays_per_s"] /
+                                                out["cfg2_plain"]["eval_400x400"]["rays_per_s"])
     seeds = {0: {k: out[k]["psnr_db"] for k in ("cfg2_plain", "cfg3_proposal")}}
     if args.psnr_seeds > 1:
         for seed in range(1, args.psnr_seeds):

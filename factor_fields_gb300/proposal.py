@@ -11,7 +11,8 @@ Training and rendering sample differently (train_uniform=True, the default): a t
 evaluates the field at n_fine stratified samples over the ray's segment, each jittered
 independently inside its stratum (sample_jitter=True), and the network learns from those
 samples' compositing weights, which are unbiased estimates of where the field's weight is;
-rendering (is_train=False) draws render_fine (96) samples from the network's histogram.
+rendering (is_train=False) draws render_fine samples from the network's histogram (by default
+n_fine = 48, the resampled count of the configuration; 96 gain 0.1-0.4 dB for 1.6x the time).
 Jittering all samples of a ray by one offset instead (like the reference's uniform sampler)
 trains the field on a lattice along each ray: 0.9-1.3 dB lower PSNR on the blob scene. Training the field on the network's own concentrated samples (train_uniform=False)
 constrains it only on a thin shell around where the network already expects density: on the
@@ -111,7 +112,7 @@ class ProposalRenderFunction(torch.autograd.Function):
 class ProposalSampler:
     def __init__(self, model, reso=64, n_bins=64, n_fine=48, hidden=64, lr_grid=2e-2, lr_mlp=1e-3,
                  density_shift=-4.0, precision="bf16", learned=True, seed=0, uniform_mix=0.0, fused_adam=True,
-                 train_uniform=True, render_fine=96, sample_jitter=True):
+                 train_uniform=True, render_fine=None, sample_jitter=True):
         self.m, self.learned, self.train_uniform = model, learned, train_uniform
         self.render_fine = render_fine or n_fine  # samples per ray when rendering (not training)
         self.sample_jitter = sample_jitter  # training: jitter each sample in its stratum (else per ray)

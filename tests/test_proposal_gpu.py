@@ -190,9 +190,9 @@ def test_proposal_matches_plain_sampler_with_far_fewer_samples():
     """What the trained proposal network gains over the method without it (the reference's
     plain uniform sampler, up to 1024 samples per ray with occupancy pruning): after the same
     training (1500 steps of 4096 rays; the field sees 48 stratified samples per ray in the
-    proposal configuration against ~125 live samples in the plain one), rendering with 96
+    proposal configuration against ~125 live samples in the plain one), rendering with 48
     proposal samples per ray is at least as accurate against the FP64 ground truth (within
-    0.1 dB; measured about +1 dB). Runs of this comparison differ by up to ~0.5 dB from the
+    0.1 dB; measured +0.3 / +1.2 dB). Runs of this comparison differ by up to ~0.5 dB from the
     seed alone, so it is made on two seeds and a 10-view test set (their mean)."""
     from factor_fields_gb300 import FactorFields
     from factor_fields_gb300 import workloads as W
