@@ -193,7 +193,10 @@ __device__ __forceinline__ void linear_corners_inside(const float* ix_in, const 
   }
 }
 
-// Nearest corner (nearbyint = round half to even), stored in slot 0 with weight 1.
+// Nearest corner (nearbyint = round half to even), stored in slot 0 with weight 1. Outside the
+// grid (zero padding; also a NaN coordinate) slot 0 keeps an in-range index, clamped, with weight
+// 0, so that gathers which read slot 0 unconditionally stay inside the buffer; the checked
+// gather / scatter skip it by its zero weight.
 template <int D>
 __device__ __forceinline__ void nearest_corner(const float* ix, const int* size, Corners<D>& c) {
   int flat = 0;
@@ -202,9 +205,10 @@ __device__ __forceinline__ void nearest_corner(const float* ix, const int* size,
   for (int k = D - 1; k >= 0; --k) {
     const float r = rintf(ix[k]);
     ok = ok && (r >= 0.f) && (r < (float)size[k]);
-    flat = flat * size[k] + (int)r;
+    const int ri = min(max((int)fminf(fmaxf(r, 0.f), (float)(size[k] - 1)), 0), size[k] - 1);
+    flat = flat * size[k] + ri;
   }
-  c.idx[0] = ok ? flat : -1;
+  c.idx[0] = flat;
   c.w[0] = ok ? 1.f : 0.f;
 #pragma unroll
   for (int b = 1; b < (1 << D); ++b) {
