@@ -1,6 +1,7 @@
 """Field-fit training steps (the notebooks' regression loop, scripts/2D_regression.ipynb cell 4,
 scripts/sdf_regression.ipynb cell 2) without autograd: explicit native launches per step."""
 import ctypes
+from collections import OrderedDict
 
 import torch
 
@@ -198,7 +199,6 @@ class FieldFitRunner:
         copied into static buffers whose graph then replays. Graphs are re-captured when the batch
         shape, a parameter buffer or the binning workspace changes. The returned 0-d loss belongs
         to the replayed graph: the next replay of the same graph overwrites it."""
-        from collections import OrderedDict
         key, in_place = self._graph_key(x, y)
         graphs = self.__dict__.setdefault("_graphs", OrderedDict())
         ent = graphs.get(key)
@@ -223,7 +223,6 @@ class FieldFitRunner:
     def capture_graphs(self, batches):
         """Capture (without replaying) the graphs graph_step will use for these (x, y) batches,
         e.g. a ring of batches resident in HBM, so that no step pays for a capture."""
-        from collections import OrderedDict
         graphs = self.__dict__.setdefault("_graphs", OrderedDict())
         if len(batches) > self._GRAPHS_KEPT:
             raise ValueError(f"at most {self._GRAPHS_KEPT} batches keep their graphs")
