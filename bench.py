@@ -10,7 +10,7 @@ the batch and D2H of the loss inside the timed region). L2 is flushed (256 MB wr
 every timed step and each step is timed alone with CUDA events.
 
 --impl reference times the reference's own CPU PyTorch op sequence (oracle/ref_torch.py) on
-the host cores, on a bounded sample of the same workload. Under torchrun each rank runs an
+all host cores, on the same workload (262,144-point batches, K steps after W warm-up steps). Under torchrun each rank runs an
 independent replica on its own GPU (the path shards by points: no collective on the data
 path); `value` is the sum over ranks of points / max-over-ranks time.
 """
@@ -31,6 +31,13 @@ sys.path.insert(0, ROOT)
 WORKLOAD = "cfg1: 3-D SDF fit, 6-level grid basis [4,4,4,2,2,2] @ [32..128]^3, coeff 18x32^3, 2x64 ReLU head, L1"
 N_POINTS = 262144
 METRIC = "fwd+bwd field samples/s"
+
+
+def bench_config(ws):
+    """The workload both arms run (native and --impl reference): one dict, so the two JSON lines
+    carry the same config."""
+    return {"workload": WORKLOAD, "points_per_step": N_POINTS, "loss": "l1",
+            "l2": "flushed (256 MB write) before every timed step (native arm)", "parallelism": f"replicas x{ws}"}
 
 
 def dist_env():
@@ -253,8 +260,7 @@ def run_native(args, ws, rank, local):
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "bf16 storage, fp32 accumulation" if m.precision == "bf16" else "fp32",
         "data": "synthetic (seeded analytic SDF: 16 spheres + 8 boxes)",
-        "config": {"workload": WORKLOAD, "points_per_step": n, "loss": "l1", "path": runner.path_name,
-                   "l2": "flushed (256 MB write) before every timed step", "parallelism": f"replicas x{ws}"},
+        "config": bench_config(ws), "path": runner.path_name,
         "e2e": {"value": pts / (ms_e2e / 1e3), "unit": "samples/s", "h2d_bytes_per_step": n * 16,
                 "d2h_bytes_per_step": 4},
         "fp32_dropin": {"value": pts / (ms_drop / 1e3), "unit": "samples/s",
@@ -391,8 +397,9 @@ def run_radiance(args, dev):
     return out
 
 
-def run_cpu_baseline(n_points, steps, warmup=1):
-    """The reference's CPU op sequence on a bounded sample of the workload: samples/s."""
+def _cpu_reference_field():
+    """The reference's CPU op sequence (oracle/ref_torch.py) holding configuration 1's initial
+    state (DCT basis, seeded random coefficients, a seeded MLP head) and all host threads."""
     from factor_fields_gb300 import workloads as W
     from oracle.ref_torch import RefField
     from factor_fields_gb300.config import FieldGeometry
@@ -409,6 +416,18 @@ def run_cpu_baseline(n_points, steps, warmup=1):
     l0, l1 = torch.nn.Linear(18, 64), torch.nn.Linear(64, 1, bias=False)
     r = RefField("reconstruction", cfg.dataset.aabb, levels, coeff, [l0.weight.detach(), l1.weight.detach()],
                  [l0.bias.detach(), None], g.freq_bands, "sawtooth")
+    return r, cores
+
+
+CPU_KIND = "port"
+CPU_DESC = ("torch CPU restatement of the reference's grid_sample/MLPMixer op sequence (oracle/ref_torch.py, "
+            "pinned to outputs of the reference itself)")
+
+
+def run_cpu_baseline(n_points, steps, warmup=1):
+    """The reference's CPU op sequence on a bounded sample of the workload: samples/s (best step)."""
+    from factor_fields_gb300 import workloads as W
+    r, cores = _cpu_reference_field()
     x, y = W.sdf_batch(7, n_points)
     x, y = torch.from_numpy(x), torch.from_numpy(y)
     for _ in range(warmup):
@@ -419,10 +438,35 @@ def run_cpu_baseline(n_points, steps, warmup=1):
         r.fit_step(x, y)
         best.append(time.perf_counter() - t0)
     t = min(best)
-    return {"value": n_points / t, "unit": "samples/s", "cores": cores, "kind": "port",
+    return {"value": n_points / t, "unit": "samples/s", "cores": cores, "kind": CPU_KIND,
             "sample": f"{n_points} points of the same workload per step, best of {steps} after {warmup} warm-up "
-                      "(torch CPU restatement of the reference's grid_sample/MLPMixer op sequence, "
-                      "oracle/ref_torch.py)"}
+                      f"({CPU_DESC})"}
+
+
+def run_reference_arm(args, ws):
+    """--impl reference: the reference's CPU op sequence on the native arm's workload (the same
+    262,144-point batches of configuration 1, one batch per step), W warm-up steps then K timed
+    steps on all host cores; value = points of the K steps / their total time."""
+    from factor_fields_gb300 import workloads as W
+    r, cores = _cpu_reference_field()
+    nb = 8
+    batches = [tuple(torch.from_numpy(a) for a in W.sdf_batch(i, N_POINTS)) for i in range(nb)]
+    for i in range(args.warmup):
+        r.fit_step(*batches[i % nb])
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        r.fit_step(*batches[i % nb])
+    dt = time.perf_counter() - t0
+    value = N_POINTS * args.steps / dt
+    return {"metric": METRIC, "value": value, "unit": "samples/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
+            "data": "synthetic (seeded analytic SDF: 16 spheres + 8 boxes)", "config": bench_config(ws),
+            "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": "samples/s", "cores": cores, "kind": CPU_KIND,
+                             "sample": f"the whole workload: {args.steps} steps of {N_POINTS} points after "
+                                       f"{args.warmup} warm-up steps ({CPU_DESC})"},
+            "e2e": {"value": value, "unit": "samples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
 def main():
@@ -431,7 +475,8 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="native", choices=["native", "reference"])
-    ap.add_argument("--cpu-points", type=int, default=32768)
+    ap.add_argument("--cpu-points", type=int, default=N_POINTS,
+                    help="points per step of the cpu_baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-render", action="store_true", help="skip the radiance-field configurations")
     ap.add_argument("--render-iters", type=int, default=1500)
@@ -441,14 +486,7 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return 0
-        cb = run_cpu_baseline(args.cpu_points, max(args.steps // 5, 3), warmup=min(args.warmup, 1))
-        line = {"metric": METRIC, "value": cb["value"], "unit": "samples/s", "n_gpus": ws, "steps": args.steps,
-                "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-                "dtype": "fp32", "data": "synthetic (seeded analytic SDF: 16 spheres + 8 boxes)",
-                "config": {"workload": WORKLOAD, "points_per_step": args.cpu_points}, "impl": "reference",
-                "cpu_baseline": cb, "e2e": {"value": cb["value"], "unit": "samples/s", "h2d_bytes_per_step": 0,
-                                            "d2h_bytes_per_step": 0}}
-        print(json.dumps(line))
+        print(json.dumps(run_reference_arm(args, ws)))
         return 0
     if ws > 1:
         torch.distributed.init_process_group("nccl", device_id=torch.device("cuda", local))

@@ -1,5 +1,6 @@
 // extern "C" entry points of libffgb.so (declared in include/ff_native.h): argument
 // validation, error reporting and dispatch to the kernel launchers.
+#include <atomic>
 #include <cstdio>
 #include <string>
 
@@ -17,16 +18,18 @@ int set_error(int code, const std::string& msg) {
   return code;
 }
 
+// SM count per device ordinal, looked up on first use. The cache entries are atomics: two
+// threads that race on the first lookup both store the same value.
 int sm_count() {
-  static int cached[64] = {0};
+  static std::atomic<int> cached[64];
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 148;
-  if (cached[dev] == 0) {
-    int v = 0;
+  int v = cached[dev].load(std::memory_order_relaxed);
+  if (v == 0) {
     if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0) v = 148;
-    cached[dev] = v;
+    cached[dev].store(v, std::memory_order_relaxed);
   }
-  return cached[dev];
+  return v;
 }
 
 static int cuda_status(cudaError_t e, const char* what) {

@@ -27,6 +27,7 @@
 // MLP: in 18 -> 64 (bias, ReLU) -> out <= 32 (no bias): MLPMixer with num_layers = 2.
 #pragma once
 
+#include <atomic>
 #include <type_traits>
 #include <utility>
 
@@ -649,12 +650,13 @@ template <int MODE, int BD, int CD, int OUTT, typename T>
 cudaError_t launch_one(const FusedArgs& a, cudaStream_t st) {
   constexpr int64_t smem = smem_bytes<MODE, OUTT>();
   auto kern = fused_field_mlp_kernel<MODE, BD, CD, OUTT, T>;
-  // the shared-memory opt-in and the occupancy query, once per process and device
-  static int per_sm_cache[64] = {0};
+  // the shared-memory opt-in and the occupancy query, once per process and device (atomic cache
+  // entries: threads racing on the first launch repeat the same idempotent set-up)
+  static std::atomic<int> per_sm_cache[64];
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
-  int per_sm = (dev >= 0 && dev < 64) ? per_sm_cache[dev] : 0;
+  int per_sm = (dev >= 0 && dev < 64) ? per_sm_cache[dev].load(std::memory_order_relaxed) : 0;
   if (per_sm == 0) {
     e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
@@ -663,7 +665,7 @@ cudaError_t launch_one(const FusedArgs& a, cudaStream_t st) {
       (void)cudaGetLastError();
       per_sm = 1;
     }
-    if (dev >= 0 && dev < 64) per_sm_cache[dev] = per_sm;
+    if (dev >= 0 && dev < 64) per_sm_cache[dev].store(per_sm, std::memory_order_relaxed);
   }
   const int64_t tiles = ceil_div(a.n, kTile);
   const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>(tiles, (int64_t)sm_count() * per_sm));

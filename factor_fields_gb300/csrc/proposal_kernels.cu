@@ -308,7 +308,10 @@ __global__ void __launch_bounds__(256) proposal_loss_kernel(const FFProposal p, 
     bin_weights(p, o_prop + ray * nb, s.len, lane, B, st);
     for (int k = lane; k < nb; k += 32) mass[k] = 0.f;
     __syncwarp();
-    for (int i = lane; i < nf; i += 32) atomicAdd(&mass[bin_of[ray * nf + i]], w_field[ray * nf + i]);
+    for (int i = lane; i < nf; i += 32) {
+      const int b = bin_of[ray * nf + i];
+      if (b >= 0 && b < nb) atomicAdd(&mass[b], w_field[ray * nf + i]);  // bins outside the histogram add nothing
+    }
     __syncwarp();
     // loss and dL/dw per bin
     float gw[kMaxBinsPerLane];

@@ -559,9 +559,9 @@ int ray_blocks(int64_t n_rays) {
 int64_t scan_workspace_bytes(int64_t n) { return (ceil_div(n, kScanBlock) + 1) * (int64_t)sizeof(int64_t); }
 
 // ---- the scan without a caller workspace ------------------------------------------------
-// Some callers cannot allocate device memory at all (a render loop replayed inside a captured
-// CUDA graph, where cudaMalloc is not permitted, or a host engine that owns every device
-// buffer and hands this library only its inputs and outputs). For them the per-block partial
+// Some callers cannot allocate device memory at all (a host engine that owns every device
+// buffer and hands this library only its inputs and outputs, or code that must not touch the
+// device allocator). For them the per-block partial
 // sums live in this fixed file-scope device array instead of a workspace. Every process that
 // loads the library holds these 32 KiB on each GPU it uses until it exits; all calls share
 // them, so calls that overlap on the GPU (different streams, no ordering) race on the array.
@@ -574,7 +574,9 @@ int64_t scan_noalloc_max_counts() { return kNoAllocScanBlocks * kScanBlock; }
 
 cudaError_t launch_scan_noalloc(const int32_t* counts, int64_t n, int64_t* offsets, cudaStream_t s) {
   // Host code cannot use g_scan_scratch directly (its name is a host-side stand-in); the
-  // device address is looked up once per device, with that device current, on the first call.
+  // device address is looked up once per device, with that device current, on the first call,
+  // in the device's primary context, and kept for the life of the process (a cudaDeviceReset
+  // does not refresh it).
   static std::mutex mu;
   static void* addr[64] = {nullptr};
   int dev = 0;

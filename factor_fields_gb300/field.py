@@ -251,6 +251,69 @@ class FactorFields(torch.nn.Module):
             groups.append({"params": self.renderModule.parameters(), "lr": lr_small})
         return groups
 
+    def set_optimizable(self, items, statue):
+        """models/FactorFields.py:556-567, with the reference's effects kept as they are:
+        'basis' and 'coeff' both switch requires_grad of the basis grids (the reference's
+        'coeff' branch loops over self.basises), 'proj' and 'renderer' set a plain
+        `requires_grad` attribute on linear_mat / renderModule (which leaves their parameters
+        as they were)."""
+        for item in items:
+            if item in ("basis", "coeff"):
+                self.basis_flat.requires_grad_(statue)
+            elif item == "proj":
+                self.linear_mat.requires_grad = statue
+            elif item == "renderer":
+                self.renderModule.requires_grad = statue
+
+    def TV_loss(self, reg):
+        """models/FactorFields.py:569-573: sum over the basis levels of reg(level) * 1e-2, the
+        levels passed as the reference's [1, C, R..] tensors (views of basis_flat, so the
+        gradient reaches it)."""
+        total = 0
+        for level in self.basises:
+            total = total + reg(level) * 1e-2
+        return total
+
+    @torch.no_grad()
+    def normalize_basis(self):
+        """models/FactorFields.py:519-521: each level divided by its norm over dims (2, 3) of
+        the [1, C, R, R(, R)] tensor, in place."""
+        for level in self.basises:
+            level.copy_(level / torch.norm(level, dim=(2, 3), keepdim=True))
+
+    @torch.no_grad()
+    def upsample_volume_grid(self, res_target):
+        """models/FactorFields.py:701-707: new render parameters for res_target; for the
+        google_objs dataset with one scene, the coefficient grid is also resampled by 1.3
+        (trilinear, align_corners=True) and rebuilt at its new resolution, as a new
+        parameter: build a new optimizer afterwards, as the reference's training loop does
+        (train_per_scene.py:214-218)."""
+        self.update_renderParams(res_target)
+        if self.cfg.dataset.dataset_name == "google_objs" and self.n_scene == 1 and self.coeff_type == "grid":
+            grid = F.interpolate(self.coeffs[0].detach().contiguous(), size=None, scale_factor=1.3,
+                                 align_corners=True, mode="trilinear")
+            self.coeff_reso = list(grid.shape[2:])
+            self.geom.coeff_reso = self.coeff_reso
+            self.layout = FieldLayout(self.basis_dims, self.basis_reso, self.in_dim, self.coeff_reso, self.n_scene)
+            self.coeff_flat = torch.nn.Parameter(self.layout.coeff_from_reference([grid], device=self.device))
+            self.T_coeff = self.n_feat * int(np.prod(self.coeff_reso))
+            self._desc_cache = {}
+            self._bf16 = None
+
+    @torch.no_grad()
+    def cal_mean_coef(self, state_dict):
+        """models/FactorFields.py:645-667 for grid coefficients: the scenes' coefficient grids
+        averaged into coeffs.0 (the others dropped)."""
+        keys = [k for k in state_dict.keys() if "coeffs.0" in k]
+        for key in keys:
+            average = torch.zeros_like(state_dict[key])
+            for i in range(self.n_scene):
+                item = key.replace("0", f"{i}", 1)
+                average += state_dict[item]
+                state_dict.pop(item, None)
+            state_dict[key] = average / self.n_scene
+        return state_dict
+
     def normalize_coord(self, xyz):
         """models/FactorFields.py:635-637."""
         inv = 2.0 / (self.aabb[1] - self.aabb[0])
@@ -422,19 +485,25 @@ class FactorFields(torch.nn.Module):
         return unexpected
 
     def save(self, path):
+        """models/FactorFields.py:669-680: the reference's keys and layouts, the packbits alpha
+        mask, and in the reconstruction modes the scenes' coefficients averaged into coeffs.0
+        (cal_mean_coef)."""
         ckpt = {"state_dict": self.reference_state_dict(), "cfg": dict(self.cfg)}
         if self.alphaMask is not None:
             vol = self.alphaMask.alpha_volume.bool().cpu().numpy()
             ckpt.update({"alphaMask.shape": vol.shape, "alphaMask.mask": np.packbits(vol.reshape(-1)),
                          "alphaMask.aabb": self.alphaMask.aabb.cpu()})
+        if "reconstruction" in self.cfg.defaults.mode:
+            ckpt["state_dict"] = self.cal_mean_coef(ckpt["state_dict"])
         torch.save(ckpt, path)
 
     def load(self, ckpt):
+        """models/FactorFields.py:682-691 (render parameters recomputed for volume_resoFinal,
+        as the reference does, whatever the mode)."""
         if "alphaMask.aabb" in ckpt:
             from .renderer import AlphaGridMask
             length = int(np.prod(ckpt["alphaMask.shape"]))
             vol = torch.from_numpy(np.unpackbits(ckpt["alphaMask.mask"])[:length].reshape(ckpt["alphaMask.shape"]))
             self.alphaMask = AlphaGridMask(self.device, ckpt["alphaMask.aabb"].to(self.device), vol.float().to(self.device))
         self.load_reference_state_dict(ckpt["state_dict"])
-        if "reconstruction" in self.cfg.defaults.mode:
-            self.update_renderParams(n_to_reso(self.cfg.training.volume_resoFinal ** self.in_dim, self.aabb.cpu()))
+        self.update_renderParams(n_to_reso(self.cfg.training.volume_resoFinal ** self.in_dim, self.aabb.cpu()))

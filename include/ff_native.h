@@ -11,8 +11,17 @@
  *   - The return value is FF_OK (0) or a negative FF_ERR_* code; ff_last_error() returns a
  *     thread-local description of the most recent failure on the calling thread.
  *   - Gradient outputs are ACCUMULATED (+=) in float32, like autograd's .grad: zero them first.
- *   - Launches are stream-ordered. There is no mutable global state: two calls on different
- *     streams are independent unless they write the same output buffers.
+ *   - Launches are stream-ordered: two calls on different streams are independent unless they
+ *     write the same output buffers (ff_scan_counts_noalloc excepted: its calls share one
+ *     library-owned array). The library's only process-wide state is a per-device cache of
+ *     launch parameters (SM count, occupancy, kernel attributes) and, for
+ *     ff_scan_counts_noalloc, the device address of its array; the caches are filled on first
+ *     use with atomic or mutex-guarded writes, so concurrent host threads are safe. They are
+ *     keyed by device ordinal and assume the device's primary context (the one the CUDA runtime
+ *     and torch use); they are not cleared by cudaDeviceReset.
+ *   - Two entry points synchronise the stream before returning because they read a small
+ *     result back to the host: ff_occupancy_mask (a status word) and ff_image_metrics (the two
+ *     metrics). Every other entry point only enqueues work.
  *
  * Every entry point replaces a specific piece of the reference's PyTorch code
  * (autonomousvision/factor-fields); the citation is given beside each declaration.
@@ -287,15 +296,16 @@ FF_API int64_t ff_scan_workspace_bytes(int64_t n);
 FF_API int ff_scan_counts(const int32_t* counts, int64_t n, int64_t* offsets, void* workspace,
                           int64_t workspace_bytes, void* stream);
 
-/* ff_scan_counts for callers that cannot allocate device memory — e.g. a render loop replayed
- * inside a captured CUDA graph (cudaMalloc is not permitted during capture) or a host engine
- * that owns every device buffer and passes this library only inputs and outputs. It has no
- * counterpart in the reference. Instead of a workspace it uses a fixed scratch array inside
- * the library (32 KiB per GPU, held until the process exits), so it takes at most
- * ff_scan_noalloc_max_counts() = 16,777,216 counts and returns FF_ERR_SIZE beyond that.
- * The first call on a device looks up the array's device address; make that first call
- * before any stream capture. All calls share the array: calls that overlap on the GPU race.
- * It allocates nothing (no cudaMalloc / cudaFree, no allocating library routine). */
+/* ff_scan_counts for callers that cannot allocate device memory — a host engine that owns
+ * every device buffer and hands this library only inputs and outputs, or code running under an
+ * allocator it must not touch. It has no counterpart in the reference. Instead of a workspace
+ * it uses a fixed scratch array inside the library (32 KiB per GPU, held until the process
+ * exits), so it takes at most ff_scan_noalloc_max_counts() = 16,777,216 counts and returns
+ * FF_ERR_SIZE beyond that. The first call on a device looks up the array's device address (in
+ * the device's primary context; the address is cached per device ordinal and not refreshed
+ * after cudaDeviceReset); make that first call before any stream capture. All calls share the
+ * array: calls that overlap on the GPU race. It allocates nothing (no cudaMalloc / cudaFree,
+ * no allocating library routine). */
 FF_API int64_t ff_scan_noalloc_max_counts(void);
 FF_API int ff_scan_counts_noalloc(const int32_t* counts, int64_t n, int64_t* offsets, void* stream);
 
@@ -368,7 +378,9 @@ FF_API int ff_proposal_resample(const FFProposal* p, const float* rays, int64_t 
                                 int32_t* bin_of, void* stream);
 /* Proposal loss sum_k max(0, m_k - w_k)^2 / (w_k + 1e-5) per ray, m_k = field weight mass in
  * bin k (w_field [n_rays * n_fine], bin_of from resample), scaled by loss_scale; loss_sum
- * (optional) accumulates the loss, grad_o [n_rays * n_bins] receives dL/do_prop. */
+ * (optional) accumulates the loss, grad_o [n_rays * n_bins] receives dL/do_prop. bin_of must
+ * come from ff_proposal_resample with the same descriptor; entries outside [0, n_bins) are
+ * ignored (they add no mass). */
 FF_API int ff_proposal_loss(const FFProposal* p, const float* rays, int64_t n_rays, const float* o_prop,
                             const float* w_field, const int32_t* bin_of, float loss_scale, float* loss_sum,
                             float* grad_o, void* stream);

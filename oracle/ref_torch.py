@@ -86,7 +86,7 @@ class RefField(torch.nn.Module):
         err = pred - target
         lv = err.abs().mean() if loss == "l1" else (err * err).mean()
         lv.backward()
-        return float(lv)
+        return float(lv.detach())
 
 
 def from_model(m):

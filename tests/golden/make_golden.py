@@ -1,8 +1,8 @@
 """Generate the golden fixtures in tests/golden/ by running the REFERENCE itself.
 
 This script is the only place that imports autonomousvision/factor-fields. It runs in a
-container where the reference checkout is readable at REF_ROOT (default /root/reference,
-override with FF_REFERENCE_ROOT) and writes small .npz fixtures next to itself. The tests
+container where a checkout of the reference is readable; its path is given by the
+FF_REFERENCE_ROOT environment variable (required). It writes small .npz fixtures next to itself. The tests
 and the oracle only ever read those .npz files; nothing at test time needs the reference.
 
 How the reference is imported (it is pure Python / PyTorch):
@@ -18,7 +18,7 @@ so a fixture is a complete known-answer test. Full-size configurations store the
 shapes/resolutions and checksums of the reference's DCT initialisation instead of the
 (large) parameters themselves.
 
-Run:  PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py
+Run:  FF_REFERENCE_ROOT=<checkout> PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py
 """
 import importlib.util
 import json
@@ -32,7 +32,9 @@ os.environ["PYTHONDONTWRITEBYTECODE"] = "1"
 import numpy as np
 import torch
 
-REF_ROOT = os.environ.get("FF_REFERENCE_ROOT", "/root/reference")
+REF_ROOT = os.environ.get("FF_REFERENCE_ROOT")
+if not REF_ROOT or not os.path.isdir(os.path.join(REF_ROOT, "models")):
+    sys.exit("set FF_REFERENCE_ROOT to a checkout of autonomousvision/factor-fields")
 OUT_DIR = os.path.dirname(os.path.abspath(__file__))
 
 

@@ -56,3 +56,21 @@ def rel_err(a, b):
     a = np.asarray(a.detach().cpu().numpy() if torch.is_tensor(a) else a, np.float64)
     b = np.asarray(b.detach().cpu().numpy() if torch.is_tensor(b) else b, np.float64)
     return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-30))
+
+
+def elem_err(a, b, rtol, atol_rel=1e-6):
+    """Element-wise check beside rel_err: the largest ratio |a - b| / (rtol |b| + atol) over the
+    elements, with atol = atol_rel * max|b| (<= 1 passes). rel_err alone lets entries far below
+    the maximum drift by much more than rtol of their own size; this bounds each entry by rtol
+    of itself plus a floor. The floor 1e-6 * max|ref| sits above the reference's own float32
+    rounding: its golden outputs differ from the exact (FP64 oracle) values by up to
+    ~6e-7 * max|ref| element-wise."""
+    a = np.asarray(a.detach().cpu().numpy() if torch.is_tensor(a) else a, np.float64)
+    b = np.asarray(b.detach().cpu().numpy() if torch.is_tensor(b) else b, np.float64)
+    atol = atol_rel * max(float(np.max(np.abs(b))), 1e-30)
+    return float(np.max(np.abs(a - b) / (rtol * np.abs(b) + atol)))
+
+
+def close(a, b, rtol, atol_rel=1e-6):
+    """rel_err(a, b) < rtol and elem_err(a, b, rtol, atol_rel) <= 1."""
+    return rel_err(a, b) < rtol and elem_err(a, b, rtol, atol_rel) <= 1.0

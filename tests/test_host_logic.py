@@ -7,7 +7,7 @@ import numpy as np
 import torch
 
 from factor_fields_gb300 import FactorFields, make_cfg
-from factor_fields_gb300.config import FieldGeometry, render_step
+from factor_fields_gb300.config import FieldGeometry, n_to_reso, render_step
 from factor_fields_gb300.layout import FieldLayout
 from factor_fields_gb300 import workloads as W
 
@@ -123,3 +123,89 @@ def test_occupancy_oracle_known_answer():
     assert occ.sum() == 0             # two 27-voxel components under 6-connectivity, both < 28
     occ, _, _ = O.occupancy_mask(c, 0.5, 27)
     assert occ.sum() == 54
+
+
+def _small_rec_cfg(mode="reconstruction", n_scene=1, **dataset):
+    """A small 3-D reconstruction config (levels of 5..10 cells, 6^3 coefficients)."""
+    from factor_fields_gb300.config import merged_cfg
+    aabb = [[-1.5] * 3, [1.5] * 3]
+    if mode == "reconstructions":
+        aabb = [[-1.5] * 3 + [0], [1.5] * 3 + [n_scene]]
+    return merged_cfg({"defaults": {"mode": mode},
+                       "model": {"basis_resos": [5, 6, 7, 8, 9, 10], "coeff_reso": 6, "total_params": 11106,
+                                 "out_dim": 28, "basis_mapping": "triangle"},
+                       "dataset": {"aabb": aabb, "scene_reso": 1024, **dataset}})
+
+
+def _tv(x):
+    """TV regulariser of utils.py:160-175 (restated for the check)."""
+    h, w = x.size()[2], x.size()[3]
+    count_h = x[:, :, 1:, :].numel() // x.size()[0]
+    count_w = x[:, :, :, 1:].numel() // x.size()[0]
+    h_tv = torch.pow(x[:, :, 1:, :] - x[:, :, :h - 1, :], 2).sum()
+    w_tv = torch.pow(x[:, :, :, 1:] - x[:, :, :, :w - 1], 2).sum()
+    return 2 * (h_tv / count_h + w_tv / count_w) / x.size()[0]
+
+
+def test_surface_methods_follow_reference():
+    """normalize_basis (:519-521), TV_loss (:569-573), set_optimizable (:556-567) and
+    upsample_volume_grid (:701-707) on the reference-layout views of the flat parameters."""
+    torch.manual_seed(0)
+    m = FactorFields(_small_rec_cfg(), device="cpu")
+    with torch.no_grad():
+        m.basis_flat.normal_()
+    ref_levels = [b.detach().clone() for b in m.basises]
+    m.normalize_basis()
+    for got, ref in zip(m.basises, ref_levels):
+        want = ref / torch.norm(ref, dim=(2, 3), keepdim=True)
+        assert torch.allclose(got, want, rtol=1e-6, atol=1e-7)
+    # TV_loss: the reference's sum over levels, gradient reaching the flat basis
+    total = m.TV_loss(_tv)
+    want = sum(_tv(b.detach().contiguous()) * 1e-2 for b in m.basises)
+    assert torch.allclose(total.detach(), want, rtol=1e-5)
+    total.backward()
+    assert m.basis_flat.grad is not None and float(m.basis_flat.grad.abs().sum()) > 0
+    # set_optimizable: 'basis' and 'coeff' both toggle the basis grids, as in the reference
+    m.set_optimizable(["coeff"], False)
+    assert not m.basis_flat.requires_grad and m.coeff_flat.requires_grad
+    m.set_optimizable(["basis", "proj", "renderer"], True)
+    assert m.basis_flat.requires_grad and m.linear_mat.requires_grad is True and m.renderModule.requires_grad is True
+    # upsample_volume_grid: render parameters for the new resolution; coefficients unchanged
+    coeff0 = m.coeffs[0].detach().clone()
+    m.upsample_volume_grid([64, 64, 64])
+    assert m.gridSize.tolist() == [64, 64, 64]
+    assert torch.equal(m.coeffs[0], coeff0)
+    step, n = render_step(torch.tensor(m.cfg.dataset.aabb), [64, 64, 64], 0.5)
+    assert float(m.stepSize) == float(step) and m.nSamples == n
+    # google_objs with one scene: the coefficient grid resampled by 1.3 (trilinear, align_corners)
+    g = FactorFields(_small_rec_cfg(dataset_name="google_objs"), device="cpu")
+    with torch.no_grad():
+        g.coeff_flat.normal_()
+    old = g.coeffs[0].detach().contiguous()
+    g.upsample_volume_grid([32, 32, 32])
+    want = torch.nn.functional.interpolate(old, scale_factor=1.3, align_corners=True, mode="trilinear")
+    assert g.coeffs[0].shape == want.shape == (1, 18, 7, 7, 7)
+    assert torch.equal(g.coeffs[0], want)
+    assert g.descriptor(0).coeff_reso[0] == 7
+
+
+def test_save_averages_scene_coefficients(tmp_path):
+    """save() in the reconstruction modes writes the scenes' mean coefficients as coeffs.0
+    (cal_mean_coef, :645-667, :677-679); load() recomputes the render parameters (:689-691)."""
+    cfg = _small_rec_cfg("reconstructions", n_scene=3)
+    m = FactorFields(cfg, device="cpu")
+    assert m.n_scene == 3
+    with torch.no_grad():
+        m.coeff_flat.normal_()
+    mean = sum(c.detach() for c in m.coeffs) / 3
+    p = tmp_path / "multi.th"
+    m.save(str(p))
+    ck = torch.load(str(p), weights_only=False)
+    keys = [k for k in ck["state_dict"] if k.startswith("coeffs.")]
+    assert keys == ["coeffs.0"]
+    assert torch.allclose(ck["state_dict"]["coeffs.0"], mean, rtol=1e-6, atol=1e-7)
+    m2 = FactorFields(cfg, device="cpu")
+    m2.load(ck)
+    for c in m2.coeffs:
+        assert torch.allclose(c, mean, rtol=1e-6, atol=1e-7)
+    assert m2.gridSize.tolist() == n_to_reso(300 ** 3, m2.aabb.cpu())

@@ -2,7 +2,8 @@
 golden renders and the FP64 oracle.
 
 Bit-exact: live-sample set and order (the reference's xyz_sampled[ray_valid]), sample
-positions, occupancy decisions. Float32 drop-in path: rgb / depth 1e-5, gradients 1e-4.
+positions, occupancy decisions. Float32 drop-in path: rgb / depth 1e-5, gradients 1e-4, also
+element-wise (gpu_util.close).
 Fused BF16 path: 2e-2 / 3e-2 against the oracle of the BF16-stored model."""
 import ctypes
 
@@ -10,7 +11,7 @@ import numpy as np
 import pytest
 import torch
 
-from gpu_util import load_golden, model_from_golden, need_gpu, rel_err, render_cases
+from gpu_util import close, load_golden, model_from_golden, need_gpu, rel_err, render_cases
 from oracle import ff_oracle as O
 
 pytestmark = pytest.mark.gpu
@@ -58,16 +59,16 @@ def test_render_dropin_matches_reference(case):
     d, meta, m, rays, jitter = setup(case, "fp32")
     ns = int(d["n_samples"])
     rgb, depth, _ = m(rays, white_bg=meta["white_bg"], is_train=False, N_samples=ns, jitter=jitter, fused=False)
-    assert rel_err(rgb, d["rgb"]) < 1e-5
-    assert rel_err(depth, d["depth"]) < 1e-5
+    assert close(rgb, d["rgb"], 1e-5)
+    assert close(depth, d["depth"], 1e-5)
     (rgb * torch.from_numpy(d["g_rgb"]).cuda()).sum().backward()
     for l in range(6):
-        assert rel_err(m.layout.basis_view(m.basis_flat.grad, l), d[f"grad_basis{l}"]) < 1e-4, l
-    assert rel_err(m.layout.coeff_view(m.coeff_flat.grad, 0), d["grad_coeffs0"]) < 1e-4
+        assert close(m.layout.basis_view(m.basis_flat.grad, l), d[f"grad_basis{l}"], 1e-4), l
+    assert close(m.layout.coeff_view(m.coeff_flat.grad, 0), d["grad_coeffs0"], 1e-4)
     for i, lin in enumerate(m.linear_mat.backbone):
-        assert rel_err(lin.weight.grad, d[f"grad_mlp_w{i}"]) < 1e-4
+        assert close(lin.weight.grad, d[f"grad_mlp_w{i}"], 1e-4)
         if lin.bias is not None:
-            assert rel_err(lin.bias.grad, d[f"grad_mlp_b{i}"]) < 1e-4
+            assert close(lin.bias.grad, d[f"grad_mlp_b{i}"], 1e-4)
 
 
 @pytest.mark.parametrize("case", CASES)

@@ -1,6 +1,6 @@
 """ff_scan_counts_noalloc: the ray-count scan for callers that cannot allocate device memory
-(for example a render loop replayed inside a captured CUDA graph, where cudaMalloc is not
-permitted, or a host engine that owns every device buffer). It keeps its partial sums in a
+(for example a host engine that owns every device buffer and hands the library only inputs
+and outputs, or code that must not touch the device allocator). It keeps its partial sums in a
 fixed scratch array inside the library instead of a caller workspace.
 
 Checked through the C ABI against ff_scan_counts (the workspace variant) on two calls in a
