@@ -57,6 +57,12 @@ class FFRender(ctypes.Structure):
                 ("occ_origin", c_f32 * 3), ("occ_inv", c_f32 * 3)]
 
 
+class FFRenderMlp(ctypes.Structure):
+    _fields_ = [("n_layers", c_i32), ("in_channels", c_i32), ("hidden_dim", c_i32), ("view_pe", c_i32),
+                ("fea_pe", c_i32), ("in_dim", c_i32), ("weight", c_vp * FF_MAX_MLP_LAYERS),
+                ("bias", c_vp * FF_MAX_MLP_LAYERS)]
+
+
 class FFAdamParam(ctypes.Structure):
     _fields_ = [("param", c_vp), ("grad", c_vp), ("exp_avg", c_vp), ("exp_avg_sq", c_vp), ("param_bf16", c_vp),
                 ("n", c_i64), ("step", c_i64), ("lr", c_f32), ("reserved", c_f32)]
@@ -110,6 +116,20 @@ SIGNATURES = {
                                       c_vp]),
     "ff_composite_forward_zd": (c_i32, [_P(FFRender), c_vp, c_i64, c_vp, c_vp, c_vp, c_i32, c_vp, c_vp, c_vp, c_vp]),
     "ff_composite_backward_zd": (c_i32, [_P(FFRender), c_vp, c_i64, c_vp, c_vp, c_vp, c_i32, c_vp, c_vp, c_vp]),
+    "ff_composite_weights": (c_i32, [_P(FFRender), c_vp, c_vp, c_i64, c_vp, c_vp, c_vp, c_i32, c_vp, c_vp, c_vp]),
+    "ff_app_emit": (c_i32, [c_i64, c_vp, c_vp, c_f32, c_vp, c_vp, c_vp, c_vp]),
+    "ff_render_head_workspace_bytes": (c_i64, [_P(FFRenderMlp), c_i64]),
+    "ff_render_head_forward": (c_i32, [_P(FFRenderMlp), c_vp, c_i32, c_vp, c_vp, c_vp, c_i64, c_vp, c_vp, c_i64,
+                                       c_vp]),
+    "ff_render_head_backward": (c_i32, [_P(FFRenderMlp), c_vp, c_i32, c_vp, c_vp, c_vp, c_i64, c_vp, c_vp,
+                                        _P(FFMlpGrad), c_vp, c_i64, c_vp]),
+    "ff_render_head_forward_tc": (c_i32, [_P(FFRenderMlp), c_vp, c_i32, c_vp, c_vp, c_vp, c_i64, c_vp, c_vp, c_vp]),
+    "ff_render_head_backward_tc": (c_i32, [_P(FFRenderMlp), c_vp, c_i32, c_vp, c_vp, c_vp, c_i64, c_vp, c_vp,
+                                           _P(FFMlpGrad), c_vp, c_vp]),
+    "ff_composite_forward_rgb": (c_i32, [_P(FFRender), c_vp, c_vp, c_i64, c_vp, c_vp, c_vp, c_i32, c_vp, c_vp, c_vp,
+                                         c_vp, c_vp, c_vp]),
+    "ff_composite_backward_rgb": (c_i32, [_P(FFRender), c_vp, c_vp, c_i64, c_vp, c_vp, c_vp, c_i32, c_vp, c_vp,
+                                          c_vp, c_vp, c_vp, c_vp]),
     "ff_proposal_encode": (c_i32, [_P(FFProposal), c_vp, c_vp, c_i64, c_vp, c_vp]),
     "ff_proposal_resample": (c_i32, [_P(FFProposal), c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
     "ff_proposal_loss": (c_i32, [_P(FFProposal), c_vp, c_i64, c_vp, c_vp, c_vp, c_f32, c_vp, c_vp, c_vp]),
@@ -171,7 +191,7 @@ def stream_ptr():
 _launches = [0]
 _NON_LAUNCHING = {"ff_abi_version", "ff_last_error", "ff_device_info", "ff_struct_size", "ff_scan_workspace_bytes",
                   "ff_field_fit_binned_workspace_bytes", "ff_occupancy_workspace_bytes",
-                  "ff_image_metrics_workspace_bytes",
+                  "ff_image_metrics_workspace_bytes", "ff_render_head_workspace_bytes",
                   "ff_scan_noalloc_max_counts"}
 
 

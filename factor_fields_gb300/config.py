@@ -42,7 +42,7 @@ DEFAULTS = {
                 "dataset_name": "blender"},
     "training": {"volume_resoInit": 128, "volume_resoFinal": 300, "linear_mat": True, "coeff": True,
                  "basis": True, "renderModule": True},
-    "renderer": {"shadingMode": "SH", "num_layers": 3, "hidden_dim": 128, "fea2denseAct": "softplus",
+    "renderer": {"shadingMode": "MLP_Fea", "num_layers": 3, "hidden_dim": 128, "fea2denseAct": "softplus",
                  "density_shift": -10.0, "distance_scale": 25.0, "view_pe": 6, "fea_pe": 2, "step_ratio": 0.5,
                  "rayMarch_weight_thres": 1e-3, "alphaMask_thres": 0.02},
 }

@@ -112,6 +112,7 @@ int64_t ff_struct_size(int32_t which) {
     case 3: return (int64_t)sizeof(FFRender);
     case 4: return (int64_t)sizeof(FFProposal);
     case 5: return (int64_t)sizeof(FFAdamParam);
+    case 6: return (int64_t)sizeof(FFRenderMlp);
     default: return -1;
   }
 }
@@ -488,6 +489,136 @@ int ff_composite_backward_zd(const FFRender* r, const float* rays, int64_t n_ray
   return cuda_status(launch_composite_backward(*r, rays, nullptr, n_rays, offsets, nullptr, feat, feat_stride,
                                                nullptr, grad_rgb, grad_feat, zd, (cudaStream_t)stream),
                      "ff_composite_backward_zd launch");
+}
+
+int ff_composite_weights(const FFRender* r, const float* rays, const float* jitter, int64_t n_rays,
+                         const int64_t* offsets, const int32_t* sample_idx, const float* feat, int32_t feat_stride,
+                         float* w_out, int32_t* app_counts, void* stream) {
+  int rc = validate_render(r, rays, n_rays);
+  if (rc) return rc;
+  if (feat_stride < 1) return set_error(FF_ERR_ARG, "feat_stride must be >= 1");
+  if (n_rays > 0 && (!offsets || !sample_idx || !feat || !w_out || !app_counts))
+    return set_error(FF_ERR_ARG, "ff_composite_weights: a buffer is NULL");
+  return cuda_status(launch_composite_weights(*r, rays, jitter, n_rays, offsets, sample_idx, feat, feat_stride, w_out,
+                                              app_counts, (cudaStream_t)stream),
+                     "ff_composite_weights launch");
+}
+
+int ff_app_emit(int64_t n_rays, const int64_t* offsets, const float* w, float weight_thres, const int64_t* app_offsets,
+                int32_t* app_idx, int32_t* app_ray, void* stream) {
+  if (n_rays < 0 || (n_rays > 0 && (!offsets || !w || !app_offsets || !app_idx || !app_ray)))
+    return set_error(FF_ERR_ARG, "ff_app_emit: bad arguments");
+  return cuda_status(launch_app_emit(n_rays, offsets, w, weight_thres, app_offsets, app_idx, app_ray,
+                                     (cudaStream_t)stream),
+                     "ff_app_emit launch");
+}
+
+static int validate_render_head(const FFRenderMlp* h, const float* feat, int32_t feat_stride, const float* rays,
+                                const int32_t* app_idx, const int32_t* app_ray, int64_t n) {
+  if (!h) return set_error(FF_ERR_ARG, "render head descriptor is NULL");
+  if (h->n_layers < 1 || h->n_layers > FF_MAX_MLP_LAYERS) return set_error(FF_ERR_ARG, "n_layers must be 1..4");
+  if (h->in_channels < 1 || h->hidden_dim < 1 || h->view_pe < 0 || h->fea_pe < 0 || h->view_pe > 24 || h->fea_pe > 24)
+    return set_error(FF_ERR_ARG, "bad render head dimensions");
+  const int64_t in = 3 + (int64_t)h->in_channels + 6 * (int64_t)h->view_pe + 2 * (int64_t)h->fea_pe * h->in_channels;
+  if (h->in_dim != in) return set_error(FF_ERR_ARG, "in_dim must be 3 + C + 6 view_pe + 2 fea_pe C");
+  for (int l = 0; l < h->n_layers; ++l) {
+    if (!h->weight[l]) return set_error(FF_ERR_ARG, "a render head weight is NULL");
+    if (l == h->n_layers - 1 && h->bias[l]) return set_error(FF_ERR_ARG, "the last layer has no bias");
+  }
+  if (feat_stride < h->in_channels + 1) return set_error(FF_ERR_ARG, "feat_stride must be >= in_channels + 1");
+  if (n < 0 || (n > 0 && (!feat || !rays || !app_idx || !app_ray))) return set_error(FF_ERR_ARG, "bad head inputs");
+  return FF_OK;
+}
+
+int64_t ff_render_head_workspace_bytes(const FFRenderMlp* h, int64_t n_app) {
+  if (!h || n_app < 0 || h->n_layers < 1 || h->n_layers > FF_MAX_MLP_LAYERS) return -1;
+  return render_head_workspace_bytes(*h, n_app);
+}
+
+int ff_render_head_forward(const FFRenderMlp* h, const float* feat, int32_t feat_stride, const float* rays,
+                           const int32_t* app_idx, const int32_t* app_ray, int64_t n_app, float* rgb_sample,
+                           void* workspace, int64_t workspace_bytes, void* stream) {
+  int rc = validate_render_head(h, feat, feat_stride, rays, app_idx, app_ray, n_app);
+  if (rc) return rc;
+  if (n_app > 0 && !rgb_sample) return set_error(FF_ERR_ARG, "rgb_sample is NULL");
+  if (workspace_bytes < render_head_workspace_bytes(*h, n_app) || (n_app > 0 && !workspace))
+    return set_error(FF_ERR_SIZE, "render head workspace too small");
+  if (!aligned(workspace, 256)) return set_error(FF_ERR_ALIGN, "workspace must be 256-byte aligned");
+  return cuda_status(launch_render_head_forward(*h, feat, feat_stride, 1, rays, app_idx, app_ray, n_app, rgb_sample,
+                                                workspace, (cudaStream_t)stream),
+                     "ff_render_head_forward launch");
+}
+
+int ff_render_head_backward(const FFRenderMlp* h, const float* feat, int32_t feat_stride, const float* rays,
+                            const int32_t* app_idx, const int32_t* app_ray, int64_t n_app, const float* grad_rgb_sample,
+                            float* grad_feat, const FFMlpGrad* g, void* workspace, int64_t workspace_bytes,
+                            void* stream) {
+  int rc = validate_render_head(h, feat, feat_stride, rays, app_idx, app_ray, n_app);
+  if (rc) return rc;
+  if (n_app > 0 && (!grad_rgb_sample || !grad_feat)) return set_error(FF_ERR_ARG, "backward buffers are NULL");
+  if (workspace_bytes < render_head_workspace_bytes(*h, n_app) || (n_app > 0 && !workspace))
+    return set_error(FF_ERR_SIZE, "render head workspace too small");
+  if (!aligned(workspace, 256)) return set_error(FF_ERR_ALIGN, "workspace must be 256-byte aligned");
+  FFMlpGrad none = {};
+  return cuda_status(launch_render_head_backward(*h, feat, feat_stride, 1, rays, app_idx, app_ray, n_app,
+                                                 grad_rgb_sample, grad_feat, g ? *g : none, workspace,
+                                                 (cudaStream_t)stream),
+                     "ff_render_head_backward launch");
+}
+
+int ff_render_head_forward_tc(const FFRenderMlp* h, const float* feat, int32_t feat_stride, const float* rays,
+                              const int32_t* app_idx, const int32_t* app_ray, int64_t n_app, float* rgb_sample,
+                              int32_t* status, void* stream) {
+  int rc = validate_render_head(h, feat, feat_stride, rays, app_idx, app_ray, n_app);
+  if (rc) return rc;
+  if (const char* why = render_head_tc_unsupported(*h)) return set_error(FF_ERR_UNSUPPORTED, why);
+  if (n_app > 0 && !rgb_sample) return set_error(FF_ERR_ARG, "rgb_sample is NULL");
+  return cuda_status(launch_render_head_tc_forward(*h, feat, feat_stride, rays, app_idx, app_ray, n_app, rgb_sample,
+                                                   status, (cudaStream_t)stream),
+                     "ff_render_head_forward_tc launch");
+}
+
+int ff_render_head_backward_tc(const FFRenderMlp* h, const float* feat, int32_t feat_stride, const float* rays,
+                               const int32_t* app_idx, const int32_t* app_ray, int64_t n_app,
+                               const float* grad_rgb_sample, float* grad_feat, const FFMlpGrad* g, int32_t* status,
+                               void* stream) {
+  int rc = validate_render_head(h, feat, feat_stride, rays, app_idx, app_ray, n_app);
+  if (rc) return rc;
+  if (const char* why = render_head_tc_unsupported(*h)) return set_error(FF_ERR_UNSUPPORTED, why);
+  if (n_app > 0 && (!grad_rgb_sample || !grad_feat)) return set_error(FF_ERR_ARG, "backward buffers are NULL");
+  FFMlpGrad none = {};
+  return cuda_status(launch_render_head_tc_backward(*h, feat, feat_stride, rays, app_idx, app_ray, n_app,
+                                                    grad_rgb_sample, grad_feat, g ? *g : none, status,
+                                                    (cudaStream_t)stream),
+                     "ff_render_head_backward_tc launch");
+}
+
+int ff_composite_forward_rgb(const FFRender* r, const float* rays, const float* jitter, int64_t n_rays,
+                             const int64_t* offsets, const int32_t* sample_idx, const float* feat, int32_t feat_stride,
+                             const float* rgb_sample, const int32_t* white_bg, float* rgb, float* depth, float* acc,
+                             void* stream) {
+  int rc = validate_render(r, rays, n_rays);
+  if (rc) return rc;
+  if (feat_stride < 1) return set_error(FF_ERR_ARG, "feat_stride must be >= 1");
+  if (n_rays > 0 && (!offsets || !rgb || !sample_idx)) return set_error(FF_ERR_ARG, "offsets/sample_idx/rgb are NULL");
+  return cuda_status(launch_composite_forward_rgb(*r, rays, jitter, n_rays, offsets, sample_idx, feat, feat_stride,
+                                                  rgb_sample, white_bg, rgb, depth, acc, (cudaStream_t)stream),
+                     "ff_composite_forward_rgb launch");
+}
+
+int ff_composite_backward_rgb(const FFRender* r, const float* rays, const float* jitter, int64_t n_rays,
+                              const int64_t* offsets, const int32_t* sample_idx, const float* feat,
+                              int32_t feat_stride, const float* rgb_sample, const int32_t* white_bg,
+                              const float* grad_rgb, float* grad_feat, float* grad_rgb_sample, void* stream) {
+  int rc = validate_render(r, rays, n_rays);
+  if (rc) return rc;
+  if (feat_stride < 1) return set_error(FF_ERR_ARG, "feat_stride must be >= 1");
+  if (n_rays > 0 && (!offsets || !sample_idx || !grad_rgb || !grad_feat || !grad_rgb_sample))
+    return set_error(FF_ERR_ARG, "backward buffers are NULL");
+  return cuda_status(launch_composite_backward_rgb(*r, rays, jitter, n_rays, offsets, sample_idx, feat, feat_stride,
+                                                   rgb_sample, white_bg, grad_rgb, grad_feat, grad_rgb_sample,
+                                                   (cudaStream_t)stream),
+                     "ff_composite_backward_rgb launch");
 }
 
 static int validate_proposal(const FFProposal* p, const float* rays, int64_t n) {

@@ -120,6 +120,41 @@ cudaError_t launch_composite_backward(const FFRender& r, const float* rays, cons
                                       int feat_stride, const int32_t* white_bg, const float* grad_rgb,
                                       float* grad_feat, const float* zd, cudaStream_t s);
 
+cudaError_t launch_composite_forward_rgb(const FFRender& r, const float* rays, const float* jitter, int64_t n,
+                                         const int64_t* offsets, const int32_t* sample_idx, const float* feat,
+                                         int feat_stride, const float* rgb_sample, const int32_t* white_bg, float* rgb,
+                                         float* depth, float* acc, cudaStream_t s);
+cudaError_t launch_composite_backward_rgb(const FFRender& r, const float* rays, const float* jitter, int64_t n,
+                                          const int64_t* offsets, const int32_t* sample_idx, const float* feat,
+                                          int feat_stride, const float* rgb_sample, const int32_t* white_bg,
+                                          const float* grad_rgb, float* grad_feat, float* grad_rgb_sample,
+                                          cudaStream_t s);
+cudaError_t launch_composite_weights(const FFRender& r, const float* rays, const float* jitter, int64_t n,
+                                     const int64_t* offsets, const int32_t* sample_idx, const float* feat,
+                                     int feat_stride, float* w_out, int32_t* app_counts, cudaStream_t s);
+cudaError_t launch_app_emit(int64_t n, const int64_t* offsets, const float* w, float thres, const int64_t* app_offsets,
+                            int32_t* app_idx, int32_t* app_ray, cudaStream_t s);
+
+// render_head_kernels.cu (MLPRender_Fea, float32 drop-in); features are channels 1..C of feat rows
+int64_t render_head_workspace_bytes(const FFRenderMlp& h, int64_t n);
+cudaError_t launch_render_head_forward(const FFRenderMlp& h, const float* feat, int feat_stride, int feat_off,
+                                       const float* rays, const int32_t* app_idx, const int32_t* app_ray, int64_t n,
+                                       float* rgb_rows, void* workspace, cudaStream_t s);
+cudaError_t launch_render_head_backward(const FFRenderMlp& h, const float* feat, int feat_stride, int feat_off,
+                                        const float* rays, const int32_t* app_idx, const int32_t* app_ray, int64_t n,
+                                        const float* grad_rgb_rows, float* grad_feat, const FFMlpGrad& gr,
+                                        void* workspace, cudaStream_t s);
+
+// render_head_tc.cu (MLPRender_Fea on tcgen05 tensor cores)
+const char* render_head_tc_unsupported(const FFRenderMlp& h);  // nullptr when supported
+cudaError_t launch_render_head_tc_forward(const FFRenderMlp& h, const float* feat, int feat_stride, const float* rays,
+                                          const int32_t* app_idx, const int32_t* app_ray, int64_t n, float* rgb_rows,
+                                          int32_t* status, cudaStream_t s);
+cudaError_t launch_render_head_tc_backward(const FFRenderMlp& h, const float* feat, int feat_stride, const float* rays,
+                                           const int32_t* app_idx, const int32_t* app_ray, int64_t n,
+                                           const float* grad_rgb_rows, float* grad_feat, const FFMlpGrad& g,
+                                           int32_t* status, cudaStream_t s);
+
 // proposal_kernels.cu
 cudaError_t launch_proposal_head_forward(const FFProposal& p, const void* grid, const FFMlp& m, const float* rays,
                                          int64_t n, float* o_out, cudaStream_t s);

@@ -1,0 +1,533 @@
+// MLPRender_Fea colour head (models/FactorFields.py:162-203) on the fifth-generation tensor
+// cores: tcgen05.mma with BF16 operands in shared memory and FP32 accumulators in tensor memory.
+//
+// One persistent CTA per SM (128 threads: thread t owns sample t of a 128-sample tile and TMEM
+// lane t) walks tiles of the listed head samples. Per tile, for 3 layers 128 hidden units wide:
+//
+//   X   = [feat, dir, PE(feat, 2), PE(dir, 6)]        built per thread, BF16, in shared memory
+//   F1  S = X W0^T                  (tcgen05, M 128, N 128, K = in_dim padded to 16)
+//       H0 = relu(S + b0)           -> shared memory (BF16), ReLU mask kept in registers
+//   F2  S = H0 W1^T                 (N 128, K 128)
+//       H1 = relu(S + b1), y = H1 W2^T, rgb = sigmoid(y)   (3 outputs: CUDA cores)
+// and for the backward (the forward recomputed, nothing stored between launches):
+//       dy = dL/drgb rgb (1 - rgb), dH1 = (dy W2) [H1 > 0] -> shared memory (BF16)
+//   B1  S  = dH1 W1                 (B = W1 read MN-major)
+//   B2  dW1 += dH1^T H0             (A = dH1, B = H0, both read MN-major; TMEM-resident over tiles)
+//       dH0 = S [H0 > 0]            -> shared memory, over H0 (consumed by B2)
+//   B3  dW0 += dH0^T X              (TMEM-resident over tiles)
+//   B4  S  = dH0 W0                 (the feature-related input columns only)
+//       dL/dfeat = chain rule through the positional encoding, written to grad_feat
+// dW2, db0 and db1 are reduced with warp shuffles into per-lane registers. At the end each CTA
+// adds its dW0 / dW1 (read from TMEM, one row per thread) and the register sums to the float32
+// gradients with one atomic per entry.
+//
+// Operands are stored once, in the core-matrix-row layout of tc_util.cuh, and read as K-major or
+// MN-major operands as each product needs (transposes cost nothing). TMEM columns (backward):
+// [0, S) the per-tile accumulator S, then dW1 (128), then dW0 (in_dim padded): at most 512.
+// Every wait on an mbarrier has an iteration limit: when it runs out the kernel reports
+// FF_ERR_LIMIT through `status`, stops, waits (again with a limit) for its MMAs and frees TMEM.
+#include "ff_common.cuh"
+#include "ff_internal.h"
+#include "tc_util.cuh"
+
+namespace ffgb {
+
+namespace {
+
+constexpr int kH = 128;        // hidden units of both hidden layers
+constexpr int kTile = 128;     // samples per tile = threads = TMEM lanes
+constexpr uint32_t kPolls = 1u << 22;  // mbarrier polls before a wait gives up (MMAs finish in microseconds)
+
+template <int C, int F, int V>
+struct Shape {
+  static constexpr int IN = 3 + C + 6 * V + 2 * F * C;
+  static constexpr int IN_PAD = (IN + 15) / 16 * 16;
+  static constexpr int NX = (C + 3 + 2 * F * C + 15) / 16 * 16;  // input columns whose gradient is needed
+  static constexpr int S_COLS = NX > 128 ? (NX + 31) / 32 * 32 : 128;
+  static constexpr int COL_DW1 = S_COLS;
+  static constexpr int COL_DW0 = S_COLS + 128;
+  static_assert(COL_DW0 + IN_PAD <= 512, "tensor-memory budget");
+  static_assert(NX <= 256 && IN_PAD <= 256, "MMA N limit");
+  static constexpr int W0_B = kH * IN_PAD * 2;
+  static constexpr int W1_B = kH * kH * 2;
+  static constexpr int X_B = kTile * IN_PAD * 2;
+  static constexpr int H_B = kTile * kH * 2;
+  static constexpr int F32_B = (3 * kH + 2 * kH) * 4;  // W2 [3][128], b0, b1
+  static constexpr int smem(bool bwd) { return W0_B + W1_B + X_B + H_B + (bwd ? H_B : 0) + F32_B + 64; }
+};
+
+struct HeadArgs {
+  const float* w[3];
+  const float* b[2];
+  const float* feat;
+  int feat_stride;
+  const float* rays;
+  const int32_t* app_idx;
+  const int32_t* app_ray;
+  int64_t n;
+  float* rgb_out;          // forward: rows app_idx of [M, 3]
+  const float* grad_rgb;   // backward: rows app_idx of [M, 3]
+  float* grad_feat;        // backward: channels 1..C of rows app_idx
+  float* gw[3];
+  float* gb[2];
+  int32_t* status;
+};
+
+// K-major / MN-major descriptors of a core-matrix-row buffer with `cols` columns: the 16-wide
+// K step s of a K-major operand (rows = M or N) starts at column 16 s; of an MN-major operand
+// (rows = K) at row 16 s. LBO = the core stride along K, SBO = along M / N.
+__device__ __forceinline__ uint64_t desc_k(uint32_t base, int cols, int s) {
+  return tc::smem_desc(base + (uint32_t)(s * 2 * 128), 128u, (uint32_t)(cols / 8 * 128));
+}
+__device__ __forceinline__ uint64_t desc_mn(uint32_t base, int cols, int s) {
+  return tc::smem_desc(base + (uint32_t)(s * 2 * (cols / 8) * 128), (uint32_t)(cols / 8 * 128), 128u);
+}
+
+__device__ __forceinline__ void st_shared_v4(uint32_t saddr, uint32_t a, uint32_t b, uint32_t c, uint32_t d) {
+  asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(saddr), "r"(a), "r"(b), "r"(c), "r"(d) : "memory");
+}
+
+// Eight consecutive values of row t (columns k0 .. k0 + 7, k0 % 8 == 0) as one 16-byte store.
+__device__ __forceinline__ void store8(uint32_t buf, int cols, int t, int k0, const float* v) {
+  st_shared_v4(buf + tc::core_off(t, k0, cols), tc::pack2_bf16(v[0], v[1]), tc::pack2_bf16(v[2], v[3]),
+               tc::pack2_bf16(v[4], v[5]), tc::pack2_bf16(v[6], v[7]));
+}
+
+// The head's input row of one sample, in the reference's column order, written as BF16 into row
+// t of X (zero for an invalid row and for the padding). sin / cos of x 2^f come from one sincosf
+// and the double-angle identities.
+template <int C, int F, int V>
+__device__ __forceinline__ void build_x(uint32_t X, int t, bool valid, const float* frow, const float* drow) {
+  using S = Shape<C, F, V>;
+  float fv[C], dv[3];
+#pragma unroll
+  for (int c = 0; c < C; ++c) fv[c] = valid ? frow[c] : 0.f;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) dv[i] = valid ? drow[i] : 0.f;
+  float buf[8];
+  int k = 0;  // compile-time after unrolling
+  auto emit = [&](float v) {
+    buf[k & 7] = v;
+    if ((k & 7) == 7) store8(X, S::IN_PAD, t, k - 7, buf);
+    ++k;
+  };
+#pragma unroll
+  for (int c = 0; c < C; ++c) emit(fv[c]);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) emit(dv[i]);
+  float cf[C][F];
+#pragma unroll
+  for (int c = 0; c < C; ++c) {
+    float s, co;
+    sincosf(fv[c], &s, &co);
+#pragma unroll
+    for (int f = 0; f < F; ++f) {
+      emit(s);
+      cf[c][f] = co;
+      const float s2 = 2.f * s * co, c2 = 1.f - 2.f * s * s;
+      s = s2;
+      co = c2;
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < C; ++c)
+#pragma unroll
+    for (int f = 0; f < F; ++f) emit(cf[c][f]);
+  float cd[3][V];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    float s, co;
+    sincosf(dv[i], &s, &co);
+#pragma unroll
+    for (int f = 0; f < V; ++f) {
+      emit(s);
+      cd[i][f] = co;
+      const float s2 = 2.f * s * co, c2 = 1.f - 2.f * s * s;
+      s = s2;
+      co = c2;
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int f = 0; f < V; ++f) emit(cd[i][f]);
+#pragma unroll
+  for (int p = S::IN; p < S::IN_PAD; ++p) emit(0.f);
+}
+
+// Warp reduce-scatter: lane l returns the sum over the warp's lanes of v[l].
+__device__ __forceinline__ float warp_reduce_scatter32(float* v, int lane) {
+#pragma unroll
+  for (int o = 16, n = 16; o >= 1; o >>= 1, n >>= 1) {
+    const bool upper = (lane & o) != 0;
+#pragma unroll
+    for (int i = 0; i < n; ++i) {
+      const float send = upper ? v[i] : v[i + n];
+      const float keep = upper ? v[i + n] : v[i];
+      v[i] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+    }
+  }
+  return v[0];
+}
+
+template <int C, int F, int V, bool BWD>
+__global__ void __launch_bounds__(kTile, 1) head_tc_kernel(const HeadArgs a) {
+  using S = Shape<C, F, V>;
+  extern __shared__ __align__(1024) unsigned char smem[];
+  const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+  unsigned char* p = smem;
+  const uint32_t sW0 = tc::smem_u32(p); p += S::W0_B;
+  const uint32_t sW1 = tc::smem_u32(p); p += S::W1_B;
+  const uint32_t sX = tc::smem_u32(p); p += S::X_B;
+  const uint32_t sH0 = tc::smem_u32(p); p += S::H_B;
+  uint32_t sDH1 = 0;
+  if constexpr (BWD) { sDH1 = tc::smem_u32(p); p += S::H_B; }
+  float* w2s = reinterpret_cast<float*>(p); p += 3 * kH * 4;
+  float* b0s = reinterpret_cast<float*>(p); p += kH * 4;
+  float* b1s = reinterpret_cast<float*>(p); p += kH * 4;
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(p);
+  uint32_t* taddr_s = reinterpret_cast<uint32_t*>(p + 8);
+  const uint32_t mb = tc::smem_u32(mbar);
+  constexpr uint32_t kTmemCols = BWD ? 512u : 128u;
+
+  // ---- weights -> shared memory (BF16 core layout; W2 and biases float32) ----
+  for (int e = t; e < kH * S::IN_PAD; e += kTile) {
+    const int r = e / S::IN_PAD, c = e % S::IN_PAD;
+    const float v = c < S::IN ? a.w[0][r * S::IN + c] : 0.f;
+    *reinterpret_cast<__nv_bfloat16*>(smem + tc::core_off(r, c, S::IN_PAD)) = __float2bfloat16_rn(v);
+  }
+  for (int e = t; e < kH * kH; e += kTile) {
+    const int r = e / kH, c = e % kH;
+    *reinterpret_cast<__nv_bfloat16*>(smem + S::W0_B + tc::core_off(r, c, kH)) = __float2bfloat16_rn(a.w[1][e]);
+  }
+  for (int e = t; e < 3 * kH; e += kTile) w2s[e] = a.w[2][e];
+  b0s[t] = a.b[0] ? a.b[0][t] : 0.f;
+  b1s[t] = a.b[1] ? a.b[1][t] : 0.f;
+  tc::fence_smem_to_async();
+  if (t == 0) {
+    tc::mbar_init(mb, 1);
+    tc::fence_mbar_init();
+  }
+  __syncthreads();
+  if (warp == 0) tc::tmem_alloc(tc::smem_u32(taddr_s), kTmemCols);
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = *taddr_s;
+  const uint32_t lane_off = (uint32_t)(warp * 32) << 16;
+  const uint32_t tS = tmem;
+  const uint32_t tDW1 = tmem + S::COL_DW1, tDW0 = tmem + S::COL_DW0;
+
+  uint32_t phase = 0;
+  bool ok = true, any_tile = false;
+  float acc_db0[4] = {0.f, 0.f, 0.f, 0.f}, acc_db1[4] = {0.f, 0.f, 0.f, 0.f};
+  float acc_dw2[3][4] = {};
+
+  // waits for the MMAs committed last; all threads agree on the outcome
+  auto wait_mma = [&]() {
+    const bool done = tc::mbar_wait(mb, phase & 1u, kPolls);
+    ++phase;
+    ok = __syncthreads_and(done) != 0;
+    tc::fence_after_sync();
+    return ok;
+  };
+
+  const int64_t n_tiles = ceil_div(a.n, kTile);
+  for (int64_t tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x) {
+    const int64_t row = tile * kTile + t;
+    const bool valid = row < a.n;
+    const int64_t sidx = valid ? (int64_t)a.app_idx[row] : 0;
+    const float* frow = a.feat + sidx * a.feat_stride + 1;
+    const float* drow = a.rays + (valid ? (int64_t)a.app_ray[row] : 0) * 6 + 3;
+    // ---- X ----
+    build_x<C, F, V>(sX, t, valid, frow, drow);
+    tc::fence_smem_to_async();
+    tc::fence_before_sync();
+    __syncthreads();
+    // ---- F1: S = X W0^T ----
+    if (t == 0) {
+      tc::fence_after_sync();
+      const uint32_t id = tc::idesc_bf16(128, kH, false, false);
+#pragma unroll 1
+      for (int s = 0; s < S::IN_PAD / 16; ++s)
+        tc::mma_bf16(tS, desc_k(sX, S::IN_PAD, s), desc_k(sW0, S::IN_PAD, s), id, s > 0);
+      tc::mma_commit(mb);
+    }
+    if (!wait_mma()) break;
+    // ---- H0 = relu(S + b0) ----
+    uint32_t mask0[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      float v[32];
+      tc::tmem_ld32(tS + lane_off + q * 32, v);
+      uint32_t m = 0;
+#pragma unroll
+      for (int j = 0; j < 32; ++j) {
+        const float h = v[j] + b0s[q * 32 + j];
+        m |= (h > 0.f ? 1u : 0u) << j;
+        v[j] = fmaxf(h, 0.f);
+      }
+      mask0[q] = m;
+#pragma unroll
+      for (int g = 0; g < 4; ++g) store8(sH0, kH, t, q * 32 + g * 8, v + g * 8);
+    }
+    tc::fence_smem_to_async();
+    tc::fence_before_sync();
+    __syncthreads();
+    // ---- F2: S = H0 W1^T ----
+    if (t == 0) {
+      tc::fence_after_sync();
+      const uint32_t id = tc::idesc_bf16(128, kH, false, false);
+#pragma unroll 1
+      for (int s = 0; s < kH / 16; ++s) tc::mma_bf16(tS, desc_k(sH0, kH, s), desc_k(sW1, kH, s), id, s > 0);
+      tc::mma_commit(mb);
+    }
+    if (!wait_mma()) break;
+    // ---- y = relu(S + b1) W2^T, rgb = sigmoid(y) ----
+    float y[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      float v[32];
+      tc::tmem_ld32(tS + lane_off + q * 32, v);
+#pragma unroll
+      for (int j = 0; j < 32; ++j) {
+        const float h = fmaxf(v[j] + b1s[q * 32 + j], 0.f);
+#pragma unroll
+        for (int o = 0; o < 3; ++o) y[o] += h * w2s[o * kH + q * 32 + j];
+      }
+    }
+    float rgb[3];
+#pragma unroll
+    for (int o = 0; o < 3; ++o) rgb[o] = 1.f / (1.f + expf(-y[o]));
+    if constexpr (!BWD) {
+      if (valid) {
+#pragma unroll
+        for (int o = 0; o < 3; ++o) a.rgb_out[sidx * 3 + o] = rgb[o];
+      }
+      tc::fence_before_sync();
+      __syncthreads();  // S is read before the next tile's F1 overwrites it
+      any_tile = true;
+      continue;
+    } else {
+      float dy[3];
+#pragma unroll
+      for (int o = 0; o < 3; ++o) dy[o] = valid ? a.grad_rgb[sidx * 3 + o] * rgb[o] * (1.f - rgb[o]) : 0.f;
+      // dH1 = (dy W2) [H1 > 0]; dW2 += dy^T H1, db1 += sum dH1 (warp reduce-scatter per chunk)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        float v[32], dh[32];
+        tc::tmem_ld32(tS + lane_off + q * 32, v);
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+          const int u = q * 32 + j;
+          const float h = fmaxf(v[j] + b1s[u], 0.f);
+          dh[j] = h > 0.f ? dy[0] * w2s[u] + dy[1] * w2s[kH + u] + dy[2] * w2s[2 * kH + u] : 0.f;
+          v[j] = h;
+        }
+#pragma unroll
+        for (int g = 0; g < 4; ++g) store8(sDH1, kH, t, q * 32 + g * 8, dh + g * 8);
+        acc_db1[q] += warp_reduce_scatter32(dh, lane);
+#pragma unroll
+        for (int o = 0; o < 3; ++o) {
+          float pr[32];
+#pragma unroll
+          for (int j = 0; j < 32; ++j) pr[j] = dy[o] * v[j];
+          acc_dw2[o][q] += warp_reduce_scatter32(pr, lane);
+        }
+      }
+      tc::fence_smem_to_async();
+      tc::fence_before_sync();
+      __syncthreads();
+      // ---- B1: S = dH1 W1;  B2: dW1 += dH1^T H0 ----
+      if (t == 0) {
+        tc::fence_after_sync();
+        const uint32_t id1 = tc::idesc_bf16(128, kH, false, true);
+#pragma unroll 1
+        for (int s = 0; s < kH / 16; ++s) tc::mma_bf16(tS, desc_k(sDH1, kH, s), desc_mn(sW1, kH, s), id1, s > 0);
+        const uint32_t id2 = tc::idesc_bf16(128, kH, true, true);
+#pragma unroll 1
+        for (int s = 0; s < kTile / 16; ++s)
+          tc::mma_bf16(tDW1, desc_mn(sDH1, kH, s), desc_mn(sH0, kH, s), id2, (any_tile || s > 0) ? 1u : 0u);
+        tc::mma_commit(mb);
+      }
+      if (!wait_mma()) break;
+      // ---- dH0 = S [H0 > 0] (over H0), db0 ----
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        float v[32];
+        tc::tmem_ld32(tS + lane_off + q * 32, v);
+#pragma unroll
+        for (int j = 0; j < 32; ++j) v[j] = ((mask0[q] >> j) & 1u) ? v[j] : 0.f;
+#pragma unroll
+        for (int g = 0; g < 4; ++g) store8(sH0, kH, t, q * 32 + g * 8, v + g * 8);
+        acc_db0[q] += warp_reduce_scatter32(v, lane);
+      }
+      tc::fence_smem_to_async();
+      tc::fence_before_sync();
+      __syncthreads();
+      // ---- B3: dW0 += dH0^T X;  B4: S = dH0 W0 (columns [0, NX)) ----
+      if (t == 0) {
+        tc::fence_after_sync();
+        const uint32_t id3 = tc::idesc_bf16(128, S::IN_PAD, true, true);
+#pragma unroll 1
+        for (int s = 0; s < kTile / 16; ++s)
+          tc::mma_bf16(tDW0, desc_mn(sH0, kH, s), desc_mn(sX, S::IN_PAD, s), id3, (any_tile || s > 0) ? 1u : 0u);
+        const uint32_t id4 = tc::idesc_bf16(128, S::NX, false, true);
+#pragma unroll 1
+        for (int s = 0; s < kH / 16; ++s) tc::mma_bf16(tS, desc_k(sH0, kH, s), desc_mn(sW0, S::IN_PAD, s), id4, s > 0);
+        tc::mma_commit(mb);
+      }
+      if (!wait_mma()) break;
+      any_tile = true;
+      // ---- dL/dfeat through the positional encoding ----
+      float gf[C];
+      float sn[C], cs[C];
+#pragma unroll
+      for (int c = 0; c < C; ++c) {
+        gf[c] = 0.f;
+        sincosf(valid ? frow[c] : 0.f, &sn[c], &cs[c]);
+      }
+      // 32-column loads over [0, NX rounded up to 32) (inside S); columns past NX are ignored
+#pragma unroll
+      for (int q = 0; q < (S::NX + 31) / 32; ++q) {
+        float v[32];
+        tc::tmem_ld32(tS + lane_off + q * 32, v);
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+          const int k = q * 32 + j;
+          if (k >= S::NX) continue;
+          if (k < C) {
+            gf[k] += v[j];
+          } else if (k >= C + 3 && k < C + 3 + 2 * F * C) {
+            const bool cosine = k >= C + 3 + F * C;
+            const int jj = k - C - 3 - (cosine ? F * C : 0);
+            const int c = jj / F, f = jj % F;
+            // sin / cos of x 2^f by repeated doubling, d/dx = 2^f (cos, -sin)
+            float s = sn[c], co = cs[c];
+#pragma unroll
+            for (int r = 0; r < f; ++r) {
+              const float s2 = 2.f * s * co, c2 = 1.f - 2.f * s * s;
+              s = s2;
+              co = c2;
+            }
+            gf[c] += (float)(1 << f) * (cosine ? -s : co) * v[j];
+          }
+        }
+      }
+      if (valid) {
+        float* gr = a.grad_feat + sidx * a.feat_stride + 1;
+#pragma unroll
+        for (int c = 0; c < C; ++c) gr[c] = gf[c];
+      }
+      tc::fence_before_sync();
+      __syncthreads();
+    }
+  }
+
+  if (!ok) {
+    if (t == 0 && a.status) atomicExch(a.status, FF_ERR_LIMIT);
+    (void)tc::mbar_wait(mb, phase & 1u, kPolls);  // the MMAs in flight, if they ever finish
+  } else if (BWD && any_tile) {
+    // ---- flush: dW1 / dW0 rows from TMEM (row = this thread's lane), the register sums ----
+#pragma unroll 1
+    for (int q = 0; q < kH / 32; ++q) {
+      float v[32];
+      tc::tmem_ld32(tDW1 + lane_off + q * 32, v);
+      if (a.gw[1])
+#pragma unroll
+        for (int j = 0; j < 32; ++j) atomicAdd(a.gw[1] + t * kH + q * 32 + j, v[j]);
+    }
+#pragma unroll 1
+    for (int q = 0; q < (S::IN_PAD + 31) / 32; ++q) {
+      float v[32];
+      tc::tmem_ld32(tDW0 + lane_off + q * 32, v);  // columns past IN_PAD (inside the allocation) unused
+      if (a.gw[0])
+#pragma unroll
+        for (int j = 0; j < 32; ++j)
+          if (q * 32 + j < S::IN) atomicAdd(a.gw[0] + t * S::IN + q * 32 + j, v[j]);
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      if (a.gb[0]) atomicAdd(a.gb[0] + q * 32 + lane, acc_db0[q]);
+      if (a.gb[1]) atomicAdd(a.gb[1] + q * 32 + lane, acc_db1[q]);
+#pragma unroll
+      for (int o = 0; o < 3; ++o)
+        if (a.gw[2]) atomicAdd(a.gw[2] + o * kH + q * 32 + lane, acc_dw2[o][q]);
+    }
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tmem, kTmemCols);
+}
+
+template <int C, int F, int V, bool BWD>
+cudaError_t launch_tc(const HeadArgs& a, cudaStream_t s) {
+  constexpr int smem = Shape<C, F, V>::smem(BWD);
+  auto kern = head_tc_kernel<C, F, V, BWD>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return e;
+  const int64_t tiles = ceil_div(a.n, kTile);
+  const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>(tiles, (int64_t)sm_count()));
+  kern<<<blocks, kTile, smem, s>>>(a);
+  return cudaGetLastError();
+}
+
+template <bool BWD>
+cudaError_t dispatch_tc(const FFRenderMlp& h, const HeadArgs& a, cudaStream_t s) {
+  if (h.fea_pe == 2 && h.view_pe == 6) {
+    if (h.in_channels == 27) return launch_tc<27, 2, 6, BWD>(a, s);
+    if (h.in_channels == 31) return launch_tc<31, 2, 6, BWD>(a, s);
+  }
+  return cudaErrorInvalidValue;
+}
+
+HeadArgs head_args(const FFRenderMlp& h, const float* feat, int feat_stride, const float* rays,
+                   const int32_t* app_idx, const int32_t* app_ray, int64_t n, int32_t* status) {
+  HeadArgs a = {};
+  for (int l = 0; l < 3; ++l) a.w[l] = h.weight[l];
+  a.b[0] = h.bias[0];
+  a.b[1] = h.bias[1];
+  a.feat = feat;
+  a.feat_stride = feat_stride;
+  a.rays = rays;
+  a.app_idx = app_idx;
+  a.app_ray = app_ray;
+  a.n = n;
+  a.status = status;
+  return a;
+}
+
+}  // namespace
+
+const char* render_head_tc_unsupported(const FFRenderMlp& h) {
+  if (h.n_layers != 3 || h.hidden_dim != kH) return "the tensor-core head needs num_layers = 3 and hidden_dim = 128";
+  if (h.fea_pe != 2 || h.view_pe != 6) return "the tensor-core head needs fea_pe = 2 and view_pe = 6";
+  if (h.in_channels != 27 && h.in_channels != 31)
+    return "the tensor-core head needs in_channels 27 or 31 (model.out_dim 28 or 32)";
+  return nullptr;
+}
+
+cudaError_t launch_render_head_tc_forward(const FFRenderMlp& h, const float* feat, int feat_stride, const float* rays,
+                                          const int32_t* app_idx, const int32_t* app_ray, int64_t n, float* rgb_rows,
+                                          int32_t* status, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  HeadArgs a = head_args(h, feat, feat_stride, rays, app_idx, app_ray, n, status);
+  a.rgb_out = rgb_rows;
+  return dispatch_tc<false>(h, a, s);
+}
+
+cudaError_t launch_render_head_tc_backward(const FFRenderMlp& h, const float* feat, int feat_stride, const float* rays,
+                                           const int32_t* app_idx, const int32_t* app_ray, int64_t n,
+                                           const float* grad_rgb_rows, float* grad_feat, const FFMlpGrad& g,
+                                           int32_t* status, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  HeadArgs a = head_args(h, feat, feat_stride, rays, app_idx, app_ray, n, status);
+  a.grad_rgb = grad_rgb_rows;
+  a.grad_feat = grad_feat;
+  for (int l = 0; l < 3; ++l) a.gw[l] = g.weight[l];
+  a.gb[0] = g.bias[0];
+  a.gb[1] = g.bias[1];
+  return dispatch_tc<true>(h, a, s);
+}
+
+}  // namespace ffgb

@@ -387,13 +387,20 @@ __device__ __forceinline__ void sample_rgb(const float* feat_row, const float* y
   }
 }
 
+// Colour source of the compositing kernels: the SH-2 head evaluated from the feature row
+// (kColSH), or per-sample colours computed beforehand by another head (kColExt: rgb_sample
+// [M, 3], read for the samples whose weight passes the threshold; MLPRender_Fea, :884-885).
+enum { kColSH = 0, kColExt = 1 };
+
+template <int kCol>
 __global__ void __launch_bounds__(kRayWarps * 32) composite_forward_kernel(
     const FFRender r, const float* __restrict__ rays, const float* __restrict__ jitter, int64_t n_rays,
     const int64_t* __restrict__ offsets, const int32_t* __restrict__ sample_idx, const float* __restrict__ feat,
     int feat_stride, const int32_t* __restrict__ white_bg, float* __restrict__ rgb_out, float* __restrict__ depth_out,
-    float* __restrict__ acc_out, const float* __restrict__ zd, float* __restrict__ w_out) {
+    float* __restrict__ acc_out, const float* __restrict__ zd, float* __restrict__ w_out,
+    const float* __restrict__ rgb_sample) {
   const int lane = threadIdx.x & 31;
-  const bool vec = rows_vec(feat, feat_stride);
+  const bool vec = kCol == kColSH && rows_vec(feat, feat_stride);
   for (int64_t ray = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; ray < n_rays;
        ray += ((int64_t)gridDim.x * blockDim.x) >> 5) {
     const RayGeo g = ray_setup(r, rays, jitter, ray);
@@ -407,7 +414,10 @@ __global__ void __launch_bounds__(kRayWarps * 32) composite_forward_kernel(
       SampleVals s = {0.f, 0.f, 0.f, 0.f, 0.f, 1.f};
       float row[kRow];
       if (active) {
-        load_row(feat + j * feat_stride, vec, row);
+        if constexpr (kCol == kColSH)
+          load_row(feat + j * feat_stride, vec, row);
+        else
+          row[0] = feat[j * feat_stride];
         s = sample_vals(r, g, zd ? 0 : sample_idx[j], row, zd ? zd + 2 * j : nullptr);
       }
       float excl;
@@ -417,8 +427,13 @@ __global__ void __launch_bounds__(kRayWarps * 32) composite_forward_kernel(
       acc += w;
       depth += w * s.z;
       if (active && w > r.weight_thres) {
-        float c[3], lin[3];
-        sample_rgb(row, yb, c, lin);
+        float c[3];
+        if constexpr (kCol == kColSH) {
+          float lin[3];
+          sample_rgb(row, yb, c, lin);
+        } else {
+          c[0] = rgb_sample[j * 3]; c[1] = rgb_sample[j * 3 + 1]; c[2] = rgb_sample[j * 3 + 2];
+        }
         col[0] += w * c[0]; col[1] += w * c[1]; col[2] += w * c[2];
       }
       T *= prod;
@@ -440,13 +455,18 @@ __global__ void __launch_bounds__(kRayWarps * 32) composite_forward_kernel(
   }
 }
 
+// kColExt: grad_feat rows get dL/dfeat0 in channel 0 and zeros in channels 1 .. feat_stride - 1
+// (the colour head's backward fills the channels of its samples afterwards), and
+// grad_rgb_sample [M, 3] receives dL/dcolour = w * dL/drgb (zero below the weight threshold).
+template <int kCol>
 __global__ void __launch_bounds__(kRayWarps * 32) composite_backward_kernel(
     const FFRender r, const float* __restrict__ rays, const float* __restrict__ jitter, int64_t n_rays,
     const int64_t* __restrict__ offsets, const int32_t* __restrict__ sample_idx, const float* __restrict__ feat,
     int feat_stride, const int32_t* __restrict__ white_bg, const float* __restrict__ grad_rgb,
-    float* __restrict__ grad_feat, const float* __restrict__ zd) {
+    float* __restrict__ grad_feat, const float* __restrict__ zd, const float* __restrict__ rgb_sample,
+    float* __restrict__ grad_rgb_sample) {
   const int lane = threadIdx.x & 31;
-  const bool vec = rows_vec(feat, feat_stride) && rows_vec(grad_feat, feat_stride);
+  const bool vec = kCol == kColSH && rows_vec(feat, feat_stride) && rows_vec(grad_feat, feat_stride);
   for (int64_t ray = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; ray < n_rays;
        ray += ((int64_t)gridDim.x * blockDim.x) >> 5) {
     const RayGeo g = ray_setup(r, rays, jitter, ray);
@@ -463,7 +483,10 @@ __global__ void __launch_bounds__(kRayWarps * 32) composite_backward_kernel(
       SampleVals s = {0.f, 0.f, 0.f, 0.f, 0.f, 1.f};
       float row[kRow];
       if (active) {
-        load_row(feat + j * feat_stride, vec, row);
+        if constexpr (kCol == kColSH)
+          load_row(feat + j * feat_stride, vec, row);
+        else
+          row[0] = feat[j * feat_stride];
         s = sample_vals(r, g, zd ? 0 : sample_idx[j], row, zd ? zd + 2 * j : nullptr);
       }
       float excl;
@@ -474,8 +497,13 @@ __global__ void __launch_bounds__(kRayWarps * 32) composite_backward_kernel(
       if (active) {
         grad_feat[j * feat_stride] = Tj;
         if (w > r.weight_thres) {
-          float c[3], lin[3];
-          sample_rgb(row, yb, c, lin);
+          float c[3];
+          if constexpr (kCol == kColSH) {
+            float lin[3];
+            sample_rgb(row, yb, c, lin);
+          } else {
+            c[0] = rgb_sample[j * 3]; c[1] = rgb_sample[j * 3 + 1]; c[2] = rgb_sample[j * 3 + 2];
+          }
           col[0] += w * c[0]; col[1] += w * c[1]; col[2] += w * c[2];
         }
       }
@@ -501,12 +529,21 @@ __global__ void __launch_bounds__(kRayWarps * 32) composite_backward_kernel(
       bool app = false;
       float w = 0.f, gw = 0.f;
       if (active) {
-        load_row(feat + j * feat_stride, vec, row);
+        if constexpr (kCol == kColSH)
+          load_row(feat + j * feat_stride, vec, row);
+        else
+          row[0] = feat[j * feat_stride];
         s = sample_vals(r, g, zd ? 0 : sample_idx[j], row, zd ? zd + 2 * j : nullptr);
         Tj = grad_feat[j * feat_stride];
         w = s.alpha * Tj;
         app = w > r.weight_thres;
-        if (app) sample_rgb(row, yb, c, lin);
+        if (app) {
+          if constexpr (kCol == kColSH) {
+            sample_rgb(row, yb, c, lin);
+          } else {
+            c[0] = rgb_sample[j * 3]; c[1] = rgb_sample[j * 3 + 1]; c[2] = rgb_sample[j * 3 + 2];
+          }
+        }
 #pragma unroll
         for (int q = 0; q < 3; ++q) gw += G[q] * (c[q] - (wb ? 1.f : 0.f));
       }
@@ -534,17 +571,83 @@ __global__ void __launch_bounds__(kRayWarps * 32) composite_backward_kernel(
           g_f0 = (x > 20.f) ? g_sigma : g_sigma * sigmoidf(x);
         else
           g_f0 = x > 0.f ? g_sigma : 0.f;
-        float out[kRow];
-        out[0] = g_f0;
+        if constexpr (kCol == kColSH) {
+          float out[kRow];
+          out[0] = g_f0;
 #pragma unroll
-        for (int q = 0; q < 3; ++q) {
-          const float gl = app ? G[q] * w * c[q] * (1.f - c[q]) : 0.f;
+          for (int q = 0; q < 3; ++q) {
+            const float gl = app ? G[q] * w * c[q] * (1.f - c[q]) : 0.f;
 #pragma unroll
-          for (int k = 0; k < 9; ++k) out[1 + q * 9 + k] = gl * yb[k];
+            for (int k = 0; k < 9; ++k) out[1 + q * 9 + k] = gl * yb[k];
+          }
+          store_row(grad_feat + j * feat_stride, vec, out);
+        } else {
+          float* gr = grad_feat + j * feat_stride;
+          gr[0] = g_f0;
+          for (int k = 1; k < feat_stride; ++k) gr[k] = 0.f;
+#pragma unroll
+          for (int q = 0; q < 3; ++q) grad_rgb_sample[j * 3 + q] = app ? G[q] * w : 0.f;
         }
-        store_row(grad_feat + j * feat_stride, vec, out);
       }
       carry = new_carry;
+    }
+  }
+}
+
+// The compositing weights alone (the forward's scan without colours): w_out [M] and, per ray,
+// the number of samples whose weight passes the threshold (app_mask, :879-881).
+__global__ void __launch_bounds__(kRayWarps * 32) composite_weights_kernel(
+    const FFRender r, const float* __restrict__ rays, const float* __restrict__ jitter, int64_t n_rays,
+    const int64_t* __restrict__ offsets, const int32_t* __restrict__ sample_idx, const float* __restrict__ feat,
+    int feat_stride, float* __restrict__ w_out, int32_t* __restrict__ app_counts) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t ray = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; ray < n_rays;
+       ray += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+    const RayGeo g = ray_setup(r, rays, jitter, ray);
+    const int64_t beg = offsets[ray], end = offsets[ray + 1];
+    float T = 1.f;
+    int cnt = 0;
+    for (int64_t c0 = beg; c0 < end; c0 += 32) {
+      const int64_t j = c0 + lane;
+      const bool active = j < end;
+      SampleVals s = {0.f, 0.f, 0.f, 0.f, 0.f, 1.f};
+      if (active) {
+        const float f0 = feat[j * feat_stride];
+        s = sample_vals(r, g, sample_idx[j], &f0);
+      }
+      float excl;
+      const float prod = excl_trans(s.fac, lane, excl);
+      const float w = active ? s.alpha * (T * excl) : 0.f;
+      if (active) w_out[j] = w;
+      cnt += __popc(__ballot_sync(0xffffffffu, active && w > r.weight_thres));
+      T *= prod;
+    }
+    if (lane == 0) app_counts[ray] = cnt;
+  }
+}
+
+// The samples whose weight passes the threshold, in ray-major order (feat[app_mask] of :884):
+// app_idx = live-sample index, app_ray = its ray, from the scanned per-ray counts.
+__global__ void __launch_bounds__(kRayWarps * 32) app_emit_kernel(int64_t n_rays, const int64_t* __restrict__ offsets,
+                                                                 const float* __restrict__ w, float thres,
+                                                                 const int64_t* __restrict__ app_offsets,
+                                                                 int32_t* __restrict__ app_idx,
+                                                                 int32_t* __restrict__ app_ray) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t ray = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; ray < n_rays;
+       ray += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+    const int64_t beg = offsets[ray], end = offsets[ray + 1];
+    int64_t pos = app_offsets[ray];
+    for (int64_t c0 = beg; c0 < end; c0 += 32) {
+      const int64_t j = c0 + lane;
+      const bool app = j < end && w[j] > thres;
+      const uint32_t m = __ballot_sync(0xffffffffu, app);
+      if (app) {
+        const int64_t k = pos + __popc(m & ((1u << lane) - 1u));
+        app_idx[k] = (int32_t)j;
+        app_ray[k] = (int32_t)ray;
+      }
+      pos += __popc(m);
     }
   }
 }
@@ -634,8 +737,35 @@ cudaError_t launch_composite_forward(const FFRender& r, const float* rays, const
                                      int feat_stride, const int32_t* white_bg, float* rgb, float* depth, float* acc,
                                      const float* zd, float* w_out, cudaStream_t s) {
   if (n == 0) return cudaSuccess;
-  composite_forward_kernel<<<ray_blocks(n), kRayWarps * 32, 0, s>>>(r, rays, jitter, n, offsets, sample_idx, feat,
-                                                                     feat_stride, white_bg, rgb, depth, acc, zd, w_out);
+  composite_forward_kernel<kColSH><<<ray_blocks(n), kRayWarps * 32, 0, s>>>(
+      r, rays, jitter, n, offsets, sample_idx, feat, feat_stride, white_bg, rgb, depth, acc, zd, w_out, nullptr);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_composite_forward_rgb(const FFRender& r, const float* rays, const float* jitter, int64_t n,
+                                         const int64_t* offsets, const int32_t* sample_idx, const float* feat,
+                                         int feat_stride, const float* rgb_sample, const int32_t* white_bg, float* rgb,
+                                         float* depth, float* acc, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  composite_forward_kernel<kColExt><<<ray_blocks(n), kRayWarps * 32, 0, s>>>(
+      r, rays, jitter, n, offsets, sample_idx, feat, feat_stride, white_bg, rgb, depth, acc, nullptr, nullptr,
+      rgb_sample);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_composite_weights(const FFRender& r, const float* rays, const float* jitter, int64_t n,
+                                     const int64_t* offsets, const int32_t* sample_idx, const float* feat,
+                                     int feat_stride, float* w_out, int32_t* app_counts, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  composite_weights_kernel<<<ray_blocks(n), kRayWarps * 32, 0, s>>>(r, rays, jitter, n, offsets, sample_idx, feat,
+                                                                     feat_stride, w_out, app_counts);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_app_emit(int64_t n, const int64_t* offsets, const float* w, float thres, const int64_t* app_offsets,
+                            int32_t* app_idx, int32_t* app_ray, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  app_emit_kernel<<<ray_blocks(n), kRayWarps * 32, 0, s>>>(n, offsets, w, thres, app_offsets, app_idx, app_ray);
   return cudaGetLastError();
 }
 
@@ -644,8 +774,20 @@ cudaError_t launch_composite_backward(const FFRender& r, const float* rays, cons
                                       int feat_stride, const int32_t* white_bg, const float* grad_rgb,
                                       float* grad_feat, const float* zd, cudaStream_t s) {
   if (n == 0) return cudaSuccess;
-  composite_backward_kernel<<<ray_blocks(n), kRayWarps * 32, 0, s>>>(r, rays, jitter, n, offsets, sample_idx, feat,
-                                                                      feat_stride, white_bg, grad_rgb, grad_feat, zd);
+  composite_backward_kernel<kColSH><<<ray_blocks(n), kRayWarps * 32, 0, s>>>(
+      r, rays, jitter, n, offsets, sample_idx, feat, feat_stride, white_bg, grad_rgb, grad_feat, zd, nullptr, nullptr);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_composite_backward_rgb(const FFRender& r, const float* rays, const float* jitter, int64_t n,
+                                          const int64_t* offsets, const int32_t* sample_idx, const float* feat,
+                                          int feat_stride, const float* rgb_sample, const int32_t* white_bg,
+                                          const float* grad_rgb, float* grad_feat, float* grad_rgb_sample,
+                                          cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  composite_backward_kernel<kColExt><<<ray_blocks(n), kRayWarps * 32, 0, s>>>(
+      r, rays, jitter, n, offsets, sample_idx, feat, feat_stride, white_bg, grad_rgb, grad_feat, nullptr, rgb_sample,
+      grad_rgb_sample);
   return cudaGetLastError();
 }
 

@@ -1,12 +1,16 @@
-"""Renderer surface: render_ray (renderer.py:8-27), the SH-2 colour head, the occupancy mask and
+"""Renderer surface: render_ray (renderer.py:8-27), the colour heads (MLPRender_Fea,
+models/FactorFields.py:162-203, and the degree-2 SH head), the occupancy mask and
 FactorFields.forward (models/FactorFields.py:843-898) for bounded scenes, on the native
 march / compact / composite kernels.
 
 Per chunk of rays: ff_march_count -> ff_scan_counts -> ff_march_emit give the live samples in
 the reference's order (xyz_sampled[ray_valid]); the field + MLP head runs on them (drop-in
-float32 kernels, or the fused BF16 kernel); ff_composite_forward alpha-composites. The backward
-is ff_composite_backward followed by the field/MLP backward kernels. One host synchronisation
-per chunk reads the number of live samples (the reference synchronises on ray_valid.any()).
+float32 kernels, or the fused BF16 kernel). With the SH head, ff_composite_forward evaluates the
+colours and alpha-composites in one pass. With MLPRender_Fea, ff_composite_weights gives the
+weights, ff_app_emit lists the samples above the weight threshold (app_mask), the colour head
+runs on them and ff_composite_forward_rgb composites. The backward runs the same chain in
+reverse. One host synchronisation per chunk reads the number of live samples (the reference
+synchronises on ray_valid.any()), and one more the number of head samples (app_mask.any()).
 """
 import ctypes
 import math
@@ -61,11 +65,144 @@ def pack_bits(flags):
     return words.to(torch.int32).contiguous()
 
 
+class MLPRender_Fea(torch.nn.Module):
+    """models/FactorFields.py:162-203: rgb = sigmoid(MLP([features, viewdirs, PE(features, feape),
+    PE(viewdirs, viewpe)])), Linear + ReLU per hidden layer, the last Linear (to 3) without bias.
+    Same parameter names (mlp.i.weight / bias) and initialisation as the reference; the math runs
+    on the native kernels (float32 drop-in, or the tensor-core head on the fused BF16 path)."""
+
+    def __init__(self, inChanel, num_layers=3, hidden_dim=64, viewpe=6, feape=2):
+        super().__init__()
+        self.in_mlpC = 3 + inChanel + 2 * viewpe * 3 + 2 * feape * inChanel
+        self.in_channels, self.num_layers, self.hidden_dim = inChanel, num_layers, hidden_dim
+        self.viewpe, self.feape = viewpe, feape
+        layers = []
+        for l in range(num_layers):
+            din = self.in_mlpC if l == 0 else hidden_dim
+            last = l == num_layers - 1
+            layers.append(torch.nn.Linear(din, 3 if last else hidden_dim, bias=not last))
+        self.mlp = torch.nn.ModuleList(layers)
+
+    def params(self):
+        return [l.weight for l in self.mlp], [l.bias for l in self.mlp]
+
+    def forward(self, viewdirs, features):
+        """Colours [N, 3] of N samples from their view directions [N, 3] and features [N, C]."""
+        return HeadFunction.apply(features, viewdirs, self, *[p for p in self.parameters()])
+
+
+def head_struct(head):
+    """FFRenderMlp of an MLPRender_Fea module (float32 parameters, contiguous)."""
+    h = N.FFRenderMlp()
+    h.n_layers, h.in_channels, h.hidden_dim = head.num_layers, head.in_channels, head.hidden_dim
+    h.view_pe, h.fea_pe, h.in_dim = head.viewpe, head.feape, head.in_mlpC
+    ws, bs = head.params()
+    for i, (w, b) in enumerate(zip(ws, bs)):
+        h.weight[i] = w.data_ptr()
+        h.bias[i] = b.data_ptr() if b is not None else None
+    return h
+
+
+def _head_workspace(h, n):
+    need = int(N.lib().ff_render_head_workspace_bytes(ctypes.byref(h), n))
+    N.check(0 if need >= 0 else need, "ff_render_head_workspace_bytes")
+    return torch.empty(max(need, 256), dtype=torch.uint8, device="cuda"), need
+
+
+def head_tc_supported(head):
+    """The tensor-core head's shapes: 3 layers, 128 hidden, fea_pe 2, view_pe 6, C = 27 or 31."""
+    return (head.num_layers == 3 and head.hidden_dim == 128 and head.feape == 2 and head.viewpe == 6
+            and head.in_channels in (27, 31))
+
+
+def head_forward(head, feat, rays, app_idx, app_ray, rgb_sample, tc=False, status=None):
+    """rgb_sample[app_idx[i]] = colour of app sample i (features = feat[app_idx[i], 1:], direction =
+    rays[app_ray[i], 3:6]): the float32 drop-in head, or with tc the tensor-core head (BF16
+    operands, FP32 accumulation; status: optional device int32 for a bounded-wait failure)."""
+    n = app_idx.shape[0]
+    if n == 0:
+        return
+    h = head_struct(head)
+    if tc:
+        N.call("ff_render_head_forward_tc", ctypes.byref(h), N.ptr(feat), feat.shape[1], N.ptr(rays), N.ptr(app_idx),
+               N.ptr(app_ray), n, N.ptr(rgb_sample), N.ptr(status), N.stream_ptr())
+        return
+    ws, need = _head_workspace(h, n)
+    N.call("ff_render_head_forward", ctypes.byref(h), N.ptr(feat), feat.shape[1], N.ptr(rays), N.ptr(app_idx),
+           N.ptr(app_ray), n, N.ptr(rgb_sample), N.ptr(ws), need, N.stream_ptr(), kernels=1 + head.num_layers)
+
+
+def head_backward(head, feat, rays, app_idx, app_ray, g_rgb_sample, g_feat, direct=True, tc=False, status=None):
+    """Backward of head_forward: g_feat rows app_idx, channels 1..C (overwritten); the head's
+    parameter gradients accumulated into their .grad (direct) or returned as a list."""
+    ws_, bs_ = head.params()
+    if direct:
+        gw = [_direct_grad(w) for w in ws_]
+        gb = [_direct_grad(b) if b is not None else None for b in bs_]
+    else:
+        gw = [torch.zeros_like(w) for w in ws_]
+        gb = [torch.zeros_like(b) if b is not None else None for b in bs_]
+    n = app_idx.shape[0]
+    if n:
+        h = head_struct(head)
+        g = N.FFMlpGrad()
+        for i in range(len(gw)):
+            g.weight[i] = gw[i].data_ptr()
+            g.bias[i] = gb[i].data_ptr() if gb[i] is not None else None
+        if tc:
+            N.call("ff_render_head_backward_tc", ctypes.byref(h), N.ptr(feat), feat.shape[1], N.ptr(rays),
+                   N.ptr(app_idx), N.ptr(app_ray), n, N.ptr(g_rgb_sample), N.ptr(g_feat), ctypes.byref(g),
+                   N.ptr(status), N.stream_ptr())
+            return gw, gb
+        ws, need = _head_workspace(h, n)
+        n_bias = sum(1 for b in bs_ if b is not None)
+        N.call("ff_render_head_backward", ctypes.byref(h), N.ptr(feat), feat.shape[1], N.ptr(rays), N.ptr(app_idx),
+               N.ptr(app_ray), n, N.ptr(g_rgb_sample), N.ptr(g_feat), ctypes.byref(g), N.ptr(ws), need,
+               N.stream_ptr(), kernels=4 + head.num_layers * 3 + n_bias)
+    return gw, gb
+
+
+class HeadFunction(torch.autograd.Function):
+    """MLPRender_Fea.forward(viewdirs, features) on its own (one app sample per row)."""
+
+    @staticmethod
+    def forward(ctx, features, viewdirs, head, *params):
+        n, c = features.shape
+        dev = features.device
+        feat = torch.zeros(n, c + 1, device=dev)
+        feat[:, 1:] = features.to(torch.float32)
+        rays = torch.zeros(n, 6, device=dev)
+        rays[:, 3:6] = viewdirs.to(torch.float32)
+        idx = torch.arange(n, dtype=torch.int32, device=dev)
+        rgb = torch.empty(n, 3, device=dev)
+        head_forward(head, feat, rays, idx, idx, rgb)
+        ctx.save_for_backward(feat, rays, idx)
+        ctx.head = head
+        return rgb
+
+    @staticmethod
+    def backward(ctx, g_rgb):
+        feat, rays, idx = ctx.saved_tensors
+        g_feat = torch.zeros_like(feat)
+        gw, gb = head_backward(ctx.head, feat, rays, idx, idx, g_rgb.contiguous(), g_feat, direct=False)
+        grads = []
+        for w, b in zip(gw, gb):
+            grads.append(w)
+            if b is not None:
+                grads.append(b)
+        return (g_feat[:, 1:], None, None, *grads)
+
+
 def make_render_module(cfg, in_channels):
-    shading = (cfg.renderer or Cfg()).get("shadingMode", "SH")
+    """The colour head: MLPRender_Fea (the reference's head, built whatever shadingMode says,
+    :243-246) unless renderer.shadingMode is 'SH' (the degree-2 SH head)."""
+    rc = cfg.renderer or Cfg()
+    shading = rc.get("shadingMode") or "MLP_Fea"
     if shading == "SH":
         return SHRender(in_channels)
-    raise NotImplementedError(f"renderer.shadingMode {shading!r} is not implemented (use 'SH')")
+    return MLPRender_Fea(inChanel=in_channels, num_layers=int(rc.get("num_layers") or 3),
+                         hidden_dim=int(rc.get("hidden_dim") or 128), viewpe=int(rc.get("view_pe", 6)),
+                         feape=int(rc.get("fea_pe", 2)))
 
 
 def render_desc(model, n_samples, white_bg):
@@ -156,6 +293,81 @@ class RenderFunction(torch.autograd.Function):
         return (None, None) + grads + (None,)
 
 
+def scan_counts(counts):
+    """Exclusive scan of int32 counts -> int64 offsets [n + 1] (ff_scan_counts)."""
+    n = counts.shape[0]
+    offsets = torch.empty(n + 1, dtype=torch.int64, device=counts.device)
+    wsb = N.lib().ff_scan_workspace_bytes(n)
+    ws = torch.empty(max(wsb, 8), dtype=torch.uint8, device=counts.device)
+    N.call("ff_scan_counts", N.ptr(counts), n, N.ptr(offsets), N.ptr(ws), wsb, N.stream_ptr())
+    return offsets
+
+
+class RenderFunctionMLP(torch.autograd.Function):
+    """rgb, depth = render(rays) with the MLPRender_Fea colour head (models/FactorFields.py:
+    862-898): march -> field + MLP -> compositing weights -> the samples above the weight
+    threshold (app_mask) -> the colour head on them -> compositing. Gradients reach the grids,
+    the field MLP and the head.
+
+    apply(rays, jitter, basis_param, coeff_param, w0, b0, w1, job, *head_params)."""
+
+    @staticmethod
+    def forward(ctx, rays, jitter, basis_param, coeff_param, w0, b0, w1, job, *head_params):
+        m, rdesc = job["model"], job["rdesc"]
+        head = m.renderModule
+        offsets, xyz, sidx = march(m, rays, jitter, rdesc)
+        feat = field_eval(m, job, xyz)
+        n, M = rays.shape[0], feat.shape[0]
+        dev = rays.device
+        st = N.stream_ptr()
+        w = torch.empty(M, device=dev)
+        app_counts = torch.empty(n, dtype=torch.int32, device=dev)
+        N.call("ff_composite_weights", ctypes.byref(rdesc), N.ptr(rays), N.ptr(jitter), n, N.ptr(offsets), N.ptr(sidx),
+               N.ptr(feat), feat.shape[1], N.ptr(w), N.ptr(app_counts), st)
+        app_off = scan_counts(app_counts)
+        n_app = int(app_off[-1].item())  # the reference synchronises on app_mask.any() (:883)
+        app_idx = torch.empty(n_app, dtype=torch.int32, device=dev)
+        app_ray = torch.empty(n_app, dtype=torch.int32, device=dev)
+        if n_app:
+            N.call("ff_app_emit", n, N.ptr(offsets), N.ptr(w), float(rdesc.weight_thres), N.ptr(app_off),
+                   N.ptr(app_idx), N.ptr(app_ray), st)
+        rgb_sample = torch.empty(M, 3, device=dev)
+        job["head_tc"] = bool(job["fused"]) and head_tc_supported(head)
+        head_forward(head, feat, rays, app_idx, app_ray, rgb_sample, tc=job["head_tc"])
+        rgb = torch.empty(n, 3, device=dev)
+        depth = torch.empty(n, device=dev)
+        N.call("ff_composite_forward_rgb", ctypes.byref(rdesc), N.ptr(rays), N.ptr(jitter), n, N.ptr(offsets),
+               N.ptr(sidx), N.ptr(feat), feat.shape[1], N.ptr(rgb_sample), None, N.ptr(rgb), N.ptr(depth), None, st)
+        ctx.save_for_backward(rays, offsets, xyz, sidx, feat, rgb_sample, app_idx, app_ray)
+        ctx.jitter, ctx.job = jitter, job
+        ctx.mark_non_differentiable(depth)
+        job["xyz"] = xyz
+        return rgb, depth
+
+    @staticmethod
+    def backward(ctx, g_rgb, g_depth):
+        rays, offsets, xyz, sidx, feat, rgb_sample, app_idx, app_ray = ctx.saved_tensors
+        job = ctx.job
+        m, rdesc = job["model"], job["rdesc"]
+        n = rays.shape[0]
+        g_feat = torch.empty_like(feat)
+        g_rgb_sample = torch.empty_like(rgb_sample)
+        g_rgb = g_rgb.contiguous()
+        N.call("ff_composite_backward_rgb", ctypes.byref(rdesc), N.ptr(rays), N.ptr(ctx.jitter), n, N.ptr(offsets),
+               N.ptr(sidx), N.ptr(feat), feat.shape[1], N.ptr(rgb_sample), None, N.ptr(g_rgb), N.ptr(g_feat),
+               N.ptr(g_rgb_sample), N.stream_ptr())
+        direct = getattr(m, "accumulate_grad_directly", True)
+        gw, gb = head_backward(m.renderModule, feat, rays, app_idx, app_ray, g_rgb_sample, g_feat, direct=direct,
+                               tc=job["head_tc"])
+        grads = field_grad(m, job, xyz, g_feat)
+        head_grads = []
+        for wg, bg in zip(gw, gb):
+            head_grads.append(None if direct else wg)
+            if bg is not None:
+                head_grads.append(None if direct else bg)
+        return (None, None) + grads + (None,) + tuple(head_grads)
+
+
 def field_eval(m, job, xyz):
     """MLP output [M, out_dim] of the field at xyz (fused BF16 path or drop-in float32 path)."""
     n = xyz.shape[0]
@@ -234,15 +446,18 @@ def field_grad(m, job, xyz, g_out):
 
 def render_forward(model, rays_chunk, white_bg=True, is_train=False, ndc_ray=False, N_samples=-1, fused=None,
                    jitter=None):
-    """FactorFields.forward (models/FactorFields.py:843-898), bounded scenes, SH-2 colour head:
-    returns (rgb_map [R, 3], depth_map [R], coeffs).
+    """FactorFields.forward (models/FactorFields.py:843-898), bounded scenes, with the model's
+    colour head (MLPRender_Fea or the SH-2 head): returns (rgb_map [R, 3], depth_map [R], coeffs).
 
     jitter: optional per-ray sample offsets [R] in [0, 1) (the reference draws them with
     torch.rand_like when is_train); given explicitly they make sampling reproducible."""
     if ndc_ray:
         raise NotImplementedError("NDC rays (sample_point_ndc) are not on this path")
-    if not isinstance(model.renderModule, SHRender) or model.linear_mat.out_dim < 28:
-        raise NotImplementedError("rendering needs the SH-2 colour head with out_dim = 28")
+    mlp_head = isinstance(model.renderModule, MLPRender_Fea)
+    if not mlp_head and model.linear_mat.out_dim < 28:
+        raise NotImplementedError("the SH-2 colour head needs out_dim >= 28")
+    if mlp_head and model.renderModule.in_channels != model.linear_mat.out_dim - 1:
+        raise ValueError("MLPRender_Fea's inChanel must be out_dim - 1")
     lm = model.linear_mat
     if lm.num_layers != 2:
         raise NotImplementedError("rendering needs an MLPMixer with num_layers = 2")
@@ -263,7 +478,12 @@ def render_forward(model, rays_chunk, white_bg=True, is_train=False, ndc_ray=Fal
     job = {"model": model, "rdesc": render_desc(model, n_samples, wb), "fdesc": model.descriptor(dt),
            "basis_r": basis_r, "coeff_r": coeff_r, "coeff_param": coeff_param, "fused": fused}
     l0, l1 = lm.backbone
-    rgb, depth = RenderFunction.apply(rays, jitter, model.basis_flat, coeff_param, l0.weight, l0.bias, l1.weight, job)
+    if mlp_head:
+        rgb, depth = RenderFunctionMLP.apply(rays, jitter, model.basis_flat, coeff_param, l0.weight, l0.bias,
+                                             l1.weight, job, *list(model.renderModule.parameters()))
+    else:
+        rgb, depth = RenderFunction.apply(rays, jitter, model.basis_flat, coeff_param, l0.weight, l0.bias, l1.weight,
+                                          job)
     coeffs = torch.zeros((1, model.n_feat), device=rays.device)
     if getattr(model, "return_coeffs", False) and job["xyz"].shape[0]:
         with torch.no_grad():

@@ -122,7 +122,7 @@ typedef struct FFMlpGrad {
 FF_API int ff_abi_version(void);
 FF_API const char* ff_last_error(void);
 /* sizeof of the ABI structs, for binding checks: 0 FFField, 1 FFMlp, 2 FFMlpGrad, 3 FFRender,
- * 4 FFProposal, 5 FFAdamParam. */
+ * 4 FFProposal, 5 FFAdamParam, 6 FFRenderMlp. */
 FF_API int64_t ff_struct_size(int32_t which);
 /* Number of SMs of the current device and the compute capability (major*10+minor). */
 FF_API int ff_device_info(int32_t* sm_count, int32_t* cc);
@@ -345,6 +345,81 @@ FF_API int ff_composite_forward_zd(const FFRender* r, const float* rays, int64_t
 FF_API int ff_composite_backward_zd(const FFRender* r, const float* rays, int64_t n_rays, const int64_t* offsets,
                                     const float* zd, const float* feat, int32_t feat_stride,
                                     const float* grad_rgb, float* grad_feat, void* stream);
+
+/* ---- MLPRender_Fea colour head (models/FactorFields.py:162-203) ------------------------------
+ * rgb = sigmoid(MLP([feat, dir, PE(feat, fea_pe), PE(dir, view_pe)])) for the samples whose
+ * compositing weight passes renderer.rayMarch_weight_thres (:879-885), with
+ * PE(x, F) = [sin(x_d 2^f)]_{d,f} ++ [cos(x_d 2^f)]_{d,f} (index d * F + f, :74-79), feat = the
+ * field MLP's channels 1 .. C of the sample's row (feat[app_mask, 1:]) and dir = its ray's
+ * direction (rays[:, 3:6], not normalised). The pipeline of FactorFields.forward with this head:
+ *   ff_composite_weights -> ff_scan_counts (app counts) -> ff_app_emit -> ff_render_head_forward
+ *   -> ff_composite_forward_rgb; backward: ff_composite_backward_rgb -> ff_render_head_backward
+ *   -> the field / MLP backward on grad_feat. */
+typedef struct FFRenderMlp {
+  int32_t n_layers;     /* renderer.num_layers, 1..FF_MAX_MLP_LAYERS */
+  int32_t in_channels;  /* C = feature channels (inChanel = model.out_dim - 1) */
+  int32_t hidden_dim;   /* renderer.hidden_dim */
+  int32_t view_pe;      /* renderer.view_pe */
+  int32_t fea_pe;       /* renderer.fea_pe */
+  int32_t in_dim;       /* 3 + C + 2 * view_pe * 3 + 2 * fea_pe * C (checked) */
+  const float* weight[FF_MAX_MLP_LAYERS]; /* [out_l, in_l] float32 (torch layout); out = 3 for the last */
+  const float* bias[FF_MAX_MLP_LAYERS];   /* [out_l] for the hidden layers; the last layer has none */
+} FFRenderMlp;
+
+/* Compositing weights without colours (the forward's transmittance scan, :82-88, :876-878):
+ * w_out [M] per live sample and app_counts [n_rays] int32 = samples per ray with weight above
+ * r->weight_thres. feat: as ff_composite_forward (channel 0 is the density feature). */
+FF_API int ff_composite_weights(const FFRender* r, const float* rays, const float* jitter, int64_t n_rays,
+                                const int64_t* offsets, const int32_t* sample_idx, const float* feat,
+                                int32_t feat_stride, float* w_out, int32_t* app_counts, void* stream);
+/* The samples with w > weight_thres in ray-major order (app_mask, :879-885): app_idx [n_app]
+ * = live-sample index, app_ray [n_app] = its ray, at app_offsets (ff_scan_counts of app_counts).
+ * Live-sample indices must fit in int32 (M < 2^31). */
+FF_API int ff_app_emit(int64_t n_rays, const int64_t* offsets, const float* w, float weight_thres,
+                       const int64_t* app_offsets, int32_t* app_idx, int32_t* app_ray, void* stream);
+
+/* The float32 drop-in head: rgb_sample rows app_idx[i] (of a [M, 3] buffer) receive the colour
+ * of app sample i. workspace: ff_render_head_workspace_bytes(h, n_app) bytes, 256-byte aligned. */
+FF_API int64_t ff_render_head_workspace_bytes(const FFRenderMlp* h, int64_t n_app);
+FF_API int ff_render_head_forward(const FFRenderMlp* h, const float* feat, int32_t feat_stride, const float* rays,
+                                  const int32_t* app_idx, const int32_t* app_ray, int64_t n_app, float* rgb_sample,
+                                  void* workspace, int64_t workspace_bytes, void* stream);
+/* Backward for grad_rgb_sample [M, 3] (rows app_idx): writes dL/dfeat into channels 1 .. C of
+ * grad_feat rows app_idx[i] (overwritten) and accumulates the weight / bias gradients g (+=). */
+FF_API int ff_render_head_backward(const FFRenderMlp* h, const float* feat, int32_t feat_stride, const float* rays,
+                                   const int32_t* app_idx, const int32_t* app_ray, int64_t n_app,
+                                   const float* grad_rgb_sample, float* grad_feat, const FFMlpGrad* g,
+                                   void* workspace, int64_t workspace_bytes, void* stream);
+
+/* The same head on the tensor cores (tcgen05 MMA, BF16 operands, FP32 accumulators in tensor
+ * memory): weights rounded to BF16 inside the kernel, inputs (the positional encoding of the
+ * features and directions) rounded to BF16, activations kept as BF16, every accumulation FP32.
+ * One persistent launch each way, no workspace. Requirements (else FF_ERR_UNSUPPORTED): n_layers
+ * 3, hidden_dim 128, fea_pe 2, view_pe 6, in_channels 27 or 31 (model.out_dim 28 or 32).
+ * status (optional, device int32): set to FF_ERR_LIMIT if a bounded wait inside the kernel ran
+ * out (results invalid); left untouched otherwise. The backward writes grad_feat and accumulates
+ * g exactly like ff_render_head_backward. */
+FF_API int ff_render_head_forward_tc(const FFRenderMlp* h, const float* feat, int32_t feat_stride, const float* rays,
+                                     const int32_t* app_idx, const int32_t* app_ray, int64_t n_app, float* rgb_sample,
+                                     int32_t* status, void* stream);
+FF_API int ff_render_head_backward_tc(const FFRenderMlp* h, const float* feat, int32_t feat_stride,
+                                      const float* rays, const int32_t* app_idx, const int32_t* app_ray, int64_t n_app,
+                                      const float* grad_rgb_sample, float* grad_feat, const FFMlpGrad* g,
+                                      int32_t* status, void* stream);
+
+/* ff_composite_forward with per-sample colours from a separate head: rgb_sample [M, 3] is read
+ * for the samples whose weight passes the threshold (the others contribute no colour, :880-887). */
+FF_API int ff_composite_forward_rgb(const FFRender* r, const float* rays, const float* jitter, int64_t n_rays,
+                                    const int64_t* offsets, const int32_t* sample_idx, const float* feat,
+                                    int32_t feat_stride, const float* rgb_sample, const int32_t* white_bg, float* rgb,
+                                    float* depth, float* acc, void* stream);
+/* Its backward for dL/drgb [n_rays, 3]: grad_feat rows [M, feat_stride] get dL/dfeat0 in channel 0
+ * and zeros elsewhere (overwritten); grad_rgb_sample [M, 3] = dL/dcolour (w * dL/drgb above the
+ * threshold, else 0). */
+FF_API int ff_composite_backward_rgb(const FFRender* r, const float* rays, const float* jitter, int64_t n_rays,
+                                     const int64_t* offsets, const int32_t* sample_idx, const float* feat,
+                                     int32_t feat_stride, const float* rgb_sample, const int32_t* white_bg,
+                                     const float* grad_rgb, float* grad_feat, float* grad_rgb_sample, void* stream);
 
 /* ---- learned proposal sampler (no counterpart in the reference; resampling follows
  * sample_pdf, dataLoader/ray_utils.py:132-174) ------------------------------------------- */

@@ -325,6 +325,50 @@ def mlp_bwd(weights, biases, x, g_out):
     return g, gw, gb
 
 
+def positional_encoding(x, freqs):
+    """models/FactorFields.py:74-79: [sin(x_d 2^f)]_{d,f} ++ [cos(x_d 2^f)]_{d,f}, index d * F + f."""
+    x = np.asarray(x, f64)
+    fb = 2.0 ** np.arange(freqs)
+    pts = (x[..., None] * fb).reshape(x.shape[:-1] + (freqs * x.shape[-1],))
+    return np.concatenate([np.sin(pts), np.cos(pts)], -1)
+
+
+def render_head_input(feat, dirs, view_pe, fea_pe):
+    """MLPRender_Fea's input rows (models/FactorFields.py:188-195): [feat, dirs, PE(feat), PE(dirs)]."""
+    parts = [np.asarray(feat, f64), np.asarray(dirs, f64)]
+    if fea_pe > 0:
+        parts.append(positional_encoding(feat, fea_pe))
+    if view_pe > 0:
+        parts.append(positional_encoding(dirs, view_pe))
+    return np.concatenate(parts, -1)
+
+
+def render_head_fwd(weights, biases, feat, dirs, view_pe, fea_pe):
+    """MLPRender_Fea.forward (models/FactorFields.py:188-203): sigmoid(MLP(input)) [N, 3]."""
+    out, _ = mlp_fwd(weights, biases, render_head_input(feat, dirs, view_pe, fea_pe))
+    return sigmoid(out)
+
+
+def render_head_bwd(weights, biases, feat, dirs, view_pe, fea_pe, g_rgb):
+    """Backward of render_head_fwd for dL/drgb: (dL/dfeat [N, C], grad_weights, grad_biases)."""
+    x = render_head_input(feat, dirs, view_pe, fea_pe)
+    out, _ = mlp_fwd(weights, biases, x)
+    rgb = sigmoid(out)
+    g_out = np.asarray(g_rgb, f64) * rgb * (1 - rgb)
+    g_x, gw, gb = mlp_bwd(weights, biases, x, g_out)
+    feat = np.asarray(feat, f64)
+    c = feat.shape[-1]
+    g_feat = g_x[:, :c].copy()
+    if fea_pe > 0:
+        off = c + 3
+        fb = 2.0 ** np.arange(fea_pe)
+        arg = feat[..., None] * fb  # [N, C, F]
+        g_sin = g_x[:, off:off + c * fea_pe].reshape(-1, c, fea_pe)
+        g_cos = g_x[:, off + c * fea_pe:off + 2 * c * fea_pe].reshape(-1, c, fea_pe)
+        g_feat += (fb * (g_sin * np.cos(arg) - g_cos * np.sin(arg))).sum(-1)
+    return g_feat, gw, gb
+
+
 # ----------------------------------------------------------------------------------------
 # rendering: sampling, occupancy, density, compositing, SH colour
 # ----------------------------------------------------------------------------------------
@@ -468,12 +512,13 @@ class RenderSpec:
 
 
 def render_rays(fspec, rspec, basis_grids, coeff_grid, mlp_w, mlp_b, rays, jitter=None,
-                alpha_volume=None, g_rgb=None):
-    """models/FactorFields.py:843-898 (bounded scene, SH-2 colour head composed from
-    models/sh.py:34) forward, and — when g_rgb is given — the backward of sum(g_rgb * rgb).
+                alpha_volume=None, g_rgb=None, head=None):
+    """models/FactorFields.py:843-898 (bounded scene) forward, and — when g_rgb is given — the
+    backward of sum(g_rgb * rgb). Colour head: the SH-2 head composed from models/sh.py:34
+    (head=None), or MLPRender_Fea (:162-203) with head = dict(w=[...], b=[...], view_pe, fea_pe).
 
     Returns dict(rgb, depth, weight, valid, z, acc) and, with g_rgb, the parameter gradients
-    grad_basis (list), grad_coeff, grad_mlp_w, grad_mlp_b."""
+    grad_basis (list), grad_coeff, grad_mlp_w, grad_mlp_b (and grad_head_w, grad_head_b)."""
     rays = np.asarray(rays, f32)
     o, d = rays[:, :3], rays[:, 3:6]
     xyz, z, inside = sample_point(o, d, rspec.aabb, rspec.step, rspec.n_samples, jitter)
@@ -492,10 +537,16 @@ def render_rays(fspec, rspec, basis_grids, coeff_grid, mlp_w, mlp_b, rays, jitte
     app = weight > rspec.weight_thres  # :879
     colour = np.zeros((r, s, 3), f64)
     dirs = np.broadcast_to(d[:, None, :], (r, s, 3))[valid]
-    sh = out[:, 1:28].reshape(-1, 3, 9)
-    lin = eval_sh2(sh, dirs)
-    c_valid = sigmoid(lin)
     app_v = app[valid]
+    if head is None:
+        sh = out[:, 1:28].reshape(-1, 3, 9)
+        lin = eval_sh2(sh, dirs)
+        c_valid = sigmoid(lin)
+    else:  # the head runs on feat[app_mask, 1:] only (:884)
+        c_valid = np.zeros((pts.shape[0], 3), f64)
+        if app_v.any():
+            c_valid[app_v] = render_head_fwd(head["w"], head["b"], out[app_v, 1:], dirs[app_v],
+                                             head["view_pe"], head["fea_pe"])
     tmp = np.zeros((pts.shape[0], 3), f64)
     tmp[app_v] = c_valid[app_v]
     colour[valid] = tmp
@@ -526,9 +577,18 @@ def render_rays(fspec, rspec, basis_grids, coeff_grid, mlp_w, mlp_b, rays, jitte
     g_out = np.zeros_like(out)
     g_out[:, 0] = g_sigma[valid] * softplus_grad(out[:, 0], rspec.density_shift)
     gc = g_col[valid] * app_v[:, None]
-    g_lin = gc * c_valid * (1 - c_valid)
-    basis9 = sh2_basis(dirs)
-    g_out[:, 1:28] = (g_lin[:, :, None] * basis9[:, None, :]).reshape(-1, 27)
+    if head is None:
+        g_lin = gc * c_valid * (1 - c_valid)
+        basis9 = sh2_basis(dirs)
+        g_out[:, 1:28] = (g_lin[:, :, None] * basis9[:, None, :]).reshape(-1, 27)
+    else:
+        hw = [np.zeros_like(np.asarray(w, f64)) for w in head["w"]]
+        hb = [None if b is None else np.zeros_like(np.asarray(b, f64)) for b in head["b"]]
+        if app_v.any():
+            g_f, hw, hb = render_head_bwd(head["w"], head["b"], out[app_v, 1:], dirs[app_v], head["view_pe"],
+                                          head["fea_pe"], gc[app_v])
+            g_out[app_v, 1:] = g_f
+        res.update(grad_head_w=hw, grad_head_b=hb)
     g_feats, gw, gb = mlp_bwd(mlp_w, mlp_b, feats, g_out)
     gbasis, gcoef = get_coding_bwd(fspec, basis_grids, coeff_grid, pts, g_feats)
     res.update(grad_basis=gbasis, grad_coeff=gcoef, grad_mlp_w=gw, grad_mlp_b=gb)

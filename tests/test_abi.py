@@ -44,7 +44,8 @@ def test_bindings_cover_header(lib):
 def test_struct_layouts_match(lib):
     from factor_fields_gb300 import _native as N
     assert lib.ff_abi_version() == 1
-    for i, st in enumerate([N.FFField, N.FFMlp, N.FFMlpGrad, N.FFRender, N.FFProposal, N.FFAdamParam]):
+    for i, st in enumerate([N.FFField, N.FFMlp, N.FFMlpGrad, N.FFRender, N.FFProposal, N.FFAdamParam,
+                            N.FFRenderMlp]):
         assert lib.ff_struct_size(i) == ctypes.sizeof(st), st.__name__
 
 
@@ -115,3 +116,28 @@ def test_binned_fit_halves_validate_their_flags(lib):
     assert lib.ff_field_fit_step_binned(ctypes.byref(desc), vp(16), vp(16), ctypes.byref(mlp), vp(16), vp(16), n,
                                         N.FF_LOSS["l1"], 1.0 / n, vp(16), vp(16), vp(16), ctypes.byref(g), 4, ws, need,
                                         None) == N.FF_ERR_ARG
+
+
+def test_render_head_validation(lib):
+    """The MLPRender_Fea entry points check the descriptor before any launch: in_dim must follow
+    the reference's formula, the last layer has no bias, and the tensor-core head rejects shapes
+    it does not implement."""
+    from factor_fields_gb300 import _native as N
+    h = N.FFRenderMlp()
+    h.n_layers, h.in_channels, h.hidden_dim, h.view_pe, h.fea_pe = 3, 31, 128, 6, 2
+    h.in_dim = 3 + 31 + 36 + 124
+    for i in range(3):
+        h.weight[i] = 256
+    h.bias[0] = h.bias[1] = 256
+    args = (ctypes.c_void_p(256), 32, ctypes.c_void_p(256), ctypes.c_void_p(256), ctypes.c_void_p(256), 0)
+    assert lib.ff_render_head_forward_tc(ctypes.byref(h), *args, None, None, None) == N.FF_OK  # n = 0: no launch
+    h.in_dim += 1
+    assert lib.ff_render_head_forward_tc(ctypes.byref(h), *args, None, None, None) == N.FF_ERR_ARG
+    h.in_dim -= 1
+    h.bias[2] = 256
+    assert lib.ff_render_head_forward_tc(ctypes.byref(h), *args, None, None, None) == N.FF_ERR_ARG
+    h.bias[2] = None
+    h.hidden_dim = 64
+    assert lib.ff_render_head_forward_tc(ctypes.byref(h), *args, None, None, None) == N.FF_ERR_UNSUPPORTED
+    assert b"hidden_dim" in lib.ff_last_error()
+    assert lib.ff_render_head_workspace_bytes(ctypes.byref(h), 100) > 0

@@ -3,12 +3,12 @@ reference's golden outputs and the FP64 oracle.
 
 Tolerances: float32 drop-in forward 1e-5 relative, gradients 1e-4;
 BF16 storage forward 2e-2, gradients 3e-2. Relative = max|a-b| / max|ref|; the float32 drop-in
-checks are also element-wise (gpu_util.close: |a-b| <= rtol |ref| + 1e-6 max|ref| per entry)."""
+checks are also element-wise (gpu_util.assert_close: |a-b| <= rtol |ref| + 1e-6 max|ref| per entry)."""
 import numpy as np
 import pytest
 import torch
 
-from gpu_util import close, field_cases, load_golden, model_from_golden, need_gpu, rel_err
+from gpu_util import assert_close, field_cases, load_golden, model_from_golden, need_gpu, rel_err
 from oracle import ff_oracle as O
 
 pytestmark = pytest.mark.gpu
@@ -25,12 +25,12 @@ def test_forward_matches_reference(case):
     m = model_from_golden(d, meta)
     x = torch.from_numpy(d["x"]).cuda()
     feats, coeff = m.get_coding(x)
-    assert close(feats, d["feats"], 1e-5)
-    assert close(coeff, d["coeff"], 1e-5)
-    assert close(m.get_basis(x), d["basis"], 1e-5)
-    assert close(m.get_coeff(x), d["coeff"], 1e-5)
+    assert_close(feats, d["feats"], 1e-5)
+    assert_close(coeff, d["coeff"], 1e-5)
+    assert_close(m.get_basis(x), d["basis"], 1e-5)
+    assert_close(m.get_coeff(x), d["coeff"], 1e-5)
     out = m.linear_mat(torch.from_numpy(d["feats"]).cuda())
-    assert close(out, d["mlp_out"], 1e-5)
+    assert_close(out, d["mlp_out"], 1e-5)
 
 
 @pytest.mark.parametrize("case", field_cases())
@@ -42,8 +42,8 @@ def test_backward_matches_reference(case):
     loss = (feats * torch.from_numpy(d["g_feats"]).cuda()).sum() + (coeff * torch.from_numpy(d["g_coeff"]).cuda()).sum()
     loss.backward()
     for l in range(len(m.basis_dims)):
-        assert close(m.layout.basis_view(m.basis_flat.grad, l), d[f"grad_basis{l}"], 1e-4), l
-    assert close(m.layout.coeff_view(m.coeff_flat.grad, 0), d["grad_coeffs0"], 1e-4)
+        assert_close(m.layout.basis_view(m.basis_flat.grad, l), d[f"grad_basis{l}"], 1e-4, what=f"level {l}")
+    assert_close(m.layout.coeff_view(m.coeff_flat.grad, 0), d["grad_coeffs0"], 1e-4)
     # padding channels of the gradient stay exactly zero
     mask = torch.ones_like(m.basis_flat.grad, dtype=torch.bool)
     for l in range(len(m.basis_dims)):
@@ -58,11 +58,11 @@ def test_mlp_backward_matches_reference(case):
     fin = torch.from_numpy(d["feats"]).cuda().requires_grad_(True)
     out = m.linear_mat(fin)
     (out * torch.from_numpy(d["g_out"]).cuda()).sum().backward()
-    assert close(fin.grad, d["grad_mlp_in"], 1e-5)
+    assert_close(fin.grad, d["grad_mlp_in"], 1e-5)
     for i, lin in enumerate(m.linear_mat.backbone):
-        assert close(lin.weight.grad, d[f"grad_mlp_w{i}"], 1e-5)
+        assert_close(lin.weight.grad, d[f"grad_mlp_w{i}"], 1e-5)
         if lin.bias is not None:
-            assert close(lin.bias.grad, d[f"grad_mlp_b{i}"], 1e-5)
+            assert_close(lin.bias.grad, d[f"grad_mlp_b{i}"], 1e-5)
 
 
 @pytest.mark.parametrize("case", field_cases())
@@ -109,13 +109,14 @@ def test_full_size_configs_against_oracle(key):
     ref_f, ref_c = O.get_coding(spec, bg, cg, x)
     xt = torch.from_numpy(x).cuda()
     feats, coeff = m.get_coding(xt)
-    assert close(feats, ref_f, 1e-5) and close(coeff, ref_c, 1e-5)
+    assert_close(feats, ref_f, 1e-5)
+    assert_close(coeff, ref_c, 1e-5)
     gf = rng.standard_normal(ref_f.shape).astype(np.float32)
     (feats * torch.from_numpy(gf).cuda()).sum().backward()
     gb, gc = O.get_coding_bwd(spec, bg, cg, x, gf)
     for l in range(len(m.basis_dims)):
-        assert close(m.layout.basis_view(m.basis_flat.grad, l)[0], gb[l], 1e-4), l
-    assert close(m.layout.coeff_view(m.coeff_flat.grad, 0)[0], gc, 1e-4)
+        assert_close(m.layout.basis_view(m.basis_flat.grad, l)[0], gb[l], 1e-4, what=f"level {l}")
+    assert_close(m.layout.coeff_view(m.coeff_flat.grad, 0)[0], gc, 1e-4)
 
 
 def test_empty_batch_and_errors():

@@ -119,7 +119,16 @@ def test_field_backward(case):
             assert rel_err(gbias[i], d[f"grad_mlp_b{i}"]) < 1e-5
 
 
-@pytest.mark.parametrize("case", [c for c in RENDER_CASES if "mlp_head" not in c])
+def head_params(d, meta):
+    """MLPRender_Fea parameters of a golden render (None for the SH-2 head)."""
+    if meta.get("head") != "mlp":
+        return None
+    ws, bs = mlp_params(d, "rm")
+    r = meta["cfg"]["renderer"]
+    return {"w": ws, "b": bs, "view_pe": r["view_pe"], "fea_pe": r["fea_pe"]}
+
+
+@pytest.mark.parametrize("case", RENDER_CASES)
 def test_render_forward_backward(case):
     d, meta = load(case)
     fspec = O.FieldSpec.from_meta(meta)
@@ -128,8 +137,9 @@ def test_render_forward_backward(case):
     rspec = O.RenderSpec(meta["aabb"], d["step_size"], int(d["n_samples"]), r["density_shift"],
                          r["distance_scale"], r["rayMarch_weight_thres"], meta["white_bg"])
     ws, bs = mlp_params(d)
+    head = head_params(d, meta)
     res = O.render_rays(fspec, rspec, bg, cg, ws, bs, d["rays"], jitter=d["u"] if meta["jitter"] else None,
-                        alpha_volume=d.get("alpha_volume"), g_rgb=d["g_rgb"])
+                        alpha_volume=d.get("alpha_volume"), g_rgb=d["g_rgb"], head=head)
     # sample positions, in-box mask and occupancy decisions are bit-exact
     np.testing.assert_array_equal(res["z"], d["z_vals"])
     np.testing.assert_array_equal(res["valid"], d["valid"])
@@ -140,6 +150,51 @@ def test_render_forward_backward(case):
     assert rel_err(res["grad_coeff"], d["grad_coeffs0"][0]) < 1e-4
     for i in range(len(ws)):
         assert rel_err(res["grad_mlp_w"][i], d[f"grad_mlp_w{i}"]) < 1e-4
+    if head is not None:  # MLPRender_Fea's own parameters
+        for i in range(len(head["w"])):
+            assert rel_err(res["grad_head_w"][i], d[f"grad_rm_w{i}"]) < 1e-4, i
+            if head["b"][i] is not None:
+                assert rel_err(res["grad_head_b"][i], d[f"grad_rm_b{i}"]) < 1e-4, i
+
+
+def test_positional_encoding_layout():
+    """positional_encoding (models/FactorFields.py:74-79): sin block then cos block, index
+    d * F + f, frequencies 2^f."""
+    x = np.array([[0.3, -1.2]])
+    pe = O.positional_encoding(x, 3)
+    want_sin = [np.sin(0.3), np.sin(0.6), np.sin(1.2), np.sin(-1.2), np.sin(-2.4), np.sin(-4.8)]
+    want_cos = [np.cos(0.3), np.cos(0.6), np.cos(1.2), np.cos(-1.2), np.cos(-2.4), np.cos(-4.8)]
+    np.testing.assert_allclose(pe[0], want_sin + want_cos, rtol=1e-12)
+
+
+def test_render_head_backward_finite_differences():
+    """MLPRender_Fea's backward through the positional encoding against FP64 central
+    differences (the oracle's analytic gradient is what the GPU kernels are checked against)."""
+    rng = np.random.default_rng(0)
+    c, hid = 5, 16
+    w = [rng.standard_normal((hid, 3 + c + 36 + 4 * c)) * 0.3, rng.standard_normal((hid, hid)) * 0.3,
+         rng.standard_normal((3, hid)) * 0.3]
+    b = [rng.standard_normal(hid) * 0.1, rng.standard_normal(hid) * 0.1, None]
+    feat = rng.standard_normal((7, c))
+    dirs = rng.standard_normal((7, 3))
+    g = rng.standard_normal((7, 3))
+    g_feat, gw, _ = O.render_head_bwd(w, b, feat, dirs, 6, 2, g)
+    eps = 1e-6
+    num = np.zeros_like(feat)
+    for i in range(feat.shape[0]):
+        for k in range(c):
+            fp, fm = feat.copy(), feat.copy()
+            fp[i, k] += eps
+            fm[i, k] -= eps
+            num[i, k] = ((O.render_head_fwd(w, b, fp, dirs, 6, 2) - O.render_head_fwd(w, b, fm, dirs, 6, 2)) * g).sum() \
+                / (2 * eps)
+    np.testing.assert_allclose(g_feat, num, rtol=1e-6, atol=1e-8)
+    wp = [x.copy() for x in w]
+    wm = [x.copy() for x in w]
+    wp[1][2, 3] += eps
+    wm[1][2, 3] -= eps
+    fd = ((O.render_head_fwd(wp, b, feat, dirs, 6, 2) - O.render_head_fwd(wm, b, feat, dirs, 6, 2)) * g).sum() / (2 * eps)
+    assert abs(gw[1][2, 3] - fd) <= 1e-6 * max(abs(fd), 1e-3)
 
 
 def test_raw2alpha_and_sh():
