@@ -4,25 +4,34 @@
 // One persistent CTA per SM (128 threads: thread t owns sample t of a 128-sample tile and TMEM
 // lane t) walks tiles of the listed head samples. Per tile, for 3 layers 128 hidden units wide:
 //
-//   X   = [feat, dir, PE(feat, 2), PE(dir, 6)]        built per thread, BF16, in shared memory
-//   F1  S = X W0^T                  (tcgen05, M 128, N 128, K = in_dim padded to 16)
-//       H0 = relu(S + b0)           -> shared memory (BF16), ReLU mask kept in registers
-//   F2  S = H0 W1^T                 (N 128, K 128)
-//       H1 = relu(S + b1), y = H1 W2^T, rgb = sigmoid(y)   (3 outputs: CUDA cores)
+//   X   = [feat, dir, PE(feat, 2), PE(dir, 6)]        built per thread, in shared memory as a
+//                                   BF16 pair X = X_hi + X_lo (~16 significant bits)
+//   F1  S = X_hi W0^T + X_lo W0^T   (tcgen05, M 128, N 128, K = in_dim padded to 16)
+//       H0 = relu(S + b0)           -> shared memory as H0_hi + H0_lo, ReLU mask kept in registers
+//   F2  S = H0_hi W1^T + H0_lo W1^T (N 128, K 128)
+//       H1 = relu(S + b1), y = H1 W2^T, rgb = sigmoid(y)   (3 outputs: CUDA cores, FP32 H1)
 // and for the backward (the forward recomputed, nothing stored between launches):
 //       dy = dL/drgb rgb (1 - rgb), dH1 = (dy W2) [H1 > 0] -> shared memory (BF16)
 //   B1  S  = dH1 W1                 (B = W1 read MN-major)
-//   B2  dW1 += dH1^T H0             (A = dH1, B = H0, both read MN-major; TMEM-resident over tiles)
+//   B2  dW1 += dH1^T H0_hi          (A = dH1, B = H0, both read MN-major; TMEM-resident over tiles)
 //       dH0 = S [H0 > 0]            -> shared memory, over H0 (consumed by B2)
-//   B3  dW0 += dH0^T X              (TMEM-resident over tiles)
+//   B3  dW0 += dH0^T X_hi           (TMEM-resident over tiles)
 //   B4  S  = dH0 W0                 (the feature-related input columns only)
 //       dL/dfeat = chain rule through the positional encoding, written to grad_feat
 // dW2, db0 and db1 are reduced with warp shuffles into per-lane registers. At the end each CTA
 // adds its dW0 / dW1 (read from TMEM, one row per thread) and the register sums to the float32
 // gradients with one atomic per entry.
 //
+// The forward operands X and H0 carry ~16 significant bits (two BF16 MMAs each): with one BF16
+// rounding, inputs near a ReLU kink land on the other side of it in a fraction of the 128 x 128
+// units per tile, and each flip moves that sample's input gradient by a whole term (up to ~20% of
+// max |dL/dfeat| on random heads). The backward operands (dH1, dH0) and the weight-gradient
+// operands are single BF16 values (~0.2% effect).
+//
 // Operands are stored once, in the core-matrix-row layout of tc_util.cuh, and read as K-major or
-// MN-major operands as each product needs (transposes cost nothing). TMEM columns (backward):
+// MN-major operands as each product needs (transposes cost nothing). Shared memory: W0, W1, X_hi
+// and a 64 KB region R that holds X_lo during F1, then H0_hi and H0_lo for F2, then H0_hi and dH1,
+// then dH0 and dH1 in the backward. TMEM columns (backward):
 // [0, S) the per-tile accumulator S, then dW1 (128), then dW0 (in_dim padded): at most 512.
 // Every wait on an mbarrier has an iteration limit: when it runs out the kernel reports
 // FF_ERR_LIMIT through `status`, stops, waits (again with a limit) for its MMAs and frees TMEM.
@@ -52,8 +61,9 @@ struct Shape {
   static constexpr int W1_B = kH * kH * 2;
   static constexpr int X_B = kTile * IN_PAD * 2;
   static constexpr int H_B = kTile * kH * 2;
-  static constexpr int F32_B = (3 * kH + 2 * kH) * 4;  // W2 [3][128], b0, b1
-  static constexpr int smem(bool bwd) { return W0_B + W1_B + X_B + H_B + (bwd ? H_B : 0) + F32_B + 64; }
+  static constexpr int R_B = X_B > 2 * H_B ? X_B : 2 * H_B;  // X_lo, or H0_hi + H0_lo / dH1
+  static constexpr int F32_B = (3 * kH + 2 * kH) * 4;        // W2 [3][128], b0, b1
+  static constexpr int smem() { return W0_B + W1_B + X_B + R_B + F32_B + 64; }
 };
 
 struct HeadArgs {
@@ -93,11 +103,26 @@ __device__ __forceinline__ void store8(uint32_t buf, int cols, int t, int k0, co
                tc::pack2_bf16(v[4], v[5]), tc::pack2_bf16(v[6], v[7]));
 }
 
-// The head's input row of one sample, in the reference's column order, written as BF16 into row
-// t of X (zero for an invalid row and for the padding). sin / cos of x 2^f come from one sincosf
-// and the double-angle identities.
+// The same as a BF16 pair: hi = bf16(v) into hi_buf, lo = bf16(v - hi) into lo_buf.
+__device__ __forceinline__ void store8_split(uint32_t hi_buf, uint32_t lo_buf, int cols, int t, int k0,
+                                             const float* v) {
+  uint32_t h[4], l[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    h[q] = tc::pack2_bf16(v[2 * q], v[2 * q + 1]);
+    l[q] = tc::pack2_bf16(v[2 * q] - __uint_as_float(h[q] << 16), v[2 * q + 1] - __uint_as_float(h[q] & 0xffff0000u));
+  }
+  const uint32_t off = tc::core_off(t, k0, cols);
+  st_shared_v4(hi_buf + off, h[0], h[1], h[2], h[3]);
+  st_shared_v4(lo_buf + off, l[0], l[1], l[2], l[3]);
+}
+
+// The head's input row of one sample, in the reference's column order, written as a BF16 pair into
+// row t of X_hi / X_lo (zero for an invalid row and for the padding). sin / cos of x 2^f come from
+// one sincosf and the double-angle identities.
 template <int C, int F, int V>
-__device__ __forceinline__ void build_x(uint32_t X, int t, bool valid, const float* frow, const float* drow) {
+__device__ __forceinline__ void build_x(uint32_t X, uint32_t Xlo, int t, bool valid, const float* frow,
+                                        const float* drow) {
   using S = Shape<C, F, V>;
   float fv[C], dv[3];
 #pragma unroll
@@ -108,7 +133,7 @@ __device__ __forceinline__ void build_x(uint32_t X, int t, bool valid, const flo
   int k = 0;  // compile-time after unrolling
   auto emit = [&](float v) {
     buf[k & 7] = v;
-    if ((k & 7) == 7) store8(X, S::IN_PAD, t, k - 7, buf);
+    if ((k & 7) == 7) store8_split(X, Xlo, S::IN_PAD, t, k - 7, buf);
     ++k;
   };
 #pragma unroll
@@ -179,9 +204,11 @@ __global__ void __launch_bounds__(kTile, 1) head_tc_kernel(const HeadArgs a) {
   const uint32_t sW0 = tc::smem_u32(p); p += S::W0_B;
   const uint32_t sW1 = tc::smem_u32(p); p += S::W1_B;
   const uint32_t sX = tc::smem_u32(p); p += S::X_B;
-  const uint32_t sH0 = tc::smem_u32(p); p += S::H_B;
-  uint32_t sDH1 = 0;
-  if constexpr (BWD) { sDH1 = tc::smem_u32(p); p += S::H_B; }
+  const uint32_t sR = tc::smem_u32(p); p += S::R_B;
+  const uint32_t sXlo = sR;               // F1
+  const uint32_t sH0 = sR;                // H0_hi (F2, B2), then dH0 (B3, B4)
+  const uint32_t sH0lo = sR + S::H_B;     // H0_lo (F2)
+  const uint32_t sDH1 = sR + S::H_B;      // dH1 (B1, B2), after F2
   float* w2s = reinterpret_cast<float*>(p); p += 3 * kH * 4;
   float* b0s = reinterpret_cast<float*>(p); p += kH * 4;
   float* b1s = reinterpret_cast<float*>(p); p += kH * 4;
@@ -200,7 +227,7 @@ __global__ void __launch_bounds__(kTile, 1) head_tc_kernel(const HeadArgs a) {
     const int r = e / kH, c = e % kH;
     *reinterpret_cast<__nv_bfloat16*>(smem + S::W0_B + tc::core_off(r, c, kH)) = __float2bfloat16_rn(a.w[1][e]);
   }
-  for (int e = t; e < 3 * kH; e += kTile) w2s[e] = a.w[2][e];
+  for (int e = t; e < 3 * kH; e += kTile) w2s[e] = __bfloat162float(__float2bfloat16_rn(a.w[2][e]));  // BF16 like W0, W1
   b0s[t] = a.b[0] ? a.b[0][t] : 0.f;
   b1s[t] = a.b[1] ? a.b[1][t] : 0.f;
   tc::fence_smem_to_async();
@@ -240,7 +267,7 @@ __global__ void __launch_bounds__(kTile, 1) head_tc_kernel(const HeadArgs a) {
     const float* frow = a.feat + sidx * a.feat_stride + 1;
     const float* drow = a.rays + (valid ? (int64_t)a.app_ray[row] : 0) * 6 + 3;
     // ---- X ----
-    build_x<C, F, V>(sX, t, valid, frow, drow);
+    build_x<C, F, V>(sX, sXlo, t, valid, frow, drow);
     tc::fence_smem_to_async();
     tc::fence_before_sync();
     __syncthreads();
@@ -251,6 +278,9 @@ __global__ void __launch_bounds__(kTile, 1) head_tc_kernel(const HeadArgs a) {
 #pragma unroll 1
       for (int s = 0; s < S::IN_PAD / 16; ++s)
         tc::mma_bf16(tS, desc_k(sX, S::IN_PAD, s), desc_k(sW0, S::IN_PAD, s), id, s > 0);
+#pragma unroll 1
+      for (int s = 0; s < S::IN_PAD / 16; ++s)
+        tc::mma_bf16(tS, desc_k(sXlo, S::IN_PAD, s), desc_k(sW0, S::IN_PAD, s), id, 1u);
       tc::mma_commit(mb);
     }
     if (!wait_mma()) break;
@@ -269,7 +299,7 @@ __global__ void __launch_bounds__(kTile, 1) head_tc_kernel(const HeadArgs a) {
       }
       mask0[q] = m;
 #pragma unroll
-      for (int g = 0; g < 4; ++g) store8(sH0, kH, t, q * 32 + g * 8, v + g * 8);
+      for (int g = 0; g < 4; ++g) store8_split(sH0, sH0lo, kH, t, q * 32 + g * 8, v + g * 8);
     }
     tc::fence_smem_to_async();
     tc::fence_before_sync();
@@ -280,6 +310,8 @@ __global__ void __launch_bounds__(kTile, 1) head_tc_kernel(const HeadArgs a) {
       const uint32_t id = tc::idesc_bf16(128, kH, false, false);
 #pragma unroll 1
       for (int s = 0; s < kH / 16; ++s) tc::mma_bf16(tS, desc_k(sH0, kH, s), desc_k(sW1, kH, s), id, s > 0);
+#pragma unroll 1
+      for (int s = 0; s < kH / 16; ++s) tc::mma_bf16(tS, desc_k(sH0lo, kH, s), desc_k(sW1, kH, s), id, 1u);
       tc::mma_commit(mb);
     }
     if (!wait_mma()) break;
@@ -462,7 +494,7 @@ __global__ void __launch_bounds__(kTile, 1) head_tc_kernel(const HeadArgs a) {
 
 template <int C, int F, int V, bool BWD>
 cudaError_t launch_tc(const HeadArgs& a, cudaStream_t s) {
-  constexpr int smem = Shape<C, F, V>::smem(BWD);
+  constexpr int smem = Shape<C, F, V>::smem();
   auto kern = head_tc_kernel<C, F, V, BWD>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;

@@ -110,7 +110,7 @@ def test_render_fused_bf16(case):
     res = O.render_rays(fspec, rspec, bg, cg, [bf(w) for w in ws], [None if b is None else b.detach().cpu().numpy()
                                                                    for b in bs],
                         d["rays"], jitter=d["u"] if meta["jitter"] else None, alpha_volume=d.get("alpha_volume"),
-                        g_rgb=g_rgb, head=head_oracle(m, meta))
+                        g_rgb=g_rgb, head=head_oracle(m, meta, bf))
     for l in range(6):
         assert rel_err(m.layout.basis_view(m.basis_flat.grad, l)[0], res["grad_basis"][l]) < 3e-2, l
     assert rel_err(m.layout.coeff_view(m.coeff_flat.grad, 0)[0], res["grad_coeff"]) < 3e-2
@@ -200,15 +200,25 @@ def _head_oracle_args(head, feat, dirs, g_rgb, bf16):
             feat.detach().cpu().numpy(), dirs.cpu().numpy(), g_rgb.cpu().numpy())
 
 
+def _kink_free(wn, bn, fsel, dsel, band=1e-4):
+    """Samples none of whose hidden pre-activations (FP64 oracle) lies within `band` of the ReLU
+    kink. There the exact gradient is a step function of the input: any rounding (even float32)
+    can put the sample on the other side and move its input gradient by a whole term, so the
+    per-sample comparison is made on the others (~1% of random samples excluded)."""
+    x = O.render_head_input(fsel, dsel, 6, 2)
+    p0 = x @ np.asarray(wn[0], np.float64).T + bn[0]
+    p1 = np.maximum(p0, 0) @ np.asarray(wn[1], np.float64).T + bn[1]
+    return (np.abs(p0).min(1) > band) & (np.abs(p1).min(1) > band)
+
+
 @pytest.mark.parametrize("channels", [27, 31])
 def test_mlp_head_tensor_cores_match_oracle(channels):
     """The tcgen05 head (ff_render_head_forward_tc / _backward_tc) through the C ABI against the
     FP64 oracle of the BF16-stored head (weights rounded to BF16): forward 2e-2, gradients 3e-2,
-    on 1,000 samples scattered over 1,500 rows (ragged last tile) of a 28 / 32-wide feature buffer;
-    rows that are not listed stay untouched. Calls twice: results repeat (the kernel's TMEM
-    accumulators start from zero on every launch)."""
-    import ctypes
-    from factor_fields_gb300 import _native as N
+    on ~1,000 samples scattered over 1,500 rows (ragged last tile) of a 28 / 32-wide feature
+    buffer, the samples within 1e-4 of a ReLU kink left out (_kink_free); rows that are not listed
+    stay untouched. Calls twice: results repeat (the kernel's TMEM accumulators start from zero on
+    every launch)."""
     from factor_fields_gb300.renderer import MLPRender_Fea, head_backward, head_forward
     torch.manual_seed(1)
     head = MLPRender_Fea(channels, num_layers=3, hidden_dim=128, viewpe=6, feape=2).cuda()
@@ -218,9 +228,15 @@ def test_mlp_head_tensor_cores_match_oracle(channels):
     rays = torch.randn(M, 6, generator=g).cuda()
     rays[:, 3:6] = torch.nn.functional.normalize(rays[:, 3:6], dim=-1)
     perm = torch.randperm(M, generator=g)[:n]
-    app_idx = perm.to(torch.int32).cuda()
-    app_ray = torch.randint(0, M, (n,), generator=g).to(torch.int32).cuda()
+    ray_pick = torch.randint(0, M, (n,), generator=g)
     g_rgb = torch.randn(M, 3, generator=g).cuda()
+    wn0, bn0, fn0, dn0, _ = _head_oracle_args(head, feat.cpu()[perm, 1:], rays.cpu()[ray_pick, 3:6],
+                                              g_rgb.cpu()[perm], bf16=True)
+    keep = torch.from_numpy(_kink_free(wn0, bn0, fn0, dn0))
+    assert int(keep.sum()) > 0.95 * n
+    app_idx = perm[keep].to(torch.int32).cuda()
+    app_ray = ray_pick[keep].to(torch.int32).cuda()
+    n = app_idx.shape[0]
     status = torch.zeros(1, dtype=torch.int32, device="cuda")
     outs = []
     for _ in range(2):
