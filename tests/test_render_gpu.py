@@ -200,11 +200,12 @@ def _head_oracle_args(head, feat, dirs, g_rgb, bf16):
             feat.detach().cpu().numpy(), dirs.cpu().numpy(), g_rgb.cpu().numpy())
 
 
-def _kink_free(wn, bn, fsel, dsel, band=1e-4):
-    """Samples none of whose hidden pre-activations (FP64 oracle) lies within `band` of the ReLU
-    kink. There the exact gradient is a step function of the input: any rounding (even float32)
-    can put the sample on the other side and move its input gradient by a whole term, so the
-    per-sample comparison is made on the others (~1% of random samples excluded)."""
+def _kink_free(wn, bn, fsel, dsel, band=5e-5):
+    """Samples none of whose 256 hidden pre-activations (FP64 oracle) lies within `band` of the
+    ReLU kink. There the exact gradient is a step function of the input: any rounding can put the
+    sample on the other side and move its input gradient by a whole term, so the per-sample
+    comparison is made on the others (~5% of random samples excluded). The band is ~20x the
+    pre-activation error of the split-BF16 operands (~2.5e-6 here)."""
     x = O.render_head_input(fsel, dsel, 6, 2)
     p0 = x @ np.asarray(wn[0], np.float64).T + bn[0]
     p1 = np.maximum(p0, 0) @ np.asarray(wn[1], np.float64).T + bn[1]
@@ -216,7 +217,7 @@ def test_mlp_head_tensor_cores_match_oracle(channels):
     """The tcgen05 head (ff_render_head_forward_tc / _backward_tc) through the C ABI against the
     FP64 oracle of the BF16-stored head (weights rounded to BF16): forward 2e-2, gradients 3e-2,
     on ~1,000 samples scattered over 1,500 rows (ragged last tile) of a 28 / 32-wide feature
-    buffer, the samples within 1e-4 of a ReLU kink left out (_kink_free); rows that are not listed
+    buffer, the samples within 5e-5 of a ReLU kink left out (_kink_free); rows that are not listed
     stay untouched. Calls twice: results repeat (the kernel's TMEM accumulators start from zero on
     every launch)."""
     from factor_fields_gb300.renderer import MLPRender_Fea, head_backward, head_forward
@@ -233,7 +234,7 @@ def test_mlp_head_tensor_cores_match_oracle(channels):
     wn0, bn0, fn0, dn0, _ = _head_oracle_args(head, feat.cpu()[perm, 1:], rays.cpu()[ray_pick, 3:6],
                                               g_rgb.cpu()[perm], bf16=True)
     keep = torch.from_numpy(_kink_free(wn0, bn0, fn0, dn0))
-    assert int(keep.sum()) > 0.95 * n
+    assert int(keep.sum()) > 0.9 * n
     app_idx = perm[keep].to(torch.int32).cuda()
     app_ray = ray_pick[keep].to(torch.int32).cuda()
     n = app_idx.shape[0]
