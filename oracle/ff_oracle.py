@@ -595,6 +595,39 @@ def render_rays(fspec, rspec, basis_grids, coeff_grid, mlp_w, mlp_b, rays, jitte
     return res
 
 
+def composite_rows(rspec, feat, z, dist, offsets, dirs, rgb_rows=None, white_bg=None):
+    """raw2alpha + colour + compositing (models/FactorFields.py:82-88, :876-896) over ragged rays
+    of live samples, in float64: feat [M, >= 1] (channel 0 density feature, 1..27 the SH-2
+    coefficients unless rgb_rows [M, 3] gives the colours), z / dist [M] (dist before
+    distance_scale), offsets [R + 1], dirs [R, 3] ray directions. Returns the clamped rgb [R, 3]."""
+    feat = np.asarray(feat, f64)
+    offsets = np.asarray(offsets)
+    wb = rspec.white_bg if white_bg is None else white_bg
+    out = np.zeros((len(offsets) - 1, 3))
+    for r in range(len(offsets) - 1):
+        a, b = int(offsets[r]), int(offsets[r + 1])
+        if b == a:
+            rgb = np.zeros(3)
+            acc = 0.0
+        else:
+            sigma = softplus_shift(feat[a:b, 0], rspec.density_shift)
+            _, w, _ = raw2alpha(sigma[None], np.asarray(dist[a:b], f64)[None] * rspec.distance_scale)
+            w = w[0]
+            app = w > rspec.weight_thres
+            if rgb_rows is None:
+                sh = feat[a:b, 1:28].reshape(-1, 3, 9)
+                col = sigmoid(eval_sh2(sh, np.broadcast_to(np.asarray(dirs[r], f64), (b - a, 3))))
+            else:
+                col = np.asarray(rgb_rows[a:b], f64)
+            col = col * app[:, None]
+            acc = w.sum()
+            rgb = (w[:, None] * col).sum(0)
+        if wb:
+            rgb = rgb + (1.0 - acc)
+        out[r] = np.clip(rgb, 0, 1)
+    return out
+
+
 # ----------------------------------------------------------------------------------------
 # inverse-CDF resampling
 # ----------------------------------------------------------------------------------------
