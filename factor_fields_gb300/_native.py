@@ -88,6 +88,9 @@ SIGNATURES = {
     "ff_field_mlp_forward": (c_i32, [_P(FFField), c_vp, c_vp, _P(FFMlp), c_vp, c_i64, c_vp, c_vp]),
     "ff_field_mlp_backward": (c_i32, [_P(FFField), c_vp, c_vp, _P(FFMlp), c_vp, c_i64, c_vp, c_vp, c_vp,
                                       _P(FFMlpGrad), c_vp]),
+    "ff_field_mlp_forward_counted": (c_i32, [_P(FFField), c_vp, c_vp, _P(FFMlp), c_vp, c_i64, c_vp, c_vp, c_vp]),
+    "ff_field_mlp_backward_counted": (c_i32, [_P(FFField), c_vp, c_vp, _P(FFMlp), c_vp, c_i64, c_vp, c_vp, c_vp,
+                                              c_vp, _P(FFMlpGrad), c_vp]),
     "ff_field_fit_step": (c_i32, [_P(FFField), c_vp, c_vp, _P(FFMlp), c_vp, c_vp, c_i64, c_i32, c_f32, c_vp, c_vp,
                                   c_vp, _P(FFMlpGrad), c_vp]),
     "ff_field_fit_binned_workspace_bytes": (c_i64, [_P(FFField), c_i64, c_i32]),

@@ -221,6 +221,31 @@ int ff_field_mlp_backward(const FFField* f, const void* basis, const void* coeff
                      "ff_field_mlp_backward launch");
 }
 
+int ff_field_mlp_forward_counted(const FFField* f, const void* basis, const void* coeff, const FFMlp* m,
+                                 const float* x, int64_t n_max, const int64_t* n_dev, float* out, void* stream) {
+  int rc = validate_fused(f, basis, coeff, m, x, n_max);
+  if (rc) return rc;
+  if (n_max > 0 && (!out || !n_dev)) return set_error(FF_ERR_ARG, "out / n_dev is NULL");
+  if (!aligned(n_dev, 8)) return set_error(FF_ERR_ALIGN, "n_dev must be 8-byte aligned");
+  return cuda_status(launch_fused_forward(*f, basis, coeff, *m, x, n_max, out, (cudaStream_t)stream, n_dev),
+                     "ff_field_mlp_forward_counted launch");
+}
+
+int ff_field_mlp_backward_counted(const FFField* f, const void* basis, const void* coeff, const FFMlp* m,
+                                  const float* x, int64_t n_max, const int64_t* n_dev, const float* grad_out,
+                                  float* grad_basis, float* grad_coeff_grid, const FFMlpGrad* g, void* stream) {
+  int rc = validate_fused(f, basis, coeff, m, x, n_max);
+  if (rc) return rc;
+  if (n_max > 0 && (!grad_out || !n_dev)) return set_error(FF_ERR_ARG, "grad_out / n_dev is NULL");
+  if (!aligned(n_dev, 8)) return set_error(FF_ERR_ALIGN, "n_dev must be 8-byte aligned");
+  if (!grad_basis || !grad_coeff_grid || !aligned(grad_basis, 16) || !aligned(grad_coeff_grid, 16))
+    return set_error(FF_ERR_ARG, "grid gradient buffers must be non-NULL and 16-byte aligned");
+  FFMlpGrad none = {};
+  return cuda_status(launch_fused_backward(*f, basis, coeff, *m, x, n_max, grad_out, grad_basis, grad_coeff_grid,
+                                           g ? *g : none, (cudaStream_t)stream, n_dev),
+                     "ff_field_mlp_backward_counted launch");
+}
+
 int ff_field_fit_step(const FFField* f, const void* basis, const void* coeff, const FFMlp* m, const float* x,
                       const float* target, int64_t n, int32_t loss_kind, float loss_scale, float* loss_sum,
                       float* grad_basis, float* grad_coeff_grid, const FFMlpGrad* g, void* stream) {

@@ -35,11 +35,14 @@ cudaError_t launch_mlp_backward(const FFMlp& m, const float* x, int64_t n, const
 
 // fused_kernels.cu
 const char* fused_unsupported(const FFField& f, const FFMlp& m);  // nullptr when supported
+// n_dev (optional): a device count; the launch is sized for n points and processes min(n, *n_dev)
 cudaError_t launch_fused_forward(const FFField& f, const void* basis, const void* coeff, const FFMlp& m,
-                                 const float* x, int64_t n, float* out, cudaStream_t st);
+                                 const float* x, int64_t n, float* out, cudaStream_t st,
+                                 const int64_t* n_dev = nullptr);
 cudaError_t launch_fused_backward(const FFField& f, const void* basis, const void* coeff, const FFMlp& m,
                                   const float* x, int64_t n, const float* grad_out, float* grad_basis,
-                                  float* grad_coeff, const FFMlpGrad& g, cudaStream_t st);
+                                  float* grad_coeff, const FFMlpGrad& g, cudaStream_t st,
+                                  const int64_t* n_dev = nullptr);
 cudaError_t launch_fused_fit(const FFField& f, const void* basis, const void* coeff, const FFMlp& m,
                              const float* x, const float* target, int64_t n, int loss_kind, float loss_scale,
                              float* loss_sum, float* grad_basis, float* grad_coeff, const FFMlpGrad& g,

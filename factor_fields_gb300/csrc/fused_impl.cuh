@@ -80,6 +80,7 @@ struct FusedArgs {
   const float* x;
   int64_t x_stride;  // floats between consecutive points' coordinates (coord_dim, or the packed row)
   int64_t n;
+  const int64_t* n_dev;  // optional device count: the points processed are min(n, *n_dev)
   float* out;             // kFwd: [n, out]
   const float* grad_out;  // kBwd: [n, out]
   const float* target;    // kFit: [n, out] rows t_stride floats apart
@@ -259,9 +260,10 @@ __global__ void __launch_bounds__(kThreads, 3) fused_field_mlp_kernel(const Fuse
 #pragma unroll
   for (int nt = 0; nt < (OUTT > 1 ? OUTT : 1); ++nt) acc_w1t[nt][0] = acc_w1t[nt][1] = acc_w1t[nt][2] = acc_w1t[nt][3] = 0.f;
 
-  for (int64_t base = (int64_t)blockIdx.x * kTile; base < a.n; base += (int64_t)gridDim.x * kTile) {
+  const int64_t n_pts = a.n_dev ? min(a.n, *a.n_dev) : a.n;
+  for (int64_t base = (int64_t)blockIdx.x * kTile; base < n_pts; base += (int64_t)gridDim.x * kTile) {
     const int64_t i = base + warp * 32 + lane;
-    const bool valid = i < a.n;
+    const bool valid = i < n_pts;
     float bv[kF], cv[kF];
     float p[CD];
     // ---------------- gather ----------------
@@ -370,8 +372,8 @@ __global__ void __launch_bounds__(kThreads, 3) fused_field_mlp_kernel(const Fuse
 #pragma unroll
           for (int j = 0; j < 2; ++j) {
             if (c0 + j < out) {
-              if (row0 < a.n) a.out[row0 * out + c0 + j] = oc[nt][j];
-              if (row1 < a.n) a.out[row1 * out + c0 + j] = oc[nt][2 + j];
+              if (row0 < n_pts) a.out[row0 * out + c0 + j] = oc[nt][j];
+              if (row1 < n_pts) a.out[row1 * out + c0 + j] = oc[nt][2 + j];
             }
           }
         }
@@ -391,7 +393,7 @@ __global__ void __launch_bounds__(kThreads, 3) fused_field_mlp_kernel(const Fuse
             const int64_t row = (q < 2) ? row0 : row1;
             const int col = c0 + (q & 1);
             float d = 0.f;
-            if (row < a.n && col < out) {
+            if (row < n_pts && col < out) {
               if constexpr (is_fit<MODE>()) {
                 const float tv = (kPackedRow && a.packed_rows) ? ((q < 2) ? tr0 : tr1)
                                                                : a.target[row * a.t_stride + col];

@@ -17,10 +17,11 @@ const char* fused_unsupported(const FFField& f, const FFMlp& m) {
 }
 
 cudaError_t launch_fused_forward(const FFField& f, const void* basis, const void* coeff, const FFMlp& m,
-                                 const float* x, int64_t n, float* out, cudaStream_t st) {
+                                 const float* x, int64_t n, float* out, cudaStream_t st, const int64_t* n_dev) {
   if (n == 0) return cudaSuccess;
   FusedArgs a = make_args(f, basis, coeff, m, x, n);
   a.out = out;
+  a.n_dev = n_dev;
   return dispatch<kFwd>(a, st);
 }
 

@@ -335,12 +335,13 @@ class FactorFields(torch.nn.Module):
         self.nSamples = n
 
     def forward(self, rays_chunk, white_bg=True, is_train=False, ndc_ray=False, N_samples=-1, jitter=None,
-                fused=None):
+                fused=None, static=False):
         """models/FactorFields.py:843-898 (bounded scenes): (rgb_map, depth_map, coeffs).
-        fused=None picks the fused BF16 field kernel when precision == 'bf16'."""
+        fused=None picks the fused BF16 field kernel when precision == 'bf16'; static=True renders
+        without host synchronisation (CUDA-graph capturable; fused path, SH-2 head)."""
         from .renderer import render_forward
         return render_forward(self, rays_chunk, white_bg=white_bg, is_train=is_train, ndc_ray=ndc_ray,
-                              N_samples=N_samples, jitter=jitter, fused=fused)
+                              N_samples=N_samples, jitter=jitter, fused=fused, static=static)
 
     # ---- occupancy maintenance (models/FactorFields.py:710-793) ----------------------------
     @torch.no_grad()

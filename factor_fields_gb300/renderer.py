@@ -256,6 +256,25 @@ def march(model, rays, jitter, rdesc):
     return offsets, xyz, sidx
 
 
+def march_static(model, rays, jitter, rdesc):
+    """march() without the host read of the live-sample count: xyz / sample_idx sized for every
+    sample slot (n_rays * n_samples rows, the first offsets[-1] of them written), the count left on
+    the device in offsets[-1]. Returns (offsets, xyz, sample_idx)."""
+    n = rays.shape[0]
+    dev = rays.device
+    st = N.stream_ptr()
+    counts = torch.empty(n, dtype=torch.int32, device=dev)
+    N.call("ff_march_count", ctypes.byref(rdesc), N.ptr(rays), N.ptr(jitter), n, N.ptr(counts), None, st)
+    offsets = scan_counts(counts)
+    m_max = n * int(rdesc.n_samples)
+    xyz = torch.empty(m_max, 3, device=dev)
+    sidx = torch.empty(m_max, dtype=torch.int32, device=dev)
+    if n:
+        N.call("ff_march_emit", ctypes.byref(rdesc), N.ptr(rays), N.ptr(jitter), n, N.ptr(offsets), N.ptr(xyz),
+               N.ptr(sidx), st)
+    return offsets, xyz, sidx
+
+
 class RenderFunction(torch.autograd.Function):
     """rgb, depth = render(rays) with gradients to the grids and the MLP head.
 
@@ -265,7 +284,11 @@ class RenderFunction(torch.autograd.Function):
     @staticmethod
     def forward(ctx, rays, jitter, basis_param, coeff_param, w0, b0, w1, job):
         m, rdesc = job["model"], job["rdesc"]
-        offsets, xyz, sidx = march(m, rays, jitter, rdesc)
+        if job.get("static"):  # no host synchronisation: capturable in a CUDA graph
+            offsets, xyz, sidx = march_static(m, rays, jitter, rdesc)
+            job["n_dev"] = offsets[rays.shape[0]:]
+        else:
+            offsets, xyz, sidx = march(m, rays, jitter, rdesc)
         feat = field_eval(m, job, xyz)
         n = rays.shape[0]
         rgb = torch.empty(n, 3, device=rays.device)
@@ -379,7 +402,10 @@ def field_eval(m, job, xyz):
     lm = m.linear_mat
     ws, bs = lm.weights()
     mlp = FN.mlp_struct(ws, bs, lm.in_dim, lm.hidden_dim, lm.out_dim)
-    if job["fused"]:
+    if job["fused"] and job.get("n_dev") is not None:
+        N.call("ff_field_mlp_forward_counted", ctypes.byref(job["fdesc"]), N.ptr(job["basis_r"]),
+               N.ptr(job["coeff_r"]), ctypes.byref(mlp), N.ptr(xyz), n, N.ptr(job["n_dev"]), N.ptr(out), st)
+    elif job["fused"]:
         N.call("ff_field_mlp_forward", ctypes.byref(job["fdesc"]), N.ptr(job["basis_r"]), N.ptr(job["coeff_r"]),
                ctypes.byref(mlp), N.ptr(xyz), n, N.ptr(out), st)
     else:
@@ -428,7 +454,11 @@ def field_grad(m, job, xyz, g_out):
         for i in range(len(ws)):
             g.weight[i] = gw[i].data_ptr()
             g.bias[i] = gbias[i].data_ptr() if gbias[i] is not None else None
-        if job["fused"]:
+        if job["fused"] and job.get("n_dev") is not None:
+            N.call("ff_field_mlp_backward_counted", ctypes.byref(job["fdesc"]), N.ptr(job["basis_r"]),
+                   N.ptr(job["coeff_r"]), ctypes.byref(mlp), N.ptr(xyz), n, N.ptr(job["n_dev"]), N.ptr(g_out),
+                   N.ptr(gb), N.ptr(gc), ctypes.byref(g), st)
+        elif job["fused"]:
             N.call("ff_field_mlp_backward", ctypes.byref(job["fdesc"]), N.ptr(job["basis_r"]),
                    N.ptr(job["coeff_r"]), ctypes.byref(mlp), N.ptr(xyz), n, N.ptr(g_out), N.ptr(gb), N.ptr(gc),
                    ctypes.byref(g), st)
@@ -445,12 +475,15 @@ def field_grad(m, job, xyz, g_out):
 
 
 def render_forward(model, rays_chunk, white_bg=True, is_train=False, ndc_ray=False, N_samples=-1, fused=None,
-                   jitter=None):
+                   jitter=None, static=False):
     """FactorFields.forward (models/FactorFields.py:843-898), bounded scenes, with the model's
     colour head (MLPRender_Fea or the SH-2 head): returns (rgb_map [R, 3], depth_map [R], coeffs).
 
     jitter: optional per-ray sample offsets [R] in [0, 1) (the reference draws them with
-    torch.rand_like when is_train); given explicitly they make sampling reproducible."""
+    torch.rand_like when is_train); given explicitly they make sampling reproducible.
+    static: no host synchronisation (live-sample buffers sized for every sample slot, the
+    live count read by the kernels on the device), so the call can be captured in a CUDA graph;
+    the fused BF16 path with the SH-2 head only."""
     if ndc_ray:
         raise NotImplementedError("NDC rays (sample_point_ndc) are not on this path")
     mlp_head = isinstance(model.renderModule, MLPRender_Fea)
@@ -476,7 +509,9 @@ def render_forward(model, rays_chunk, white_bg=True, is_train=False, ndc_ray=Fal
         coeff_param = model._coeff_scene(model.coeff_flat)
         coeff_r = model._coeff_scene(coeff_r)
     job = {"model": model, "rdesc": render_desc(model, n_samples, wb), "fdesc": model.descriptor(dt),
-           "basis_r": basis_r, "coeff_r": coeff_r, "coeff_param": coeff_param, "fused": fused}
+           "basis_r": basis_r, "coeff_r": coeff_r, "coeff_param": coeff_param, "fused": fused, "static": static}
+    if static and (mlp_head or not fused):
+        raise NotImplementedError("static (graph-capturable) rendering needs the fused BF16 path and the SH-2 head")
     l0, l1 = lm.backbone
     if mlp_head:
         rgb, depth = RenderFunctionMLP.apply(rays, jitter, model.basis_flat, coeff_param, l0.weight, l0.bias,
@@ -485,7 +520,7 @@ def render_forward(model, rays_chunk, white_bg=True, is_train=False, ndc_ray=Fal
         rgb, depth = RenderFunction.apply(rays, jitter, model.basis_flat, coeff_param, l0.weight, l0.bias, l1.weight,
                                           job)
     coeffs = torch.zeros((1, model.n_feat), device=rays.device)
-    if getattr(model, "return_coeffs", False) and job["xyz"].shape[0]:
+    if getattr(model, "return_coeffs", False) and not static and job["xyz"].shape[0]:
         with torch.no_grad():
             coeffs = model.get_coeff(job["xyz"])
     return rgb, depth, coeffs

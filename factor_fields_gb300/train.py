@@ -28,13 +28,14 @@ class RadianceFieldTrainer:
         self._grads_clean = False  # every gradient is known to be zero (a fused step zeroed them)
         self.lr_factor = decay_ratio ** (1.0 / max(n_iters, 1))
         self.sampler = sampler  # None: the plain uniform sampler; else a ProposalSampler
-        self.jitter = None  # proposal sampler: fixed per-ray stratification jitter [R]; None: random per step
+        self.jitter = None  # fixed per-ray sample jitter [R] for training renders; None: random per step
 
-    def render(self, rays, is_train):
+    def render(self, rays, is_train, static=False):
         if self.sampler is not None:
             return self.sampler.render(rays, is_train=is_train, white_bg=self.white_bg,
                                        jitter=self.jitter if is_train else None)
-        rgb, depth, _ = self.m(rays, white_bg=self.white_bg, is_train=is_train, N_samples=self.n_samples)
+        rgb, depth, _ = self.m(rays, white_bg=self.white_bg, is_train=is_train, N_samples=self.n_samples,
+                               jitter=self.jitter if is_train else None, static=static)
         return rgb, depth
 
     def _side_stream(self):
@@ -50,8 +51,8 @@ class RadianceFieldTrainer:
             params += self.sampler.params
         zero_grads(params)
 
-    def step(self, rays, rgb_gt, optimize=True):
-        rgb, _ = self.render(rays, is_train=True)
+    def step(self, rays, rgb_gt, optimize=True, static=False):
+        rgb, _ = self.render(rays, is_train=True, static=static)
         loss = torch.mean((rgb - rgb_gt) ** 2)
         if not self._grads_clean:
             self._zero_grads()
@@ -79,12 +80,13 @@ class RadianceFieldTrainer:
         return loss.detach()
 
     def graph_step(self, rays, rgb_gt):
-        """step(optimize=False) replayed from a CUDA graph (fixed-size sampling only: the
-        proposal sampler). The batch is copied into static buffers; the capture covers the
-        gradient zeroing, rendering, loss, the field backward and the proposal loss/backward.
-        Re-captured when the batch shape changes."""
-        if self.sampler is None:
-            raise ValueError("the plain sampler's live-sample count varies per batch: use step()")
+        """step(optimize=False) replayed from a CUDA graph. The batch is copied into static
+        buffers; the capture covers the gradient zeroing, rendering, loss, the field backward and
+        (proposal sampler) the proposal loss/backward. The plain sampler renders without host
+        synchronisation for this (static=True: live-sample buffers sized for all n_rays *
+        n_samples slots, the live count read on the device; fused BF16 path, SH-2 head). The per-ray
+        jitter is drawn inside the graph (or self.jitter). Re-captured when the batch shape changes."""
+        static = self.sampler is None
         key = (tuple(rays.shape), tuple(rgb_gt.shape))
         if getattr(self, "_gkey", None) != key:
             dev = self.m.basis_flat.device
@@ -96,14 +98,15 @@ class RadianceFieldTrainer:
             side.wait_stream(torch.cuda.current_stream())
             with torch.cuda.stream(side):
                 for _ in range(2):
-                    self.step(self._gr, self._gg, optimize=False)
+                    self.step(self._gr, self._gg, optimize=False, static=static)
             torch.cuda.current_stream().wait_stream(side)
             self._graph = torch.cuda.CUDAGraph()
             with torch.cuda.graph(self._graph):
-                self._gloss = self.step(self._gr, self._gg, optimize=False)
+                self._gloss = self.step(self._gr, self._gg, optimize=False, static=static)
             self._gkey = key
         self.m._read_buffers()
-        self.sampler.grid_read()
+        if self.sampler is not None:
+            self.sampler.grid_read()
         self._gr.copy_(rays, non_blocking=True)
         self._gg.copy_(rgb_gt, non_blocking=True)
         self._graph.replay()

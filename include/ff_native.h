@@ -170,6 +170,18 @@ FF_API int ff_field_mlp_backward(const FFField* f, const void* basis, const void
                                  const float* x, int64_t n, const float* grad_out, float* grad_basis,
                                  float* grad_coeff_grid, const FFMlpGrad* g, void* stream);
 
+/* ff_field_mlp_forward / _backward for a point count known only on the device: the launch is
+ * sized for n_max points and processes the first min(n_max, *n_dev) of them (n_dev: device
+ * int64, e.g. the last entry of ff_scan_counts' offsets: the number of live ray samples), so a
+ * render step needs no host read of the live-sample count. Rows past the count are not touched. */
+FF_API int ff_field_mlp_forward_counted(const FFField* f, const void* basis, const void* coeff, const FFMlp* m,
+                                        const float* x, int64_t n_max, const int64_t* n_dev, float* out,
+                                        void* stream);
+FF_API int ff_field_mlp_backward_counted(const FFField* f, const void* basis, const void* coeff, const FFMlp* m,
+                                         const float* x, int64_t n_max, const int64_t* n_dev,
+                                         const float* grad_out, float* grad_basis, float* grad_coeff_grid,
+                                         const FFMlpGrad* g, void* stream);
+
 /* One regression step of the notebooks' field fit (scripts/2D_regression.ipynb cell 4,
  * scripts/sdf_regression.ipynb cell 2) up to the optimizer: forward, loss against target
  * [n, out_dim] (FF_LOSS_L1: mean |o - t|, FF_LOSS_MSE: mean (o - t)^2; gradients scaled by

@@ -275,3 +275,39 @@ def test_mlp_head_tensor_cores_match_oracle(channels):
     assert torch.equal(r2[0], outs[0][0]) and torch.equal(r2[1], outs[0][1])
     for a, b in zip(r2[2], outs[0][2]):
         assert rel_err(a, b) < 1e-5  # weight-gradient atomics: summation order may differ
+
+
+def test_static_render_and_plain_graph_step():
+    """Rendering without host synchronisation (static=True: live-sample buffers sized for every
+    sample slot, the count read on the device by ff_field_mlp_*_counted) equals the default path
+    (rgb / depth bit-identical, gradients to float32 rounding), and the plain sampler's training
+    step replays from a CUDA graph with the same loss and gradients as the eager step."""
+    from factor_fields_gb300 import FactorFields
+    from factor_fields_gb300 import workloads as W
+    from factor_fields_gb300.train import RadianceFieldTrainer
+    torch.manual_seed(0)
+    m = FactorFields(W.field_cfg("cfg2"), device="cuda", precision="bf16")
+    rays = torch.from_numpy(W.BlobScene(0).ray_pool(1024, 21)).float().cuda()
+    jit = torch.rand(1024, generator=torch.Generator().manual_seed(2)).cuda()
+    res = []
+    for static in (False, True):
+        m.zero_grad(set_to_none=True)
+        rgb, depth, _ = m(rays, white_bg=True, is_train=True, N_samples=1024, jitter=jit, static=static)
+        (rgb * rgb).sum().backward()
+        res.append((rgb.detach().clone(), depth.clone(), m.basis_flat.grad.clone(), m.coeff_flat.grad.clone(),
+                    m.linear_mat.backbone[0].weight.grad.clone()))
+    assert torch.equal(res[0][0], res[1][0]) and torch.equal(res[0][1], res[1][1])
+    for a, b in zip(res[0][2:], res[1][2:]):
+        assert rel_err(a, b) < 1e-6
+    gt = torch.rand(1024, 3, generator=torch.Generator().manual_seed(3)).cuda()
+    tr = RadianceFieldTrainer(m, n_samples=1024)
+    tr.jitter = jit
+    params = [m.basis_flat, m.coeff_flat] + list(m.linear_mat.parameters())
+    l_eager = float(tr.step(rays, gt, optimize=False))
+    g_eager = [p.grad.clone() for p in params]
+    for _ in range(2):  # capture, then a replay
+        l_graph = float(tr.graph_step(rays, gt))
+    g_graph = [p.grad.clone() for p in params]
+    assert abs(l_graph - l_eager) <= 1e-6 * abs(l_eager)
+    for a, b in zip(g_eager, g_graph):
+        assert rel_err(b, a) < 1e-5
