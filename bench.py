@@ -97,11 +97,38 @@ def flush_l2(buf):
     buf.zero_()
 
 
-def make_model(precision):
+# The field-fit workloads measured (configurations 0, 1 and 4): points per step, loss, workload.
+FIELD_CONFIGS = {
+    "cfg1": {"points": 262144, "loss": "l1",
+             "workload": WORKLOAD},
+    "cfg0": {"points": 65536, "loss": "mse",
+             "workload": "cfg0: 2-D image fit, 512x512x3 procedural image, 6-level grid basis [4,4,4,2,2,2] @ "
+                         "[32..128]^2, coeff 18x271^2, 2x64 ReLU head to RGB, MSE"},
+    "cfg4": {"points": 262144, "loss": "mse",
+             "workload": "cfg4: image set, 256 procedural 256x256x3 images, shared 6-level 2-D basis, "
+                         "per-image coeff 18x32^2 ([1,18,256,32,32]), 2x64 head, MSE"},
+}
+
+
+def field_batches(key, seed0, nb):
+    """nb seeded batches (points, targets) of configuration `key`, generated on the host."""
+    from factor_fields_gb300 import workloads as W
+    n = FIELD_CONFIGS[key]["points"]
+    if key == "cfg1":
+        return [W.sdf_batch(seed0 + i, n) for i in range(nb)]
+    if key == "cfg0":
+        img = W.ProceduralImage(0, 512, 512)
+        return [W.image_batch(seed0 + i, n, img=img) for i in range(nb)]
+    return [W.image_set_batch(seed0 + i, n) for i in range(nb)]
+
+
+def make_model(precision, key="cfg1"):
     from factor_fields_gb300 import FactorFields
     from factor_fields_gb300 import workloads as W
     torch.manual_seed(0)
-    m = FactorFields(W.field_cfg("cfg1"), device="cuda", precision=precision)
+    m = FactorFields(W.field_cfg(key), device="cuda", precision=precision)
+    if key == "cfg0":
+        m.freq_bands = W.FREQ6
     g = torch.Generator(device="cpu").manual_seed(1)
     with torch.no_grad():  # a mid-training-like state: random coefficients
         for c in m.coeffs:
@@ -119,11 +146,12 @@ def bytes_per_point(m, gathers, param_bytes):
     """Algorithmic bytes per point: `gathers` passes over K corners x (sum C + C_coeff)
     channels at param_bytes, one float32 scatter of the same, coords + targets (4 B each).
     The fwd+bwd algorithm gathers twice (the backward re-reads the grid values it multiplies
-    by): 2 G + S + IO = 2,320 B for the 3-D BF16 point; the fused kernel keeps the values in
-    registers and reads them once (1 G + S + IO = 1,744 B)."""
+    by): 2 G + S + IO = 2,320 B for the 3-D BF16 point (1,172 B for a 2-D point, 1,176 B for the
+    image set's (x, y, image) point); the fused kernel keeps the values in registers and reads
+    them once (1 G + S + IO = 1,744 B in 3-D)."""
     k = 2 ** m.in_dim
     ch = m.n_feat * 2
-    return gathers * k * ch * param_bytes + k * ch * 4 + 4 * m.in_dim + 4 * m.linear_mat.out_dim
+    return gathers * k * ch * param_bytes + k * ch * 4 + 4 * m.geom.coord_dim + 4 * m.linear_mat.out_dim
 
 
 def max_over_ranks(vals):
@@ -146,23 +174,29 @@ def whole_job_rate(points_per_rank_step, steps, world_size, ms_max):
     return points_per_rank_step * steps * world_size / (ms_max / 1e3)
 
 
-def run_native(args, ws, rank, local):
+def load_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except OSError:
+        return {}
+
+
+def measure_field(key, args, ws, rank, local, flush, with_dropin):
+    """One field-fit configuration (FIELD_CONFIGS): the fused BF16 binned step replayed from CUDA
+    graphs over resident batches (value), the fit kernel alone under CUDA events (roofline), the
+    public API from pinned host memory (e2e) and optionally the float32 drop-in path."""
     from factor_fields_gb300 import _native as N
-    from factor_fields_gb300 import workloads as W
     from factor_fields_gb300 import train as T
-    torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    n = N_POINTS
-    nb = 8  # distinct batches cycled through (seeded, generated on the host)
-    batches = [W.sdf_batch(1000 * rank + i, n) for i in range(nb)]
+    fc = FIELD_CONFIGS[key]
+    n = fc["points"]
+    nb = 8 if key != "cfg4" else 4  # distinct batches cycled through (seeded, generated on the host)
+    batches = field_batches(key, 1000 * rank, nb)
     host = [(torch.from_numpy(x).pin_memory(), torch.from_numpy(y).pin_memory()) for x, y in batches]
     devb = [(x.to(dev), y.to(dev)) for x, y in host]
-    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MB > L2
-
-    res = {}
-    # ---- fast path: the fused BF16 fit step (binned), replayed from CUDA graphs ----
-    m = make_model("bf16")
-    runner = T.FieldFitRunner(m, loss="l1")
+    m = make_model("bf16", key)
+    runner = T.FieldFitRunner(m, loss=fc["loss"])
     stream = torch.cuda.current_stream()
 
     def timed(step_fn, k, with_kernel_events):
@@ -201,13 +235,12 @@ def run_native(args, ws, rank, local):
     clocks = Clocks(local)
     clocks.start()
     t_fast, _ = timed(lambda i: runner.graph_step(*devb[i % nb]), args.steps, False)
-    launches = per_step * args.steps
     # the dominant kernel alone, CUDA events around its launch on the launching stream
     _, k_fast = timed(lambda i: runner.step(*devb[i % nb], kernel_events=True), args.steps, "kernel")
     ck = clocks.stop()
     ms = float(np.sum(t_fast))
 
-    # ---- end to end through the public API from pinned host memory ----
+    # end to end through the public API from pinned host memory
     loss_host = torch.empty(1, pin_memory=True)
 
     def e2e_step(i):
@@ -220,65 +253,85 @@ def run_native(args, ws, rank, local):
         e2e_step(i)
     t_e2e, _ = timed(e2e_step, args.steps, False)
 
-    # ---- the float32 drop-in path (autograd through get_coding / linear_mat) ----
-    md = make_model("fp32")
+    ms_drop = None
+    if with_dropin:  # the float32 drop-in path (autograd through get_coding / linear_mat)
+        md = make_model("fp32", key)
 
-    def dropin_step(i):
-        x, y = devb[i % nb]
-        md.zero_grad(set_to_none=True)
-        feats, _ = md.get_coding(x)
-        pred = md.linear_mat(feats)
-        (pred - y).abs().mean().backward()
-        return None
+        def dropin_step(i):
+            x, y = devb[i % nb]
+            md.zero_grad(set_to_none=True)
+            feats, _ = md.get_coding(x)
+            pred = md.linear_mat(feats)
+            err = pred - y
+            (err.abs().mean() if fc["loss"] == "l1" else (err * err).mean()).backward()
+            return None
 
-    for i in range(args.warmup):
-        dropin_step(i)
-    t_drop, _ = timed(dropin_step, args.steps, False)
+        for i in range(args.warmup):
+            dropin_step(i)
+        t_drop, _ = timed(dropin_step, args.steps, False)
+        ms_drop = float(np.sum(t_drop))
 
-    # ---- max over ranks ----
-    ms, ms_e2e, ms_drop = max_over_ranks([ms, float(np.sum(t_e2e)), float(np.sum(t_drop))])
+    vals = max_over_ranks([ms, float(np.sum(t_e2e))] + ([ms_drop] if with_dropin else []))
+    ms, ms_e2e = vals[0], vals[1]
     pts = n * args.steps * ws
-    value = whole_job_rate(n, args.steps, ws, ms)
     kern_ms = float(np.mean(k_fast)) if k_fast else None  # the fit kernel alone
     # the whole ff_field_fit_step_binned call (binning with the gradient zeroing + the fit kernel):
     # the graph-replayed step is exactly that call, so its time is the step's
     call_ms = ms / args.steps
-    pb = 2 if m.precision == "bf16" else 4
-    bpp = bytes_per_point(m, 2, pb)  # the fwd+bwd algorithm's bytes
-    bpp_read_once = bytes_per_point(m, 1, pb)  # what the fused kernel reads and writes
-    peaks = {}
-    try:
-        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
-            peaks = json.load(f)
-    except OSError:
-        pass
+    bpp = bytes_per_point(m, 2, 2)  # the fwd+bwd algorithm's bytes (BF16 grids)
+    bpp_read_once = bytes_per_point(m, 1, 2)  # what the fused kernel reads and writes
+    peaks = load_peaks()
     peak = peaks.get("hbm_gbs", 6800.0)
     achieved = (bpp * n) / (kern_ms / 1e3) / 1e9 if kern_ms else None
     achieved_call = (bpp * n) / (call_ms / 1e3) / 1e9 if call_ms else None
-    res = {
-        "metric": METRIC, "value": value, "unit": "samples/s", "n_gpus": ws, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "bf16 storage, fp32 accumulation" if m.precision == "bf16" else "fp32",
-        "data": "synthetic (seeded analytic SDF: 16 spheres + 8 boxes)",
-        "config": bench_config(ws), "path": runner.path_name,
-        "e2e": {"value": pts / (ms_e2e / 1e3), "unit": "samples/s", "h2d_bytes_per_step": n * 16,
-                "d2h_bytes_per_step": 4},
-        "fp32_dropin": {"value": pts / (ms_drop / 1e3), "unit": "samples/s",
-                        "ms_per_step": ms_drop / args.steps},
+    xin, yin = host[0]
+    out = {
+        "workload": fc["workload"], "points_per_step": n, "loss": fc["loss"],
+        "value": whole_job_rate(n, args.steps, ws, ms), "unit": "samples/s", "ms_per_step": ms / args.steps,
+        "path": runner.path_name,
+        "e2e": {"value": pts / (ms_e2e / 1e3), "unit": "samples/s",
+                "h2d_bytes_per_step": int(xin.numel() * 4 + yin.numel() * 4), "d2h_bytes_per_step": 4},
         "roofline": {"bound": "hbm", "kernel": runner.dominant_kernel, "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": (achieved / peak) if achieved else None,
-                     "traffic": NCU_TRAFFIC.get(runner.dominant_kernel),
-                     "traffic_source": "ncu dram read+write of the fit kernel, one 262,144-point launch "
-                                       "(profiles/fused_fit_kernel_cfg1_ncu.md)",
                      "bytes_per_point": bpp, "bytes_per_point_read_once": bpp_read_once,
                      "frac_read_once": (achieved * bpp_read_once / bpp / peak) if achieved else None,
-                     "kernel_ms": kern_ms,
-                     "call": runner.dominant_call, "call_ms": call_ms,
+                     "kernel_ms": kern_ms, "call": runner.dominant_call, "call_ms": call_ms,
                      "call_frac": (achieved_call / peak) if achieved_call else None,
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if "hbm_gbs" in peaks else "fallback"},
-        "gpu_launches": launches,
+        "gpu_launches": per_step * args.steps,
         "clocks": ck,
     }
+    if with_dropin:
+        out["fp32_dropin"] = {"value": pts / (vals[2] / 1e3), "unit": "samples/s", "ms_per_step": vals[2] / args.steps}
+    return out, m
+
+
+def run_native(args, ws, rank, local):
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MB > L2
+    r1, _ = measure_field("cfg1", args, ws, rank, local, flush, with_dropin=True)
+    roof = dict(r1["roofline"])
+    roof["traffic"] = NCU_TRAFFIC.get(roof["kernel"])
+    roof["traffic_source"] = ("ncu dram read+write of the fit kernel, one 262,144-point launch "
+                              "(profiles/fused_fit_kernel_cfg1_ncu.md)")
+    res = {
+        "metric": METRIC, "value": r1["value"], "unit": "samples/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": r1["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "bf16 storage, fp32 accumulation",
+        "data": "synthetic (seeded analytic SDF: 16 spheres + 8 boxes)",
+        "config": bench_config(ws), "path": r1["path"],
+        "e2e": r1["e2e"], "fp32_dropin": r1["fp32_dropin"], "roofline": roof,
+        "gpu_launches": r1["gpu_launches"], "clocks": r1["clocks"],
+    }
+    if not args.no_field_configs:
+        # the 2-D configurations: the image fit and the image set (shared basis, per-image coefficients)
+        res["field_configs"] = {}
+        for key in ("cfg0", "cfg4"):
+            r, mk = measure_field(key, args, ws, rank, local, flush, with_dropin=True)
+            if rank == 0 and not args.no_cpu_baseline:
+                r["cpu_baseline"] = run_cpu_baseline_model(mk, key, 3)
+            res["field_configs"][key] = r
     return res
 
 
@@ -326,27 +379,30 @@ def run_radiance(args, dev):
         with torch.no_grad():
             dep = torch.cat([tr.render(test[s:s + 16384], is_train=False)[1] for s in range(0, test.shape[0], 16384)])
         depth_err = float((dep - gtd).abs().mean())
-        # timed fwd+bwd steps at the configuration's batch (no optimizer step). The proposal
-        # path has a fixed sample count and replays from a CUDA graph; the plain sampler's
-        # live-sample count is data dependent (one host read per step, as in the reference).
-        run = (lambda r, t: tr.graph_step(r, t)) if sampler is not None else \
-            (lambda r, t: tr.step(r, t, optimize=False))
-        for _ in range(args.warmup):
-            idx = torch.randint(0, pool.shape[0], (batch,), device=dev, generator=g)
-            run(pool[idx], gt[idx])
-        times = []
-        for _ in range(args.steps):
-            idx = torch.randint(0, pool.shape[0], (batch,), device=dev, generator=g)
-            rb, gb = pool[idx], gt[idx]
-            flush.zero_()
-            torch.cuda.synchronize()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record()
-            run(rb, gb)
-            e1.record()
-            torch.cuda.synchronize()
-            times.append(e0.elapsed_time(e1))
-        ms = float(np.mean(times))
+        # timed fwd+bwd steps (no optimizer step), both samplers replayed from CUDA graphs: the
+        # proposal path has a fixed sample count; the plain sampler renders without host
+        # synchronisation (live-sample buffers for every sample slot, the count on the device)
+
+        def timed_steps(b):
+            for _ in range(args.warmup):
+                idx = torch.randint(0, pool.shape[0], (b,), device=dev, generator=g)
+                tr.graph_step(pool[idx], gt[idx])
+            times = []
+            for _ in range(args.steps):
+                idx = torch.randint(0, pool.shape[0], (b,), device=dev, generator=g)
+                rb, gb = pool[idx], gt[idx]
+                flush.zero_()
+                torch.cuda.synchronize()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                tr.graph_step(rb, gb)
+                e1.record()
+                torch.cuda.synchronize()
+                times.append(e0.elapsed_time(e1))
+            return float(np.mean(times))
+
+        ms = timed_steps(batch)
+        ms_8192 = timed_steps(8192) if batch != 8192 else ms
         # a whole training step (fwd + bwd + the fused Adam update of field and proposal) at the
         # training batch, after the measurements above
         ttimes = []
@@ -367,6 +423,7 @@ def run_radiance(args, dev):
         evaluation(eval_ds, m, N_vis=-1, N_samples=1024, white_bg=True, sampler=sampler)  # warm-up
         e_psnr, e_extra = evaluation(eval_ds, m, N_vis=-1, N_samples=1024, white_bg=True, sampler=sampler)
         rec = {"rays_per_s": batch / (ms / 1e3), "ms_per_step": ms, "rays_per_step": batch,
+               "rays_per_s_at_8192": 8192 / (ms_8192 / 1e3), "mode": "CUDA graph replay, fwd+bwd",
                "psnr_db": psnr, "depth_mae": depth_err, "train_steps": iters, "train_rays_per_step": 4096,
                "train_step_ms_with_adam": tms, "train_rays_per_s_with_adam": 4096 / (tms / 1e3),
                "eval_400x400": {"ms_per_image": e_extra["ms_per_image"][0], "psnr_db": e_psnr[0],
@@ -380,6 +437,9 @@ def run_radiance(args, dev):
             rec["samples_per_ray"] = sampler.n_fine
         out[kind] = rec
     out["proposal_rays_per_s_vs_plain"] = out["cfg3_proposal"]["rays_per_s"] / out["cfg2_plain"]["rays_per_s"]
+    # like for like: both samplers at 8,192 rays per step, both replayed from CUDA graphs
+    out["proposal_rays_per_s_vs_plain_same_batch"] = (out["cfg3_proposal"]["rays_per_s_at_8192"] /
+                                                      out["cfg2_plain"]["rays_per_s_at_8192"])
     # rendering alone (the evaluation renderer, no backward): 48 proposal samples per ray
     # against the plain sampler's ~125 live samples after occupancy pruning
     out["proposal_eval_rays_per_s_vs_plain"] = (out["cfg3_proposal"]["eval_400x400"]["rays_per_s"] /
@@ -443,6 +503,116 @@ def run_cpu_baseline(n_points, steps, warmup=1):
                       f"({CPU_DESC})"}
 
 
+def head_flops_per_sample(c, hidden=128, view_pe=6, fea_pe=2):
+    """Algorithmic FLOPs of MLPRender_Fea per head sample (models/FactorFields.py:162-203), forward
+    and backward as autograd computes them (no recomputation counted): forward 2 (in H + H H + 3 H);
+    backward dW0, dX (2 in H each), dW1, dH0 (2 H H each), dW2, dH1 (2 3 H each)."""
+    i = 3 + c + 6 * view_pe + 2 * fea_pe * c
+    fwd = 2 * (i * hidden + hidden * hidden + hidden * 3)
+    bwd = 2 * (2 * i * hidden + 2 * hidden * hidden + 2 * 3 * hidden)
+    return fwd, bwd
+
+
+def measure_mlp_head(args, dev, flush):
+    """The MLPRender_Fea colour head (the reference's head, nerf.yaml sizes with model.out_dim 28:
+    27 feature channels, 174 inputs, 128 hidden): the tcgen05 kernels timed alone on 262,144 head
+    samples (CUDA events, forward and backward), as TFLOP/s of the algorithmic FLOPs against the
+    measured BF16 tensor peak; and a configuration-2 fwd+bwd step (4,096 rays) with this head."""
+    from factor_fields_gb300 import FactorFields
+    from factor_fields_gb300 import workloads as W
+    from factor_fields_gb300.renderer import MLPRender_Fea, head_backward, head_forward
+    torch.manual_seed(0)
+    head = MLPRender_Fea(27, num_layers=3, hidden_dim=128, viewpe=6, feape=2).to(dev)
+    n = 262144
+    g = torch.Generator(device="cpu").manual_seed(3)
+    feat = (torch.randn(n, 28, generator=g) * 0.5).to(dev)
+    rays = torch.randn(n, 6, generator=g).to(dev)
+    idx = torch.arange(n, dtype=torch.int32, device=dev)
+    rgb = torch.empty(n, 3, device=dev)
+    g_rgb = torch.randn(n, 3, generator=g).to(dev)
+    g_feat = torch.empty_like(feat)
+    for p in head.parameters():
+        p.grad = torch.zeros_like(p)
+
+    def run(fn, k):
+        ts = []
+        for _ in range(k):
+            torch.cuda.synchronize()
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fn()
+            e1.record()
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        return float(np.mean(ts))
+
+    fwd = lambda: head_forward(head, feat, rays, idx, idx, rgb, tc=True)  # noqa: E731
+    bwd = lambda: head_backward(head, feat, rays, idx, idx, g_rgb, g_feat, direct=True, tc=True)  # noqa: E731
+    for _ in range(args.warmup):
+        fwd()
+        bwd()
+    t_f, t_b = run(fwd, args.steps), run(bwd, args.steps)
+    ff, fb = head_flops_per_sample(27)
+    peaks = load_peaks()
+    peak = peaks.get("bf16_tflops", 1900.0)
+    ach_f, ach_b = ff * n / (t_f / 1e3) / 1e12, (ff + fb) * n / (t_b / 1e3) / 1e12
+    out = {"head": "MLPRender_Fea, in 174 (27 features + PE 2, dirs + PE 6) -> 128 -> 128 -> 3, tcgen05 BF16 / FP32",
+           "samples": n, "fwd_ms": t_f, "bwd_ms": t_b, "fwd_samples_per_s": n / (t_f / 1e3),
+           "flops_per_sample": {"fwd": ff, "bwd": fb},
+           "roofline": {"bound": "tensor", "kernel": "head_tc_kernel<27,2,6,bwd>",
+                        "achieved": ach_b, "peak": peak, "unit": "TFLOP/s", "frac": ach_b / peak,
+                        "fwd_achieved": ach_f, "fwd_frac": ach_f / peak,
+                        "note": "algorithmic FLOPs (the backward launch recomputes the forward and is counted "
+                                "as fwd + bwd); the kernel also runs the split-BF16 second MMA of layers 0 and 1",
+                        "peak_source": ("MEASURED_PEAKS.json bf16_tflops (measured burst)" if "bf16_tflops" in peaks
+                                        else "fallback")}}
+    cfg = W.field_cfg("cfg2")
+    cfg.renderer["shadingMode"] = "MLP_Fea"
+    torch.manual_seed(0)
+    m = FactorFields(cfg, device=dev, precision="bf16")
+    pool = torch.from_numpy(W.BlobScene(0).ray_pool(1 << 16, 5)).float().to(dev)
+    gen = torch.Generator(device=dev).manual_seed(0)
+    ts = []
+    for i in range(args.warmup + args.steps):
+        r = pool[torch.randint(0, pool.shape[0], (4096,), device=dev, generator=gen)]
+        flush.zero_()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        rgb_r, _, _ = m(r, white_bg=True, is_train=True, N_samples=1024)
+        (rgb_r * rgb_r).sum().backward()
+        e1.record()
+        torch.cuda.synchronize()
+        if i >= args.warmup:
+            ts.append(e0.elapsed_time(e1))
+    out["cfg2_step_with_mlp_head"] = {"rays_per_step": 4096, "ms_per_step": float(np.mean(ts)),
+                                     "rays_per_s": 4096 / (float(np.mean(ts)) / 1e3),
+                                     "note": "untrained field (random-init), fwd+bwd, no optimizer"}
+    return out
+
+
+def run_cpu_baseline_model(m, key, steps, warmup=1):
+    """The reference's CPU op sequence (oracle/ref_torch.py) holding model m's parameters, on one
+    batch of configuration `key` (all host threads): samples/s, best step."""
+    from oracle.ref_torch import from_model
+    cores = os.cpu_count() or 1
+    torch.set_num_threads(cores)
+    r = from_model(m)
+    x, y = (torch.from_numpy(a) for a in field_batches(key, 7, 1)[0])
+    loss = FIELD_CONFIGS[key]["loss"]
+    for _ in range(warmup):
+        r.fit_step(x, y, loss)
+    best = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        r.fit_step(x, y, loss)
+        best.append(time.perf_counter() - t0)
+    n = x.shape[0]
+    return {"value": n / min(best), "unit": "samples/s", "cores": cores, "kind": CPU_KIND,
+            "sample": f"{n} points of the same workload per step, best of {steps} after {warmup} warm-up ({CPU_DESC})"}
+
+
 def run_reference_arm(args, ws):
     """--impl reference: the reference's CPU op sequence on the native arm's workload (the same
     262,144-point batches of configuration 1, one batch per step), W warm-up steps then K timed
@@ -479,6 +649,7 @@ def main():
                     help="points per step of the cpu_baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-render", action="store_true", help="skip the radiance-field configurations")
+    ap.add_argument("--no-field-configs", action="store_true", help="skip the 2-D field configurations (0 and 4)")
     ap.add_argument("--render-iters", type=int, default=1500)
     ap.add_argument("--psnr-seeds", type=int, default=3, help="training seeds of the PSNR comparison")
     args = ap.parse_args()
@@ -493,6 +664,8 @@ def main():
     res = run_native(args, ws, rank, local)
     if not args.no_render:
         res["radiance_field"] = run_radiance(args, torch.device("cuda", local))
+        flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=torch.device("cuda", local))
+        res["radiance_field"]["mlp_fea_head"] = measure_mlp_head(args, torch.device("cuda", local), flush)
     if rank == 0:
         if not args.no_cpu_baseline:
             res["cpu_baseline"] = run_cpu_baseline(args.cpu_points, 3)
