@@ -650,6 +650,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-render", action="store_true", help="skip the radiance-field configurations")
     ap.add_argument("--no-field-configs", action="store_true", help="skip the 2-D field configurations (0 and 4)")
+    ap.add_argument("--head-only", action="store_true",
+                    help="measure the MLPRender_Fea tensor-core head alone (prints its JSON record)")
     ap.add_argument("--render-iters", type=int, default=1500)
     ap.add_argument("--psnr-seeds", type=int, default=3, help="training seeds of the PSNR comparison")
     args = ap.parse_args()
@@ -658,6 +660,12 @@ def main():
         if rank != 0:
             return 0
         print(json.dumps(run_reference_arm(args, ws)))
+        return 0
+    if args.head_only:
+        dev = torch.device("cuda", local)
+        torch.cuda.set_device(dev)
+        flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
+        print(json.dumps(measure_mlp_head(args, dev, flush)))
         return 0
     if ws > 1:
         torch.distributed.init_process_group("nccl", device_id=torch.device("cuda", local))
