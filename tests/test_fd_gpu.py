@@ -192,7 +192,7 @@ def _marched_batch(model_seed=0):
     rdesc = render_desc(m, 256, True)
     offsets, xyz, sidx = march(m, rays, jitter, rdesc)
     # z and dist of each live sample as the kernels compute them (sample_point, :586-602, :861)
-    zs, _, _ = O.sample_point(rays.cpu().numpy()[:, :3], rays.cpu().numpy()[:, 3:6], m.aabb.cpu().numpy(),
+    _, zs, _ = O.sample_point(rays.cpu().numpy()[:, :3], rays.cpu().numpy()[:, 3:6], m.aabb.cpu().numpy(),
                               np.float32(m.stepSize.cpu()), 256, jitter.cpu().numpy()[:, None])
     dist = np.concatenate([(zs[:, 1:] - zs[:, :-1]).astype(np.float32), np.zeros((48, 1), np.float32)], 1)
     off = offsets.cpu().numpy()
