@@ -64,7 +64,7 @@ def test_atomics_determinism():
     """Two identical fused fit steps (binned, configuration 1 at 262,144 points) and two identical
     renders with backward (configuration 2): the forward outputs and the loss inputs are
     bit-identical; every gradient agrees within 1e-5 of its largest entry (float32 atomics add
-    thousands of terms per entry in an order that varies between runs: ~1e-6 observed).
+    thousands of terms per entry in an order that varies between runs: ~1e-6 observed)."""
     from factor_fields_gb300 import FactorFields
     from factor_fields_gb300 import workloads as W
     from factor_fields_gb300.train import FieldFitRunner
