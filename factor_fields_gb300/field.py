@@ -333,6 +333,8 @@ class FactorFields(torch.nn.Module):
         step, n = render_step(aabb, gridSize, self.cfg.renderer.step_ratio)
         self.stepSize = step.to(self.device)
         self.nSamples = n
+        # host copies for the render descriptor (valid while self.aabb is this tensor, unmodified)
+        self._render_host = (self.aabb, self.aabb._version, aabb, float(step))
 
     def forward(self, rays_chunk, white_bg=True, is_train=False, ndc_ray=False, N_samples=-1, jitter=None,
                 fused=None, static=False):

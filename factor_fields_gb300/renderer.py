@@ -43,6 +43,8 @@ class AlphaGridMask(torch.nn.Module):
         self.aabb = aabb.to(device)
         self.aabbSize = self.aabb[1] - self.aabb[0]
         self.invgridSize = 1.0 / self.aabbSize * 2
+        self.aabb_host = aabb.detach().cpu()  # host copies for the render descriptor
+        self.inv_host = 1.0 / (self.aabb_host[1] - self.aabb_host[0]) * 2
         self.alpha_volume = alpha_volume.view(1, 1, *alpha_volume.shape[-3:]).to(device)
         self.gridSize = torch.tensor([alpha_volume.shape[-1], alpha_volume.shape[-2], alpha_volume.shape[-3]],
                                      dtype=torch.long, device=device)
@@ -206,13 +208,20 @@ def make_render_module(cfg, in_channels):
 
 
 def render_desc(model, n_samples, white_bg):
-    """FFRender for a FactorFields model (float32 constants computed as the reference does)."""
+    """FFRender for a FactorFields model (float32 constants computed as the reference does).
+    Reads the host copies of aabb / stepSize that update_renderParams keeps (no device read, so a
+    render can be captured in a CUDA graph) while model.aabb is the tensor they were taken from,
+    unmodified; otherwise the device values."""
     r = N.FFRender()
-    aabb = model.aabb.detach().cpu()
+    host = getattr(model, "_render_host", None)
+    if host is not None and host[0] is model.aabb and host[1] == model.aabb._version:
+        aabb, step = host[2], host[3]
+    else:
+        aabb, step = model.aabb.detach().cpu(), float(model.stepSize.detach().cpu())
     for k in range(3):
         r.aabb_min[k] = float(aabb[0, k])
         r.aabb_max[k] = float(aabb[1, k])
-    r.step = float(model.stepSize.detach().cpu())
+    r.step = step
     r.n_samples = int(n_samples)
     rc = model.cfg.renderer
     r.distance_scale = float(rc.distance_scale)
@@ -228,8 +237,7 @@ def render_desc(model, n_samples, white_bg):
         r.occ_bits = mask.bits.data_ptr()
         vol = mask.alpha_volume
         r.occ_reso[0], r.occ_reso[1], r.occ_reso[2] = vol.shape[-1], vol.shape[-2], vol.shape[-3]
-        a0 = mask.aabb.detach().cpu()
-        inv = mask.invgridSize.detach().cpu()
+        a0, inv = mask.aabb_host, mask.inv_host
         for k in range(3):
             r.occ_origin[k] = float(a0[0, k])
             r.occ_inv[k] = float(inv[k])

@@ -62,9 +62,9 @@ def test_march_bit_exact_at_bench_shape():
 
 def test_atomics_determinism():
     """Two identical fused fit steps (binned, configuration 1 at 262,144 points) and two identical
-    renders with backward (configuration 2): the forward outputs and the loss inputs are
-    bit-identical; every gradient agrees within 1e-5 of its largest entry (float32 atomics add
-    thousands of terms per entry in an order that varies between runs: ~1e-6 observed)."""
+    renders with backward (configuration 2): the rendered outputs are bit-identical; the mean
+    loss (accumulated with atomics) and every gradient agree within 1e-5 of their size (float32
+    atomics add thousands of terms per entry in an order that varies between runs: ~1e-6 seen)."""
     from factor_fields_gb300 import FactorFields
     from factor_fields_gb300 import workloads as W
     from factor_fields_gb300.train import FieldFitRunner
@@ -78,7 +78,7 @@ def test_atomics_determinism():
         loss = runner.step(xt, yt)
         torch.cuda.synchronize()
         res.append([float(loss)] + [p.grad.clone() for p in runner._params()])
-    assert abs(res[0][0] - res[1][0]) <= 1e-6 * abs(res[0][0])
+    assert abs(res[0][0] - res[1][0]) <= 1e-5 * abs(res[0][0])
     for a, b in zip(res[0][1:], res[1][1:]):
         assert rel_err(a, b) < 1e-5
     # rendering: forward bit-identical, gradients to rounding
