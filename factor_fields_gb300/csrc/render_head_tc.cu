@@ -1,38 +1,47 @@
 // MLPRender_Fea colour head (models/FactorFields.py:162-203) on the fifth-generation tensor
 // cores: tcgen05.mma with BF16 operands in shared memory and FP32 accumulators in tensor memory.
 //
-// One persistent CTA per SM (128 threads: thread t owns sample t of a 128-sample tile and TMEM
-// lane t) walks tiles of the listed head samples. Per tile, for 3 layers 128 hidden units wide:
+// One persistent CTA per SM walks tiles of 128 listed head samples (sample r of a tile = TMEM
+// lane r). 512 threads: warp w serves TMEM lane quadrant w % 4 (rows 32 (w % 4) .. + 31) and the
+// 32-column slice w / 4 of every 128-wide accumulator, so each epilogue is one tcgen05.ld x32 per
+// thread. Per tile, for 3 layers 128 hidden units wide:
 //
-//   X   = [feat, dir, PE(feat, 2), PE(dir, 6)]        built per thread, in shared memory as a
-//                                   BF16 pair X = X_hi + X_lo (~16 significant bits)
+//   stage  the tile's feature rows (channels 0..C) and ray directions into shared memory,
+//          warp per row (coalesced), through app_idx / app_ray
+//   X   = [feat, dir, PE(feat, 2), PE(dir, 6)]  in shared memory as a BF16 pair X_hi + X_lo
+//          (~16 significant bits), written one 128-byte core matrix per warp store
 //   F1  S = X_hi W0^T + X_lo W0^T   (tcgen05, M 128, N 128, K = in_dim padded to 16)
-//       H0 = relu(S + b0)           -> shared memory as H0_hi + H0_lo, ReLU mask kept in registers
+//       H0 = relu(S + b0)           -> shared memory as H0_hi + H0_lo, ReLU mask in registers
 //   F2  S = H0_hi W1^T + H0_lo W1^T (N 128, K 128)
-//       H1 = relu(S + b1), y = H1 W2^T, rgb = sigmoid(y)   (3 outputs: CUDA cores, FP32 H1)
+//       H1 = relu(S + b1), y = H1 W2^T (row partials of the 4 column slices summed through
+//       shared memory), rgb = sigmoid(y)
 // and for the backward (the forward recomputed, nothing stored between launches):
 //       dy = dL/drgb rgb (1 - rgb), dH1 = (dy W2) [H1 > 0] -> shared memory (BF16)
 //   B1  S  = dH1 W1                 (B = W1 read MN-major)
 //   B2  dW1 += dH1^T H0_hi          (A = dH1, B = H0, both read MN-major; TMEM-resident over tiles)
-//       dH0 = S [H0 > 0]            -> shared memory, over H0 (consumed by B2)
+//       dH0 = S [H0 > 0]            -> shared memory, over H0_hi (consumed by B2)
 //   B3  dW0 += dH0^T X_hi           (TMEM-resident over tiles)
 //   B4  S  = dH0 W0                 (the feature-related input columns only)
-//       dL/dfeat = chain rule through the positional encoding, written to grad_feat
-// dW2, db0 and db1 are reduced with warp shuffles into per-lane registers. At the end each CTA
-// adds its dW0 / dW1 (read from TMEM, one row per thread) and the register sums to the float32
+//       dL/dfeat = the chain rule through the positional encoding: each thread adds its columns'
+//       terms to a per-row shared-memory sum, and a warp per row writes the rows out
+// dW2, db0 and db1 are warp reduce-scatters into per-lane registers. At the end each CTA adds its
+// dW0 / dW1 (read from TMEM, one row per quadrant thread) and the register sums to the float32
 // gradients with one atomic per entry.
 //
 // The forward operands X and H0 carry ~16 significant bits (two BF16 MMAs each): with one BF16
 // rounding, inputs near a ReLU kink land on the other side of it in a fraction of the 128 x 128
 // units per tile, and each flip moves that sample's input gradient by a whole term (up to ~20% of
 // max |dL/dfeat| on random heads). The backward operands (dH1, dH0) and the weight-gradient
-// operands are single BF16 values (~0.2% effect).
+// operands are single BF16 values (~0.2% effect). The positional encoding uses the hardware
+// sin/cos (__sincosf; absolute error ~1e-5 at the largest arguments, |x| <= 32 |d|), below the
+// resolution of the BF16 pair.
 //
 // Operands are stored once, in the core-matrix-row layout of tc_util.cuh, and read as K-major or
-// MN-major operands as each product needs (transposes cost nothing). Shared memory: W0, W1, X_hi
-// and a 64 KB region R that holds X_lo during F1, then H0_hi and H0_lo for F2, then H0_hi and dH1,
-// then dH0 and dH1 in the backward. TMEM columns (backward):
-// [0, S) the per-tile accumulator S, then dW1 (128), then dW0 (in_dim padded): at most 512.
+// MN-major operands as each product needs (transposes cost nothing). Shared memory: W0, W1, X_hi,
+// a 64 KB region R that holds X_lo during F1, then H0_hi and H0_lo for F2, then H0_hi and dH1 (the
+// row partials of y pass through the second half first), then dH0 and dH1, then the dL/dfeat row
+// sums; the staged feature rows, directions and row indices. TMEM columns (backward): [0, S) the
+// per-tile accumulator S, then dW1 (128), then dW0 (in_dim padded): at most 512.
 // Every wait on an mbarrier has an iteration limit: when it runs out the kernel reports
 // FF_ERR_LIMIT through `status`, stops, waits (again with a limit) for its MMAs and frees TMEM.
 #include "ff_common.cuh"
@@ -43,8 +52,9 @@ namespace ffgb {
 
 namespace {
 
-constexpr int kH = 128;        // hidden units of both hidden layers
-constexpr int kTile = 128;     // samples per tile = threads = TMEM lanes
+constexpr int kH = 128;          // hidden units of both hidden layers
+constexpr int kTile = 128;       // samples per tile = TMEM lanes
+constexpr int kThreads = 512;    // 16 warps: lane quadrant w % 4, column slice w / 4
 constexpr uint32_t kPolls = 1u << 22;  // mbarrier polls before a wait gives up (MMAs finish in microseconds)
 
 template <int C, int F, int V>
@@ -55,15 +65,21 @@ struct Shape {
   static constexpr int S_COLS = NX > 128 ? (NX + 31) / 32 * 32 : 128;
   static constexpr int COL_DW1 = S_COLS;
   static constexpr int COL_DW0 = S_COLS + 128;
-  static_assert(COL_DW0 + IN_PAD <= 512, "tensor-memory budget");
+  static_assert(COL_DW0 + (IN_PAD + 31) / 32 * 32 <= 512, "tensor-memory budget");
   static_assert(NX <= 256 && IN_PAD <= 256, "MMA N limit");
+  static_assert(C + 1 <= 32, "a feature row is staged by one warp");
+  static constexpr int FS = (C + 1) | 1;  // staged row stride in floats (odd: rows on distinct banks)
   static constexpr int W0_B = kH * IN_PAD * 2;
   static constexpr int W1_B = kH * kH * 2;
   static constexpr int X_B = kTile * IN_PAD * 2;
   static constexpr int H_B = kTile * kH * 2;
   static constexpr int R_B = X_B > 2 * H_B ? X_B : 2 * H_B;  // X_lo, or H0_hi + H0_lo / dH1
-  static constexpr int F32_B = (3 * kH + 2 * kH) * 4;        // W2 [3][128], b0, b1
-  static constexpr int smem() { return W0_B + W1_B + X_B + R_B + F32_B + 64; }
+  static constexpr int FEAT_B = kTile * FS * 4;
+  static constexpr int DIR_B = kTile * 4 * 4;
+  static constexpr int IDX_B = kTile * 4;
+  static constexpr int F32_B = 5 * kH * 4;  // W2 [3][128], b0, b1
+  static_assert(kTile * 4 * 4 * 4 <= H_B && FEAT_B <= R_B, "aliased buffers fit");
+  static constexpr int smem() { return W0_B + W1_B + X_B + R_B + FEAT_B + DIR_B + IDX_B + F32_B + 64; }
 };
 
 struct HeadArgs {
@@ -96,6 +112,9 @@ __device__ __forceinline__ uint64_t desc_mn(uint32_t base, int cols, int s) {
 __device__ __forceinline__ void st_shared_v4(uint32_t saddr, uint32_t a, uint32_t b, uint32_t c, uint32_t d) {
   asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(saddr), "r"(a), "r"(b), "r"(c), "r"(d) : "memory");
 }
+__device__ __forceinline__ void st_shared_b32(uint32_t saddr, uint32_t v) {
+  asm volatile("st.shared.b32 [%0], %1;" ::"r"(saddr), "r"(v) : "memory");
+}
 
 // Eight consecutive values of row t (columns k0 .. k0 + 7, k0 % 8 == 0) as one 16-byte store.
 __device__ __forceinline__ void store8(uint32_t buf, int cols, int t, int k0, const float* v) {
@@ -117,67 +136,29 @@ __device__ __forceinline__ void store8_split(uint32_t hi_buf, uint32_t lo_buf, i
   st_shared_v4(lo_buf + off, l[0], l[1], l[2], l[3]);
 }
 
-// The head's input row of one sample, in the reference's column order, written as a BF16 pair into
-// row t of X_hi / X_lo (zero for an invalid row and for the padding). sin / cos of x 2^f come from
-// one sincosf and the double-angle identities.
+// Column k of the head's input row (the reference's order, models/FactorFields.py:188-195):
+// fr = the staged feature row (fr[1 + c] = feature c), dr = the ray direction; 0 past in_dim.
 template <int C, int F, int V>
-__device__ __forceinline__ void build_x(uint32_t X, uint32_t Xlo, int t, bool valid, const float* frow,
-                                        const float* drow) {
-  using S = Shape<C, F, V>;
-  float fv[C], dv[3];
-#pragma unroll
-  for (int c = 0; c < C; ++c) fv[c] = valid ? frow[c] : 0.f;
-#pragma unroll
-  for (int i = 0; i < 3; ++i) dv[i] = valid ? drow[i] : 0.f;
-  float buf[8];
-  int k = 0;  // compile-time after unrolling
-  auto emit = [&](float v) {
-    buf[k & 7] = v;
-    if ((k & 7) == 7) store8_split(X, Xlo, S::IN_PAD, t, k - 7, buf);
-    ++k;
-  };
-#pragma unroll
-  for (int c = 0; c < C; ++c) emit(fv[c]);
-#pragma unroll
-  for (int i = 0; i < 3; ++i) emit(dv[i]);
-  float cf[C][F];
-#pragma unroll
-  for (int c = 0; c < C; ++c) {
-    float s, co;
-    sincosf(fv[c], &s, &co);
-#pragma unroll
-    for (int f = 0; f < F; ++f) {
-      emit(s);
-      cf[c][f] = co;
-      const float s2 = 2.f * s * co, c2 = 1.f - 2.f * s * s;
-      s = s2;
-      co = c2;
-    }
+__device__ __forceinline__ float x_col(int k, const float* fr, const float* dr) {
+  if (k < C) return fr[1 + k];
+  k -= C;
+  if (k < 3) return dr[k];
+  k -= 3;
+  float s, co;
+  if (k < 2 * C * F) {
+    const bool cosine = k >= C * F;
+    const int j = cosine ? k - C * F : k;
+    __sincosf(fr[1 + j / F] * (float)(1 << (j % F)), &s, &co);
+    return cosine ? co : s;
   }
-#pragma unroll
-  for (int c = 0; c < C; ++c)
-#pragma unroll
-    for (int f = 0; f < F; ++f) emit(cf[c][f]);
-  float cd[3][V];
-#pragma unroll
-  for (int i = 0; i < 3; ++i) {
-    float s, co;
-    sincosf(dv[i], &s, &co);
-#pragma unroll
-    for (int f = 0; f < V; ++f) {
-      emit(s);
-      cd[i][f] = co;
-      const float s2 = 2.f * s * co, c2 = 1.f - 2.f * s * s;
-      s = s2;
-      co = c2;
-    }
+  k -= 2 * C * F;
+  if (k < 6 * V) {
+    const bool cosine = k >= 3 * V;
+    const int j = cosine ? k - 3 * V : k;
+    __sincosf(dr[j / V] * (float)(1 << (j % V)), &s, &co);
+    return cosine ? co : s;
   }
-#pragma unroll
-  for (int i = 0; i < 3; ++i)
-#pragma unroll
-    for (int f = 0; f < V; ++f) emit(cd[i][f]);
-#pragma unroll
-  for (int p = S::IN; p < S::IN_PAD; ++p) emit(0.f);
+  return 0.f;
 }
 
 // Warp reduce-scatter: lane l returns the sum over the warp's lanes of v[l].
@@ -196,19 +177,27 @@ __device__ __forceinline__ float warp_reduce_scatter32(float* v, int lane) {
 }
 
 template <int C, int F, int V, bool BWD>
-__global__ void __launch_bounds__(kTile, 1) head_tc_kernel(const HeadArgs a) {
+__global__ void __launch_bounds__(kThreads, 1) head_tc_kernel(const HeadArgs a) {
   using S = Shape<C, F, V>;
   extern __shared__ __align__(1024) unsigned char smem[];
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+  const int quad = warp & 3, part = warp >> 2;  // TMEM lane quadrant and 32-column slice
+  const int r = quad * 32 + lane;               // this thread's row (sample) in the epilogues
   unsigned char* p = smem;
   const uint32_t sW0 = tc::smem_u32(p); p += S::W0_B;
   const uint32_t sW1 = tc::smem_u32(p); p += S::W1_B;
   const uint32_t sX = tc::smem_u32(p); p += S::X_B;
+  unsigned char* pR = p;
   const uint32_t sR = tc::smem_u32(p); p += S::R_B;
   const uint32_t sXlo = sR;               // F1
   const uint32_t sH0 = sR;                // H0_hi (F2, B2), then dH0 (B3, B4)
   const uint32_t sH0lo = sR + S::H_B;     // H0_lo (F2)
   const uint32_t sDH1 = sR + S::H_B;      // dH1 (B1, B2), after F2
+  float4* yp = reinterpret_cast<float4*>(pR + S::H_B);  // [4 slices][128 rows] partial y, before dH1
+  float* gfs = reinterpret_cast<float*>(pR);            // [128][FS] dL/dfeat row sums, after B3 / B4
+  float* fs = reinterpret_cast<float*>(p); p += S::FEAT_B;
+  float* ds = reinterpret_cast<float*>(p); p += S::DIR_B;
+  int32_t* idx_s = reinterpret_cast<int32_t*>(p); p += S::IDX_B;
   float* w2s = reinterpret_cast<float*>(p); p += 3 * kH * 4;
   float* b0s = reinterpret_cast<float*>(p); p += kH * 4;
   float* b1s = reinterpret_cast<float*>(p); p += kH * 4;
@@ -217,19 +206,21 @@ __global__ void __launch_bounds__(kTile, 1) head_tc_kernel(const HeadArgs a) {
   const uint32_t mb = tc::smem_u32(mbar);
   constexpr uint32_t kTmemCols = BWD ? 512u : 128u;
 
-  // ---- weights -> shared memory (BF16 core layout; W2 and biases float32) ----
-  for (int e = t; e < kH * S::IN_PAD; e += kTile) {
-    const int r = e / S::IN_PAD, c = e % S::IN_PAD;
-    const float v = c < S::IN ? a.w[0][r * S::IN + c] : 0.f;
-    *reinterpret_cast<__nv_bfloat16*>(smem + tc::core_off(r, c, S::IN_PAD)) = __float2bfloat16_rn(v);
+  // ---- weights -> shared memory (BF16 core layout; W2 rounded to BF16 like W0, W1; biases float32) ----
+  for (int e = t; e < kH * S::IN_PAD; e += kThreads) {
+    const int rr = e / S::IN_PAD, c = e % S::IN_PAD;
+    const float v = c < S::IN ? a.w[0][rr * S::IN + c] : 0.f;
+    *reinterpret_cast<__nv_bfloat16*>(smem + tc::core_off(rr, c, S::IN_PAD)) = __float2bfloat16_rn(v);
   }
-  for (int e = t; e < kH * kH; e += kTile) {
-    const int r = e / kH, c = e % kH;
-    *reinterpret_cast<__nv_bfloat16*>(smem + S::W0_B + tc::core_off(r, c, kH)) = __float2bfloat16_rn(a.w[1][e]);
+  for (int e = t; e < kH * kH; e += kThreads) {
+    const int rr = e / kH, c = e % kH;
+    *reinterpret_cast<__nv_bfloat16*>(smem + S::W0_B + tc::core_off(rr, c, kH)) = __float2bfloat16_rn(a.w[1][e]);
   }
-  for (int e = t; e < 3 * kH; e += kTile) w2s[e] = __bfloat162float(__float2bfloat16_rn(a.w[2][e]));  // BF16 like W0, W1
-  b0s[t] = a.b[0] ? a.b[0][t] : 0.f;
-  b1s[t] = a.b[1] ? a.b[1][t] : 0.f;
+  for (int e = t; e < 3 * kH; e += kThreads) w2s[e] = __bfloat162float(__float2bfloat16_rn(a.w[2][e]));
+  if (t < kH) {
+    b0s[t] = a.b[0] ? a.b[0][t] : 0.f;
+    b1s[t] = a.b[1] ? a.b[1][t] : 0.f;
+  }
   tc::fence_smem_to_async();
   if (t == 0) {
     tc::mbar_init(mb, 1);
@@ -241,14 +232,13 @@ __global__ void __launch_bounds__(kTile, 1) head_tc_kernel(const HeadArgs a) {
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tmem = *taddr_s;
-  const uint32_t lane_off = (uint32_t)(warp * 32) << 16;
+  const uint32_t lane_off = (uint32_t)(quad * 32) << 16;
   const uint32_t tS = tmem;
   const uint32_t tDW1 = tmem + S::COL_DW1, tDW0 = tmem + S::COL_DW0;
 
   uint32_t phase = 0;
   bool ok = true, any_tile = false;
-  float acc_db0[4] = {0.f, 0.f, 0.f, 0.f}, acc_db1[4] = {0.f, 0.f, 0.f, 0.f};
-  float acc_dw2[3][4] = {};
+  float acc_db0 = 0.f, acc_db1 = 0.f, acc_dw2[3] = {0.f, 0.f, 0.f};  // column 32 part + lane
 
   // waits for the MMAs committed last; all threads agree on the outcome
   auto wait_mma = [&]() {
@@ -261,17 +251,39 @@ __global__ void __launch_bounds__(kTile, 1) head_tc_kernel(const HeadArgs a) {
 
   const int64_t n_tiles = ceil_div(a.n, kTile);
   for (int64_t tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x) {
-    const int64_t row = tile * kTile + t;
-    const bool valid = row < a.n;
-    const int64_t sidx = valid ? (int64_t)a.app_idx[row] : 0;
-    const float* frow = a.feat + sidx * a.feat_stride + 1;
-    const float* drow = a.rays + (valid ? (int64_t)a.app_ray[row] : 0) * 6 + 3;
-    // ---- X ----
-    build_x<C, F, V>(sX, sXlo, t, valid, frow, drow);
+    // ---- stage the tile's feature rows (channels 0..C), directions and row indices ----
+#pragma unroll 1
+    for (int i = 0; i < kTile / 16; ++i) {
+      const int rr = warp * (kTile / 16) + i;
+      const int64_t row = tile * kTile + rr;
+      const bool valid = row < a.n;
+      const int64_t sidx = valid ? (int64_t)a.app_idx[row] : 0;
+      if (lane <= C) fs[rr * S::FS + lane] = valid ? a.feat[sidx * a.feat_stride + lane] : 0.f;
+      if (lane < 3) ds[rr * 4 + lane] = valid ? a.rays[(int64_t)a.app_ray[row] * 6 + 3 + lane] : 0.f;
+      if (lane == 0) idx_s[rr] = valid ? (int32_t)sidx : -1;
+    }
+    __syncthreads();
+    // ---- X: one core matrix (8 rows x 8 columns) per warp store, thread = (row, column pair) ----
+    {
+      constexpr int kChunks = S::IN_PAD / 8;
+      const int sub = lane >> 2, pr = lane & 3;
+#pragma unroll 1
+      for (int j = warp; j < (kTile / 8) * kChunks; j += kThreads / 32) {
+        const int rr = (j / kChunks) * 8 + sub, k0 = (j % kChunks) * 8 + 2 * pr;
+        const float* fr = fs + rr * S::FS;
+        const float* dr = ds + rr * 4;
+        const float v0 = x_col<C, F, V>(k0, fr, dr), v1 = x_col<C, F, V>(k0 + 1, fr, dr);
+        const uint32_t h = tc::pack2_bf16(v0, v1);
+        const uint32_t l = tc::pack2_bf16(v0 - __uint_as_float(h << 16), v1 - __uint_as_float(h & 0xffff0000u));
+        const uint32_t off = tc::core_off(rr, k0, S::IN_PAD);
+        st_shared_b32(sX + off, h);
+        st_shared_b32(sXlo + off, l);
+      }
+    }
     tc::fence_smem_to_async();
     tc::fence_before_sync();
     __syncthreads();
-    // ---- F1: S = X W0^T ----
+    // ---- F1: S = X_hi W0^T + X_lo W0^T ----
     if (t == 0) {
       tc::fence_after_sync();
       const uint32_t id = tc::idesc_bf16(128, kH, false, false);
@@ -284,27 +296,24 @@ __global__ void __launch_bounds__(kTile, 1) head_tc_kernel(const HeadArgs a) {
       tc::mma_commit(mb);
     }
     if (!wait_mma()) break;
-    // ---- H0 = relu(S + b0) ----
-    uint32_t mask0[4];
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
+    // ---- H0 = relu(S + b0) (this thread's 32 columns) ----
+    uint32_t mask0 = 0;
+    {
       float v[32];
-      tc::tmem_ld32(tS + lane_off + q * 32, v);
-      uint32_t m = 0;
+      tc::tmem_ld32(tS + lane_off + part * 32, v);
 #pragma unroll
       for (int j = 0; j < 32; ++j) {
-        const float h = v[j] + b0s[q * 32 + j];
-        m |= (h > 0.f ? 1u : 0u) << j;
+        const float h = v[j] + b0s[part * 32 + j];
+        mask0 |= (h > 0.f ? 1u : 0u) << j;
         v[j] = fmaxf(h, 0.f);
       }
-      mask0[q] = m;
 #pragma unroll
-      for (int g = 0; g < 4; ++g) store8_split(sH0, sH0lo, kH, t, q * 32 + g * 8, v + g * 8);
+      for (int g = 0; g < 4; ++g) store8_split(sH0, sH0lo, kH, r, part * 32 + g * 8, v + g * 8);
     }
     tc::fence_smem_to_async();
     tc::fence_before_sync();
     __syncthreads();
-    // ---- F2: S = H0 W1^T ----
+    // ---- F2: S = H0_hi W1^T + H0_lo W1^T ----
     if (t == 0) {
       tc::fence_after_sync();
       const uint32_t id = tc::idesc_bf16(128, kH, false, false);
@@ -315,62 +324,73 @@ __global__ void __launch_bounds__(kTile, 1) head_tc_kernel(const HeadArgs a) {
       tc::mma_commit(mb);
     }
     if (!wait_mma()) break;
-    // ---- y = relu(S + b1) W2^T, rgb = sigmoid(y) ----
-    float y[3] = {0.f, 0.f, 0.f};
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      float v[32];
-      tc::tmem_ld32(tS + lane_off + q * 32, v);
+    // ---- y = relu(S + b1) W2^T: the slice's partial sums, summed over the 4 slices ----
+    float h1[32];
+    {
+      float y0 = 0.f, y1 = 0.f, y2 = 0.f;
+      tc::tmem_ld32(tS + lane_off + part * 32, h1);
 #pragma unroll
       for (int j = 0; j < 32; ++j) {
-        const float h = fmaxf(v[j] + b1s[q * 32 + j], 0.f);
-#pragma unroll
-        for (int o = 0; o < 3; ++o) y[o] += h * w2s[o * kH + q * 32 + j];
+        const int u = part * 32 + j;
+        const float h = fmaxf(h1[j] + b1s[u], 0.f);
+        h1[j] = h;
+        y0 += h * w2s[u];
+        y1 += h * w2s[kH + u];
+        y2 += h * w2s[2 * kH + u];
       }
+      yp[part * kTile + r] = make_float4(y0, y1, y2, 0.f);
     }
+    __syncthreads();
     float rgb[3];
+    {
+      float4 ys = yp[r];
 #pragma unroll
-    for (int o = 0; o < 3; ++o) rgb[o] = 1.f / (1.f + expf(-y[o]));
+      for (int q = 1; q < 4; ++q) {
+        const float4 o = yp[q * kTile + r];
+        ys.x += o.x; ys.y += o.y; ys.z += o.z;
+      }
+      rgb[0] = 1.f / (1.f + expf(-ys.x));
+      rgb[1] = 1.f / (1.f + expf(-ys.y));
+      rgb[2] = 1.f / (1.f + expf(-ys.z));
+    }
+    const int32_t sidx = idx_s[r];
     if constexpr (!BWD) {
-      if (valid) {
+      if (part == 0 && sidx >= 0) {
 #pragma unroll
-        for (int o = 0; o < 3; ++o) a.rgb_out[sidx * 3 + o] = rgb[o];
+        for (int o = 0; o < 3; ++o) a.rgb_out[(int64_t)sidx * 3 + o] = rgb[o];
       }
       tc::fence_before_sync();
-      __syncthreads();  // S is read before the next tile's F1 overwrites it
+      __syncthreads();  // S and the staged rows are read before the next tile overwrites them
       any_tile = true;
       continue;
     } else {
       float dy[3];
 #pragma unroll
-      for (int o = 0; o < 3; ++o) dy[o] = valid ? a.grad_rgb[sidx * 3 + o] * rgb[o] * (1.f - rgb[o]) : 0.f;
-      // dH1 = (dy W2) [H1 > 0]; dW2 += dy^T H1, db1 += sum dH1 (warp reduce-scatter per chunk)
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        float v[32], dh[32];
-        tc::tmem_ld32(tS + lane_off + q * 32, v);
+      for (int o = 0; o < 3; ++o) dy[o] = sidx >= 0 ? a.grad_rgb[(int64_t)sidx * 3 + o] * rgb[o] * (1.f - rgb[o]) : 0.f;
+      __syncthreads();  // every slice has read yp before dH1 overwrites it
+      // dH1 = (dy W2) [H1 > 0]; dW2 += dy^T H1, db1 += sum dH1 (warp reduce-scatters)
+      {
+        float dh[32];
 #pragma unroll
         for (int j = 0; j < 32; ++j) {
-          const int u = q * 32 + j;
-          const float h = fmaxf(v[j] + b1s[u], 0.f);
-          dh[j] = h > 0.f ? dy[0] * w2s[u] + dy[1] * w2s[kH + u] + dy[2] * w2s[2 * kH + u] : 0.f;
-          v[j] = h;
+          const int u = part * 32 + j;
+          dh[j] = h1[j] > 0.f ? dy[0] * w2s[u] + dy[1] * w2s[kH + u] + dy[2] * w2s[2 * kH + u] : 0.f;
         }
 #pragma unroll
-        for (int g = 0; g < 4; ++g) store8(sDH1, kH, t, q * 32 + g * 8, dh + g * 8);
-        acc_db1[q] += warp_reduce_scatter32(dh, lane);
+        for (int g = 0; g < 4; ++g) store8(sDH1, kH, r, part * 32 + g * 8, dh + g * 8);
+        acc_db1 += warp_reduce_scatter32(dh, lane);
 #pragma unroll
         for (int o = 0; o < 3; ++o) {
           float pr[32];
 #pragma unroll
-          for (int j = 0; j < 32; ++j) pr[j] = dy[o] * v[j];
-          acc_dw2[o][q] += warp_reduce_scatter32(pr, lane);
+          for (int j = 0; j < 32; ++j) pr[j] = dy[o] * h1[j];
+          acc_dw2[o] += warp_reduce_scatter32(pr, lane);
         }
       }
       tc::fence_smem_to_async();
       tc::fence_before_sync();
       __syncthreads();
-      // ---- B1: S = dH1 W1;  B2: dW1 += dH1^T H0 ----
+      // ---- B1: S = dH1 W1;  B2: dW1 += dH1^T H0_hi ----
       if (t == 0) {
         tc::fence_after_sync();
         const uint32_t id1 = tc::idesc_bf16(128, kH, false, true);
@@ -383,21 +403,20 @@ __global__ void __launch_bounds__(kTile, 1) head_tc_kernel(const HeadArgs a) {
         tc::mma_commit(mb);
       }
       if (!wait_mma()) break;
-      // ---- dH0 = S [H0 > 0] (over H0), db0 ----
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
+      // ---- dH0 = S [H0 > 0] (over H0_hi), db0 ----
+      {
         float v[32];
-        tc::tmem_ld32(tS + lane_off + q * 32, v);
+        tc::tmem_ld32(tS + lane_off + part * 32, v);
 #pragma unroll
-        for (int j = 0; j < 32; ++j) v[j] = ((mask0[q] >> j) & 1u) ? v[j] : 0.f;
+        for (int j = 0; j < 32; ++j) v[j] = ((mask0 >> j) & 1u) ? v[j] : 0.f;
 #pragma unroll
-        for (int g = 0; g < 4; ++g) store8(sH0, kH, t, q * 32 + g * 8, v + g * 8);
-        acc_db0[q] += warp_reduce_scatter32(v, lane);
+        for (int g = 0; g < 4; ++g) store8(sH0, kH, r, part * 32 + g * 8, v + g * 8);
+        acc_db0 += warp_reduce_scatter32(v, lane);
       }
       tc::fence_smem_to_async();
       tc::fence_before_sync();
       __syncthreads();
-      // ---- B3: dW0 += dH0^T X;  B4: S = dH0 W0 (columns [0, NX)) ----
+      // ---- B3: dW0 += dH0^T X_hi;  B4: S = dH0 W0 (columns [0, NX)) ----
       if (t == 0) {
         tc::fence_after_sync();
         const uint32_t id3 = tc::idesc_bf16(128, S::IN_PAD, true, true);
@@ -411,45 +430,39 @@ __global__ void __launch_bounds__(kTile, 1) head_tc_kernel(const HeadArgs a) {
       }
       if (!wait_mma()) break;
       any_tile = true;
-      // ---- dL/dfeat through the positional encoding ----
-      float gf[C];
-      float sn[C], cs[C];
+      // ---- dL/dfeat through the positional encoding: per-row sums in shared memory ----
+      for (int e = t; e < kTile * S::FS; e += kThreads) gfs[e] = 0.f;
+      __syncthreads();
+      {
+        const float* fr = fs + r * S::FS;
+        float* gr = gfs + r * S::FS;
+#pragma unroll 1
+        for (int ci = part; ci < (S::NX + 31) / 32; ci += 4) {  // 32-column loads inside S
+          float v[32];
+          tc::tmem_ld32(tS + lane_off + ci * 32, v);
 #pragma unroll
-      for (int c = 0; c < C; ++c) {
-        gf[c] = 0.f;
-        sincosf(valid ? frow[c] : 0.f, &sn[c], &cs[c]);
-      }
-      // 32-column loads over [0, NX rounded up to 32) (inside S); columns past NX are ignored
-#pragma unroll
-      for (int q = 0; q < (S::NX + 31) / 32; ++q) {
-        float v[32];
-        tc::tmem_ld32(tS + lane_off + q * 32, v);
-#pragma unroll
-        for (int j = 0; j < 32; ++j) {
-          const int k = q * 32 + j;
-          if (k >= S::NX) continue;
-          if (k < C) {
-            gf[k] += v[j];
-          } else if (k >= C + 3 && k < C + 3 + 2 * F * C) {
-            const bool cosine = k >= C + 3 + F * C;
-            const int jj = k - C - 3 - (cosine ? F * C : 0);
-            const int c = jj / F, f = jj % F;
-            // sin / cos of x 2^f by repeated doubling, d/dx = 2^f (cos, -sin)
-            float s = sn[c], co = cs[c];
-#pragma unroll
-            for (int r = 0; r < f; ++r) {
-              const float s2 = 2.f * s * co, c2 = 1.f - 2.f * s * s;
-              s = s2;
-              co = c2;
+          for (int j = 0; j < 32; ++j) {
+            const int k = ci * 32 + j;
+            if (k >= S::NX) break;
+            if (k < C) {
+              atomicAdd(gr + k, v[j]);
+            } else if (k >= C + 3 && k < C + 3 + 2 * F * C) {
+              const bool cosine = k >= C + 3 + F * C;
+              const int jj = k - C - 3 - (cosine ? F * C : 0);
+              const int c = jj / F, f = jj % F;
+              float sn, cs;
+              __sincosf(fr[1 + c] * (float)(1 << f), &sn, &cs);  // d/dx: 2^f (cos, -sin)
+              atomicAdd(gr + c, (float)(1 << f) * (cosine ? -sn : cs) * v[j]);
             }
-            gf[c] += (float)(1 << f) * (cosine ? -s : co) * v[j];
           }
         }
       }
-      if (valid) {
-        float* gr = a.grad_feat + sidx * a.feat_stride + 1;
-#pragma unroll
-        for (int c = 0; c < C; ++c) gr[c] = gf[c];
+      __syncthreads();
+#pragma unroll 1
+      for (int i = 0; i < kTile / 16; ++i) {  // a warp per row: coalesced writes of channels 1..C
+        const int rr = warp * (kTile / 16) + i;
+        const int32_t si = idx_s[rr];
+        if (si >= 0 && lane < C) a.grad_feat[(int64_t)si * a.feat_stride + 1 + lane] = gfs[rr * S::FS + lane];
       }
       tc::fence_before_sync();
       __syncthreads();
@@ -461,31 +474,28 @@ __global__ void __launch_bounds__(kTile, 1) head_tc_kernel(const HeadArgs a) {
     (void)tc::mbar_wait(mb, phase & 1u, kPolls);  // the MMAs in flight, if they ever finish
   } else if (BWD && any_tile) {
     // ---- flush: dW1 / dW0 rows from TMEM (row = this thread's lane), the register sums ----
-#pragma unroll 1
-    for (int q = 0; q < kH / 32; ++q) {
+    {
       float v[32];
-      tc::tmem_ld32(tDW1 + lane_off + q * 32, v);
+      tc::tmem_ld32(tDW1 + lane_off + part * 32, v);
       if (a.gw[1])
 #pragma unroll
-        for (int j = 0; j < 32; ++j) atomicAdd(a.gw[1] + t * kH + q * 32 + j, v[j]);
+        for (int j = 0; j < 32; ++j) atomicAdd(a.gw[1] + r * kH + part * 32 + j, v[j]);
     }
 #pragma unroll 1
-    for (int q = 0; q < (S::IN_PAD + 31) / 32; ++q) {
+    for (int ci = part; ci < (S::IN_PAD + 31) / 32; ci += 4) {
       float v[32];
-      tc::tmem_ld32(tDW0 + lane_off + q * 32, v);  // columns past IN_PAD (inside the allocation) unused
+      tc::tmem_ld32(tDW0 + lane_off + ci * 32, v);  // columns past IN_PAD (inside the allocation) unused
       if (a.gw[0])
 #pragma unroll
         for (int j = 0; j < 32; ++j)
-          if (q * 32 + j < S::IN) atomicAdd(a.gw[0] + t * S::IN + q * 32 + j, v[j]);
+          if (ci * 32 + j < S::IN) atomicAdd(a.gw[0] + r * S::IN + ci * 32 + j, v[j]);
     }
+    const int col = part * 32 + lane;
+    if (a.gb[0]) atomicAdd(a.gb[0] + col, acc_db0);
+    if (a.gb[1]) atomicAdd(a.gb[1] + col, acc_db1);
+    if (a.gw[2])
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      if (a.gb[0]) atomicAdd(a.gb[0] + q * 32 + lane, acc_db0[q]);
-      if (a.gb[1]) atomicAdd(a.gb[1] + q * 32 + lane, acc_db1[q]);
-#pragma unroll
-      for (int o = 0; o < 3; ++o)
-        if (a.gw[2]) atomicAdd(a.gw[2] + o * kH + q * 32 + lane, acc_dw2[o][q]);
-    }
+      for (int o = 0; o < 3; ++o) atomicAdd(a.gw[2] + o * kH + col, acc_dw2[o]);
   }
   tc::fence_before_sync();
   __syncthreads();
@@ -495,12 +505,13 @@ __global__ void __launch_bounds__(kTile, 1) head_tc_kernel(const HeadArgs a) {
 template <int C, int F, int V, bool BWD>
 cudaError_t launch_tc(const HeadArgs& a, cudaStream_t s) {
   constexpr int smem = Shape<C, F, V>::smem();
+  static_assert(smem <= 227 * 1024, "shared memory per CTA");
   auto kern = head_tc_kernel<C, F, V, BWD>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;
   const int64_t tiles = ceil_div(a.n, kTile);
   const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>(tiles, (int64_t)sm_count()));
-  kern<<<blocks, kTile, smem, s>>>(a);
+  kern<<<blocks, kThreads, smem, s>>>(a);
   return cudaGetLastError();
 }
 
