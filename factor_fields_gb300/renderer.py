@@ -283,6 +283,38 @@ def march_static(model, rays, jitter, rdesc):
     return offsets, xyz, sidx
 
 
+def sh_render_forward(job, rays, jitter):
+    """The SH-2 render forward on the native kernels: (rgb, depth, saved tensors for the
+    backward). Static jobs (job['static']) make no host read."""
+    m, rdesc = job["model"], job["rdesc"]
+    if job.get("static"):  # no host synchronisation: capturable in a CUDA graph
+        offsets, xyz, sidx = march_static(m, rays, jitter, rdesc)
+        job["n_dev"] = offsets[rays.shape[0]:]
+    else:
+        offsets, xyz, sidx = march(m, rays, jitter, rdesc)
+    feat = field_eval(m, job, xyz)
+    n = rays.shape[0]
+    rgb = torch.empty(n, 3, device=rays.device)
+    depth = torch.empty(n, device=rays.device)
+    N.call("ff_composite_forward", ctypes.byref(rdesc), N.ptr(rays), N.ptr(jitter), n, N.ptr(offsets),
+           N.ptr(sidx), N.ptr(feat), feat.shape[1], None, N.ptr(rgb), N.ptr(depth), None, N.stream_ptr())
+    job["xyz"] = xyz
+    return rgb, depth, (rays, offsets, xyz, sidx, feat)
+
+
+def sh_render_backward(job, jitter, saved, g_rgb):
+    """Backward of sh_render_forward for dL/drgb: the compositing reverse scan, then the field
+    and MLP backward (field_grad)."""
+    rays, offsets, xyz, sidx, feat = saved
+    rdesc = job["rdesc"]
+    n = rays.shape[0]
+    g_feat = torch.empty_like(feat)
+    g_rgb = g_rgb.contiguous()
+    N.call("ff_composite_backward", ctypes.byref(rdesc), N.ptr(rays), N.ptr(jitter), n, N.ptr(offsets),
+           N.ptr(sidx), N.ptr(feat), feat.shape[1], None, N.ptr(g_rgb), N.ptr(g_feat), N.stream_ptr())
+    return field_grad(job["model"], job, xyz, g_feat)
+
+
 class RenderFunction(torch.autograd.Function):
     """rgb, depth = render(rays) with gradients to the grids and the MLP head.
 
@@ -291,36 +323,15 @@ class RenderFunction(torch.autograd.Function):
 
     @staticmethod
     def forward(ctx, rays, jitter, basis_param, coeff_param, w0, b0, w1, job):
-        m, rdesc = job["model"], job["rdesc"]
-        if job.get("static"):  # no host synchronisation: capturable in a CUDA graph
-            offsets, xyz, sidx = march_static(m, rays, jitter, rdesc)
-            job["n_dev"] = offsets[rays.shape[0]:]
-        else:
-            offsets, xyz, sidx = march(m, rays, jitter, rdesc)
-        feat = field_eval(m, job, xyz)
-        n = rays.shape[0]
-        rgb = torch.empty(n, 3, device=rays.device)
-        depth = torch.empty(n, device=rays.device)
-        N.call("ff_composite_forward", ctypes.byref(rdesc), N.ptr(rays), N.ptr(jitter), n, N.ptr(offsets),
-               N.ptr(sidx), N.ptr(feat), feat.shape[1], None, N.ptr(rgb), N.ptr(depth), None, N.stream_ptr())
-        ctx.save_for_backward(rays, offsets, xyz, sidx, feat)
+        rgb, depth, saved = sh_render_forward(job, rays, jitter)
+        ctx.save_for_backward(*saved)
         ctx.jitter, ctx.job = jitter, job
         ctx.mark_non_differentiable(depth)
-        job["xyz"] = xyz
         return rgb, depth
 
     @staticmethod
     def backward(ctx, g_rgb, g_depth):
-        rays, offsets, xyz, sidx, feat = ctx.saved_tensors
-        job = ctx.job
-        m, rdesc = job["model"], job["rdesc"]
-        n = rays.shape[0]
-        g_feat = torch.empty_like(feat)
-        g_rgb = g_rgb.contiguous()
-        N.call("ff_composite_backward", ctypes.byref(rdesc), N.ptr(rays), N.ptr(ctx.jitter), n, N.ptr(offsets),
-               N.ptr(sidx), N.ptr(feat), feat.shape[1], None, N.ptr(g_rgb), N.ptr(g_feat),
-               N.stream_ptr())
-        grads = field_grad(m, job, xyz, g_feat)
+        grads = sh_render_backward(ctx.job, ctx.jitter, ctx.saved_tensors, g_rgb)
         return (None, None) + grads + (None,)
 
 
@@ -482,6 +493,17 @@ def field_grad(m, job, xyz, g_out):
     return (gb, gc, gw[0], gbias[0], gw[1] if len(gw) > 1 else None)
 
 
+def render_job(model, rays, n_samples, white_bg, fused, static):
+    """The descriptors and read buffers of one render call."""
+    basis_r, coeff_r, dt = model._read_buffers()
+    coeff_param = model.coeff_flat
+    if model.n_scene > 1:
+        coeff_param = model._coeff_scene(model.coeff_flat)
+        coeff_r = model._coeff_scene(coeff_r)
+    return {"model": model, "rdesc": render_desc(model, n_samples, white_bg), "fdesc": model.descriptor(dt),
+            "basis_r": basis_r, "coeff_r": coeff_r, "coeff_param": coeff_param, "fused": fused, "static": static}
+
+
 def render_forward(model, rays_chunk, white_bg=True, is_train=False, ndc_ray=False, N_samples=-1, fused=None,
                    jitter=None, static=False):
     """FactorFields.forward (models/FactorFields.py:843-898), bounded scenes, with the model's
@@ -511,13 +533,8 @@ def render_forward(model, rays_chunk, white_bg=True, is_train=False, ndc_ray=Fal
     wb = bool(white_bg or (is_train and torch.rand((1,)) < 0.5))  # :890
     if fused is None:
         fused = model.precision == "bf16"
-    basis_r, coeff_r, dt = model._read_buffers()
-    coeff_param = model.coeff_flat
-    if model.n_scene > 1:
-        coeff_param = model._coeff_scene(model.coeff_flat)
-        coeff_r = model._coeff_scene(coeff_r)
-    job = {"model": model, "rdesc": render_desc(model, n_samples, wb), "fdesc": model.descriptor(dt),
-           "basis_r": basis_r, "coeff_r": coeff_r, "coeff_param": coeff_param, "fused": fused, "static": static}
+    job = render_job(model, rays, n_samples, wb, fused, static)
+    coeff_param = job["coeff_param"]
     if static and (mlp_head or not fused):
         raise NotImplementedError("static (graph-capturable) rendering needs the fused BF16 path and the SH-2 head")
     l0, l1 = lm.backbone

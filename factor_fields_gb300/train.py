@@ -79,13 +79,31 @@ class RadianceFieldTrainer:
             self._grads_clean = self.fused_adam and (self.sampler is None or self.sampler.fused_adam)
         return loss.detach()
 
+    def _plain_step_static(self, rays, rgb_gt):
+        """The plain sampler's fwd+bwd training step without autograd and without host reads
+        (the body of its CUDA graph): gradients zeroed, static render forward, MSE, its gradient
+        2 (rgb - gt) / (3 R), render backward into the .grad buffers. Returns the loss (device)."""
+        from .renderer import render_job, sh_render_backward, sh_render_forward
+        m = self.m
+        if not self._grads_clean:
+            self._zero_grads()
+        self._grads_clean = False
+        jitter = self.jitter if self.jitter is not None else torch.rand(rays.shape[0], device=rays.device)
+        job = render_job(m, rays, self.n_samples, self.white_bg, True, True)
+        rgb, _, saved = sh_render_forward(job, rays, jitter)
+        diff = rgb - rgb_gt
+        loss = torch.mean(diff * diff)
+        sh_render_backward(job, jitter, saved, diff * (2.0 / diff.numel()))
+        return loss
+
     def graph_step(self, rays, rgb_gt):
         """step(optimize=False) replayed from a CUDA graph. The batch is copied into static
         buffers; the capture covers the gradient zeroing, rendering, loss, the field backward and
-        (proposal sampler) the proposal loss/backward. The plain sampler renders without host
-        synchronisation for this (static=True: live-sample buffers sized for all n_rays *
-        n_samples slots, the live count read on the device; fused BF16 path, SH-2 head). The per-ray
-        jitter is drawn inside the graph (or self.jitter). Re-captured when the batch shape changes."""
+        (proposal sampler) the proposal loss/backward. The plain sampler's step is captured as the
+        explicit _plain_step_static (no autograd, no host reads: live-sample buffers sized for all
+        n_rays * n_samples slots, the live count read on the device; fused BF16 path, SH-2 head).
+        The per-ray jitter is drawn inside the graph (or self.jitter). Re-captured when the batch
+        shape changes."""
         static = self.sampler is None
         key = (tuple(rays.shape), tuple(rgb_gt.shape))
         if getattr(self, "_gkey", None) != key:
@@ -96,13 +114,15 @@ class RadianceFieldTrainer:
             self._gg.copy_(rgb_gt)
             side = torch.cuda.Stream()
             side.wait_stream(torch.cuda.current_stream())
+            body = (lambda: self._plain_step_static(self._gr, self._gg)) if static else \
+                (lambda: self.step(self._gr, self._gg, optimize=False))
             with torch.cuda.stream(side):
                 for _ in range(2):
-                    self.step(self._gr, self._gg, optimize=False, static=static)
+                    body()
             torch.cuda.current_stream().wait_stream(side)
             self._graph = torch.cuda.CUDAGraph()
             with torch.cuda.graph(self._graph):
-                self._gloss = self.step(self._gr, self._gg, optimize=False, static=static)
+                self._gloss = body()
             self._gkey = key
         self.m._read_buffers()
         if self.sampler is not None:
