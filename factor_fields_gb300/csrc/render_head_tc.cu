@@ -7,9 +7,11 @@
 // thread. Per tile, for 3 layers 128 hidden units wide:
 //
 //   stage  the tile's feature rows (channels 0..C) and ray directions into shared memory,
-//          warp per row (coalesced), through app_idx / app_ray
+//          warp per row (coalesced), through app_idx / app_ray; the loads of the next tile are
+//          issued into registers right after, so their latency overlaps this tile's work
 //   X   = [feat, dir, PE(feat, 2), PE(dir, 6)]  in shared memory as a BF16 pair X_hi + X_lo
-//          (~16 significant bits), written one 128-byte core matrix per warp store
+//          (~16 significant bits); a thread builds one row's 8-column chunk (columns decoded at
+//          compile time) with one 16-byte store into each of X_hi and X_lo
 //   F1  S = X_hi W0^T + X_lo W0^T   (tcgen05, M 128, N 128, K = in_dim padded to 16)
 //       H0 = relu(S + b0)           -> shared memory as H0_hi + H0_lo, ReLU mask in registers
 //   F2  S = H0_hi W1^T + H0_lo W1^T (N 128, K 128)
@@ -44,6 +46,8 @@
 // per-tile accumulator S, then dW1 (128), then dW0 (in_dim padded): at most 512.
 // Every wait on an mbarrier has an iteration limit: when it runs out the kernel reports
 // FF_ERR_LIMIT through `status`, stops, waits (again with a limit) for its MMAs and frees TMEM.
+#include <utility>
+
 #include "ff_common.cuh"
 #include "ff_internal.h"
 #include "tc_util.cuh"
@@ -112,9 +116,6 @@ __device__ __forceinline__ uint64_t desc_mn(uint32_t base, int cols, int s) {
 __device__ __forceinline__ void st_shared_v4(uint32_t saddr, uint32_t a, uint32_t b, uint32_t c, uint32_t d) {
   asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(saddr), "r"(a), "r"(b), "r"(c), "r"(d) : "memory");
 }
-__device__ __forceinline__ void st_shared_b32(uint32_t saddr, uint32_t v) {
-  asm volatile("st.shared.b32 [%0], %1;" ::"r"(saddr), "r"(v) : "memory");
-}
 
 // Eight consecutive values of row t (columns k0 .. k0 + 7, k0 % 8 == 0) as one 16-byte store.
 __device__ __forceinline__ void store8(uint32_t buf, int cols, int t, int k0, const float* v) {
@@ -136,29 +137,83 @@ __device__ __forceinline__ void store8_split(uint32_t hi_buf, uint32_t lo_buf, i
   st_shared_v4(lo_buf + off, l[0], l[1], l[2], l[3]);
 }
 
-// Column k of the head's input row (the reference's order, models/FactorFields.py:188-195):
-// fr = the staged feature row (fr[1 + c] = feature c), dr = the ray direction; 0 past in_dim.
-template <int C, int F, int V>
-__device__ __forceinline__ float x_col(int k, const float* fr, const float* dr) {
-  if (k < C) return fr[1 + k];
-  k -= C;
-  if (k < 3) return dr[k];
-  k -= 3;
-  float s, co;
-  if (k < 2 * C * F) {
-    const bool cosine = k >= C * F;
-    const int j = cosine ? k - C * F : k;
-    __sincosf(fr[1 + j / F] * (float)(1 << (j % F)), &s, &co);
-    return cosine ? co : s;
+// Column K of the head's input row (the reference's order, models/FactorFields.py:188-195),
+// decoded at compile time: fr = the staged feature row (fr[1 + c] = feature c), dr = the ray
+// direction; 0 past in_dim. Positional-encoding columns use the hardware sin / cos.
+template <int C, int F, int V, int K>
+__device__ __forceinline__ float x_col(const float* fr, const float* dr) {
+  if constexpr (K < C) {
+    return fr[1 + K];
+  } else if constexpr (K < C + 3) {
+    return dr[K - C];
+  } else if constexpr (K < C + 3 + 2 * C * F) {
+    constexpr int k = K - C - 3;
+    constexpr bool kCos = k >= C * F;
+    constexpr int j = kCos ? k - C * F : k;
+    const float x = fr[1 + j / F] * (float)(1 << (j % F));
+    return kCos ? __cosf(x) : __sinf(x);
+  } else if constexpr (K < C + 3 + 2 * C * F + 6 * V) {
+    constexpr int k = K - C - 3 - 2 * C * F;
+    constexpr bool kCos = k >= 3 * V;
+    constexpr int j = kCos ? k - 3 * V : k;
+    const float x = dr[j / V] * (float)(1 << (j % V));
+    return kCos ? __cosf(x) : __sinf(x);
+  } else {
+    return 0.f;
   }
-  k -= 2 * C * F;
-  if (k < 6 * V) {
-    const bool cosine = k >= 3 * V;
-    const int j = cosine ? k - 3 * V : k;
-    __sincosf(dr[j / V] * (float)(1 << (j % V)), &s, &co);
-    return cosine ? co : s;
+}
+
+// Columns 8 CH .. 8 CH + 7 of row rr as a BF16 pair (one 16-byte store into each of X_hi, X_lo).
+template <int C, int F, int V, int CH, int... J>
+__device__ __forceinline__ void build_chunk(uint32_t X, uint32_t Xlo, int rr, const float* fr, const float* dr,
+                                            std::integer_sequence<int, J...>) {
+  const float v[8] = {x_col<C, F, V, CH * 8 + J>(fr, dr)...};
+  store8_split(X, Xlo, Shape<C, F, V>::IN_PAD, rr, CH * 8, v);
+}
+
+// Chunk `ch` (warp-uniform) dispatched to its compile-time builder.
+template <int C, int F, int V, int CH = 0>
+__device__ __forceinline__ void build_chunk_at(int ch, uint32_t X, uint32_t Xlo, int rr, const float* fr,
+                                               const float* dr) {
+  if constexpr (CH < Shape<C, F, V>::IN_PAD / 8) {
+    if (ch == CH) {
+      build_chunk<C, F, V, CH>(X, Xlo, rr, fr, dr, std::make_integer_sequence<int, 8>{});
+      return;
+    }
+    build_chunk_at<C, F, V, CH + 1>(ch, X, Xlo, rr, fr, dr);
   }
-  return 0.f;
+}
+
+// dL/dfeat terms of the 32 dX columns 32 CI .. 32 CI + 31 (inside [0, NX)) of row r, added to the
+// row sums gr: raw feature columns directly, PE columns through d/dx sin(x 2^f) = 2^f cos(x 2^f),
+// d/dx cos(x 2^f) = -2^f sin(x 2^f).
+template <int C, int F, int V, int CI, int... J>
+__device__ __forceinline__ void pe_back_chunk(const float* v, const float* fr, float* gr,
+                                              std::integer_sequence<int, J...>) {
+  auto one = [&](auto jc) {
+    constexpr int k = CI * 32 + decltype(jc)::value;
+    if constexpr (k < C) {
+      atomicAdd(gr + k, v[decltype(jc)::value]);
+    } else if constexpr (k >= C + 3 && k < C + 3 + 2 * F * C) {
+      constexpr bool kCos = k >= C + 3 + F * C;
+      constexpr int jj = k - C - 3 - (kCos ? F * C : 0);
+      constexpr int c = jj / F, f = jj % F;
+      const float x = fr[1 + c] * (float)(1 << f);
+      atomicAdd(gr + c, (float)(1 << f) * (kCos ? -__sinf(x) : __cosf(x)) * v[decltype(jc)::value]);
+    }
+  };
+  (one(std::integral_constant<int, J>{}), ...);
+}
+
+template <int C, int F, int V, int CI = 0>
+__device__ __forceinline__ void pe_back_at(int ci, const float* v, const float* fr, float* gr) {
+  if constexpr (CI < (Shape<C, F, V>::NX + 31) / 32) {
+    if (ci == CI) {
+      pe_back_chunk<C, F, V, CI>(v, fr, gr, std::make_integer_sequence<int, 32>{});
+      return;
+    }
+    pe_back_at<C, F, V, CI + 1>(ci, v, fr, gr);
+  }
 }
 
 // Warp reduce-scatter: lane l returns the sum over the warp's lanes of v[l].
@@ -250,34 +305,46 @@ __global__ void __launch_bounds__(kThreads, 1) head_tc_kernel(const HeadArgs a) 
   };
 
   const int64_t n_tiles = ceil_div(a.n, kTile);
-  for (int64_t tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x) {
-    // ---- stage the tile's feature rows (channels 0..C), directions and row indices ----
-#pragma unroll 1
-    for (int i = 0; i < kTile / 16; ++i) {
-      const int rr = warp * (kTile / 16) + i;
-      const int64_t row = tile * kTile + rr;
+  // rows staged by this warp: its feature channel (lane <= C), direction component (lane < 3) and
+  // row index, held in registers from the previous tile's prefetch
+  constexpr int kRowsPerWarp = kTile / (kThreads / 32);
+  float pf[kRowsPerWarp], pd[kRowsPerWarp];
+  int32_t pix[kRowsPerWarp];
+  auto load_rows = [&](int64_t tl) {
+    int64_t ray[kRowsPerWarp];
+#pragma unroll
+    for (int i = 0; i < kRowsPerWarp; ++i) {
+      const int64_t row = tl * kTile + warp * kRowsPerWarp + i;
       const bool valid = row < a.n;
-      const int64_t sidx = valid ? (int64_t)a.app_idx[row] : 0;
-      if (lane <= C) fs[rr * S::FS + lane] = valid ? a.feat[sidx * a.feat_stride + lane] : 0.f;
-      if (lane < 3) ds[rr * 4 + lane] = valid ? a.rays[(int64_t)a.app_ray[row] * 6 + 3 + lane] : 0.f;
-      if (lane == 0) idx_s[rr] = valid ? (int32_t)sidx : -1;
+      pix[i] = valid ? a.app_idx[row] : -1;
+      ray[i] = valid ? (int64_t)a.app_ray[row] : -1;
+    }
+#pragma unroll
+    for (int i = 0; i < kRowsPerWarp; ++i) {
+      pf[i] = (pix[i] >= 0 && lane <= C) ? a.feat[(int64_t)pix[i] * a.feat_stride + lane] : 0.f;
+      pd[i] = (ray[i] >= 0 && lane < 3) ? a.rays[ray[i] * 6 + 3 + lane] : 0.f;
+    }
+  };
+  if ((int64_t)blockIdx.x < n_tiles) load_rows(blockIdx.x);
+  for (int64_t tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x) {
+    // ---- the tile's feature rows (channels 0..C), directions and row indices -> shared memory
+    // (loaded into registers one tile ahead), then the next tile's loads are issued ----
+#pragma unroll
+    for (int i = 0; i < kRowsPerWarp; ++i) {
+      const int rr = warp * kRowsPerWarp + i;
+      if (lane <= C) fs[rr * S::FS + lane] = pf[i];
+      if (lane < 3) ds[rr * 4 + lane] = pd[i];
+      if (lane == 0) idx_s[rr] = pix[i];
     }
     __syncthreads();
-    // ---- X: one core matrix (8 rows x 8 columns) per warp store, thread = (row, column pair) ----
+    if (tile + gridDim.x < n_tiles) load_rows(tile + gridDim.x);
+    // ---- X: thread = (row, 8-column chunk), one 16-byte store into each of X_hi and X_lo ----
     {
       constexpr int kChunks = S::IN_PAD / 8;
-      const int sub = lane >> 2, pr = lane & 3;
 #pragma unroll 1
-      for (int j = warp; j < (kTile / 8) * kChunks; j += kThreads / 32) {
-        const int rr = (j / kChunks) * 8 + sub, k0 = (j % kChunks) * 8 + 2 * pr;
-        const float* fr = fs + rr * S::FS;
-        const float* dr = ds + rr * 4;
-        const float v0 = x_col<C, F, V>(k0, fr, dr), v1 = x_col<C, F, V>(k0 + 1, fr, dr);
-        const uint32_t h = tc::pack2_bf16(v0, v1);
-        const uint32_t l = tc::pack2_bf16(v0 - __uint_as_float(h << 16), v1 - __uint_as_float(h & 0xffff0000u));
-        const uint32_t off = tc::core_off(rr, k0, S::IN_PAD);
-        st_shared_b32(sX + off, h);
-        st_shared_b32(sXlo + off, l);
+      for (int it = warp; it < 4 * kChunks; it += kThreads / 32) {
+        const int rr = (it & 3) * 32 + lane;
+        build_chunk_at<C, F, V>(it >> 2, sX, sXlo, rr, fs + rr * S::FS, ds + rr * 4);
       }
     }
     tc::fence_smem_to_async();
@@ -440,21 +507,7 @@ __global__ void __launch_bounds__(kThreads, 1) head_tc_kernel(const HeadArgs a) 
         for (int ci = part; ci < (S::NX + 31) / 32; ci += 4) {  // 32-column loads inside S
           float v[32];
           tc::tmem_ld32(tS + lane_off + ci * 32, v);
-#pragma unroll
-          for (int j = 0; j < 32; ++j) {
-            const int k = ci * 32 + j;
-            if (k >= S::NX) break;
-            if (k < C) {
-              atomicAdd(gr + k, v[j]);
-            } else if (k >= C + 3 && k < C + 3 + 2 * F * C) {
-              const bool cosine = k >= C + 3 + F * C;
-              const int jj = k - C - 3 - (cosine ? F * C : 0);
-              const int c = jj / F, f = jj % F;
-              float sn, cs;
-              __sincosf(fr[1 + c] * (float)(1 << f), &sn, &cs);  // d/dx: 2^f (cos, -sin)
-              atomicAdd(gr + c, (float)(1 << f) * (cosine ? -sn : cs) * v[j]);
-            }
-          }
+          pe_back_at<C, F, V>(ci, v, fr, gr);
         }
       }
       __syncthreads();
