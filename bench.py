@@ -353,6 +353,80 @@ def _train_radiance(kind, seed, iters, pool, gt, dev):
     return m, sampler, tr, g
 
 
+def measure_radiance_field_kernels(m, rays, dev, flush, steps, warmup, seed=3):
+    """The fused field + 18->64->28 head kernels alone (ff_field_mlp_forward / _backward) on the
+    live samples of one 4,096-ray plain-sampler batch (ray order, as the render calls them), each
+    launch bracketed by CUDA events on its stream after an L2 flush. The backward's contract bytes
+    per sample are those of the field backward (two BF16 gathers of the 8 corners x 36 channels,
+    one float32 scatter, coordinates and dL/dout: 2,428 B); the forward's one gather plus the
+    coordinates and outputs (700 B)."""
+    import ctypes
+    from factor_fields_gb300 import _native as N
+    from factor_fields_gb300 import functional as FN
+    from factor_fields_gb300.renderer import march, render_desc
+    g = torch.Generator(device=dev).manual_seed(seed)
+    jit = torch.rand(rays.shape[0], device=dev, generator=g)
+    with torch.no_grad():
+        _, xyz, _ = march(m, rays, jit, render_desc(m, 1024, True))
+    n = xyz.shape[0]
+    lm = m.linear_mat
+    ws, bs = lm.weights()
+    mlp = FN.mlp_struct(ws, bs, lm.in_dim, lm.hidden_dim, lm.out_dim)
+    basis_r, coeff_r, dt = m._read_buffers()
+    fdesc = m.descriptor(dt)
+    out = torch.empty(n, lm.out_dim, device=dev)
+    g_out = torch.randn(n, lm.out_dim, device=dev, generator=g) * 1e-3
+    gb, gc = torch.zeros_like(m.basis_flat), torch.zeros_like(m.coeff_flat)  # scratch gradients
+    gw = [torch.zeros_like(w) for w in ws]
+    gbias = [torch.zeros_like(b) if b is not None else None for b in bs]
+    grad = N.FFMlpGrad()
+    for i in range(len(ws)):
+        grad.weight[i] = gw[i].data_ptr()
+        grad.bias[i] = gbias[i].data_ptr() if gbias[i] is not None else None
+    stream = torch.cuda.current_stream()
+    st = N.stream_ptr()
+
+    def fwd():
+        N.call("ff_field_mlp_forward", ctypes.byref(fdesc), N.ptr(basis_r), N.ptr(coeff_r), ctypes.byref(mlp),
+               N.ptr(xyz), n, N.ptr(out), st)
+
+    def bwd():
+        N.call("ff_field_mlp_backward", ctypes.byref(fdesc), N.ptr(basis_r), N.ptr(coeff_r), ctypes.byref(mlp),
+               N.ptr(xyz), n, N.ptr(g_out), N.ptr(gb), N.ptr(gc), ctypes.byref(grad), st)
+
+    def timed(fn):
+        for _ in range(warmup):
+            fn()
+        ts = []
+        for _ in range(steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        return float(np.mean(ts))
+
+    fwd_ms, bwd_ms = timed(fwd), timed(bwd)
+    k, ch = 2 ** m.in_dim, m.n_feat * 2
+    io = 4 * m.geom.coord_dim + 4 * lm.out_dim
+    b_bwd = bytes_per_point(m, 2, 2)
+    b_fwd = k * ch * 2 + io
+    peaks = load_peaks()
+    peak = peaks.get("hbm_gbs", 6800.0)
+    ach = b_bwd * n / (bwd_ms / 1e3) / 1e9
+    ach_f = b_fwd * n / (fwd_ms / 1e3) / 1e9
+    return {"samples": n, "fwd_ms": fwd_ms, "bwd_ms": bwd_ms,
+            "roofline": {"bound": "hbm", "kernel": "fused_field_mlp_kernel<1,3,3,4,bf16> (field backward, 28-wide head)",
+                         "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak, "bytes_per_sample": b_bwd,
+                         "fwd_kernel": "fused_field_mlp_kernel<0,3,3,4,bf16>", "fwd_achieved": ach_f,
+                         "fwd_frac": ach_f / peak, "fwd_bytes_per_sample": b_fwd,
+                         "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if "hbm_gbs" in peaks else "fallback",
+                         "l2": "flushed (256 MB write) before every timed launch"}}
+
+
 def run_radiance(args, dev):
     """Configurations 2 and 3 on the synthetic blob scene: rays/s of one fwd+bwd training step
     (plain sampler: 4,096 rays x up to 1,024 samples with 128^3 occupancy-bitfield pruning;
@@ -433,6 +507,9 @@ def run_radiance(args, dev):
             offs, _, _ = march(m, test, None, render_desc(m, 1024, True))
             rec["live_samples_per_ray"] = float(offs[-1]) / test.shape[0]
             rec["max_samples_per_ray"] = 1024
+            idx = torch.randint(0, pool.shape[0], (batch,), device=dev, generator=g)
+            rec["field_kernels"] = measure_radiance_field_kernels(m, pool[idx], dev, flush, args.steps,
+                                                                  max(args.warmup, 3))
         else:
             rec["samples_per_ray"] = sampler.n_fine
         out[kind] = rec

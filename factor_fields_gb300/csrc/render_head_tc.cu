@@ -83,6 +83,7 @@ struct Shape {
   static constexpr int IDX_B = kTile * 4;
   static constexpr int F32_B = 5 * kH * 4;  // W2 [3][128], b0, b1
   static_assert(kTile * 4 * 4 * 4 <= H_B && FEAT_B <= R_B, "aliased buffers fit");
+  static_assert((W0_B + W1_B + X_B + R_B + FEAT_B + DIR_B + IDX_B) % 16 == 0, "float4 reads of W2 / b0 / b1");
   static constexpr int smem() { return W0_B + W1_B + X_B + R_B + FEAT_B + DIR_B + IDX_B + F32_B + 64; }
 };
 
@@ -368,11 +369,18 @@ __global__ void __launch_bounds__(kThreads, 1) head_tc_kernel(const HeadArgs a) 
     {
       float v[32];
       tc::tmem_ld32(tS + lane_off + part * 32, v);
+      const float4* b0v = reinterpret_cast<const float4*>(b0s + part * 32);  // warp-uniform: broadcasts
 #pragma unroll
-      for (int j = 0; j < 32; ++j) {
-        const float h = v[j] + b0s[part * 32 + j];
-        mask0 |= (h > 0.f ? 1u : 0u) << j;
-        v[j] = fmaxf(h, 0.f);
+      for (int j4 = 0; j4 < 8; ++j4) {
+        const float4 b = b0v[j4];
+        const float bb[4] = {b.x, b.y, b.z, b.w};
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int j = 4 * j4 + q;
+          const float h = v[j] + bb[q];
+          mask0 |= (h > 0.f ? 1u : 0u) << j;
+          v[j] = fmaxf(h, 0.f);
+        }
       }
 #pragma unroll
       for (int g = 0; g < 4; ++g) store8_split(sH0, sH0lo, kH, r, part * 32 + g * 8, v + g * 8);
@@ -396,14 +404,22 @@ __global__ void __launch_bounds__(kThreads, 1) head_tc_kernel(const HeadArgs a) 
     {
       float y0 = 0.f, y1 = 0.f, y2 = 0.f;
       tc::tmem_ld32(tS + lane_off + part * 32, h1);
+      const float4* b1v = reinterpret_cast<const float4*>(b1s + part * 32);
+      const float4* w2v = reinterpret_cast<const float4*>(w2s + part * 32);  // rows kH / 4 float4 apart
 #pragma unroll
-      for (int j = 0; j < 32; ++j) {
-        const int u = part * 32 + j;
-        const float h = fmaxf(h1[j] + b1s[u], 0.f);
-        h1[j] = h;
-        y0 += h * w2s[u];
-        y1 += h * w2s[kH + u];
-        y2 += h * w2s[2 * kH + u];
+      for (int j4 = 0; j4 < 8; ++j4) {
+        const float4 b = b1v[j4], wa = w2v[j4], wb = w2v[kH / 4 + j4], wc = w2v[kH / 2 + j4];
+        const float bb[4] = {b.x, b.y, b.z, b.w}, w0[4] = {wa.x, wa.y, wa.z, wa.w};
+        const float w1[4] = {wb.x, wb.y, wb.z, wb.w}, w2[4] = {wc.x, wc.y, wc.z, wc.w};
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int j = 4 * j4 + q;
+          const float h = fmaxf(h1[j] + bb[q], 0.f);
+          h1[j] = h;
+          y0 += h * w0[q];
+          y1 += h * w1[q];
+          y2 += h * w2[q];
+        }
       }
       yp[part * kTile + r] = make_float4(y0, y1, y2, 0.f);
     }
@@ -438,10 +454,17 @@ __global__ void __launch_bounds__(kThreads, 1) head_tc_kernel(const HeadArgs a) 
       // dH1 = (dy W2) [H1 > 0]; dW2 += dy^T H1, db1 += sum dH1 (warp reduce-scatters)
       {
         float dh[32];
+        const float4* w2v = reinterpret_cast<const float4*>(w2s + part * 32);
 #pragma unroll
-        for (int j = 0; j < 32; ++j) {
-          const int u = part * 32 + j;
-          dh[j] = h1[j] > 0.f ? dy[0] * w2s[u] + dy[1] * w2s[kH + u] + dy[2] * w2s[2 * kH + u] : 0.f;
+        for (int j4 = 0; j4 < 8; ++j4) {
+          const float4 wa = w2v[j4], wb = w2v[kH / 4 + j4], wc = w2v[kH / 2 + j4];
+          const float w0[4] = {wa.x, wa.y, wa.z, wa.w}, w1[4] = {wb.x, wb.y, wb.z, wb.w};
+          const float w2[4] = {wc.x, wc.y, wc.z, wc.w};
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            const int j = 4 * j4 + q;
+            dh[j] = h1[j] > 0.f ? dy[0] * w0[q] + dy[1] * w1[q] + dy[2] * w2[q] : 0.f;
+          }
         }
 #pragma unroll
         for (int g = 0; g < 4; ++g) store8(sDH1, kH, r, part * 32 + g * 8, dh + g * 8);

@@ -163,15 +163,18 @@ class FieldFitRunner:
             raise ValueError("binned=True needs fused=True")
         self._ws = None
         self._ws_gen = 0
+        # the fused kernel's template arguments: mode, basis dim, coordinate dim, 8-wide output tiles
+        out = model.linear_mat.out_dim
+        dims = f"{model.in_dim},{model.geom.coord_dim},{1 if out == 1 else (2 if out <= 16 else 4)}"
         if fused and self.binned:
             self.path_name = ("fused, binned: one ff_field_fit_step_binned call per step (bin by coefficient cell "
                               "with the gradient zeroing, allocate cell ranges, permute, fit)")
-            self.dominant_kernel = "fused_field_mlp_kernel<3,3,3,1,bf16> (binned fit)"
+            self.dominant_kernel = f"fused_field_mlp_kernel<3,{dims},bf16> (binned fit)"
             self.dominant_call = "ff_field_fit_step_binned"
             self.gathers_per_point = 1
         elif fused:
             self.path_name = "fused: one ff_field_fit_step launch per step (+ gradient zeroing)"
-            self.dominant_kernel = "fused_field_mlp_kernel<2,3,3,1,bf16> (fit)"
+            self.dominant_kernel = f"fused_field_mlp_kernel<2,{dims},bf16> (fit)"
             self.dominant_call = "ff_field_fit_step"
             self.gathers_per_point = 1
         else:
