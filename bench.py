@@ -138,8 +138,14 @@ def make_model(precision, key="cfg1"):
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one full-size launch of the fit
 # kernel from the ncu captures summarised in profiles/fused_fit_kernel_cfg1_ncu.md.
-NCU_TRAFFIC = {"fused_field_mlp_kernel<3,3,3,1,bf16> (binned fit)": 69.586688e6 + 0.454144e6,
+NCU_TRAFFIC = {"fused_field_mlp_kernel<3,3,3,1,bf16> (binned fit)": 69.600256e6 + 1.299968e6,
                "fused_field_mlp_kernel<2,3,3,1,bf16> (fit)": 69.626112e6 + 1.560832e6}
+# The binned fit kernel's L2-side work per 262,144-point launch (same capture): warp-level
+# global red instructions (l1tex__t_requests_pipe_lsu_mem_global_op_red.sum) and L2 red requests
+# (lts__t_requests_srcunit_tex_op_red.sum); and the rate of warp-wide float4 reds with one line
+# per lane that a standalone probe sustained on this GPU, the ceiling those reds run against.
+NCU_FIT_REDS = {"warp_reds": 791374, "l2_red_requests": 11301333}
+PROBE_WARP_REDS_PER_S = 6.5e9
 
 
 def bytes_per_point(m, gathers, param_bytes):
@@ -315,6 +321,16 @@ def run_native(args, ws, rank, local):
     roof["traffic"] = NCU_TRAFFIC.get(roof["kernel"])
     roof["traffic_source"] = ("ncu dram read+write of the fit kernel, one 262,144-point launch "
                               "(profiles/fused_fit_kernel_cfg1_ncu.md)")
+    if roof.get("kernel_ms") and roof["kernel"] in NCU_TRAFFIC and "<3,3,3,1" in roof["kernel"]:
+        # the L2-side fraction: warp-level gradient reds per second against the probe's rate
+        rate = NCU_FIT_REDS["warp_reds"] / (roof["kernel_ms"] / 1e3)
+        roof["l2_reds"] = {"warp_reds_per_launch": NCU_FIT_REDS["warp_reds"],
+                           "l2_red_requests_per_point": NCU_FIT_REDS["l2_red_requests"] / N_POINTS,
+                           "achieved_warp_reds_per_s": rate, "peak_warp_reds_per_s": PROBE_WARP_REDS_PER_S,
+                           "frac": rate / PROBE_WARP_REDS_PER_S,
+                           "source": "ncu counts of one launch (profiles/fused_fit_kernel_cfg1_ncu.md) over the "
+                                     "event time of the kernel; peak = a warp-wide float4 red probe, one line "
+                                     "per lane"}
     res = {
         "metric": METRIC, "value": r1["value"], "unit": "samples/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": r1["ms_per_step"], "higher_is_better": True, "scaling": "weak",
