@@ -1,10 +1,15 @@
 // MLPRender_Fea colour head (models/FactorFields.py:162-203) on the fifth-generation tensor
-// cores: tcgen05.mma with BF16 operands in shared memory and FP32 accumulators in tensor memory.
+// cores: tcgen05.mma with 16-bit operands in shared memory and FP32 accumulators in tensor memory.
+// Two kernels, each one persistent CTA per SM walking tiles of 128 listed head samples (sample r
+// of a tile = TMEM lane r):
 //
-// One persistent CTA per SM walks tiles of 128 listed head samples (sample r of a tile = TMEM
-// lane r). 512 threads: warp w serves TMEM lane quadrant w % 4 (rows 32 (w % 4) .. + 31) and the
-// 32-column slice w / 4 of every 128-wide accumulator, so each epilogue is one tcgen05.ld x32 per
-// thread. Per tile, for 3 layers 128 hidden units wide:
+// head_fwd16_kernel (the forward): FP16 operands, one MMA pass per layer, two tiles in flight
+// (two 8-warp groups with their own buffers, TMEM columns and barriers); described above it.
+//
+// head_tc_kernel (the backward, with the forward recomputed): 512 threads, warp w serves TMEM
+// lane quadrant w % 4 (rows 32 (w % 4) .. + 31) and the 32-column slice w / 4 of every 128-wide
+// accumulator, so each epilogue is one tcgen05.ld x32 per thread. Per tile, for 3 layers 128
+// hidden units wide:
 //
 //   stage  the tile's feature rows (channels 0..C) and ray directions into shared memory,
 //          warp per row (coalesced), through app_idx / app_ray; the loads of the next tile are
@@ -17,7 +22,7 @@
 //   F2  S = H0_hi W1^T + H0_lo W1^T (N 128, K 128)
 //       H1 = relu(S + b1), y = H1 W2^T (row partials of the 4 column slices summed through
 //       shared memory), rgb = sigmoid(y)
-// and for the backward (the forward recomputed, nothing stored between launches):
+// and then the backward (nothing is stored between the launches):
 //       dy = dL/drgb rgb (1 - rgb), dH1 = (dy W2) [H1 > 0] -> shared memory (BF16)
 //   B1  S  = dH1 W1                 (B = W1 read MN-major)
 //   B2  dW1 += dH1^T H0_hi          (A = dH1, B = H0, both read MN-major; TMEM-resident over tiles)
@@ -164,24 +169,29 @@ __device__ __forceinline__ float x_col(const float* fr, const float* dr) {
   }
 }
 
-// Columns 8 CH .. 8 CH + 7 of row rr as a BF16 pair (one 16-byte store into each of X_hi, X_lo).
-template <int C, int F, int V, int CH, int... J>
+// Columns 8 CH .. 8 CH + 7 of row rr: as a BF16 pair (one 16-byte store into each of X_hi and
+// X_lo), or with kF16 as FP16 values (one 16-byte store into X; Xlo unused).
+template <int C, int F, int V, bool kF16, int CH, int... J>
 __device__ __forceinline__ void build_chunk(uint32_t X, uint32_t Xlo, int rr, const float* fr, const float* dr,
                                             std::integer_sequence<int, J...>) {
   const float v[8] = {x_col<C, F, V, CH * 8 + J>(fr, dr)...};
-  store8_split(X, Xlo, Shape<C, F, V>::IN_PAD, rr, CH * 8, v);
+  if constexpr (kF16)
+    st_shared_v4(X + tc::core_off(rr, CH * 8, Shape<C, F, V>::IN_PAD), tc::pack2_f16(v[0], v[1]),
+                 tc::pack2_f16(v[2], v[3]), tc::pack2_f16(v[4], v[5]), tc::pack2_f16(v[6], v[7]));
+  else
+    store8_split(X, Xlo, Shape<C, F, V>::IN_PAD, rr, CH * 8, v);
 }
 
 // Chunk `ch` (warp-uniform) dispatched to its compile-time builder.
-template <int C, int F, int V, int CH = 0>
+template <int C, int F, int V, bool kF16, int CH = 0>
 __device__ __forceinline__ void build_chunk_at(int ch, uint32_t X, uint32_t Xlo, int rr, const float* fr,
                                                const float* dr) {
   if constexpr (CH < Shape<C, F, V>::IN_PAD / 8) {
     if (ch == CH) {
-      build_chunk<C, F, V, CH>(X, Xlo, rr, fr, dr, std::make_integer_sequence<int, 8>{});
+      build_chunk<C, F, V, kF16, CH>(X, Xlo, rr, fr, dr, std::make_integer_sequence<int, 8>{});
       return;
     }
-    build_chunk_at<C, F, V, CH + 1>(ch, X, Xlo, rr, fr, dr);
+    build_chunk_at<C, F, V, kF16, CH + 1>(ch, X, Xlo, rr, fr, dr);
   }
 }
 
@@ -232,7 +242,7 @@ __device__ __forceinline__ float warp_reduce_scatter32(float* v, int lane) {
   return v[0];
 }
 
-template <int C, int F, int V, bool BWD>
+template <int C, int F, int V>
 __global__ void __launch_bounds__(kThreads, 1) head_tc_kernel(const HeadArgs a) {
   using S = Shape<C, F, V>;
   extern __shared__ __align__(1024) unsigned char smem[];
@@ -260,7 +270,7 @@ __global__ void __launch_bounds__(kThreads, 1) head_tc_kernel(const HeadArgs a) 
   uint64_t* mbar = reinterpret_cast<uint64_t*>(p);
   uint32_t* taddr_s = reinterpret_cast<uint32_t*>(p + 8);
   const uint32_t mb = tc::smem_u32(mbar);
-  constexpr uint32_t kTmemCols = BWD ? 512u : 128u;
+  constexpr uint32_t kTmemCols = 512u;
 
   // ---- weights -> shared memory (BF16 core layout; W2 rounded to BF16 like W0, W1; biases float32) ----
   for (int e = t; e < kH * S::IN_PAD; e += kThreads) {
@@ -345,7 +355,7 @@ __global__ void __launch_bounds__(kThreads, 1) head_tc_kernel(const HeadArgs a) 
 #pragma unroll 1
       for (int it = warp; it < 4 * kChunks; it += kThreads / 32) {
         const int rr = (it & 3) * 32 + lane;
-        build_chunk_at<C, F, V>(it >> 2, sX, sXlo, rr, fs + rr * S::FS, ds + rr * 4);
+        build_chunk_at<C, F, V, false>(it >> 2, sX, sXlo, rr, fs + rr * S::FS, ds + rr * 4);
       }
     }
     tc::fence_smem_to_async();
@@ -357,10 +367,10 @@ __global__ void __launch_bounds__(kThreads, 1) head_tc_kernel(const HeadArgs a) 
       const uint32_t id = tc::idesc_bf16(128, kH, false, false);
 #pragma unroll 1
       for (int s = 0; s < S::IN_PAD / 16; ++s)
-        tc::mma_bf16(tS, desc_k(sX, S::IN_PAD, s), desc_k(sW0, S::IN_PAD, s), id, s > 0);
+        tc::mma_f16kind(tS, desc_k(sX, S::IN_PAD, s), desc_k(sW0, S::IN_PAD, s), id, s > 0);
 #pragma unroll 1
       for (int s = 0; s < S::IN_PAD / 16; ++s)
-        tc::mma_bf16(tS, desc_k(sXlo, S::IN_PAD, s), desc_k(sW0, S::IN_PAD, s), id, 1u);
+        tc::mma_f16kind(tS, desc_k(sXlo, S::IN_PAD, s), desc_k(sW0, S::IN_PAD, s), id, 1u);
       tc::mma_commit(mb);
     }
     if (!wait_mma()) break;
@@ -393,9 +403,9 @@ __global__ void __launch_bounds__(kThreads, 1) head_tc_kernel(const HeadArgs a) 
       tc::fence_after_sync();
       const uint32_t id = tc::idesc_bf16(128, kH, false, false);
 #pragma unroll 1
-      for (int s = 0; s < kH / 16; ++s) tc::mma_bf16(tS, desc_k(sH0, kH, s), desc_k(sW1, kH, s), id, s > 0);
+      for (int s = 0; s < kH / 16; ++s) tc::mma_f16kind(tS, desc_k(sH0, kH, s), desc_k(sW1, kH, s), id, s > 0);
 #pragma unroll 1
-      for (int s = 0; s < kH / 16; ++s) tc::mma_bf16(tS, desc_k(sH0lo, kH, s), desc_k(sW1, kH, s), id, 1u);
+      for (int s = 0; s < kH / 16; ++s) tc::mma_f16kind(tS, desc_k(sH0lo, kH, s), desc_k(sW1, kH, s), id, 1u);
       tc::mma_commit(mb);
     }
     if (!wait_mma()) break;
@@ -437,16 +447,7 @@ __global__ void __launch_bounds__(kThreads, 1) head_tc_kernel(const HeadArgs a) 
       rgb[2] = 1.f / (1.f + expf(-ys.z));
     }
     const int32_t sidx = idx_s[r];
-    if constexpr (!BWD) {
-      if (part == 0 && sidx >= 0) {
-#pragma unroll
-        for (int o = 0; o < 3; ++o) a.rgb_out[(int64_t)sidx * 3 + o] = rgb[o];
-      }
-      tc::fence_before_sync();
-      __syncthreads();  // S and the staged rows are read before the next tile overwrites them
-      any_tile = true;
-      continue;
-    } else {
+    {
       float dy[3];
 #pragma unroll
       for (int o = 0; o < 3; ++o) dy[o] = sidx >= 0 ? a.grad_rgb[(int64_t)sidx * 3 + o] * rgb[o] * (1.f - rgb[o]) : 0.f;
@@ -485,11 +486,11 @@ __global__ void __launch_bounds__(kThreads, 1) head_tc_kernel(const HeadArgs a) 
         tc::fence_after_sync();
         const uint32_t id1 = tc::idesc_bf16(128, kH, false, true);
 #pragma unroll 1
-        for (int s = 0; s < kH / 16; ++s) tc::mma_bf16(tS, desc_k(sDH1, kH, s), desc_mn(sW1, kH, s), id1, s > 0);
+        for (int s = 0; s < kH / 16; ++s) tc::mma_f16kind(tS, desc_k(sDH1, kH, s), desc_mn(sW1, kH, s), id1, s > 0);
         const uint32_t id2 = tc::idesc_bf16(128, kH, true, true);
 #pragma unroll 1
         for (int s = 0; s < kTile / 16; ++s)
-          tc::mma_bf16(tDW1, desc_mn(sDH1, kH, s), desc_mn(sH0, kH, s), id2, (any_tile || s > 0) ? 1u : 0u);
+          tc::mma_f16kind(tDW1, desc_mn(sDH1, kH, s), desc_mn(sH0, kH, s), id2, (any_tile || s > 0) ? 1u : 0u);
         tc::mma_commit(mb);
       }
       if (!wait_mma()) break;
@@ -512,10 +513,10 @@ __global__ void __launch_bounds__(kThreads, 1) head_tc_kernel(const HeadArgs a) 
         const uint32_t id3 = tc::idesc_bf16(128, S::IN_PAD, true, true);
 #pragma unroll 1
         for (int s = 0; s < kTile / 16; ++s)
-          tc::mma_bf16(tDW0, desc_mn(sH0, kH, s), desc_mn(sX, S::IN_PAD, s), id3, (any_tile || s > 0) ? 1u : 0u);
+          tc::mma_f16kind(tDW0, desc_mn(sH0, kH, s), desc_mn(sX, S::IN_PAD, s), id3, (any_tile || s > 0) ? 1u : 0u);
         const uint32_t id4 = tc::idesc_bf16(128, S::NX, false, true);
 #pragma unroll 1
-        for (int s = 0; s < kH / 16; ++s) tc::mma_bf16(tS, desc_k(sH0, kH, s), desc_mn(sW0, S::IN_PAD, s), id4, s > 0);
+        for (int s = 0; s < kH / 16; ++s) tc::mma_f16kind(tS, desc_k(sH0, kH, s), desc_mn(sW0, S::IN_PAD, s), id4, s > 0);
         tc::mma_commit(mb);
       }
       if (!wait_mma()) break;
@@ -548,7 +549,7 @@ __global__ void __launch_bounds__(kThreads, 1) head_tc_kernel(const HeadArgs a) 
   if (!ok) {
     if (t == 0 && a.status) atomicExch(a.status, FF_ERR_LIMIT);
     (void)tc::mbar_wait(mb, phase & 1u, kPolls);  // the MMAs in flight, if they ever finish
-  } else if (BWD && any_tile) {
+  } else if (any_tile) {
     // ---- flush: dW1 / dW0 rows from TMEM (row = this thread's lane), the register sums ----
     {
       float v[32];
@@ -578,11 +579,272 @@ __global__ void __launch_bounds__(kThreads, 1) head_tc_kernel(const HeadArgs a) 
   if (warp == 0) tc::tmem_dealloc(tmem, kTmemCols);
 }
 
-template <int C, int F, int V, bool BWD>
+// ---- forward: FP16 operands, two tiles in flight ----
+//
+// The forward alone has no gradient operands, so X and H0 are single FP16 values (11
+// significant bits; W0 and W1 hold BF16 values, which FP16 represents exactly in its normal
+// range): one MMA pass per layer and one operand buffer per tile. That leaves room for two tiles:
+// the 16 warps form two groups of 8, group g takes the CTA's tiles g, g + 2, ... (its own X / H0
+// buffer, staged rows, TMEM columns [128 g, 128 g + 128), mbarrier and named barrier), and one
+// group's MMAs run while the other builds X or reads its accumulators. Warp w of a group serves
+// TMEM lane quadrant w % 4 and the 64-column half w / 4 of each accumulator.
+template <int C, int F, int V>
+struct Fwd16 {
+  using S = Shape<C, F, V>;
+  static constexpr int RS = (C + 4) | 1;  // staged row: channels 0..C, then the direction (odd stride)
+  static constexpr int W0_B = S::W0_B, W1_B = S::W1_B;
+  static constexpr int X_B = kTile * S::IN_PAD * 2;  // X, then H0 [128 x 128], then the y partials
+  static constexpr int ROW_B = kTile * RS * 4;
+  static constexpr int IDX_B = kTile * 4;
+  static constexpr int SLOT_B = X_B + ROW_B + IDX_B;
+  static constexpr int F32_B = 5 * kH * 4;
+  static_assert(kH * kH * 2 <= X_B && 2 * kTile * 16 <= X_B, "H0 and the y partials fit in X's buffer");
+  static_assert((W0_B + W1_B + SLOT_B) % 16 == 0 && X_B % 16 == 0 && ROW_B % 16 == 0, "16-byte alignment");
+  static constexpr int smem() { return W0_B + W1_B + 2 * SLOT_B + F32_B + 64; }
+};
+
+// Named barrier of one 256-thread group (ids 1, 2; id 0 is __syncthreads); returns the AND of v
+// over the group.
+__device__ __forceinline__ bool group_sync_and(int id, bool v) {
+  uint32_t r;
+  asm volatile(
+      "{\n\t.reg .pred p, q;\n\t"
+      "setp.ne.u32 p, %1, 0;\n\t"
+      "bar.red.and.pred q, %2, 256, p;\n\t"
+      "selp.u32 %0, 1, 0, q;\n\t}\n"
+      : "=r"(r)
+      : "r"((uint32_t)v), "r"(id)
+      : "memory");
+  return r != 0;
+}
+__device__ __forceinline__ void group_sync(int id) { asm volatile("bar.sync %0, 256;" ::"r"(id) : "memory"); }
+
+constexpr float kF16Max = 65504.f;
+
+template <int C, int F, int V>
+__global__ void __launch_bounds__(kThreads, 1) head_fwd16_kernel(const HeadArgs a) {
+  using S = Shape<C, F, V>;
+  using L = Fwd16<C, F, V>;
+  extern __shared__ __align__(1024) unsigned char smem[];
+  const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+  const int grp = warp >> 3, wg = warp & 7;        // group, warp within the group
+  const int quad = warp & 3, half = wg >> 2;       // TMEM lane quadrant, 64-column half
+  const int r = quad * 32 + lane;                  // this thread's row in the epilogues
+  const int bar_id = 1 + grp;
+  unsigned char* p = smem;
+  const uint32_t sW0 = tc::smem_u32(p); p += L::W0_B;
+  const uint32_t sW1 = tc::smem_u32(p); p += L::W1_B;
+  unsigned char* slot = p + grp * L::SLOT_B;
+  p += 2 * L::SLOT_B;
+  const uint32_t sX = tc::smem_u32(slot);          // X, then H0, then the y partials
+  float4* yp = reinterpret_cast<float4*>(slot);    // [2 halves][128 rows]
+  float* rows = reinterpret_cast<float*>(slot + L::X_B);
+  int32_t* idx_s = reinterpret_cast<int32_t*>(slot + L::X_B + L::ROW_B);
+  float* w2s = reinterpret_cast<float*>(p); p += 3 * kH * 4;
+  float* b0s = reinterpret_cast<float*>(p); p += kH * 4;
+  float* b1s = reinterpret_cast<float*>(p); p += kH * 4;
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(p);  // one per group
+  uint32_t* taddr_s = reinterpret_cast<uint32_t*>(p + 16);
+  const uint32_t mb = tc::smem_u32(mbar + grp);
+
+  // ---- weights -> shared memory: BF16-rounded (the stored head), held as FP16 ----
+  bool range_ok = true;
+  for (int e = t; e < kH * S::IN_PAD; e += kThreads) {
+    const int rr = e / S::IN_PAD, c = e % S::IN_PAD;
+    const float v = __bfloat162float(__float2bfloat16_rn(c < S::IN ? a.w[0][rr * S::IN + c] : 0.f));
+    range_ok &= !(fabsf(v) > kF16Max);  // NaN passes (propagates as in float32)
+    *reinterpret_cast<__half*>(smem + tc::core_off(rr, c, S::IN_PAD)) = __float2half_rn(v);
+  }
+  for (int e = t; e < kH * kH; e += kThreads) {
+    const int rr = e / kH, c = e % kH;
+    const float v = __bfloat162float(__float2bfloat16_rn(a.w[1][e]));
+    range_ok &= !(fabsf(v) > kF16Max);  // NaN passes (propagates as in float32)
+    *reinterpret_cast<__half*>(smem + L::W0_B + tc::core_off(rr, c, kH)) = __float2half_rn(v);
+  }
+  for (int e = t; e < 3 * kH; e += kThreads) w2s[e] = __bfloat162float(__float2bfloat16_rn(a.w[2][e]));
+  if (t < kH) {
+    b0s[t] = a.b[0] ? a.b[0][t] : 0.f;
+    b1s[t] = a.b[1] ? a.b[1][t] : 0.f;
+  }
+  tc::fence_smem_to_async();
+  if (t == 0) {
+    tc::mbar_init(tc::smem_u32(mbar), 1);
+    tc::mbar_init(tc::smem_u32(mbar + 1), 1);
+    tc::fence_mbar_init();
+  }
+  __syncthreads();
+  if (warp == 0) tc::tmem_alloc(tc::smem_u32(taddr_s), 256u);
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = *taddr_s;
+  const uint32_t tS = tmem + (uint32_t)(grp * 128) + ((uint32_t)(quad * 32) << 16);  // + column
+  const uint32_t tS_mma = tmem + (uint32_t)(grp * 128);
+  const bool issuer = wg == 0 && lane == 0;
+
+  uint32_t phase = 0;
+  bool ok = true;
+  auto wait_mma = [&]() {
+    const bool done = tc::mbar_wait(mb, phase & 1u, kPolls);
+    ++phase;
+    ok = group_sync_and(bar_id, done);
+    tc::fence_after_sync();
+    return ok;
+  };
+
+  const int64_t n_tiles = ceil_div(a.n, kTile);
+  constexpr int kRowsPerWarp = kTile / 8;
+  for (int64_t k = grp;; k += 2) {
+    const int64_t tile = (int64_t)blockIdx.x + k * (int64_t)gridDim.x;
+    if (tile >= n_tiles) break;
+    // ---- the tile's rows (channels 0..C and the direction) and row indices -> shared memory ----
+    {
+      int32_t pix[kRowsPerWarp], pray[kRowsPerWarp];
+#pragma unroll
+      for (int i = 0; i < kRowsPerWarp; ++i) {
+        const int64_t row = tile * kTile + wg * kRowsPerWarp + i;
+        const bool valid = row < a.n;
+        pix[i] = valid ? a.app_idx[row] : -1;
+        pray[i] = valid ? a.app_ray[row] : -1;
+      }
+#pragma unroll
+      for (int i = 0; i < kRowsPerWarp; ++i) {
+        const int rr = wg * kRowsPerWarp + i;
+        const float fv = (pix[i] >= 0 && lane <= C) ? a.feat[(int64_t)pix[i] * a.feat_stride + lane] : 0.f;
+        const float dv = (pray[i] >= 0 && lane < 3) ? a.rays[(int64_t)pray[i] * 6 + 3 + lane] : 0.f;
+        range_ok &= !(fabsf(fv) > kF16Max);
+        if (lane <= C) rows[rr * L::RS + lane] = fv;
+        if (lane < 3) rows[rr * L::RS + C + 1 + lane] = dv;
+        if (lane == 0) idx_s[rr] = pix[i];
+      }
+    }
+    group_sync(bar_id);
+    // ---- X (FP16): thread = (row, 8-column chunk), one 16-byte store ----
+    {
+      constexpr int kChunks = S::IN_PAD / 8;
+#pragma unroll 1
+      for (int it = wg; it < 4 * kChunks; it += 8) {
+        const int rr = (it & 3) * 32 + lane;
+        const float* fr = rows + rr * L::RS;
+        build_chunk_at<C, F, V, true>(it >> 2, sX, 0u, rr, fr, fr + C + 1);
+      }
+    }
+    tc::fence_smem_to_async();
+    tc::fence_before_sync();
+    group_sync(bar_id);
+    // ---- F1: S = X W0^T ----
+    if (issuer) {
+      tc::fence_after_sync();
+      const uint32_t id = tc::idesc_f16kind(128, kH, false, false, false);
+#pragma unroll 1
+      for (int s = 0; s < S::IN_PAD / 16; ++s)
+        tc::mma_f16kind(tS_mma, desc_k(sX, S::IN_PAD, s), desc_k(sW0, S::IN_PAD, s), id, s > 0);
+      tc::mma_commit(mb);
+    }
+    if (!wait_mma()) break;
+    // ---- H0 = relu(S + b0) -> X's buffer as FP16 [128 x 128] (X is consumed) ----
+#pragma unroll 1
+    for (int hh = 0; hh < 2; ++hh) {
+      const int c0 = half * 64 + hh * 32;
+      float v[32];
+      tc::tmem_ld32(tS + c0, v);
+      const float4* bv = reinterpret_cast<const float4*>(b0s + c0);
+#pragma unroll
+      for (int j4 = 0; j4 < 8; ++j4) {
+        const float4 b = bv[j4];
+        v[4 * j4] = fmaxf(v[4 * j4] + b.x, 0.f);
+        v[4 * j4 + 1] = fmaxf(v[4 * j4 + 1] + b.y, 0.f);
+        v[4 * j4 + 2] = fmaxf(v[4 * j4 + 2] + b.z, 0.f);
+        v[4 * j4 + 3] = fmaxf(v[4 * j4 + 3] + b.w, 0.f);
+      }
+#pragma unroll
+      for (int g = 0; g < 4; ++g) {
+        const float* q = v + 8 * g;
+        st_shared_v4(sX + tc::core_off(r, c0 + 8 * g, kH), tc::pack2_f16(q[0], q[1]), tc::pack2_f16(q[2], q[3]),
+                     tc::pack2_f16(q[4], q[5]), tc::pack2_f16(q[6], q[7]));
+      }
+    }
+    tc::fence_smem_to_async();
+    tc::fence_before_sync();
+    group_sync(bar_id);
+    // ---- F2: S = H0 W1^T ----
+    if (issuer) {
+      tc::fence_after_sync();
+      const uint32_t id = tc::idesc_f16kind(128, kH, false, false, false);
+#pragma unroll 1
+      for (int s = 0; s < kH / 16; ++s) tc::mma_f16kind(tS_mma, desc_k(sX, kH, s), desc_k(sW1, kH, s), id, s > 0);
+      tc::mma_commit(mb);
+    }
+    if (!wait_mma()) break;
+    // ---- y = relu(S + b1) W2^T over this thread's 64 columns; the two halves meet in shared memory ----
+    {
+      float y0 = 0.f, y1 = 0.f, y2 = 0.f;
+#pragma unroll 1
+      for (int hh = 0; hh < 2; ++hh) {
+        const int c0 = half * 64 + hh * 32;
+        float h1[32];
+        tc::tmem_ld32(tS + c0, h1);
+        const float4* b1v = reinterpret_cast<const float4*>(b1s + c0);
+        const float4* w2v = reinterpret_cast<const float4*>(w2s + c0);  // rows kH / 4 float4 apart
+#pragma unroll
+        for (int j4 = 0; j4 < 8; ++j4) {
+          const float4 b = b1v[j4], wa = w2v[j4], wb = w2v[kH / 4 + j4], wc = w2v[kH / 2 + j4];
+          const float bb[4] = {b.x, b.y, b.z, b.w}, u0[4] = {wa.x, wa.y, wa.z, wa.w};
+          const float u1[4] = {wb.x, wb.y, wb.z, wb.w}, u2[4] = {wc.x, wc.y, wc.z, wc.w};
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            const float h = fmaxf(h1[4 * j4 + q] + bb[q], 0.f);
+            y0 += h * u0[q];
+            y1 += h * u1[q];
+            y2 += h * u2[q];
+          }
+        }
+      }
+      yp[half * kTile + r] = make_float4(y0, y1, y2, 0.f);  // H0 is consumed (F2 complete)
+    }
+    group_sync(bar_id);
+    if (half == 0) {
+      const int32_t sidx = idx_s[r];
+      if (sidx >= 0) {
+        const float4 u = yp[r], w = yp[kTile + r];
+        a.rgb_out[(int64_t)sidx * 3] = 1.f / (1.f + expf(-(u.x + w.x)));
+        a.rgb_out[(int64_t)sidx * 3 + 1] = 1.f / (1.f + expf(-(u.y + w.y)));
+        a.rgb_out[(int64_t)sidx * 3 + 2] = 1.f / (1.f + expf(-(u.z + w.z)));
+      }
+    }
+    tc::fence_before_sync();
+    group_sync(bar_id);  // S, the staged rows and the partials are read before the next tile reuses them
+  }
+
+  if (!ok) {
+    if (issuer && a.status) atomicExch(a.status, FF_ERR_LIMIT);
+    (void)tc::mbar_wait(mb, phase & 1u, kPolls);  // this group's MMAs in flight, if they ever finish
+  }
+  if (!range_ok && a.status) atomicCAS(a.status, 0, FF_ERR_SIZE);
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tmem, 256u);
+}
+
+template <int C, int F, int V>
+cudaError_t launch_fwd16(const HeadArgs& a, cudaStream_t s) {
+  constexpr int smem = Fwd16<C, F, V>::smem();
+  static_assert(smem <= 227 * 1024, "shared memory per CTA");
+  auto kern = head_fwd16_kernel<C, F, V>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return e;
+  const int64_t tiles = ceil_div(a.n, kTile);
+  // each CTA runs two tiles at a time: at most one CTA per two tiles
+  const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(tiles, 2), (int64_t)sm_count()));
+  kern<<<blocks, kThreads, smem, s>>>(a);
+  return cudaGetLastError();
+}
+
+template <int C, int F, int V>
 cudaError_t launch_tc(const HeadArgs& a, cudaStream_t s) {
   constexpr int smem = Shape<C, F, V>::smem();
   static_assert(smem <= 227 * 1024, "shared memory per CTA");
-  auto kern = head_tc_kernel<C, F, V, BWD>;
+  auto kern = head_tc_kernel<C, F, V>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;
   const int64_t tiles = ceil_div(a.n, kTile);
@@ -591,11 +853,18 @@ cudaError_t launch_tc(const HeadArgs& a, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-template <bool BWD>
-cudaError_t dispatch_tc(const FFRenderMlp& h, const HeadArgs& a, cudaStream_t s) {
+cudaError_t dispatch_fwd16(const FFRenderMlp& h, const HeadArgs& a, cudaStream_t s) {
   if (h.fea_pe == 2 && h.view_pe == 6) {
-    if (h.in_channels == 27) return launch_tc<27, 2, 6, BWD>(a, s);
-    if (h.in_channels == 31) return launch_tc<31, 2, 6, BWD>(a, s);
+    if (h.in_channels == 27) return launch_fwd16<27, 2, 6>(a, s);
+    if (h.in_channels == 31) return launch_fwd16<31, 2, 6>(a, s);
+  }
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t dispatch_tc_bwd(const FFRenderMlp& h, const HeadArgs& a, cudaStream_t s) {
+  if (h.fea_pe == 2 && h.view_pe == 6) {
+    if (h.in_channels == 27) return launch_tc<27, 2, 6>(a, s);
+    if (h.in_channels == 31) return launch_tc<31, 2, 6>(a, s);
   }
   return cudaErrorInvalidValue;
 }
@@ -632,7 +901,7 @@ cudaError_t launch_render_head_tc_forward(const FFRenderMlp& h, const float* fea
   if (n == 0) return cudaSuccess;
   HeadArgs a = head_args(h, feat, feat_stride, rays, app_idx, app_ray, n, status);
   a.rgb_out = rgb_rows;
-  return dispatch_tc<false>(h, a, s);
+  return dispatch_fwd16(h, a, s);
 }
 
 cudaError_t launch_render_head_tc_backward(const FFRenderMlp& h, const float* feat, int feat_stride, const float* rays,
@@ -646,7 +915,7 @@ cudaError_t launch_render_head_tc_backward(const FFRenderMlp& h, const float* fe
   for (int l = 0; l < 3; ++l) a.gw[l] = g.weight[l];
   a.gb[0] = g.bias[0];
   a.gb[1] = g.bias[1];
-  return dispatch_tc<true>(h, a, s);
+  return dispatch_tc_bwd(h, a, s);
 }
 
 }  // namespace ffgb

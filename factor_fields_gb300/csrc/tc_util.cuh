@@ -13,6 +13,7 @@
 #pragma once
 
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <stdint.h>
 
 namespace ffgb {
@@ -38,20 +39,25 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint
   return d;  // base offset 0, LBO mode 0, swizzle none (bits 61-63 = 0)
 }
 
-// Instruction descriptor of tcgen05.mma.kind::f16: BF16 A and B, FP32 D, M x N, a_mn / b_mn:
-// the operand is MN-major (transposed) instead of K-major.
-__host__ __device__ __forceinline__ uint32_t idesc_bf16(int M, int N, bool a_mn, bool b_mn) {
+// Instruction descriptor of tcgen05.mma.kind::f16: A and B both BF16 (bf16 = true) or both FP16,
+// FP32 D, M x N, a_mn / b_mn: the operand is MN-major (transposed) instead of K-major.
+__host__ __device__ __forceinline__ uint32_t idesc_f16kind(int M, int N, bool a_mn, bool b_mn, bool bf16) {
+  const uint32_t ab = bf16 ? 1u : 0u;       // operand format: 0 = F16, 1 = BF16
   return (1u << 4)                          // D format: F32
-         | (1u << 7)                        // A format: BF16
-         | (1u << 10)                       // B format: BF16
+         | (ab << 7)                        // A format
+         | (ab << 10)                       // B format
          | ((a_mn ? 1u : 0u) << 15)         // A major
          | ((b_mn ? 1u : 0u) << 16)         // B major
          | ((uint32_t)(N >> 3) << 17)       // N / 8
          | ((uint32_t)(M >> 4) << 24);      // M / 16
 }
+__host__ __device__ __forceinline__ uint32_t idesc_bf16(int M, int N, bool a_mn, bool b_mn) {
+  return idesc_f16kind(M, N, a_mn, b_mn, true);
+}
 
-// D[tmem] (+)= A[smem] * B[smem]^T, one instruction, issued by one thread.
-__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc,
+// D[tmem] (+)= A[smem] * B[smem]^T, one instruction, issued by one thread (kind::f16: BF16 or FP16
+// operands as the instruction descriptor says).
+__device__ __forceinline__ void mma_f16kind(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc,
                                          uint32_t accumulate) {
   asm volatile(
       "{\n\t.reg .pred p;\n\t"
@@ -129,6 +135,12 @@ __device__ __forceinline__ bool mbar_wait(uint32_t mbar_saddr, uint32_t parity, 
     if (done) return true;
   }
   return false;
+}
+
+// Two floats -> packed FP16 pair (round to nearest even), low half = a.
+__device__ __forceinline__ uint32_t pack2_f16(float a, float b) {
+  const __half2 v = __floats2half2_rn(a, b);
+  return *reinterpret_cast<const uint32_t*>(&v);
 }
 
 // Two floats -> packed BF16 pair (round to nearest even), low half = a.
