@@ -144,19 +144,19 @@ __device__ __forceinline__ void store8_split(uint32_t hi_buf, uint32_t lo_buf, i
 }
 
 // Column K of the head's input row (the reference's order, models/FactorFields.py:188-195),
-// decoded at compile time: fr = the staged feature row (fr[1 + c] = feature c), dr = the ray
+// decoded at compile time: fr = the staged feature row (fr[kOff + c] = feature c), dr = the ray
 // direction; 0 past in_dim. Positional-encoding columns use the hardware sin / cos.
-template <int C, int F, int V, int K>
+template <int C, int F, int V, int K, int kOff>
 __device__ __forceinline__ float x_col(const float* fr, const float* dr) {
   if constexpr (K < C) {
-    return fr[1 + K];
+    return fr[kOff + K];
   } else if constexpr (K < C + 3) {
     return dr[K - C];
   } else if constexpr (K < C + 3 + 2 * C * F) {
     constexpr int k = K - C - 3;
     constexpr bool kCos = k >= C * F;
     constexpr int j = kCos ? k - C * F : k;
-    const float x = fr[1 + j / F] * (float)(1 << (j % F));
+    const float x = fr[kOff + j / F] * (float)(1 << (j % F));
     return kCos ? __cosf(x) : __sinf(x);
   } else if constexpr (K < C + 3 + 2 * C * F + 6 * V) {
     constexpr int k = K - C - 3 - 2 * C * F;
@@ -171,10 +171,10 @@ __device__ __forceinline__ float x_col(const float* fr, const float* dr) {
 
 // Columns 8 CH .. 8 CH + 7 of row rr: as a BF16 pair (one 16-byte store into each of X_hi and
 // X_lo), or with kF16 as FP16 values (one 16-byte store into X; Xlo unused).
-template <int C, int F, int V, bool kF16, int CH, int... J>
+template <int C, int F, int V, bool kF16, int kOff, int CH, int... J>
 __device__ __forceinline__ void build_chunk(uint32_t X, uint32_t Xlo, int rr, const float* fr, const float* dr,
                                             std::integer_sequence<int, J...>) {
-  const float v[8] = {x_col<C, F, V, CH * 8 + J>(fr, dr)...};
+  const float v[8] = {x_col<C, F, V, CH * 8 + J, kOff>(fr, dr)...};
   if constexpr (kF16)
     st_shared_v4(X + tc::core_off(rr, CH * 8, Shape<C, F, V>::IN_PAD), tc::pack2_f16(v[0], v[1]),
                  tc::pack2_f16(v[2], v[3]), tc::pack2_f16(v[4], v[5]), tc::pack2_f16(v[6], v[7]));
@@ -183,15 +183,15 @@ __device__ __forceinline__ void build_chunk(uint32_t X, uint32_t Xlo, int rr, co
 }
 
 // Chunk `ch` (warp-uniform) dispatched to its compile-time builder.
-template <int C, int F, int V, bool kF16, int CH = 0>
+template <int C, int F, int V, bool kF16, int kOff, int CH = 0>
 __device__ __forceinline__ void build_chunk_at(int ch, uint32_t X, uint32_t Xlo, int rr, const float* fr,
                                                const float* dr) {
   if constexpr (CH < Shape<C, F, V>::IN_PAD / 8) {
     if (ch == CH) {
-      build_chunk<C, F, V, kF16, CH>(X, Xlo, rr, fr, dr, std::make_integer_sequence<int, 8>{});
+      build_chunk<C, F, V, kF16, kOff, CH>(X, Xlo, rr, fr, dr, std::make_integer_sequence<int, 8>{});
       return;
     }
-    build_chunk_at<C, F, V, kF16, CH + 1>(ch, X, Xlo, rr, fr, dr);
+    build_chunk_at<C, F, V, kF16, kOff, CH + 1>(ch, X, Xlo, rr, fr, dr);
   }
 }
 
@@ -355,7 +355,7 @@ __global__ void __launch_bounds__(kThreads, 1) head_tc_kernel(const HeadArgs a) 
 #pragma unroll 1
       for (int it = warp; it < 4 * kChunks; it += kThreads / 32) {
         const int rr = (it & 3) * 32 + lane;
-        build_chunk_at<C, F, V, false>(it >> 2, sX, sXlo, rr, fs + rr * S::FS, ds + rr * 4);
+        build_chunk_at<C, F, V, false, 1>(it >> 2, sX, sXlo, rr, fs + rr * S::FS, ds + rr * 4);
       }
     }
     tc::fence_smem_to_async();
@@ -579,45 +579,34 @@ __global__ void __launch_bounds__(kThreads, 1) head_tc_kernel(const HeadArgs a) 
   if (warp == 0) tc::tmem_dealloc(tmem, kTmemCols);
 }
 
-// ---- forward: FP16 operands, two tiles in flight ----
+// ---- forward: FP16 operands, software-pipelined over tiles ----
 //
 // The forward alone has no gradient operands, so X and H0 are single FP16 values (11
 // significant bits; W0 and W1 hold BF16 values, which FP16 represents exactly in its normal
-// range): one MMA pass per layer and one operand buffer per tile. That leaves room for two tiles:
-// the 16 warps form two groups of 8, group g takes the CTA's tiles g, g + 2, ... (its own X / H0
-// buffer, staged rows, TMEM columns [128 g, 128 g + 128), mbarrier and named barrier), and one
-// group's MMAs run while the other builds X or reads its accumulators. Warp w of a group serves
-// TMEM lane quadrant w % 4 and the 64-column half w / 4 of each accumulator.
+// range): one MMA pass per layer and half the operand bytes. The freed shared memory holds two
+// tiles' operand buffers, staged rows and TMEM accumulators, and the tiles are pipelined so that
+// the tensor core works while the CUDA cores do:
+//
+//   iteration i (buffer b = i & 1; F1 of tile i was issued at the end of iteration i - 2):
+//     wait F1(i); H0(i) = relu(S_b + b0) -> X_b (FP16);  issue F2(i) -> S_b
+//     stage the rows of tile i + 2 -> R_b                         (overlaps F2(i))
+//     wait F2(i); y partials -> X_b; rgb = sigmoid(y) out
+//     build X(i + 2) from R_b -> X_b;  issue F1(i + 2) -> S_b      (runs during iteration i + 1)
+//
+// 512 threads; warp w serves TMEM lane quadrant w % 4 and the 32-column slice w / 4, as in the
+// backward kernel. A staged row holds features 1..C, the direction and the row index.
 template <int C, int F, int V>
 struct Fwd16 {
   using S = Shape<C, F, V>;
-  static constexpr int RS = (C + 4) | 1;  // staged row: channels 0..C, then the direction (odd stride)
+  static constexpr int RS = (C + 4) | 1;  // features at [0, C), direction at [C, C + 3), index at C + 3
   static constexpr int W0_B = S::W0_B, W1_B = S::W1_B;
   static constexpr int X_B = kTile * S::IN_PAD * 2;  // X, then H0 [128 x 128], then the y partials
   static constexpr int ROW_B = kTile * RS * 4;
-  static constexpr int IDX_B = kTile * 4;
-  static constexpr int SLOT_B = X_B + ROW_B + IDX_B;
   static constexpr int F32_B = 5 * kH * 4;
-  static_assert(kH * kH * 2 <= X_B && 2 * kTile * 16 <= X_B, "H0 and the y partials fit in X's buffer");
-  static_assert((W0_B + W1_B + SLOT_B) % 16 == 0 && X_B % 16 == 0 && ROW_B % 16 == 0, "16-byte alignment");
-  static constexpr int smem() { return W0_B + W1_B + 2 * SLOT_B + F32_B + 64; }
+  static_assert(kH * kH * 2 <= X_B && 4 * kTile * 16 <= X_B, "H0 and the y partials fit in X's buffer");
+  static_assert(X_B % 16 == 0 && ROW_B % 16 == 0 && W0_B % 16 == 0, "16-byte alignment");
+  static constexpr int smem() { return W0_B + W1_B + 2 * X_B + 2 * ROW_B + F32_B + 64; }
 };
-
-// Named barrier of one 256-thread group (ids 1, 2; id 0 is __syncthreads); returns the AND of v
-// over the group.
-__device__ __forceinline__ bool group_sync_and(int id, bool v) {
-  uint32_t r;
-  asm volatile(
-      "{\n\t.reg .pred p, q;\n\t"
-      "setp.ne.u32 p, %1, 0;\n\t"
-      "bar.red.and.pred q, %2, 256, p;\n\t"
-      "selp.u32 %0, 1, 0, q;\n\t}\n"
-      : "=r"(r)
-      : "r"((uint32_t)v), "r"(id)
-      : "memory");
-  return r != 0;
-}
-__device__ __forceinline__ void group_sync(int id) { asm volatile("bar.sync %0, 256;" ::"r"(id) : "memory"); }
 
 constexpr float kF16Max = 65504.f;
 
@@ -627,25 +616,22 @@ __global__ void __launch_bounds__(kThreads, 1) head_fwd16_kernel(const HeadArgs 
   using L = Fwd16<C, F, V>;
   extern __shared__ __align__(1024) unsigned char smem[];
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
-  const int grp = warp >> 3, wg = warp & 7;        // group, warp within the group
-  const int quad = warp & 3, half = wg >> 2;       // TMEM lane quadrant, 64-column half
-  const int r = quad * 32 + lane;                  // this thread's row in the epilogues
-  const int bar_id = 1 + grp;
+  const int quad = warp & 3, part = warp >> 2;  // TMEM lane quadrant and 32-column slice
+  const int r = quad * 32 + lane;               // this thread's row in the epilogues
   unsigned char* p = smem;
   const uint32_t sW0 = tc::smem_u32(p); p += L::W0_B;
   const uint32_t sW1 = tc::smem_u32(p); p += L::W1_B;
-  unsigned char* slot = p + grp * L::SLOT_B;
-  p += 2 * L::SLOT_B;
-  const uint32_t sX = tc::smem_u32(slot);          // X, then H0, then the y partials
-  float4* yp = reinterpret_cast<float4*>(slot);    // [2 halves][128 rows]
-  float* rows = reinterpret_cast<float*>(slot + L::X_B);
-  int32_t* idx_s = reinterpret_cast<int32_t*>(slot + L::X_B + L::ROW_B);
+  unsigned char* const xbase = p;  // X_0, X_1
+  p += 2 * L::X_B;
+  unsigned char* const rbase = p;  // R_0, R_1
+  p += 2 * L::ROW_B;
+  auto xb = [&](int b) { return xbase + b * L::X_B; };
+  auto rb = [&](int b) { return reinterpret_cast<float*>(rbase + b * L::ROW_B); };
   float* w2s = reinterpret_cast<float*>(p); p += 3 * kH * 4;
   float* b0s = reinterpret_cast<float*>(p); p += kH * 4;
   float* b1s = reinterpret_cast<float*>(p); p += kH * 4;
-  uint64_t* mbar = reinterpret_cast<uint64_t*>(p);  // one per group
-  uint32_t* taddr_s = reinterpret_cast<uint32_t*>(p + 16);
-  const uint32_t mb = tc::smem_u32(mbar + grp);
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(p);  // [0], [1]: F1 of buffer 0 / 1; [2]: F2
+  uint32_t* taddr_s = reinterpret_cast<uint32_t*>(p + 24);
 
   // ---- weights -> shared memory: BF16-rounded (the stored head), held as FP16 ----
   bool range_ok = true;
@@ -658,7 +644,7 @@ __global__ void __launch_bounds__(kThreads, 1) head_fwd16_kernel(const HeadArgs 
   for (int e = t; e < kH * kH; e += kThreads) {
     const int rr = e / kH, c = e % kH;
     const float v = __bfloat162float(__float2bfloat16_rn(a.w[1][e]));
-    range_ok &= !(fabsf(v) > kF16Max);  // NaN passes (propagates as in float32)
+    range_ok &= !(fabsf(v) > kF16Max);
     *reinterpret_cast<__half*>(smem + L::W0_B + tc::core_off(rr, c, kH)) = __float2half_rn(v);
   }
   for (int e = t; e < 3 * kH; e += kThreads) w2s[e] = __bfloat162float(__float2bfloat16_rn(a.w[2][e]));
@@ -668,8 +654,7 @@ __global__ void __launch_bounds__(kThreads, 1) head_fwd16_kernel(const HeadArgs 
   }
   tc::fence_smem_to_async();
   if (t == 0) {
-    tc::mbar_init(tc::smem_u32(mbar), 1);
-    tc::mbar_init(tc::smem_u32(mbar + 1), 1);
+    for (int i = 0; i < 3; ++i) tc::mbar_init(tc::smem_u32(mbar + i), 1);
     tc::fence_mbar_init();
   }
   __syncthreads();
@@ -678,147 +663,173 @@ __global__ void __launch_bounds__(kThreads, 1) head_fwd16_kernel(const HeadArgs 
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tmem = *taddr_s;
-  const uint32_t tS = tmem + (uint32_t)(grp * 128) + ((uint32_t)(quad * 32) << 16);  // + column
-  const uint32_t tS_mma = tmem + (uint32_t)(grp * 128);
-  const bool issuer = wg == 0 && lane == 0;
+  const uint32_t lane_off = (uint32_t)(quad * 32) << 16;
 
-  uint32_t phase = 0;
+  uint32_t ph = 0;  // bit m: the parity of mbarrier m's next phase
   bool ok = true;
-  auto wait_mma = [&]() {
-    const bool done = tc::mbar_wait(mb, phase & 1u, kPolls);
-    ++phase;
-    ok = group_sync_and(bar_id, done);
+  auto wait_mma = [&](int m) {
+    const bool done = tc::mbar_wait(tc::smem_u32(mbar + m), (ph >> m) & 1u, kPolls);
+    ph ^= 1u << m;
+    ok = __syncthreads_and(done) != 0;
     tc::fence_after_sync();
     return ok;
   };
 
   const int64_t n_tiles = ceil_div(a.n, kTile);
-  constexpr int kRowsPerWarp = kTile / 8;
-  for (int64_t k = grp;; k += 2) {
-    const int64_t tile = (int64_t)blockIdx.x + k * (int64_t)gridDim.x;
-    if (tile >= n_tiles) break;
-    // ---- the tile's rows (channels 0..C and the direction) and row indices -> shared memory ----
-    {
-      int32_t pix[kRowsPerWarp], pray[kRowsPerWarp];
+  const int64_t stride = gridDim.x;
+  // the CTA's tiles: blockIdx.x + i * gridDim.x, i = 0, 1, ...
+  auto tile_at = [&](int64_t i) { return (int64_t)blockIdx.x + i * stride; };
+  // rows of tile `tile` -> R (a warp per row): features 1..C, the direction, the row index
+  auto stage = [&](int64_t tile, float* R) {
+    constexpr int kRowsPerWarp = kTile / (kThreads / 32);
+    int32_t pix[kRowsPerWarp], pray[kRowsPerWarp];
 #pragma unroll
-      for (int i = 0; i < kRowsPerWarp; ++i) {
-        const int64_t row = tile * kTile + wg * kRowsPerWarp + i;
-        const bool valid = row < a.n;
-        pix[i] = valid ? a.app_idx[row] : -1;
-        pray[i] = valid ? a.app_ray[row] : -1;
-      }
+    for (int i = 0; i < kRowsPerWarp; ++i) {
+      const int64_t row = tile * kTile + warp * kRowsPerWarp + i;
+      const bool valid = row < a.n;
+      pix[i] = valid ? a.app_idx[row] : -1;
+      pray[i] = valid ? a.app_ray[row] : -1;
+    }
 #pragma unroll
-      for (int i = 0; i < kRowsPerWarp; ++i) {
-        const int rr = wg * kRowsPerWarp + i;
-        const float fv = (pix[i] >= 0 && lane <= C) ? a.feat[(int64_t)pix[i] * a.feat_stride + lane] : 0.f;
-        const float dv = (pray[i] >= 0 && lane < 3) ? a.rays[(int64_t)pray[i] * 6 + 3 + lane] : 0.f;
-        range_ok &= !(fabsf(fv) > kF16Max);
-        if (lane <= C) rows[rr * L::RS + lane] = fv;
-        if (lane < 3) rows[rr * L::RS + C + 1 + lane] = dv;
-        if (lane == 0) idx_s[rr] = pix[i];
-      }
+    for (int i = 0; i < kRowsPerWarp; ++i) {
+      float* row = R + (warp * kRowsPerWarp + i) * L::RS;
+      const float fv = (pix[i] >= 0 && lane < C) ? a.feat[(int64_t)pix[i] * a.feat_stride + 1 + lane] : 0.f;
+      const float dv = (pray[i] >= 0 && lane < 3) ? a.rays[(int64_t)pray[i] * 6 + 3 + lane] : 0.f;
+      range_ok &= !(fabsf(fv) > kF16Max);
+      if (lane < C) row[lane] = fv;
+      if (lane < 3) row[C + lane] = dv;
+      if (lane == 0) row[C + 3] = __int_as_float(pix[i]);
     }
-    group_sync(bar_id);
-    // ---- X (FP16): thread = (row, 8-column chunk), one 16-byte store ----
+  };
+  // X (FP16) of the rows in R -> buffer X: thread = (row, 8-column chunk), one 16-byte store
+  auto build = [&](const float* R, uint32_t X) {
+    constexpr int kChunks = S::IN_PAD / 8;
+#pragma unroll 1
+    for (int it = warp; it < 4 * kChunks; it += kThreads / 32) {
+      const int rr = (it & 3) * 32 + lane;
+      const float* fr = R + rr * L::RS;
+      build_chunk_at<C, F, V, true, 0>(it >> 2, X, 0u, rr, fr, fr + C);
+    }
+  };
+  auto issue_f1 = [&](int b) {  // by thread 0, after the barrier that published X_b
+    tc::fence_after_sync();
+    const uint32_t id = tc::idesc_f16kind(128, kH, false, false, false);
+    const uint32_t sx = tc::smem_u32(xb(b));
+#pragma unroll 1
+    for (int s = 0; s < S::IN_PAD / 16; ++s)
+      tc::mma_f16kind(tmem + 128 * b, desc_k(sx, S::IN_PAD, s), desc_k(sW0, S::IN_PAD, s), id, s > 0);
+    tc::mma_commit(tc::smem_u32(mbar + b));
+  };
+
+  // ---- prologue: tiles 0 and 1 staged and built, their F1 issued ----
+  for (int b = 0; b < 2; ++b)
+    if (tile_at(b) < n_tiles) stage(tile_at(b), rb(b));
+  __syncthreads();
+  for (int b = 0; b < 2; ++b) {
+    if (tile_at(b) < n_tiles) {
+      build(rb(b), tc::smem_u32(xb(b)));
+      tc::fence_smem_to_async();
+      tc::fence_before_sync();
+      __syncthreads();
+      if (t == 0) issue_f1(b);
+    }
+  }
+
+  for (int64_t i = 0; tile_at(i) < n_tiles && ok; ++i) {
+    const int b = (int)(i & 1);
+    const uint32_t sx = tc::smem_u32(xb(b));
+    const uint32_t tS = tmem + 128 * b;
+    // this row's sample index, read before R_b is restaged with tile i + 2
+    const int32_t sidx = part == 0 ? __float_as_int(rb(b)[r * L::RS + C + 3]) : -1;
+    // ---- H0 = relu(S + b0) -> X_b as FP16 [128 x 128] (F1 has consumed X) ----
+    if (!wait_mma(b)) break;
     {
-      constexpr int kChunks = S::IN_PAD / 8;
-#pragma unroll 1
-      for (int it = wg; it < 4 * kChunks; it += 8) {
-        const int rr = (it & 3) * 32 + lane;
-        const float* fr = rows + rr * L::RS;
-        build_chunk_at<C, F, V, true>(it >> 2, sX, 0u, rr, fr, fr + C + 1);
-      }
-    }
-    tc::fence_smem_to_async();
-    tc::fence_before_sync();
-    group_sync(bar_id);
-    // ---- F1: S = X W0^T ----
-    if (issuer) {
-      tc::fence_after_sync();
-      const uint32_t id = tc::idesc_f16kind(128, kH, false, false, false);
-#pragma unroll 1
-      for (int s = 0; s < S::IN_PAD / 16; ++s)
-        tc::mma_f16kind(tS_mma, desc_k(sX, S::IN_PAD, s), desc_k(sW0, S::IN_PAD, s), id, s > 0);
-      tc::mma_commit(mb);
-    }
-    if (!wait_mma()) break;
-    // ---- H0 = relu(S + b0) -> X's buffer as FP16 [128 x 128] (X is consumed) ----
-#pragma unroll 1
-    for (int hh = 0; hh < 2; ++hh) {
-      const int c0 = half * 64 + hh * 32;
       float v[32];
-      tc::tmem_ld32(tS + c0, v);
-      const float4* bv = reinterpret_cast<const float4*>(b0s + c0);
+      tc::tmem_ld32(tS + lane_off + part * 32, v);
+      const float4* bv = reinterpret_cast<const float4*>(b0s + part * 32);
+      float hmax = 0.f;
 #pragma unroll
       for (int j4 = 0; j4 < 8; ++j4) {
-        const float4 b = bv[j4];
-        v[4 * j4] = fmaxf(v[4 * j4] + b.x, 0.f);
-        v[4 * j4 + 1] = fmaxf(v[4 * j4 + 1] + b.y, 0.f);
-        v[4 * j4 + 2] = fmaxf(v[4 * j4 + 2] + b.z, 0.f);
-        v[4 * j4 + 3] = fmaxf(v[4 * j4 + 3] + b.w, 0.f);
+        const float4 bb = bv[j4];
+        v[4 * j4] = fmaxf(v[4 * j4] + bb.x, 0.f);
+        v[4 * j4 + 1] = fmaxf(v[4 * j4 + 1] + bb.y, 0.f);
+        v[4 * j4 + 2] = fmaxf(v[4 * j4 + 2] + bb.z, 0.f);
+        v[4 * j4 + 3] = fmaxf(v[4 * j4 + 3] + bb.w, 0.f);
+        hmax = fmaxf(hmax, fmaxf(fmaxf(v[4 * j4], v[4 * j4 + 1]), fmaxf(v[4 * j4 + 2], v[4 * j4 + 3])));
       }
+      range_ok &= !(hmax > kF16Max);
 #pragma unroll
       for (int g = 0; g < 4; ++g) {
         const float* q = v + 8 * g;
-        st_shared_v4(sX + tc::core_off(r, c0 + 8 * g, kH), tc::pack2_f16(q[0], q[1]), tc::pack2_f16(q[2], q[3]),
+        st_shared_v4(sx + tc::core_off(r, part * 32 + 8 * g, kH), tc::pack2_f16(q[0], q[1]), tc::pack2_f16(q[2], q[3]),
                      tc::pack2_f16(q[4], q[5]), tc::pack2_f16(q[6], q[7]));
       }
     }
     tc::fence_smem_to_async();
     tc::fence_before_sync();
-    group_sync(bar_id);
+    __syncthreads();
     // ---- F2: S = H0 W1^T ----
-    if (issuer) {
+    if (t == 0) {
       tc::fence_after_sync();
       const uint32_t id = tc::idesc_f16kind(128, kH, false, false, false);
 #pragma unroll 1
-      for (int s = 0; s < kH / 16; ++s) tc::mma_f16kind(tS_mma, desc_k(sX, kH, s), desc_k(sW1, kH, s), id, s > 0);
-      tc::mma_commit(mb);
+      for (int s = 0; s < kH / 16; ++s) tc::mma_f16kind(tS, desc_k(sx, kH, s), desc_k(sW1, kH, s), id, s > 0);
+      tc::mma_commit(tc::smem_u32(mbar + 2));
     }
-    if (!wait_mma()) break;
-    // ---- y = relu(S + b1) W2^T over this thread's 64 columns; the two halves meet in shared memory ----
+    // ---- the rows of tile i + 2 -> R_b (its rows were consumed when X(i) was built) ----
+    const bool next2 = tile_at(i + 2) < n_tiles;
+    if (next2) stage(tile_at(i + 2), rb(b));
+    // ---- y = relu(S + b1) W2^T: the slice's partial sums, summed over the 4 slices ----
+    if (!wait_mma(2)) break;
+    float4* yp = reinterpret_cast<float4*>(xb(b));  // [4 slices][128 rows]; H0 is consumed
     {
+      float h1[32];
       float y0 = 0.f, y1 = 0.f, y2 = 0.f;
-#pragma unroll 1
-      for (int hh = 0; hh < 2; ++hh) {
-        const int c0 = half * 64 + hh * 32;
-        float h1[32];
-        tc::tmem_ld32(tS + c0, h1);
-        const float4* b1v = reinterpret_cast<const float4*>(b1s + c0);
-        const float4* w2v = reinterpret_cast<const float4*>(w2s + c0);  // rows kH / 4 float4 apart
+      tc::tmem_ld32(tS + lane_off + part * 32, h1);
+      const float4* b1v = reinterpret_cast<const float4*>(b1s + part * 32);
+      const float4* w2v = reinterpret_cast<const float4*>(w2s + part * 32);  // rows kH / 4 float4 apart
 #pragma unroll
-        for (int j4 = 0; j4 < 8; ++j4) {
-          const float4 b = b1v[j4], wa = w2v[j4], wb = w2v[kH / 4 + j4], wc = w2v[kH / 2 + j4];
-          const float bb[4] = {b.x, b.y, b.z, b.w}, u0[4] = {wa.x, wa.y, wa.z, wa.w};
-          const float u1[4] = {wb.x, wb.y, wb.z, wb.w}, u2[4] = {wc.x, wc.y, wc.z, wc.w};
+      for (int j4 = 0; j4 < 8; ++j4) {
+        const float4 bb = b1v[j4], wa = w2v[j4], wb = w2v[kH / 4 + j4], wc = w2v[kH / 2 + j4];
+        const float bq[4] = {bb.x, bb.y, bb.z, bb.w}, u0[4] = {wa.x, wa.y, wa.z, wa.w};
+        const float u1[4] = {wb.x, wb.y, wb.z, wb.w}, u2[4] = {wc.x, wc.y, wc.z, wc.w};
 #pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            const float h = fmaxf(h1[4 * j4 + q] + bb[q], 0.f);
-            y0 += h * u0[q];
-            y1 += h * u1[q];
-            y2 += h * u2[q];
-          }
+        for (int q = 0; q < 4; ++q) {
+          const float h = fmaxf(h1[4 * j4 + q] + bq[q], 0.f);
+          y0 += h * u0[q];
+          y1 += h * u1[q];
+          y2 += h * u2[q];
         }
       }
-      yp[half * kTile + r] = make_float4(y0, y1, y2, 0.f);  // H0 is consumed (F2 complete)
-    }
-    group_sync(bar_id);
-    if (half == 0) {
-      const int32_t sidx = idx_s[r];
-      if (sidx >= 0) {
-        const float4 u = yp[r], w = yp[kTile + r];
-        a.rgb_out[(int64_t)sidx * 3] = 1.f / (1.f + expf(-(u.x + w.x)));
-        a.rgb_out[(int64_t)sidx * 3 + 1] = 1.f / (1.f + expf(-(u.y + w.y)));
-        a.rgb_out[(int64_t)sidx * 3 + 2] = 1.f / (1.f + expf(-(u.z + w.z)));
-      }
+      yp[part * kTile + r] = make_float4(y0, y1, y2, 0.f);
     }
     tc::fence_before_sync();
-    group_sync(bar_id);  // S, the staged rows and the partials are read before the next tile reuses them
+    __syncthreads();  // every slice's partials are written
+    if (sidx >= 0) {
+      float4 ys = yp[r];
+#pragma unroll
+      for (int q = 1; q < 4; ++q) {
+        const float4 o = yp[q * kTile + r];
+        ys.x += o.x; ys.y += o.y; ys.z += o.z;
+      }
+      a.rgb_out[(int64_t)sidx * 3] = 1.f / (1.f + expf(-ys.x));
+      a.rgb_out[(int64_t)sidx * 3 + 1] = 1.f / (1.f + expf(-ys.y));
+      a.rgb_out[(int64_t)sidx * 3 + 2] = 1.f / (1.f + expf(-ys.z));
+    }
+    __syncthreads();  // the partials are read before X(i + 2) overwrites them
+    // ---- X(i + 2) -> X_b, then its F1 -> S_b (S_b was read above) ----
+    if (next2) {
+      build(rb(b), sx);
+      tc::fence_smem_to_async();
+      tc::fence_before_sync();
+      __syncthreads();
+      if (t == 0) issue_f1(b);
+    }
   }
 
   if (!ok) {
-    if (issuer && a.status) atomicExch(a.status, FF_ERR_LIMIT);
-    (void)tc::mbar_wait(mb, phase & 1u, kPolls);  // this group's MMAs in flight, if they ever finish
+    if (t == 0 && a.status) atomicExch(a.status, FF_ERR_LIMIT);
+    for (int m = 0; m < 3; ++m) (void)tc::mbar_wait(tc::smem_u32(mbar + m), (ph >> m) & 1u, kPolls);
   }
   if (!range_ok && a.status) atomicCAS(a.status, 0, FF_ERR_SIZE);
   tc::fence_before_sync();
@@ -834,8 +845,7 @@ cudaError_t launch_fwd16(const HeadArgs& a, cudaStream_t s) {
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;
   const int64_t tiles = ceil_div(a.n, kTile);
-  // each CTA runs two tiles at a time: at most one CTA per two tiles
-  const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(tiles, 2), (int64_t)sm_count()));
+  const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>(tiles, (int64_t)sm_count()));
   kern<<<blocks, kThreads, smem, s>>>(a);
   return cudaGetLastError();
 }
