@@ -588,8 +588,8 @@ __global__ void __launch_bounds__(kThreads, 1) head_tc_kernel(const HeadArgs a) 
 // the tensor core works while the CUDA cores do:
 //
 //   iteration i (buffer b = i & 1; F1 of tile i was issued at the end of iteration i - 2):
-//     wait F1(i); H0(i) = relu(S_b + b0) -> X_b (FP16);  issue F2(i) -> S_b
-//     stage the rows of tile i + 2 -> R_b                         (overlaps F2(i))
+//     load the row indices of tile i + 2;  wait F1(i); H0(i) = relu(S_b + b0) -> X_b (FP16)
+//     issue F2(i) -> S_b;  copy the rows of tile i + 2 -> R_b (cp.async)   (overlaps F2(i))
 //     wait F2(i); y partials -> X_b; rgb = sigmoid(y) out
 //     build X(i + 2) from R_b -> X_b;  issue F1(i + 2) -> S_b      (runs during iteration i + 1)
 //
@@ -609,6 +609,15 @@ struct Fwd16 {
 };
 
 constexpr float kF16Max = 65504.f;
+
+// 4-byte asynchronous global -> shared copy; with v false the destination is zero-filled and
+// nothing is read (src is any valid address).
+__device__ __forceinline__ void cp_async4(float* dst, const float* src, bool v) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(tc::smem_u32(dst)), "l"(src), "r"(v ? 4 : 0)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
 template <int C, int F, int V>
 __global__ void __launch_bounds__(kThreads, 1) head_fwd16_kernel(const HeadArgs a) {
@@ -679,10 +688,11 @@ __global__ void __launch_bounds__(kThreads, 1) head_fwd16_kernel(const HeadArgs 
   const int64_t stride = gridDim.x;
   // the CTA's tiles: blockIdx.x + i * gridDim.x, i = 0, 1, ...
   auto tile_at = [&](int64_t i) { return (int64_t)blockIdx.x + i * stride; };
-  // rows of tile `tile` -> R (a warp per row): features 1..C, the direction, the row index
-  auto stage = [&](int64_t tile, float* R) {
-    constexpr int kRowsPerWarp = kTile / (kThreads / 32);
-    int32_t pix[kRowsPerWarp], pray[kRowsPerWarp];
+  // Staging of tile `tile`'s rows into R (a warp per row): features 1..C, the direction, the row
+  // index. First the row indices (into registers), later the rows themselves as asynchronous
+  // 4-byte copies (cp.async; completed by cp_async_wait_all before the rows are read).
+  constexpr int kRowsPerWarp = kTile / (kThreads / 32);
+  auto stage_idx = [&](int64_t tile, int32_t* pix, int32_t* pray) {
 #pragma unroll
     for (int i = 0; i < kRowsPerWarp; ++i) {
       const int64_t row = tile * kTile + warp * kRowsPerWarp + i;
@@ -690,16 +700,22 @@ __global__ void __launch_bounds__(kThreads, 1) head_fwd16_kernel(const HeadArgs 
       pix[i] = valid ? a.app_idx[row] : -1;
       pray[i] = valid ? a.app_ray[row] : -1;
     }
+  };
+  auto stage_rows = [&](const int32_t* pix, const int32_t* pray, float* R) {
 #pragma unroll
     for (int i = 0; i < kRowsPerWarp; ++i) {
       float* row = R + (warp * kRowsPerWarp + i) * L::RS;
-      const float fv = (pix[i] >= 0 && lane < C) ? a.feat[(int64_t)pix[i] * a.feat_stride + 1 + lane] : 0.f;
-      const float dv = (pray[i] >= 0 && lane < 3) ? a.rays[(int64_t)pray[i] * 6 + 3 + lane] : 0.f;
-      range_ok &= !(fabsf(fv) > kF16Max);
-      if (lane < C) row[lane] = fv;
-      if (lane < 3) row[C + lane] = dv;
+      if (lane < C) {
+        const bool v = pix[i] >= 0;
+        cp_async4(row + lane, v ? a.feat + (int64_t)pix[i] * a.feat_stride + 1 + lane : a.feat, v);
+      }
+      if (lane < 3) {
+        const bool v = pray[i] >= 0;
+        cp_async4(row + C + lane, v ? a.rays + (int64_t)pray[i] * 6 + 3 + lane : a.rays, v);
+      }
       if (lane == 0) row[C + 3] = __int_as_float(pix[i]);
     }
+    cp_async_commit();
   };
   // X (FP16) of the rows in R -> buffer X: thread = (row, 8-column chunk), one 16-byte store
   auto build = [&](const float* R, uint32_t X) {
@@ -722,8 +738,14 @@ __global__ void __launch_bounds__(kThreads, 1) head_fwd16_kernel(const HeadArgs 
   };
 
   // ---- prologue: tiles 0 and 1 staged and built, their F1 issued ----
-  for (int b = 0; b < 2; ++b)
-    if (tile_at(b) < n_tiles) stage(tile_at(b), rb(b));
+  for (int b = 0; b < 2; ++b) {
+    if (tile_at(b) < n_tiles) {
+      int32_t pix[kRowsPerWarp], pray[kRowsPerWarp];
+      stage_idx(tile_at(b), pix, pray);
+      stage_rows(pix, pray, rb(b));
+    }
+  }
+  cp_async_wait_all();
   __syncthreads();
   for (int b = 0; b < 2; ++b) {
     if (tile_at(b) < n_tiles) {
@@ -739,8 +761,20 @@ __global__ void __launch_bounds__(kThreads, 1) head_fwd16_kernel(const HeadArgs 
     const int b = (int)(i & 1);
     const uint32_t sx = tc::smem_u32(xb(b));
     const uint32_t tS = tmem + 128 * b;
-    // this row's sample index, read before R_b is restaged with tile i + 2
-    const int32_t sidx = part == 0 ? __float_as_int(rb(b)[r * L::RS + C + 3]) : -1;
+    // this row's sample index, read (with the FP16 range check of its features) before R_b is
+    // restaged with tile i + 2; the row indices of tile i + 2 are loaded meanwhile
+    int32_t sidx = -1;
+    if (part == 0) {
+      const float* fr = rb(b) + r * L::RS;
+      sidx = __float_as_int(fr[C + 3]);
+      float m = 0.f;
+#pragma unroll
+      for (int c = 0; c < C; ++c) m = fmaxf(m, fabsf(fr[c]));
+      range_ok &= !(m > kF16Max);
+    }
+    const bool next2 = tile_at(i + 2) < n_tiles;
+    int32_t pix[kRowsPerWarp], pray[kRowsPerWarp];
+    if (next2) stage_idx(tile_at(i + 2), pix, pray);
     // ---- H0 = relu(S + b0) -> X_b as FP16 [128 x 128] (F1 has consumed X) ----
     if (!wait_mma(b)) break;
     {
@@ -776,9 +810,9 @@ __global__ void __launch_bounds__(kThreads, 1) head_fwd16_kernel(const HeadArgs 
       for (int s = 0; s < kH / 16; ++s) tc::mma_f16kind(tS, desc_k(sx, kH, s), desc_k(sW1, kH, s), id, s > 0);
       tc::mma_commit(tc::smem_u32(mbar + 2));
     }
-    // ---- the rows of tile i + 2 -> R_b (its rows were consumed when X(i) was built) ----
-    const bool next2 = tile_at(i + 2) < n_tiles;
-    if (next2) stage(tile_at(i + 2), rb(b));
+    // ---- the rows of tile i + 2 -> R_b, asynchronously (R_b's rows were consumed when X(i) was
+    // built, its indices and range read above, before the barrier of the F1 wait) ----
+    if (next2) stage_rows(pix, pray, rb(b));
     // ---- y = relu(S + b1) W2^T: the slice's partial sums, summed over the 4 slices ----
     if (!wait_mma(2)) break;
     float4* yp = reinterpret_cast<float4*>(xb(b));  // [4 slices][128 rows]; H0 is consumed
@@ -819,6 +853,8 @@ __global__ void __launch_bounds__(kThreads, 1) head_fwd16_kernel(const HeadArgs 
     __syncthreads();  // the partials are read before X(i + 2) overwrites them
     // ---- X(i + 2) -> X_b, then its F1 -> S_b (S_b was read above) ----
     if (next2) {
+      cp_async_wait_all();
+      __syncthreads();  // every warp's copies of R_b have landed
       build(rb(b), sx);
       tc::fence_smem_to_async();
       tc::fence_before_sync();
@@ -832,6 +868,7 @@ __global__ void __launch_bounds__(kThreads, 1) head_fwd16_kernel(const HeadArgs 
     for (int m = 0; m < 3; ++m) (void)tc::mbar_wait(tc::smem_u32(mbar + m), (ph >> m) & 1u, kPolls);
   }
   if (!range_ok && a.status) atomicCAS(a.status, 0, FF_ERR_SIZE);
+  cp_async_wait_all();  // no copy in flight when the CTA ends (after an early exit)
   tc::fence_before_sync();
   __syncthreads();
   if (warp == 0) tc::tmem_dealloc(tmem, 256u);
