@@ -173,13 +173,29 @@ __device__ __forceinline__ float x_col(const float* fr, const float* dr) {
 // X_lo), or with kF16 as FP16 values (one 16-byte store into X; Xlo unused).
 template <int C, int F, int V, bool kF16, int kOff, int CH, int... J>
 __device__ __forceinline__ void build_chunk(uint32_t X, uint32_t Xlo, int rr, const float* fr, const float* dr,
-                                            std::integer_sequence<int, J...>) {
+                                            std::integer_sequence<int, J...>, float* raw_max = nullptr) {
   const float v[8] = {x_col<C, F, V, CH * 8 + J, kOff>(fr, dr)...};
-  if constexpr (kF16)
+  if constexpr (kF16) {
     st_shared_v4(X + tc::core_off(rr, CH * 8, Shape<C, F, V>::IN_PAD), tc::pack2_f16(v[0], v[1]),
                  tc::pack2_f16(v[2], v[3]), tc::pack2_f16(v[4], v[5]), tc::pack2_f16(v[6], v[7]));
-  else
+    if constexpr (CH * 8 < C + 3) {  // features and direction: the unbounded inputs
+#pragma unroll
+      for (int j = 0; j < 8; ++j)
+        if (CH * 8 + j < C + 3) *raw_max = fmaxf(*raw_max, fabsf(v[j]));
+    }
+  } else {
     store8_split(X, Xlo, Shape<C, F, V>::IN_PAD, rr, CH * 8, v);
+  }
+}
+
+// Chunks O, O + 4, O + 8, ... of row rr (all compile-time: one dispatch per tile, not per chunk).
+template <int C, int F, int V, int kOff, int O, int J = 0>
+__device__ __forceinline__ void build_seq16(uint32_t X, int rr, const float* fr, const float* dr, float* raw_max) {
+  constexpr int CH = 4 * J + O;
+  if constexpr (CH < Shape<C, F, V>::IN_PAD / 8) {
+    build_chunk<C, F, V, true, kOff, CH>(X, 0u, rr, fr, dr, std::make_integer_sequence<int, 8>{}, raw_max);
+    build_seq16<C, F, V, kOff, O, J + 1>(X, rr, fr, dr, raw_max);
+  }
 }
 
 // Chunk `ch` (warp-uniform) dispatched to its compile-time builder.
@@ -717,15 +733,19 @@ __global__ void __launch_bounds__(kThreads, 1) head_fwd16_kernel(const HeadArgs 
     }
     cp_async_commit();
   };
-  // X (FP16) of the rows in R -> buffer X: thread = (row, 8-column chunk), one 16-byte store
+  // X (FP16) of the rows in R -> buffer X: thread = row (warp & 3) * 32 + lane, its 8-column
+  // chunks warp / 4, + 4, + 8, ... (one 16-byte store each); the FP16 range check of the raw inputs
   auto build = [&](const float* R, uint32_t X) {
-    constexpr int kChunks = S::IN_PAD / 8;
-#pragma unroll 1
-    for (int it = warp; it < 4 * kChunks; it += kThreads / 32) {
-      const int rr = (it & 3) * 32 + lane;
-      const float* fr = R + rr * L::RS;
-      build_chunk_at<C, F, V, true, 0>(it >> 2, X, 0u, rr, fr, fr + C);
+    const int rr = quad * 32 + lane;
+    const float* fr = R + rr * L::RS;
+    float m = 0.f;
+    switch (part) {
+      case 0: build_seq16<C, F, V, 0, 0>(X, rr, fr, fr + C, &m); break;
+      case 1: build_seq16<C, F, V, 0, 1>(X, rr, fr, fr + C, &m); break;
+      case 2: build_seq16<C, F, V, 0, 2>(X, rr, fr, fr + C, &m); break;
+      default: build_seq16<C, F, V, 0, 3>(X, rr, fr, fr + C, &m); break;
     }
+    range_ok &= !(m > kF16Max);  // NaN passes (propagates as in float32)
   };
   auto issue_f1 = [&](int b) {  // by thread 0, after the barrier that published X_b
     tc::fence_after_sync();
@@ -761,17 +781,9 @@ __global__ void __launch_bounds__(kThreads, 1) head_fwd16_kernel(const HeadArgs 
     const int b = (int)(i & 1);
     const uint32_t sx = tc::smem_u32(xb(b));
     const uint32_t tS = tmem + 128 * b;
-    // this row's sample index, read (with the FP16 range check of its features) before R_b is
-    // restaged with tile i + 2; the row indices of tile i + 2 are loaded meanwhile
-    int32_t sidx = -1;
-    if (part == 0) {
-      const float* fr = rb(b) + r * L::RS;
-      sidx = __float_as_int(fr[C + 3]);
-      float m = 0.f;
-#pragma unroll
-      for (int c = 0; c < C; ++c) m = fmaxf(m, fabsf(fr[c]));
-      range_ok &= !(m > kF16Max);
-    }
+    // this row's sample index, read before R_b is restaged with tile i + 2; the row indices of
+    // tile i + 2 are loaded meanwhile
+    const int32_t sidx = part == 0 ? __float_as_int(rb(b)[r * L::RS + C + 3]) : -1;
     const bool next2 = tile_at(i + 2) < n_tiles;
     int32_t pix[kRowsPerWarp], pray[kRowsPerWarp];
     if (next2) stage_idx(tile_at(i + 2), pix, pray);
@@ -837,8 +849,9 @@ __global__ void __launch_bounds__(kThreads, 1) head_fwd16_kernel(const HeadArgs 
       }
       yp[part * kTile + r] = make_float4(y0, y1, y2, 0.f);
     }
+    cp_async_wait_all();  // this thread's copies of tile i + 2's rows (published by the barrier)
     tc::fence_before_sync();
-    __syncthreads();  // every slice's partials are written
+    __syncthreads();  // every slice's partials are written, R_b holds tile i + 2's rows
     if (sidx >= 0) {
       float4 ys = yp[r];
 #pragma unroll
@@ -853,8 +866,6 @@ __global__ void __launch_bounds__(kThreads, 1) head_fwd16_kernel(const HeadArgs 
     __syncthreads();  // the partials are read before X(i + 2) overwrites them
     // ---- X(i + 2) -> X_b, then its F1 -> S_b (S_b was read above) ----
     if (next2) {
-      cp_async_wait_all();
-      __syncthreads();  // every warp's copies of R_b have landed
       build(rb(b), sx);
       tc::fence_smem_to_async();
       tc::fence_before_sync();
