@@ -31,7 +31,8 @@
 //   B4  S  = dH0 W0                 (the feature-related input columns only)
 //       dL/dfeat = the chain rule through the positional encoding: each thread adds its columns'
 //       terms to a per-row shared-memory sum, and a warp per row writes the rows out
-// dW2, db0 and db1 are warp reduce-scatters into per-lane registers. At the end each CTA adds its
+// dW2 and db1 are warp reduce-scatters into per-lane registers; db0 accumulates in dW0's column
+// in_dim, where X holds a constant 1 (W0's column there is zero). At the end each CTA adds its
 // dW0 / dW1 (read from TMEM, one row per quadrant thread) and the register sums to the float32
 // gradients with one atomic per entry.
 //
@@ -145,7 +146,7 @@ __device__ __forceinline__ void store8_split(uint32_t hi_buf, uint32_t lo_buf, i
 
 // Column K of the head's input row (the reference's order, models/FactorFields.py:188-195),
 // decoded at compile time: fr = the staged feature row (fr[kOff + c] = feature c), dr = the ray
-// direction; 0 past in_dim. Positional-encoding columns use the hardware sin / cos.
+// direction; past in_dim a constant 1 (column in_dim, which in_pad always has), then 0. Positional-encoding columns use the hardware sin / cos.
 template <int C, int F, int V, int K, int kOff>
 __device__ __forceinline__ float x_col(const float* fr, const float* dr) {
   if constexpr (K < C) {
@@ -164,6 +165,8 @@ __device__ __forceinline__ float x_col(const float* fr, const float* dr) {
     constexpr int j = kCos ? k - 3 * V : k;
     const float x = dr[j / V] * (float)(1 << (j % V));
     return kCos ? __cosf(x) : __sinf(x);
+  } else if constexpr (K == C + 3 + 2 * C * F + 6 * V) {
+    return 1.f;  // the first pad column: W0's is zero; dW0's is the bias gradient sum_s dH0
   } else {
     return 0.f;
   }
@@ -189,25 +192,25 @@ __device__ __forceinline__ void build_chunk(uint32_t X, uint32_t Xlo, int rr, co
 }
 
 // Chunks O, O + 4, O + 8, ... of row rr (all compile-time: one dispatch per tile, not per chunk).
-template <int C, int F, int V, int kOff, int O, int J = 0>
-__device__ __forceinline__ void build_seq16(uint32_t X, int rr, const float* fr, const float* dr, float* raw_max) {
+template <int C, int F, int V, bool kF16, int kOff, int O, int J = 0>
+__device__ __forceinline__ void build_seq(uint32_t X, uint32_t Xlo, int rr, const float* fr, const float* dr,
+                                          float* raw_max) {
   constexpr int CH = 4 * J + O;
   if constexpr (CH < Shape<C, F, V>::IN_PAD / 8) {
-    build_chunk<C, F, V, true, kOff, CH>(X, 0u, rr, fr, dr, std::make_integer_sequence<int, 8>{}, raw_max);
-    build_seq16<C, F, V, kOff, O, J + 1>(X, rr, fr, dr, raw_max);
+    build_chunk<C, F, V, kF16, kOff, CH>(X, Xlo, rr, fr, dr, std::make_integer_sequence<int, 8>{}, raw_max);
+    build_seq<C, F, V, kF16, kOff, O, J + 1>(X, Xlo, rr, fr, dr, raw_max);
   }
 }
 
-// Chunk `ch` (warp-uniform) dispatched to its compile-time builder.
-template <int C, int F, int V, bool kF16, int kOff, int CH = 0>
-__device__ __forceinline__ void build_chunk_at(int ch, uint32_t X, uint32_t Xlo, int rr, const float* fr,
-                                               const float* dr) {
-  if constexpr (CH < Shape<C, F, V>::IN_PAD / 8) {
-    if (ch == CH) {
-      build_chunk<C, F, V, kF16, kOff, CH>(X, Xlo, rr, fr, dr, std::make_integer_sequence<int, 8>{});
-      return;
-    }
-    build_chunk_at<C, F, V, kF16, kOff, CH + 1>(ch, X, Xlo, rr, fr, dr);
+// X of row rr: the thread's chunk sequence `part` (0..3) dispatched once.
+template <int C, int F, int V, bool kF16, int kOff>
+__device__ __forceinline__ void build_row(int part, uint32_t X, uint32_t Xlo, int rr, const float* fr, const float* dr,
+                                          float* raw_max) {
+  switch (part) {
+    case 0: build_seq<C, F, V, kF16, kOff, 0>(X, Xlo, rr, fr, dr, raw_max); break;
+    case 1: build_seq<C, F, V, kF16, kOff, 1>(X, Xlo, rr, fr, dr, raw_max); break;
+    case 2: build_seq<C, F, V, kF16, kOff, 2>(X, Xlo, rr, fr, dr, raw_max); break;
+    default: build_seq<C, F, V, kF16, kOff, 3>(X, Xlo, rr, fr, dr, raw_max); break;
   }
 }
 
@@ -320,7 +323,7 @@ __global__ void __launch_bounds__(kThreads, 1) head_tc_kernel(const HeadArgs a) 
 
   uint32_t phase = 0;
   bool ok = true, any_tile = false;
-  float acc_db0 = 0.f, acc_db1 = 0.f, acc_dw2[3] = {0.f, 0.f, 0.f};  // column 32 part + lane
+  float acc_db1 = 0.f, acc_dw2[3] = {0.f, 0.f, 0.f};  // column 32 part + lane
 
   // waits for the MMAs committed last; all threads agree on the outcome
   auto wait_mma = [&]() {
@@ -365,15 +368,9 @@ __global__ void __launch_bounds__(kThreads, 1) head_tc_kernel(const HeadArgs a) 
     }
     __syncthreads();
     if (tile + gridDim.x < n_tiles) load_rows(tile + gridDim.x);
-    // ---- X: thread = (row, 8-column chunk), one 16-byte store into each of X_hi and X_lo ----
-    {
-      constexpr int kChunks = S::IN_PAD / 8;
-#pragma unroll 1
-      for (int it = warp; it < 4 * kChunks; it += kThreads / 32) {
-        const int rr = (it & 3) * 32 + lane;
-        build_chunk_at<C, F, V, false, 1>(it >> 2, sX, sXlo, rr, fs + rr * S::FS, ds + rr * 4);
-      }
-    }
+    // ---- X: thread = row r, its 8-column chunks part, + 4, + 8, ... (one 16-byte store each
+    // into X_hi and X_lo) ----
+    build_row<C, F, V, false, 1>(part, sX, sXlo, r, fs + r * S::FS, ds + r * 4, nullptr);
     tc::fence_smem_to_async();
     tc::fence_before_sync();
     __syncthreads();
@@ -510,7 +507,7 @@ __global__ void __launch_bounds__(kThreads, 1) head_tc_kernel(const HeadArgs a) 
         tc::mma_commit(mb);
       }
       if (!wait_mma()) break;
-      // ---- dH0 = S [H0 > 0] (over H0_hi), db0 ----
+      // ---- dH0 = S [H0 > 0] (over H0_hi); db0 accumulates in dW0's column in_dim (X = 1 there) ----
       {
         float v[32];
         tc::tmem_ld32(tS + lane_off + part * 32, v);
@@ -518,7 +515,6 @@ __global__ void __launch_bounds__(kThreads, 1) head_tc_kernel(const HeadArgs a) 
         for (int j = 0; j < 32; ++j) v[j] = ((mask0 >> j) & 1u) ? v[j] : 0.f;
 #pragma unroll
         for (int g = 0; g < 4; ++g) store8(sH0, kH, r, part * 32 + g * 8, v + g * 8);
-        acc_db0 += warp_reduce_scatter32(v, lane);
       }
       tc::fence_smem_to_async();
       tc::fence_before_sync();
@@ -578,13 +574,16 @@ __global__ void __launch_bounds__(kThreads, 1) head_tc_kernel(const HeadArgs a) 
     for (int ci = part; ci < (S::IN_PAD + 31) / 32; ci += 4) {
       float v[32];
       tc::tmem_ld32(tDW0 + lane_off + ci * 32, v);  // columns past IN_PAD (inside the allocation) unused
-      if (a.gw[0])
 #pragma unroll
-        for (int j = 0; j < 32; ++j)
-          if (ci * 32 + j < S::IN) atomicAdd(a.gw[0] + r * S::IN + ci * 32 + j, v[j]);
+      for (int j = 0; j < 32; ++j) {
+        if (ci * 32 + j < S::IN) {
+          if (a.gw[0]) atomicAdd(a.gw[0] + r * S::IN + ci * 32 + j, v[j]);
+        } else if (ci * 32 + j == S::IN) {
+          if (a.gb[0]) atomicAdd(a.gb[0] + r, v[j]);  // db0[r] = sum over samples of dH0[., r]
+        }
+      }
     }
     const int col = part * 32 + lane;
-    if (a.gb[0]) atomicAdd(a.gb[0] + col, acc_db0);
     if (a.gb[1]) atomicAdd(a.gb[1] + col, acc_db1);
     if (a.gw[2])
 #pragma unroll
@@ -739,12 +738,7 @@ __global__ void __launch_bounds__(kThreads, 1) head_fwd16_kernel(const HeadArgs 
     const int rr = quad * 32 + lane;
     const float* fr = R + rr * L::RS;
     float m = 0.f;
-    switch (part) {
-      case 0: build_seq16<C, F, V, 0, 0>(X, rr, fr, fr + C, &m); break;
-      case 1: build_seq16<C, F, V, 0, 1>(X, rr, fr, fr + C, &m); break;
-      case 2: build_seq16<C, F, V, 0, 2>(X, rr, fr, fr + C, &m); break;
-      default: build_seq16<C, F, V, 0, 3>(X, rr, fr, fr + C, &m); break;
-    }
+    build_row<C, F, V, true, 0>(part, X, 0u, rr, fr, fr + C, &m);
     range_ok &= !(m > kF16Max);  // NaN passes (propagates as in float32)
   };
   auto issue_f1 = [&](int b) {  // by thread 0, after the barrier that published X_b
