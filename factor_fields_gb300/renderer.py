@@ -119,8 +119,9 @@ def head_tc_supported(head):
 
 def head_forward(head, feat, rays, app_idx, app_ray, rgb_sample, tc=False, status=None):
     """rgb_sample[app_idx[i]] = colour of app sample i (features = feat[app_idx[i], 1:], direction =
-    rays[app_ray[i], 3:6]): the float32 drop-in head, or with tc the tensor-core head (BF16
-    operands, FP32 accumulation; status: optional device int32 for a bounded-wait failure)."""
+    rays[app_ray[i], 3:6]): the float32 drop-in head, or with tc the tensor-core head (FP16
+    operands with the BF16-rounded weights, FP32 accumulation; status: optional zeroed device
+    int32 that reports a bounded-wait failure or an input outside the FP16 range)."""
     n = app_idx.shape[0]
     if n == 0:
         return

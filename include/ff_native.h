@@ -403,14 +403,19 @@ FF_API int ff_render_head_backward(const FFRenderMlp* h, const float* feat, int3
                                    const float* grad_rgb_sample, float* grad_feat, const FFMlpGrad* g,
                                    void* workspace, int64_t workspace_bytes, void* stream);
 
-/* The same head on the tensor cores (tcgen05 MMA, BF16 operands, FP32 accumulators in tensor
- * memory): weights rounded to BF16 inside the kernel, inputs (the positional encoding of the
- * features and directions) rounded to BF16, activations kept as BF16, every accumulation FP32.
+/* The same head on the tensor cores (tcgen05 MMA, FP32 accumulators in tensor memory, every
+ * accumulation FP32), weights rounded to BF16 inside the kernel (the stored head). The forward
+ * holds the input row (features, direction, their positional encoding) and the first hidden layer
+ * as FP16 values (11 significant bits; the BF16 weights are exact in FP16). The backward
+ * recomputes the forward with BF16 hi + lo pairs for those two (~16 significant bits, so its ReLU
+ * decisions match float32 except within ~1e-5 of a kink) and uses BF16 gradient operands.
  * One persistent launch each way, no workspace. Requirements (else FF_ERR_UNSUPPORTED): n_layers
  * 3, hidden_dim 128, fea_pe 2, view_pe 6, in_channels 27 or 31 (model.out_dim 28 or 32).
- * status (optional, device int32): set to FF_ERR_LIMIT if a bounded wait inside the kernel ran
- * out (results invalid); left untouched otherwise. The backward writes grad_feat and accumulates
- * g exactly like ff_render_head_backward. */
+ * status (optional, device int32, zero on entry): set to FF_ERR_LIMIT if a bounded wait inside the
+ * kernel ran out, and by the forward to FF_ERR_SIZE when a weight, feature or first-layer
+ * activation lies outside the FP16 range (|x| > 65504); results invalid in both cases; left
+ * untouched otherwise. The backward writes grad_feat and accumulates g exactly like
+ * ff_render_head_backward. */
 FF_API int ff_render_head_forward_tc(const FFRenderMlp* h, const float* feat, int32_t feat_stride, const float* rays,
                                      const int32_t* app_idx, const int32_t* app_ray, int64_t n_app, float* rgb_sample,
                                      int32_t* status, void* stream);
