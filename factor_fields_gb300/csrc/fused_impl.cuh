@@ -221,7 +221,7 @@ __device__ __forceinline__ void coop_coeff_scatter(float* __restrict__ grad, int
 // ---- the kernel -------------------------------------------------------------------------
 
 template <int MODE, int BD, int CD, int OUTT, typename T>
-__global__ void __launch_bounds__(kThreads, 3) fused_field_mlp_kernel(const FusedArgs a) {
+__global__ void __launch_bounds__(kThreads, MODE == kFwd ? 4 : 3) fused_field_mlp_kernel(const FusedArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, g = lane >> 2, t = lane & 3;
   const Smem s = carve<MODE, OUTT>(smem_raw);
