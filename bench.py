@@ -370,9 +370,10 @@ def _train_radiance(kind, seed, iters, pool, gt, dev):
 
 
 def measure_radiance_field_kernels(m, rays, dev, flush, steps, warmup, seed=3):
-    """The fused field + 18->64->28 head kernels alone (ff_field_mlp_forward / _backward) on the
-    live samples of one 4,096-ray plain-sampler batch (ray order, as the render calls them), each
-    launch bracketed by CUDA events on its stream after an L2 flush. The backward's contract bytes
+    """The fused field + 18->64->28 head kernels alone (ff_field_mlp_forward / _backward) and the
+    compositing kernels (ff_composite_forward / _backward) on the live samples of one 4,096-ray
+    plain-sampler batch (ray order, as the render calls them), each launch bracketed by CUDA events
+    on its stream after an L2 flush. The backward's contract bytes
     per sample are those of the field backward (two BF16 gathers of the 8 corners x 36 channels,
     one float32 scatter, coordinates and dL/dout: 2,428 B); the forward's one gather plus the
     coordinates and outputs (700 B)."""
@@ -382,8 +383,9 @@ def measure_radiance_field_kernels(m, rays, dev, flush, steps, warmup, seed=3):
     from factor_fields_gb300.renderer import march, render_desc
     g = torch.Generator(device=dev).manual_seed(seed)
     jit = torch.rand(rays.shape[0], device=dev, generator=g)
+    rdesc = render_desc(m, 1024, True)
     with torch.no_grad():
-        _, xyz, _ = march(m, rays, jit, render_desc(m, 1024, True))
+        offs, xyz, sidx = march(m, rays, jit, rdesc)
     n = xyz.shape[0]
     lm = m.linear_mat
     ws, bs = lm.weights()
@@ -426,6 +428,23 @@ def measure_radiance_field_kernels(m, rays, dev, flush, steps, warmup, seed=3):
         return float(np.mean(ts))
 
     fwd_ms, bwd_ms = timed(fwd), timed(bwd)
+    # the compositing kernels on the same samples (the field's outputs as their feature rows)
+    fwd()
+    n_rays = rays.shape[0]
+    rgb = torch.empty(n_rays, 3, device=dev)
+    depth = torch.empty(n_rays, device=dev)
+    g_rgb = torch.randn(n_rays, 3, device=dev, generator=g) * 1e-3
+    g_feat = torch.empty_like(out)
+
+    def comp_fwd():
+        N.call("ff_composite_forward", ctypes.byref(rdesc), N.ptr(rays), N.ptr(jit), n_rays, N.ptr(offs),
+               N.ptr(sidx), N.ptr(out), out.shape[1], None, N.ptr(rgb), N.ptr(depth), None, st)
+
+    def comp_bwd():
+        N.call("ff_composite_backward", ctypes.byref(rdesc), N.ptr(rays), N.ptr(jit), n_rays, N.ptr(offs),
+               N.ptr(sidx), N.ptr(out), out.shape[1], None, N.ptr(g_rgb), N.ptr(g_feat), st)
+
+    cf_ms, cb_ms = timed(comp_fwd), timed(comp_bwd)
     k, ch = 2 ** m.in_dim, m.n_feat * 2
     io = 4 * m.geom.coord_dim + 4 * lm.out_dim
     b_bwd = bytes_per_point(m, 2, 2)
@@ -434,7 +453,13 @@ def measure_radiance_field_kernels(m, rays, dev, flush, steps, warmup, seed=3):
     peak = peaks.get("hbm_gbs", 6800.0)
     ach = b_bwd * n / (bwd_ms / 1e3) / 1e9
     ach_f = b_fwd * n / (fwd_ms / 1e3) / 1e9
+    counts = (offs[1:] - offs[:-1]).float()
     return {"samples": n, "fwd_ms": fwd_ms, "bwd_ms": bwd_ms,
+            "composite": {"fwd_ms": cf_ms, "bwd_ms": cb_ms, "rays": n_rays,
+                          "live_samples_per_ray": {"mean": float(counts.mean()), "max": float(counts.max())},
+                          # forward: the 28-float row + the sample index; backward: the row and the
+                          # index, 8 parked floats written and read back, the 28-float gradient row
+                          "bytes_per_sample": {"fwd": 28 * 4 + 4, "bwd": 28 * 4 + 4 + 2 * 32 + 28 * 4}},
             "roofline": {"bound": "hbm", "kernel": "fused_field_mlp_kernel<1,3,3,4,bf16> (field backward, 28-wide head)",
                          "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak, "bytes_per_sample": b_bwd,
                          "fwd_kernel": "fused_field_mlp_kernel<0,3,3,4,bf16>", "fwd_achieved": ach_f,

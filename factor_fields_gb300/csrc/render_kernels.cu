@@ -27,6 +27,11 @@ namespace ffgb {
 namespace {
 
 constexpr int kRayWarps = 8;  // warps (rays) per block
+// The compositing kernels: blocks of 4 rays, registers capped so that 7 blocks fit per SM (1,064
+// resident rays): a 4,096-ray batch runs in one wave, so the kernel lasts about as long as its
+// longest ray instead of two block generations.
+constexpr int kCompWarps = 4;
+constexpr int kCompBlocksPerSM = 7;
 
 struct RayGeo {
   float o[3], d[3], t_min, u;
@@ -393,7 +398,7 @@ __device__ __forceinline__ void sample_rgb(const float* feat_row, const float* y
 enum { kColSH = 0, kColExt = 1 };
 
 template <int kCol>
-__global__ void __launch_bounds__(kRayWarps * 32) composite_forward_kernel(
+__global__ void __launch_bounds__(kCompWarps * 32, kCompBlocksPerSM) composite_forward_kernel(
     const FFRender r, const float* __restrict__ rays, const float* __restrict__ jitter, int64_t n_rays,
     const int64_t* __restrict__ offsets, const int32_t* __restrict__ sample_idx, const float* __restrict__ feat,
     int feat_stride, const int32_t* __restrict__ white_bg, float* __restrict__ rgb_out, float* __restrict__ depth_out,
@@ -455,11 +460,56 @@ __global__ void __launch_bounds__(kRayWarps * 32) composite_forward_kernel(
   }
 }
 
+// Values of one live sample that the reverse pass needs, parked by the forward pass in the
+// sample's gradient row (which the reverse pass overwrites) when the row has >= 8 floats:
+// exclusive transmittance T, alpha, fac = 1 - alpha + 1e-10, exp(-sigma delta) delta (d alpha /
+// d sigma), d sigma / d f0, and the colour (zero below the weight threshold).
+constexpr int kPark = 8;
+
+struct Parked {
+  float T, alpha, fac, ed, dsig, c[3];
+};
+
+__device__ __forceinline__ float dsigma_df0(const FFRender& r, float f0) {
+  const float x = f0 + r.density_shift;
+  if (r.density_act == 0) return (x > 20.f) ? 1.f : sigmoidf(x);  // softplus, threshold 20
+  return x > 0.f ? 1.f : 0.f;
+}
+
+__device__ __forceinline__ void park_store(float* row, bool vec, const Parked& p) {
+  if (vec) {
+    reinterpret_cast<float4*>(row)[0] = make_float4(p.T, p.alpha, p.fac, p.ed);
+    reinterpret_cast<float4*>(row)[1] = make_float4(p.dsig, p.c[0], p.c[1], p.c[2]);
+  } else {
+    row[0] = p.T; row[1] = p.alpha; row[2] = p.fac; row[3] = p.ed;
+    row[4] = p.dsig; row[5] = p.c[0]; row[6] = p.c[1]; row[7] = p.c[2];
+  }
+}
+
+__device__ __forceinline__ Parked park_load(const float* row, bool vec) {
+  Parked p;
+  if (vec) {
+    const float4 u = reinterpret_cast<const float4*>(row)[0], v = reinterpret_cast<const float4*>(row)[1];
+    p.T = u.x; p.alpha = u.y; p.fac = u.z; p.ed = u.w;
+    p.dsig = v.x; p.c[0] = v.y; p.c[1] = v.z; p.c[2] = v.w;
+  } else {
+    p.T = row[0]; p.alpha = row[1]; p.fac = row[2]; p.ed = row[3];
+    p.dsig = row[4]; p.c[0] = row[5]; p.c[1] = row[6]; p.c[2] = row[7];
+  }
+  return p;
+}
+
 // kColExt: grad_feat rows get dL/dfeat0 in channel 0 and zeros in channels 1 .. feat_stride - 1
 // (the colour head's backward fills the channels of its samples afterwards), and
 // grad_rgb_sample [M, 3] receives dL/dcolour = w * dL/drgb (zero below the weight threshold).
+//
+// Two passes per ray (warp per ray, 32-sample chunks): the forward again (the colour before the
+// clamp decides which channels pass gradient), then the reverse scan. With rows of >= 8 floats the
+// forward pass parks what the reverse pass needs in the gradient row (struct Parked), so the
+// reverse pass reads 32 bytes per sample (the next chunk's prefetched) instead of the feature row,
+// and recomputes neither the density nor the colours; narrower rows park T alone and recompute.
 template <int kCol>
-__global__ void __launch_bounds__(kRayWarps * 32) composite_backward_kernel(
+__global__ void __launch_bounds__(kCompWarps * 32, kCompBlocksPerSM) composite_backward_kernel(
     const FFRender r, const float* __restrict__ rays, const float* __restrict__ jitter, int64_t n_rays,
     const int64_t* __restrict__ offsets, const int32_t* __restrict__ sample_idx, const float* __restrict__ feat,
     int feat_stride, const int32_t* __restrict__ white_bg, const float* __restrict__ grad_rgb,
@@ -467,6 +517,8 @@ __global__ void __launch_bounds__(kRayWarps * 32) composite_backward_kernel(
     float* __restrict__ grad_rgb_sample) {
   const int lane = threadIdx.x & 31;
   const bool vec = kCol == kColSH && rows_vec(feat, feat_stride) && rows_vec(grad_feat, feat_stride);
+  const bool park = kCol == kColSH || feat_stride >= kPark;  // SH rows are >= 28 wide
+  const bool pvec = park && rows_vec(grad_feat, feat_stride);
   for (int64_t ray = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; ray < n_rays;
        ray += ((int64_t)gridDim.x * blockDim.x) >> 5) {
     const RayGeo g = ray_setup(r, rays, jitter, ray);
@@ -474,19 +526,29 @@ __global__ void __launch_bounds__(kRayWarps * 32) composite_backward_kernel(
     sh2_basis(g.d, yb);
     const int64_t beg = offsets[ray], end = offsets[ray + 1];
     const bool wb = white_bg ? (*white_bg != 0) : (r.white_bg != 0);
-    // pass 1: the forward again (rgb before the clamp decides which channels pass gradient);
-    // the exclusive transmittance of each sample is parked in grad_feat[j][0]
+    // pass 1: the forward again; each sample's values are parked in its gradient row. The SH
+    // colour's three dot products are taken before the transmittance scan, so the 28-value row
+    // is dead during it; the sigmoid follows for the samples above the weight threshold.
     float T = 1.f, acc = 0.f, col[3] = {0.f, 0.f, 0.f};
     for (int64_t c0 = beg; c0 < end; c0 += 32) {
       const int64_t j = c0 + lane;
       const bool active = j < end;
       SampleVals s = {0.f, 0.f, 0.f, 0.f, 0.f, 1.f};
-      float row[kRow];
+      float lin[3] = {0.f, 0.f, 0.f};
       if (active) {
-        if constexpr (kCol == kColSH)
+        float row[kRow];
+        if constexpr (kCol == kColSH) {
           load_row(feat + j * feat_stride, vec, row);
-        else
+#pragma unroll
+          for (int q = 0; q < 3; ++q) {
+            float v = 0.f;
+#pragma unroll
+            for (int k = 0; k < 9; ++k) v += yb[k] * row[1 + q * 9 + k];
+            lin[q] = v;
+          }
+        } else {
           row[0] = feat[j * feat_stride];
+        }
         s = sample_vals(r, g, zd ? 0 : sample_idx[j], row, zd ? zd + 2 * j : nullptr);
       }
       float excl;
@@ -495,16 +557,24 @@ __global__ void __launch_bounds__(kRayWarps * 32) composite_backward_kernel(
       const float w = active ? s.alpha * Tj : 0.f;
       acc += w;
       if (active) {
-        grad_feat[j * feat_stride] = Tj;
+        float c[3] = {0.f, 0.f, 0.f};
         if (w > r.weight_thres) {
-          float c[3];
           if constexpr (kCol == kColSH) {
-            float lin[3];
-            sample_rgb(row, yb, c, lin);
+            c[0] = sigmoidf(lin[0]); c[1] = sigmoidf(lin[1]); c[2] = sigmoidf(lin[2]);
           } else {
             c[0] = rgb_sample[j * 3]; c[1] = rgb_sample[j * 3 + 1]; c[2] = rgb_sample[j * 3 + 2];
           }
           col[0] += w * c[0]; col[1] += w * c[1]; col[2] += w * c[2];
+        }
+        if (park) {
+          Parked p;
+          p.T = Tj; p.alpha = s.alpha; p.fac = s.fac;
+          p.ed = expf(-s.sigma * s.delta) * s.delta;
+          p.dsig = dsigma_df0(r, s.f0);
+          p.c[0] = c[0]; p.c[1] = c[1]; p.c[2] = c[2];
+          park_store(grad_feat + j * feat_stride, pvec, p);
+        } else {
+          grad_feat[j * feat_stride] = Tj;
         }
       }
       T *= prod;
@@ -520,35 +590,48 @@ __global__ void __launch_bounds__(kRayWarps * 32) composite_backward_kernel(
     // pass 2: reverse. E_j = A_j + F_j * E_{j+1} with A = dL/dw * alpha, F = fac; S_j = E_{j+1}.
     float carry = 0.f;
     const int64_t n = end - beg;
-    for (int64_t k0 = ((n - 1) / 32) * 32; n > 0 && k0 >= 0; k0 -= 32) {
+    const int64_t k_last = n > 0 ? ((n - 1) / 32) * 32 : -1;
+    Parked nxt = {};
+    if (park && k_last >= 0 && beg + k_last + lane < end) nxt = park_load(grad_feat + (beg + k_last + lane) * feat_stride, pvec);
+    for (int64_t k0 = k_last; k0 >= 0; k0 -= 32) {
       const int64_t j = beg + k0 + lane;
       const bool active = j < end;
-      SampleVals s = {0.f, 0.f, 0.f, 0.f, 0.f, 1.f};
-      float row[kRow];
-      float Tj = 0.f, c[3] = {0.f, 0.f, 0.f}, lin[3] = {0.f, 0.f, 0.f};
-      bool app = false;
-      float w = 0.f, gw = 0.f;
-      if (active) {
+      Parked p = {};
+      if (park) {
+        p = nxt;  // the next (earlier) chunk's values are loaded while this one is scanned
+        if (k0 >= 32) nxt = park_load(grad_feat + (j - 32) * feat_stride, pvec);
+      } else if (active) {
+        // narrow rows: recompute from the feature row and the parked T
+        SampleVals s;
+        float row[kRow];
         if constexpr (kCol == kColSH)
           load_row(feat + j * feat_stride, vec, row);
         else
           row[0] = feat[j * feat_stride];
         s = sample_vals(r, g, zd ? 0 : sample_idx[j], row, zd ? zd + 2 * j : nullptr);
-        Tj = grad_feat[j * feat_stride];
-        w = s.alpha * Tj;
-        app = w > r.weight_thres;
-        if (app) {
+        p.T = grad_feat[j * feat_stride];
+        p.alpha = s.alpha; p.fac = s.fac;
+        p.ed = expf(-s.sigma * s.delta) * s.delta;
+        p.dsig = dsigma_df0(r, s.f0);
+        if (s.alpha * p.T > r.weight_thres) {
           if constexpr (kCol == kColSH) {
-            sample_rgb(row, yb, c, lin);
+            float lin[3];
+            sample_rgb(row, yb, p.c, lin);
           } else {
-            c[0] = rgb_sample[j * 3]; c[1] = rgb_sample[j * 3 + 1]; c[2] = rgb_sample[j * 3 + 2];
+            p.c[0] = rgb_sample[j * 3]; p.c[1] = rgb_sample[j * 3 + 1]; p.c[2] = rgb_sample[j * 3 + 2];
           }
         }
+      }
+      float w = 0.f, gw = 0.f;
+      bool app = false;
+      if (active) {
+        w = p.alpha * p.T;
+        app = w > r.weight_thres;
 #pragma unroll
-        for (int q = 0; q < 3; ++q) gw += G[q] * (c[q] - (wb ? 1.f : 0.f));
+        for (int q = 0; q < 3; ++q) gw += G[q] * (p.c[q] - (wb ? 1.f : 0.f));
       }
       // reverse inclusive affine scan over lanes l..31: (a, f) o (a', f') = (a + f a', f f')
-      float a = active ? gw * s.alpha : 0.f, f = active ? s.fac : 1.f;
+      float a = active ? gw * p.alpha : 0.f, f = active ? p.fac : 1.f;
 #pragma unroll
       for (int o = 1; o < 32; o <<= 1) {
         const float a2 = __shfl_down_sync(0xffffffffu, a, o);
@@ -563,24 +646,24 @@ __global__ void __launch_bounds__(kRayWarps * 32) composite_backward_kernel(
       if (lane == 31) s_next = carry;
       const float new_carry = __shfl_sync(0xffffffffu, e_incl, 0);
       if (active) {
-        const float g_alpha = Tj * (gw - s_next);
-        const float g_sigma = g_alpha * expf(-s.sigma * s.delta) * s.delta;
-        const float x = s.f0 + r.density_shift;
-        float g_f0;
-        if (r.density_act == 0)
-          g_f0 = (x > 20.f) ? g_sigma : g_sigma * sigmoidf(x);
-        else
-          g_f0 = x > 0.f ? g_sigma : 0.f;
+        const float g_alpha = p.T * (gw - s_next);
+        const float g_f0 = g_alpha * p.ed * p.dsig;
         if constexpr (kCol == kColSH) {
-          float out[kRow];
-          out[0] = g_f0;
+          float gl[3];
 #pragma unroll
-          for (int q = 0; q < 3; ++q) {
-            const float gl = app ? G[q] * w * c[q] * (1.f - c[q]) : 0.f;
+          for (int q = 0; q < 3; ++q) gl[q] = app ? G[q] * w * p.c[q] * (1.f - p.c[q]) : 0.f;
+          // value m of the row: dL/dfeat0, then dL/dsh[q][k] = gl[q] * yb[k] (m = 1 + 9 q + k)
+          auto val = [&](int m) { return m == 0 ? g_f0 : gl[(m - 1) / 9] * yb[(m - 1) % 9]; };
+          float* gr = grad_feat + j * feat_stride;
+          if (vec) {
 #pragma unroll
-            for (int k = 0; k < 9; ++k) out[1 + q * 9 + k] = gl * yb[k];
+            for (int q4 = 0; q4 < kRow / 4; ++q4)
+              reinterpret_cast<float4*>(gr)[q4] = make_float4(val(4 * q4), val(4 * q4 + 1), val(4 * q4 + 2),
+                                                              val(4 * q4 + 3));
+          } else {
+#pragma unroll
+            for (int m = 0; m < kRow; ++m) gr[m] = val(m);
           }
-          store_row(grad_feat + j * feat_stride, vec, out);
         } else {
           float* gr = grad_feat + j * feat_stride;
           gr[0] = g_f0;
@@ -650,6 +733,11 @@ __global__ void __launch_bounds__(kRayWarps * 32) app_emit_kernel(int64_t n_rays
       pos += __popc(m);
     }
   }
+}
+
+int comp_blocks(int64_t n_rays) {
+  const int64_t want = ceil_div(n_rays, kCompWarps);
+  return (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)sm_count() * kCompBlocksPerSM * 4));
 }
 
 int ray_blocks(int64_t n_rays) {
@@ -737,7 +825,7 @@ cudaError_t launch_composite_forward(const FFRender& r, const float* rays, const
                                      int feat_stride, const int32_t* white_bg, float* rgb, float* depth, float* acc,
                                      const float* zd, float* w_out, cudaStream_t s) {
   if (n == 0) return cudaSuccess;
-  composite_forward_kernel<kColSH><<<ray_blocks(n), kRayWarps * 32, 0, s>>>(
+  composite_forward_kernel<kColSH><<<comp_blocks(n), kCompWarps * 32, 0, s>>>(
       r, rays, jitter, n, offsets, sample_idx, feat, feat_stride, white_bg, rgb, depth, acc, zd, w_out, nullptr);
   return cudaGetLastError();
 }
@@ -747,7 +835,7 @@ cudaError_t launch_composite_forward_rgb(const FFRender& r, const float* rays, c
                                          int feat_stride, const float* rgb_sample, const int32_t* white_bg, float* rgb,
                                          float* depth, float* acc, cudaStream_t s) {
   if (n == 0) return cudaSuccess;
-  composite_forward_kernel<kColExt><<<ray_blocks(n), kRayWarps * 32, 0, s>>>(
+  composite_forward_kernel<kColExt><<<comp_blocks(n), kCompWarps * 32, 0, s>>>(
       r, rays, jitter, n, offsets, sample_idx, feat, feat_stride, white_bg, rgb, depth, acc, nullptr, nullptr,
       rgb_sample);
   return cudaGetLastError();
@@ -774,7 +862,7 @@ cudaError_t launch_composite_backward(const FFRender& r, const float* rays, cons
                                       int feat_stride, const int32_t* white_bg, const float* grad_rgb,
                                       float* grad_feat, const float* zd, cudaStream_t s) {
   if (n == 0) return cudaSuccess;
-  composite_backward_kernel<kColSH><<<ray_blocks(n), kRayWarps * 32, 0, s>>>(
+  composite_backward_kernel<kColSH><<<comp_blocks(n), kCompWarps * 32, 0, s>>>(
       r, rays, jitter, n, offsets, sample_idx, feat, feat_stride, white_bg, grad_rgb, grad_feat, zd, nullptr, nullptr);
   return cudaGetLastError();
 }
@@ -785,7 +873,7 @@ cudaError_t launch_composite_backward_rgb(const FFRender& r, const float* rays, 
                                           const float* grad_rgb, float* grad_feat, float* grad_rgb_sample,
                                           cudaStream_t s) {
   if (n == 0) return cudaSuccess;
-  composite_backward_kernel<kColExt><<<ray_blocks(n), kRayWarps * 32, 0, s>>>(
+  composite_backward_kernel<kColExt><<<comp_blocks(n), kCompWarps * 32, 0, s>>>(
       r, rays, jitter, n, offsets, sample_idx, feat, feat_stride, white_bg, grad_rgb, grad_feat, nullptr, rgb_sample,
       grad_rgb_sample);
   return cudaGetLastError();
