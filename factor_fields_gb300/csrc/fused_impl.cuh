@@ -18,7 +18,10 @@
 //            dW0 = dH^T [X | 1] over the block's 128 points (ldmatrix.trans operands), keeping
 //            the slice in registers for the whole launch; the constant-1 column yields the
 //            bias gradient. dW1 comes from registers when out_dim == 1, else from a second
-//            block-wide MMA over H^T dO. One global atomic per weight entry per block at exit.
+//            block-wide MMA over H^T dO; then dH^T is not stored but recomputed in the
+//            block-wide phase as (W1^T dO^T) [H^T > 0] from the dO and H tiles (one tile less of
+//            shared memory: 3 blocks per SM with the 28-wide head). One global atomic per weight
+//            entry per block at exit.
 //   scatter dL/dbasis = dX * coeff, dL/dcoeff = dX * basis with float4 / float2 atomics into
 //            the float32 gradient grids (interpolation weights recomputed, never stored).
 //
@@ -120,17 +123,17 @@ struct Smem {
   __nv_bfloat16 *w0, *w0t, *w1, *w1t;
   float* b0;
   float* xf;            // [kWarps][32][LD_XF]
-  __nv_bfloat16* dh;    // [kWarps][32][LD_H]
-  __nv_bfloat16* h;     // [kWarps][32][LD_H]        (out_dim > 8)
-  __nv_bfloat16* dout;  // [kWarps][32][ld_do]       (out_dim > 8)
+  __nv_bfloat16* dh;    // [kWarps][32][LD_H]        (out_dim == 1)
+  __nv_bfloat16* h;     // [kWarps][32][LD_H]        (out_dim > 1)
+  __nv_bfloat16* dout;  // [kWarps][32][ld_do]       (out_dim > 1)
 };
 
 template <int MODE, int OUTT>
 __host__ __device__ constexpr int64_t smem_bytes() {
   int64_t b = 64 * LD_W0 * 2 + 32 * LD_W0T * 2 + 32 * LD_W1 * 2 + 64 * LD_W1T * 2 + 64 * 4;
   b += (int64_t)kWarps * 32 * LD_XF * 4;
-  if (MODE != kFwd) b += (int64_t)kWarps * 32 * LD_H * 2;
-  if (MODE != kFwd && OUTT > 1) b += (int64_t)kWarps * 32 * (LD_H + ld_do<OUTT>()) * 2;
+  if (MODE != kFwd && OUTT == 1) b += (int64_t)kWarps * 32 * LD_H * 2;                  // dH
+  if (MODE != kFwd && OUTT > 1) b += (int64_t)kWarps * 32 * (LD_H + ld_do<OUTT>()) * 2;  // H, dO
   return b;
 }
 
@@ -146,7 +149,7 @@ __device__ __forceinline__ Smem carve(unsigned char* base) {
   s.b0 = (float*)take(64 * 4);
   s.xf = (float*)take((int64_t)kWarps * 32 * LD_XF * 4);
   s.dh = s.h = s.dout = nullptr;
-  if (MODE != kFwd) s.dh = (__nv_bfloat16*)take((int64_t)kWarps * 32 * LD_H * 2);
+  if (MODE != kFwd && OUTT == 1) s.dh = (__nv_bfloat16*)take((int64_t)kWarps * 32 * LD_H * 2);
   if (MODE != kFwd && OUTT > 1) {
     s.h = (__nv_bfloat16*)take((int64_t)kWarps * 32 * LD_H * 2);
     s.dout = (__nv_bfloat16*)take((int64_t)kWarps * 32 * ld_do<OUTT>() * 2);
@@ -435,7 +438,7 @@ __global__ void __launch_bounds__(kThreads, MODE == kFwd ? 4 : 3) fused_field_ml
         // ---------------- dH = (dO W1) * [H > 0], dX = dH W0 ----------------
         // dO and dH enter their GEMMs as BF16 pairs hi + lo (two MMAs each), so the gradients
         // keep ~16 mantissa bits through the sums over outputs and hidden units.
-        __nv_bfloat16* dhw = s.dh + warp * 32 * LD_H;
+        __nv_bfloat16* dhw = s.dh + warp * 32 * LD_H;  // out_dim == 1 only (else unused)
 #pragma unroll
         for (int nt = 0; nt < kNtIn; ++nt) dx[mt][nt][0] = dx[mt][nt][1] = dx[mt][nt][2] = dx[mt][nt][3] = 0.f;
 #pragma unroll
@@ -479,9 +482,11 @@ __global__ void __launch_bounds__(kThreads, MODE == kFwd ? 4 : 3) fused_field_ml
             split_pair(dh[2 * kk + 1][0], dh[2 * kk + 1][1], d[2], dl[2]);
             split_pair(dh[2 * kk + 1][2], dh[2 * kk + 1][3], d[3], dl[3]);
             const int ks = 2 * half + kk;
-            __nv_bfloat16* p0 = dhw + r0 * LD_H + 16 * ks + 2 * t;
-            __nv_bfloat16* p1 = dhw + r1 * LD_H + 16 * ks + 2 * t;
-            sts32(p0, d[0]); sts32(p1, d[1]); sts32(p0 + 8, d[2]); sts32(p1 + 8, d[3]);
+            if constexpr (OUTT == 1) {
+              __nv_bfloat16* p0 = dhw + r0 * LD_H + 16 * ks + 2 * t;
+              __nv_bfloat16* p1 = dhw + r1 * LD_H + 16 * ks + 2 * t;
+              sts32(p0, d[0]); sts32(p1, d[1]); sts32(p0 + 8, d[2]); sts32(p1 + 8, d[3]);
+            }
             // dX += dH[:, 16 ks .. 16 ks + 15] W0[16 ks .. 16 ks + 15, :]
 #pragma unroll
             for (int nt = 0; nt < kNtIn; ++nt) {
@@ -504,10 +509,41 @@ __global__ void __launch_bounds__(kThreads, MODE == kFwd ? 4 : 3) fused_field_ml
 #pragma unroll 2
       for (int kk = 0; kk < 8; ++kk) {
         const int src = kk >> 1, h16 = (kk & 1) * 16;
-        const __nv_bfloat16* dhs = s.dh + src * 32 * LD_H;
         const float* xs = s.xf + src * 32 * LD_XF;
-        uint32_t af[4];
-        ldsm_x4_t(af, dhs + (h16 + (lane & 7) + (lane >> 4) * 8) * LD_H + 16 * warp + ((lane >> 3) & 1) * 8);
+        uint32_t af[4];  // dH^T of hidden units 16 warp .. + 15 over the 16 points: an A fragment
+        uint32_t ah[4];  // H^T of the same (out_dim > 1)
+        if constexpr (OUTT == 1) {
+          const __nv_bfloat16* dhs = s.dh + src * 32 * LD_H;
+          ldsm_x4_t(af, dhs + (h16 + (lane & 7) + (lane >> 4) * 8) * LD_H + 16 * warp + ((lane >> 3) & 1) * 8);
+        } else {
+          // no dH tile: dH^T = (W1^T dO^T) [H^T > 0], recomputed here from the dO tile (BF16) and
+          // the H tile's mask, so that 3 blocks fit per SM with the 28-wide head
+          const __nv_bfloat16* hs = s.h + src * 32 * LD_H;
+          ldsm_x4_t(ah, hs + (h16 + (lane & 7) + (lane >> 4) * 8) * LD_H + 16 * warp + ((lane >> 3) & 1) * 8);
+          const __nv_bfloat16* ds = s.dout + src * 32 * ld_do<OUTT>();
+          float c[2][4];
+#pragma unroll
+          for (int n2 = 0; n2 < 2; ++n2) c[n2][0] = c[n2][1] = c[n2][2] = c[n2][3] = 0.f;
+#pragma unroll
+          for (int ks = 0; ks < (OUTT + 1) / 2; ++ks) {  // K = the outputs, 16 per step
+            uint32_t a4[4];
+            const __nv_bfloat16* wp = s.w1t + (16 * warp + g) * LD_W1T + 16 * ks + 2 * t;
+            a4[0] = lds32(wp);
+            a4[1] = lds32(wp + 8 * LD_W1T);
+            a4[2] = lds32(wp + 8);
+            a4[3] = lds32(wp + 8 * LD_W1T + 8);
+#pragma unroll
+            for (int n2 = 0; n2 < 2; ++n2) {  // points h16 + 8 n2 .. + 7 (B = dO^T, rows of the dO tile)
+              const __nv_bfloat16* bp = ds + (h16 + 8 * n2 + g) * ld_do<OUTT>() + 16 * ks + 2 * t;
+              mma_bf16(c[n2], a4, lds32(bp), lds32(bp + 8));
+            }
+          }
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            const float* cc = c[i >> 1] + 2 * (i & 1);
+            af[i] = pack_bf16(bf_lo(ah[i]) > 0.f ? cc[0] : 0.f, bf_hi(ah[i]) > 0.f ? cc[1] : 0.f);
+          }
+        }
 #pragma unroll
         for (int nt = 0; nt < kNtIn; ++nt) {
           const int col = nt * 8 + g;
@@ -519,10 +555,7 @@ __global__ void __launch_bounds__(kThreads, MODE == kFwd ? 4 : 3) fused_field_ml
           mma_bf16(acc_w0[nt], af, b0, b1);
         }
         if constexpr (OUTT > 1) {
-          const __nv_bfloat16* hs = s.h + src * 32 * LD_H;
           const __nv_bfloat16* ds = s.dout + src * 32 * ld_do<OUTT>();
-          uint32_t ah[4];
-          ldsm_x4_t(ah, hs + (h16 + (lane & 7) + (lane >> 4) * 8) * LD_H + 16 * warp + ((lane >> 3) & 1) * 8);
 #pragma unroll
           for (int nt = 0; nt < OUTT; ++nt) {
             uint32_t bf[2];
@@ -575,8 +608,9 @@ __global__ void __launch_bounds__(kThreads, MODE == kFwd ? 4 : 3) fused_field_ml
             cc.w[b] = 0.f;
           }
         }
+        // scratch for the segment weights: this warp's dH (out_dim 1) or H tile, both consumed
         coop_coeff_scatter<CD>(a.grad_coeff, f.coeff_stride, cc, gc, valid, xf,
-                               reinterpret_cast<float*>(s.dh + warp * 32 * LD_H), lane);
+                               reinterpret_cast<float*>((OUTT == 1 ? s.dh : s.h) + warp * 32 * LD_H), lane);
       } else if (valid) {
         float gc[kF];
         const float* xr = xf + lane * LD_XF;
