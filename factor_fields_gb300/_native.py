@@ -135,6 +135,8 @@ SIGNATURES = {
                                           c_vp, c_vp, c_vp, c_vp]),
     "ff_proposal_encode": (c_i32, [_P(FFProposal), c_vp, c_vp, c_i64, c_vp, c_vp]),
     "ff_proposal_resample": (c_i32, [_P(FFProposal), c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
+    "ff_proposal_resample_occupied": (c_i32, [_P(FFProposal), _P(FFRender), c_vp, c_i64, c_vp, c_vp, c_vp, c_vp,
+                                              c_vp, c_i64, c_vp, c_vp, c_vp]),
     "ff_proposal_loss": (c_i32, [_P(FFProposal), c_vp, c_i64, c_vp, c_vp, c_vp, c_f32, c_vp, c_vp, c_vp]),
     "ff_proposal_scatter": (c_i32, [_P(FFProposal), c_vp, c_i64, c_vp, c_vp, c_vp]),
     "ff_proposal_head_forward": (c_i32, [_P(FFProposal), c_vp, _P(FFMlp), c_vp, c_i64, c_vp, c_vp]),

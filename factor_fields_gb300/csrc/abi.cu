@@ -678,6 +678,23 @@ int ff_proposal_resample(const FFProposal* p, const float* rays, int64_t n_rays,
                      "ff_proposal_resample launch");
 }
 
+int ff_proposal_resample_occupied(const FFProposal* p, const FFRender* r, const float* rays, int64_t n_rays,
+                                  const float* o_prop, const float* jitter, int32_t* counts, int64_t* offsets,
+                                  void* workspace, int64_t workspace_bytes, float* xyz, float* zd, void* stream) {
+  int rc = validate_proposal(p, rays, n_rays);
+  if (rc) return rc;
+  rc = validate_render(r, rays, n_rays);
+  if (rc) return rc;
+  if (!r->occ_bits) return set_error(FF_ERR_ARG, "ff_proposal_resample_occupied needs an occupancy volume (occ_bits)");
+  if (!offsets) return set_error(FF_ERR_ARG, "offsets is NULL");
+  if (n_rays > 0 && (!counts || !xyz || !zd)) return set_error(FF_ERR_ARG, "buffers are NULL");
+  if (workspace_bytes < scan_workspace_bytes(n_rays) || (n_rays > 0 && !workspace))
+    return set_error(FF_ERR_ARG, "workspace smaller than ff_scan_workspace_bytes(n_rays)");
+  return cuda_status(launch_proposal_resample_occupied(*p, *r, rays, n_rays, o_prop, jitter, counts, offsets, workspace,
+                                                       xyz, zd, (cudaStream_t)stream),
+                     "ff_proposal_resample_occupied launch");
+}
+
 int ff_proposal_loss(const FFProposal* p, const float* rays, int64_t n_rays, const float* o_prop,
                      const float* w_field, const int32_t* bin_of, float loss_scale, float* loss_sum, float* grad_o,
                      void* stream) {

@@ -171,6 +171,10 @@ cudaError_t launch_proposal_scatter(const FFProposal& p, const float* rays, int6
 cudaError_t launch_proposal_resample(const FFProposal& p, const float* rays, int64_t n, const float* o_prop,
                                      const float* jitter, const float* u, float* w_prop, float* xyz, float* zd,
                                      int32_t* bin_of, cudaStream_t s);
+cudaError_t launch_proposal_resample_occupied(const FFProposal& p, const FFRender& r, const float* rays, int64_t n,
+                                              const float* o_prop, const float* jitter, int32_t* counts,
+                                              int64_t* offsets, void* workspace, float* xyz, float* zd,
+                                              cudaStream_t s);
 cudaError_t launch_proposal_loss(const FFProposal& p, const float* rays, int64_t n, const float* o_prop,
                                  const float* w_field, const int32_t* bin_of, float loss_scale, float* loss_sum,
                                  float* grad_o, cudaStream_t s);

@@ -192,10 +192,25 @@ __device__ __forceinline__ float warp_sum_f(float v) {
   return v;
 }
 
+// Position of the sample at distance t along the segment's ray (one rounding per coordinate, the
+// same in every resampling mode so that the occupied rows equal the unculled ones bit for bit).
+__device__ __forceinline__ void sample_pos(const Segment& s, float t, float* x) {
+#pragma unroll
+  for (int q = 0; q < 3; ++q) x[q] = fmaf(s.d[q], t, s.o[q]);
+}
+
+// Resampling modes: every sample with its bin and the proposal weights (training and the
+// unculled render), or, for rendering through an occupancy volume, the occupied samples alone:
+// a counting pass (counts[ray]) and, after the scan of the counts, an emitting pass that writes
+// each ray's occupied samples in sample order from offsets[ray].
+enum { kResampleAll = 0, kResampleCount = 1, kResampleEmit = 2 };
+
+template <int MODE>
 __global__ void __launch_bounds__(256) proposal_resample_kernel(
-    const FFProposal p, const float* __restrict__ rays, int64_t n_rays, const float* __restrict__ o_prop,
-    const float* __restrict__ jitter, const float* __restrict__ u_given, float* __restrict__ w_prop,
-    float* __restrict__ xyz, float* __restrict__ zd, int32_t* __restrict__ bin_of) {
+    const FFProposal p, const FFRender occ, const float* __restrict__ rays, int64_t n_rays,
+    const float* __restrict__ o_prop, const float* __restrict__ jitter, const float* __restrict__ u_given,
+    float* __restrict__ w_prop, float* __restrict__ xyz, float* __restrict__ zd, int32_t* __restrict__ bin_of,
+    int32_t* __restrict__ counts, const int64_t* __restrict__ offsets) {
   __shared__ float cdf_s[8][kMaxBinsPerLane * 32 + 1];
   __shared__ float t_s[8][kMaxFine];
   __shared__ float e_s[8][kMaxFine + 1];
@@ -214,7 +229,7 @@ __global__ void __launch_bounds__(256) proposal_resample_kernel(
 #pragma unroll
     for (int b = 0; b < kMaxBinsPerLane; ++b)
       if (b < B) {
-        w_prop[ray * nb + lane * B + b] = st.w[b];
+        if constexpr (MODE == kResampleAll) w_prop[ray * nb + lane * B + b] = st.w[b];
         lsum += st.w[b] + 1e-5f;
       }
     const float tot = warp_sum_f(lsum);
@@ -259,9 +274,13 @@ __global__ void __launch_bounds__(256) proposal_resample_kernel(
       int bin;
       const float t = inv_cdf(u, bin);
       ts[i] = t;
-      bin_of[ray * nf + i] = bin;
+      if constexpr (MODE == kResampleAll) {
+        bin_of[ray * nf + i] = bin;
+        float x[3];
+        sample_pos(s, t, x);
 #pragma unroll
-      for (int q = 0; q < 3; ++q) xyz[(ray * nf + i) * 3 + q] = s.o[q] + s.d[q] * t;
+        for (int q = 0; q < 3; ++q) xyz[(ray * nf + i) * 3 + q] = x[q];
+      }
     }
     // Stratified samples (u = (i + jitter) / n_fine, or given u with p.u_stratified): sample i
     // stands for its CDF stratum [F^-1(i / n), F^-1((i + 1) / n)]; the strata tile
@@ -274,17 +293,56 @@ __global__ void __launch_bounds__(256) proposal_resample_kernel(
       }
     }
     __syncwarp();
-    for (int i = lane; i < nf; i += 32) {
-      const float t = ts[i];
-      float d;
-      if (!strata) {
-        const float nxt = (i + 1 < nf) ? ts[i + 1] : s.t_out;
-        d = nxt - t;
-      } else {
-        d = es[i + 1] - es[i];
+    if constexpr (MODE == kResampleAll) {
+      for (int i = lane; i < nf; i += 32) {
+        const float t = ts[i];
+        float d;
+        if (!strata) {
+          const float nxt = (i + 1 < nf) ? ts[i + 1] : s.t_out;
+          d = nxt - t;
+        } else {
+          d = es[i + 1] - es[i];
+        }
+        zd[(ray * nf + i) * 2 + 0] = t;
+        zd[(ray * nf + i) * 2 + 1] = fmaxf(d, 0.f);
       }
-      zd[(ray * nf + i) * 2 + 0] = t;
-      zd[(ray * nf + i) * 2 + 1] = fmaxf(d, 0.f);
+    } else {
+      // occupied samples only (AlphaGridMask's test, models/FactorFields.py:865-867): the others
+      // would have zero density, alpha 0 and weight 0, and leave the transmittance unchanged
+      int64_t pos = (MODE == kResampleEmit) ? offsets[ray] : 0;
+      int cnt = 0;
+      for (int i0 = 0; i0 < nf; i0 += 32) {
+        const int i = i0 + lane;
+        float x[3] = {0.f, 0.f, 0.f}, t = 0.f, d = 0.f;
+        bool live = false;
+        if (i < nf) {
+          t = ts[i];
+          if (!strata) {
+            const float nxt = (i + 1 < nf) ? ts[i + 1] : s.t_out;
+            d = nxt - t;
+          } else {
+            d = es[i + 1] - es[i];
+          }
+          sample_pos(s, t, x);
+          live = occupied(occ, x);
+        }
+        const uint32_t m = __ballot_sync(0xffffffffu, live);
+        if constexpr (MODE == kResampleEmit) {
+          if (live) {
+            const int64_t j = pos + __popc(m & ((1u << lane) - 1u));
+#pragma unroll
+            for (int q = 0; q < 3; ++q) xyz[j * 3 + q] = x[q];
+            zd[j * 2 + 0] = t;
+            zd[j * 2 + 1] = fmaxf(d, 0.f);
+          }
+          pos += __popc(m);
+        } else {
+          cnt += __popc(m);
+        }
+      }
+      if constexpr (MODE == kResampleCount) {
+        if (lane == 0) counts[ray] = cnt;
+      }
     }
     __syncwarp();
   }
@@ -698,8 +756,26 @@ cudaError_t launch_proposal_resample(const FFProposal& p, const float* rays, int
                                      const float* jitter, const float* u, float* w_prop, float* xyz, float* zd,
                                      int32_t* bin_of, cudaStream_t s) {
   if (n == 0) return cudaSuccess;
-  proposal_resample_kernel<<<grid_blocks(n * 32, 256), 256, 0, s>>>(p, rays, n, o_prop, jitter, u, w_prop, xyz, zd,
-                                                                    bin_of);
+  const FFRender none = {};
+  proposal_resample_kernel<kResampleAll><<<grid_blocks(n * 32, 256), 256, 0, s>>>(
+      p, none, rays, n, o_prop, jitter, u, w_prop, xyz, zd, bin_of, nullptr, nullptr);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_proposal_resample_occupied(const FFProposal& p, const FFRender& r, const float* rays, int64_t n,
+                                              const float* o_prop, const float* jitter, int32_t* counts,
+                                              int64_t* offsets, void* workspace, float* xyz, float* zd,
+                                              cudaStream_t s) {
+  if (n == 0) return cudaMemsetAsync(offsets, 0, sizeof(int64_t), s);
+  const int blocks = grid_blocks(n * 32, 256);
+  proposal_resample_kernel<kResampleCount><<<blocks, 256, 0, s>>>(p, r, rays, n, o_prop, jitter, nullptr, nullptr,
+                                                                   nullptr, nullptr, nullptr, counts, nullptr);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  e = launch_scan(counts, n, offsets, workspace, s);
+  if (e != cudaSuccess) return e;
+  proposal_resample_kernel<kResampleEmit><<<blocks, 256, 0, s>>>(p, r, rays, n, o_prop, jitter, nullptr, nullptr,
+                                                                  xyz, zd, nullptr, nullptr, offsets);
   return cudaGetLastError();
 }
 

@@ -60,33 +60,6 @@ __device__ __forceinline__ float sample_z(const FFRender& r, const RayGeo& g, in
   return __fadd_rn(g.t_min, __fmul_rn(r.step, rng));
 }
 
-// Trilinear value of the 0/1 occupancy volume at p (AlphaGridMask.sample_alpha, :103-107):
-// float32 sum of the weights of the occupied corners in ATen's corner order, zero padding.
-__device__ __forceinline__ float occupancy_value(const FFRender& r, const float* p) {
-  float ix[3];
-  int sz[3];
-#pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    sz[k] = r.occ_reso[k];
-    const float u = __fsub_rn(__fmul_rn(__fsub_rn(p[k], r.occ_origin[k]), r.occ_inv[k]), 1.f);
-    ix[k] = unnorm_align(u, sz[k]);
-  }
-  Corners<3> c;
-  linear_corners<3>(ix, sz, c);
-  float val = 0.f;
-#pragma unroll
-  for (int b = 0; b < 8; ++b) {
-    if (c.idx[b] >= 0) {
-      const uint32_t word = __ldg(r.occ_bits + (c.idx[b] >> 5));
-      if ((word >> (c.idx[b] & 31)) & 1u) val = __fadd_rn(val, c.w[b]);
-    }
-  }
-  return val;
-}
-
-// The march's mask test (:866): sample_alpha > 0.5.
-__device__ __forceinline__ bool occupied(const FFRender& r, const float* p) { return occupancy_value(r, p) > 0.5f; }
-
 // Sample i of the ray: live (in the box and, with a mask, occupied) and its position.
 __device__ __forceinline__ bool sample_live(const FFRender& r, const RayGeo& g, int i, float* p) {
   const float z = sample_z(r, g, i);

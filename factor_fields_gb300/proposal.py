@@ -71,21 +71,35 @@ class ProposalRenderFunction(torch.autograd.Function):
             # training samples stratified over the segment (a flat histogram); the network still
             # predicts o_p and learns (proposal loss) from these samples' unbiased weights
             o_sample = None
-        w_p = torch.empty(n * nb, device=dev)
         xyz = torch.empty(n * nf, 3, device=dev)
         zd = torch.empty(n * nf, 2, device=dev)
-        bin_of = torch.empty(n * nf, dtype=torch.int32, device=dev)
-        u = None
-        if job["is_train"] and sam.sample_jitter:
-            # each training sample jittered independently inside its stratum
-            u = (torch.arange(nf, device=dev, dtype=torch.float32) + torch.rand(n, nf, device=dev)) / nf
-            if pdesc is sam.desc:
-                pdesc = N.FFProposal.from_buffer_copy(sam.desc)
-            pdesc.u_stratified = 1
-        N.call("ff_proposal_resample", ctypes.byref(pdesc), N.ptr(rays), n, N.ptr(o_sample), N.ptr(job["jitter"]),
-               N.ptr(u), N.ptr(w_p), N.ptr(xyz), N.ptr(zd), N.ptr(bin_of), st)
+        w_p = bin_of = None
+        if not job["is_train"] and sam.cull_render and job["fused"] and job["rdesc"].occ_bits:
+            # rendering through the field's occupancy volume: only the samples that pass the alpha
+            # mask are evaluated and composited (the others would have zero weight); their count
+            # stays on the device, where the field kernel reads it
+            counts = torch.empty(n, dtype=torch.int32, device=dev)
+            offsets = torch.empty(n + 1, dtype=torch.int64, device=dev)
+            wsb = int(N.lib().ff_scan_workspace_bytes(n))
+            ws = torch.empty(max(wsb, 8), dtype=torch.uint8, device=dev)
+            N.call("ff_proposal_resample_occupied", ctypes.byref(pdesc), ctypes.byref(job["rdesc"]), N.ptr(rays), n,
+                   N.ptr(o_p), N.ptr(job["jitter"]), N.ptr(counts), N.ptr(offsets), N.ptr(ws), wsb, N.ptr(xyz),
+                   N.ptr(zd), st)
+            job["n_dev"] = offsets[n:]
+        else:
+            u = None
+            if job["is_train"] and sam.sample_jitter:
+                # each training sample jittered independently inside its stratum
+                u = (torch.arange(nf, device=dev, dtype=torch.float32) + torch.rand(n, nf, device=dev)) / nf
+                if pdesc is sam.desc:
+                    pdesc = N.FFProposal.from_buffer_copy(sam.desc)
+                pdesc.u_stratified = 1
+            w_p = torch.empty(n * nb, device=dev)
+            bin_of = torch.empty(n * nf, dtype=torch.int32, device=dev)
+            N.call("ff_proposal_resample", ctypes.byref(pdesc), N.ptr(rays), n, N.ptr(o_sample),
+                   N.ptr(job["jitter"]), N.ptr(u), N.ptr(w_p), N.ptr(xyz), N.ptr(zd), N.ptr(bin_of), st)
+            offsets = torch.arange(n + 1, device=dev, dtype=torch.int64) * nf
         feat = field_eval(m, job, xyz)
-        offsets = torch.arange(n + 1, device=dev, dtype=torch.int64) * nf
         rgb = torch.empty(n, 3, device=dev)
         depth = torch.empty(n, device=dev)
         w_f = torch.empty(n * nf, device=dev)
@@ -112,8 +126,14 @@ class ProposalRenderFunction(torch.autograd.Function):
 class ProposalSampler:
     def __init__(self, model, reso=64, n_bins=64, n_fine=48, hidden=64, lr_grid=2e-2, lr_mlp=1e-3,
                  density_shift=-4.0, precision="bf16", learned=True, seed=0, uniform_mix=0.0, fused_adam=True,
-                 train_uniform=True, render_fine=None, sample_jitter=True):
+                 train_uniform=True, render_fine=None, sample_jitter=True, cull_render=False):
         self.m, self.learned, self.train_uniform = model, learned, train_uniform
+        # cull_render: rendering (not training) on the fused path leaves out the samples that fail
+        # the model's alpha mask (ff_proposal_resample_occupied). Off by default: a mask built by
+        # updateAlphaMask (threshold alphaMask_thres on per-voxel alpha) also removes low-density
+        # regions that are still visible along a ray; on the blob scene a mask of the final field
+        # cost 3.5-3.8 dB for 9-12% less render time.
+        self.cull_render = cull_render
         self.render_fine = render_fine or n_fine  # samples per ray when rendering (not training)
         self.sample_jitter = sample_jitter  # training: jitter each sample in its stratum (else per ray)
         self.reso, self.n_bins, self.n_fine, self.precision = reso, n_bins, n_fine, precision
@@ -203,6 +223,9 @@ class ProposalSampler:
         job = self._job
         if job is None or not self.learned:
             return self.loss_buf[0]
+        if job["bin_of"] is None:
+            raise RuntimeError("the proposal loss needs a training render (is_train=True); the last render "
+                               "left out unoccupied samples")
         rays = job["rays"]
         n, nb = rays.shape[0], self.n_bins
         st = N.stream_ptr()

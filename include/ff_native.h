@@ -468,6 +468,22 @@ FF_API int ff_proposal_encode(const FFProposal* p, const void* grid, const float
 FF_API int ff_proposal_resample(const FFProposal* p, const float* rays, int64_t n_rays, const float* o_prop,
                                 const float* jitter, const float* u, float* w_prop, float* xyz, float* zd,
                                 int32_t* bin_of, void* stream);
+/* Rendering with the proposal through an occupancy volume: ff_proposal_resample's rendering
+ * samples (u_i = (i + jitter[ray]) / n_fine, jitter optional, 0.5 when NULL; each sample's
+ * distance is the width of its CDF stratum) with the samples that fail the alpha-mask test
+ * left out (r->occ_bits required; AlphaGridMask.sample_alpha > 0.5, models/FactorFields.py:
+ * 865-867, the test ff_march_count applies). Such samples would have zero density, hence alpha 0
+ * and weight 0, and would leave the transmittance unchanged, so compositing the kept samples
+ * with their own (z, dist) gives the render of all of them with the mask applied. Outputs are
+ * compacted per ray in sample order: counts [n_rays] int32, offsets [n_rays + 1] int64 (an
+ * exclusive scan of counts; offsets[n_rays] = M stays on the device), xyz [M, 3] and zd [M, 2]
+ * in buffers sized for n_rays * n_fine rows; the kept rows equal ff_proposal_resample's rows bit
+ * for bit. workspace: ff_scan_workspace_bytes(n_rays) bytes. Of r, the occupancy fields are used
+ * (r must pass the same validation as for ff_march_count). */
+FF_API int ff_proposal_resample_occupied(const FFProposal* p, const FFRender* r, const float* rays, int64_t n_rays,
+                                         const float* o_prop, const float* jitter, int32_t* counts, int64_t* offsets,
+                                         void* workspace, int64_t workspace_bytes, float* xyz, float* zd,
+                                         void* stream);
 /* Proposal loss sum_k max(0, m_k - w_k)^2 / (w_k + 1e-5) per ray, m_k = field weight mass in
  * bin k (w_field [n_rays * n_fine], bin_of from resample), scaled by loss_scale; loss_sum
  * (optional) accumulates the loss, grad_o [n_rays * n_bins] receives dL/do_prop. bin_of must

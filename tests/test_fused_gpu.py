@@ -304,9 +304,19 @@ def test_trained_state_against_unrounded_reference():
             first = float(lv)
         opt.step()
     x, y = W.sdf_batch(7, 16384)
+    # Points with a hidden pre-activation within 1e-3 of its magnitude scale of the ReLU kink are
+    # left out of the checked step: there the exact gradient is a step function of the inputs and
+    # the kernel's ~16-bit activations may land on either side (on the coarsest level, ~4 points
+    # per cell, one flipped unit moves a cell's gradient by several percent of the largest one).
+    spec, bg_s, cg_s, ws_s, bs_s = oracle_of(m)
+    f_s, _ = O.get_coding(spec, bg_s, cg_s, x)
+    _, pre = O.mlp_fwd(ws_s, bs_s, f_s)
+    scale = np.abs(f_s) @ np.abs(np.asarray(ws_s[0], np.float64)).T + np.abs(np.asarray(bs_s[0], np.float64))
+    keep = (np.abs(pre[0]) > 1e-3 * scale).all(axis=1)
+    assert keep.mean() > 0.5
+    x, y = np.ascontiguousarray(x[keep]), np.ascontiguousarray(y[keep])
     loss = float(runner.step(torch.from_numpy(x).cuda(), torch.from_numpy(y).cuda()))
     assert loss < 0.5 * first  # the model did train
-    spec, _, _, _, _ = oracle_of(m)
     bg = [b[0].detach().cpu().numpy() for b in m.basises]  # float32 masters, unrounded
     cg = m.coeffs[0][0].detach().cpu().numpy()
     ws, bs = m.linear_mat.weights()

@@ -164,6 +164,119 @@ def test_resample_is_sample_pdf():
     assert np.all((b >= 0) & (b < nb))
 
 
+def _ball_mask(m, reso=32, seed=9):
+    """An occupancy mask on m: six random balls in a reso^3 volume over m's aabb; returns the
+    0/1 volume [D, H, W]."""
+    from factor_fields_gb300.renderer import AlphaGridMask
+    rng = np.random.default_rng(seed)
+    g = (np.arange(reso) + 0.5) / reso * 2 - 1
+    zz, yy, xx = np.meshgrid(g, g, g, indexing="ij")
+    vol = np.zeros((reso,) * 3, np.float32)
+    for _ in range(6):
+        c, r = rng.uniform(-0.7, 0.7, 3), rng.uniform(0.15, 0.4)
+        vol[(xx - c[0]) ** 2 + (yy - c[1]) ** 2 + (zz - c[2]) ** 2 < r * r] = 1
+    m.alphaMask = AlphaGridMask(m.device, m.aabb.detach().clone(), torch.from_numpy(vol))
+    return vol
+
+
+def test_resample_occupied_keeps_the_occupied_rows():
+    """ff_proposal_resample_occupied = ff_proposal_resample's rendering samples with the rows that
+    fail the alpha-mask test (the oracle's occupancy_test, models/FactorFields.py:865-867) left
+    out: counts, offsets and the kept rows bit-exact, in sample order."""
+    from factor_fields_gb300 import _native as N
+    from factor_fields_gb300.renderer import render_desc
+    m, s = make_sampler()
+    vol = _ball_mask(m)
+    rays = rays_np(300, 8)
+    rt = torch.from_numpy(rays).cuda()
+    n, nb, nf = rays.shape[0], s.n_bins, s.n_fine
+    rng = np.random.default_rng(5)
+    o_t = torch.from_numpy((rng.standard_normal((n, nb)) * 3).astype(np.float32)).cuda()
+    st = N.stream_ptr()
+    w_p = torch.empty(n * nb, device="cuda")
+    xyz = torch.empty(n * nf, 3, device="cuda")
+    zd = torch.empty(n * nf, 2, device="cuda")
+    bin_of = torch.empty(n * nf, dtype=torch.int32, device="cuda")
+    N.call("ff_proposal_resample", ctypes.byref(s.desc), N.ptr(rt), n, N.ptr(o_t), None, None, N.ptr(w_p),
+           N.ptr(xyz), N.ptr(zd), N.ptr(bin_of), st)
+    rd = render_desc(m, 1024, True)
+    counts = torch.full((n,), -1, dtype=torch.int32, device="cuda")
+    offsets = torch.full((n + 1,), -1, dtype=torch.int64, device="cuda")
+    wsb = int(N.lib().ff_scan_workspace_bytes(n))
+    ws = torch.empty(max(wsb, 8), dtype=torch.uint8, device="cuda")
+    xo = torch.full((n * nf, 3), float("nan"), device="cuda")
+    zo = torch.full((n * nf, 2), float("nan"), device="cuda")
+    N.call("ff_proposal_resample_occupied", ctypes.byref(s.desc), ctypes.byref(rd), N.ptr(rt), n, N.ptr(o_t), None,
+           N.ptr(counts), N.ptr(offsets), N.ptr(ws), wsb, N.ptr(xo), N.ptr(zo), st)
+    torch.cuda.synchronize()
+    xa, za = xyz.cpu().numpy(), zd.cpu().numpy()
+    occ = O.occupancy_test(vol, m.alphaMask.aabb.cpu().numpy(), xa).reshape(n, nf)
+    assert 0.05 < occ.mean() < 0.95
+    np.testing.assert_array_equal(counts.cpu().numpy(), occ.sum(1))
+    off = np.concatenate([[0], np.cumsum(occ.sum(1))])
+    np.testing.assert_array_equal(offsets.cpu().numpy(), off)
+    keep = occ.reshape(-1)
+    np.testing.assert_array_equal(xo[:off[-1]].cpu().numpy(), xa[keep])
+    np.testing.assert_array_equal(zo[:off[-1]].cpu().numpy(), za[keep])
+    # no rays: offsets[0] = 0 and nothing else
+    offsets.fill_(-1)
+    N.call("ff_proposal_resample_occupied", ctypes.byref(s.desc), ctypes.byref(rd), N.ptr(rt), 0, N.ptr(o_t), None,
+           N.ptr(counts), N.ptr(offsets), N.ptr(ws), wsb, N.ptr(xo), N.ptr(zo), st)
+    assert int(offsets[0]) == 0 and int(offsets[1]) == -1
+    # without an occupancy volume the call is refused
+    rd.occ_bits = None
+    with pytest.raises(N.NativeError):
+        N.call("ff_proposal_resample_occupied", ctypes.byref(s.desc), ctypes.byref(rd), N.ptr(rt), n, N.ptr(o_t),
+               None, N.ptr(counts), N.ptr(offsets), N.ptr(ws), wsb, N.ptr(xo), N.ptr(zo), st)
+
+
+def test_render_through_the_mask_equals_zero_density_samples():
+    """A proposal render that evaluates only the occupied samples equals the render of every
+    sample with the unoccupied samples' density set to zero (what the reference's alpha mask
+    does, models/FactorFields.py:865-870): rgb and depth within 1e-5 (float32 compositing sums
+    in a different lane order)."""
+    from factor_fields_gb300 import _native as N
+    from factor_fields_gb300.renderer import field_eval, render_desc
+    m, s = make_sampler(precision="bf16")
+    s.cull_render = True
+    m.cfg.renderer.density_shift = 0.0  # a random field with partly opaque rays
+    vol = _ball_mask(m)
+    rays = rays_np(512, 9)
+    rt = torch.from_numpy(rays).cuda()
+    n, nb, nf = rays.shape[0], s.n_bins, s.n_fine
+    with torch.no_grad():
+        rgb, depth = s.render(rt, is_train=False)
+    # every sample, the unoccupied ones with zero density (softplus of -1e30 is 0)
+    st = N.stream_ptr()
+    o_p = torch.empty(n * nb, 1, device="cuda")
+    N.call("ff_proposal_head_forward", ctypes.byref(s.desc), N.ptr(s.grid_read()), ctypes.byref(s.mlp_struct()),
+           N.ptr(rt), n, N.ptr(o_p), st)
+    w_p = torch.empty(n * nb, device="cuda")
+    xyz = torch.empty(n * nf, 3, device="cuda")
+    zd = torch.empty(n * nf, 2, device="cuda")
+    bin_of = torch.empty(n * nf, dtype=torch.int32, device="cuda")
+    N.call("ff_proposal_resample", ctypes.byref(s.desc), N.ptr(rt), n, N.ptr(o_p), None, None, N.ptr(w_p),
+           N.ptr(xyz), N.ptr(zd), N.ptr(bin_of), st)
+    basis_r, coeff_r, dt = m._read_buffers()
+    job = {"fused": True, "fdesc": m.descriptor(dt), "basis_r": basis_r, "coeff_r": coeff_r}
+    feat = field_eval(m, job, xyz)
+    occ = O.occupancy_test(vol, m.alphaMask.aabb.cpu().numpy(), xyz.cpu().numpy())
+    assert 0.05 < occ.mean() < 0.95
+    feat[torch.from_numpy(~occ).cuda(), 0] = -1e30
+    rd = render_desc(m, s.n_fine, True)
+    offsets = torch.arange(n + 1, device="cuda", dtype=torch.int64) * nf
+    rgb_ref = torch.empty(n, 3, device="cuda")
+    depth_ref = torch.empty(n, device="cuda")
+    w_f = torch.empty(n * nf, device="cuda")
+    N.call("ff_composite_forward_zd", ctypes.byref(rd), N.ptr(rt), n, N.ptr(offsets), N.ptr(zd), N.ptr(feat),
+           feat.shape[1], N.ptr(rgb_ref), N.ptr(depth_ref), N.ptr(w_f), st)
+    torch.cuda.synchronize()
+    acc = w_f.view(n, nf).sum(1).cpu().numpy()
+    assert (acc > 0.2).mean() > 0.2 and (acc < 0.8).mean() > 0.2  # partly opaque rays
+    assert float((rgb - rgb_ref).abs().max()) < 1e-5
+    assert float((depth - depth_ref).abs().max()) < 1e-5 * float(depth_ref.abs().max())
+
+
 def test_proposal_loss_gradient_matches_finite_differences():
     from factor_fields_gb300 import _native as N
     m, s = make_sampler()
