@@ -544,6 +544,16 @@ def run_radiance(args, dev):
                "eval_400x400": {"ms_per_image": e_extra["ms_per_image"][0], "psnr_db": e_psnr[0],
                                 "ssim": e_extra["ssim"][0],
                                 "rays_per_s": 400 * 400 / (e_extra["ms_per_image"][0] / 1e3)}}
+        if sampler is not None:
+            # the same with 32 render samples per ray (the configuration resamples 48)
+            sampler.render_fine = 32
+            evaluation(eval_ds, m, N_vis=-1, N_samples=1024, white_bg=True, sampler=sampler)  # warm-up
+            p32, x32 = evaluation(eval_ds, m, N_vis=-1, N_samples=1024, white_bg=True, sampler=sampler)
+            rec["render_32"] = {"psnr_db": tr.psnr(test, gtt), "samples_per_ray": 32,
+                                "eval_400x400": {"ms_per_image": x32["ms_per_image"][0], "psnr_db": p32[0],
+                                                 "ssim": x32["ssim"][0],
+                                                 "rays_per_s": 400 * 400 / (x32["ms_per_image"][0] / 1e3)}}
+            sampler.render_fine = sampler.n_fine
         if sampler is None:
             offs, _, _ = march(m, test, None, render_desc(m, 1024, True))
             rec["live_samples_per_ray"] = float(offs[-1]) / test.shape[0]
@@ -562,15 +572,23 @@ def run_radiance(args, dev):
     # against the plain sampler's ~125 live samples after occupancy pruning
     out["proposal_eval_rays_per_s_vs_plain"] = (out["cfg3_proposal"]["eval_400x400"]["rays_per_s"] /
                                                 out["cfg2_plain"]["eval_400x400"]["rays_per_s"])
-    seeds = {0: {k: out[k]["psnr_db"] for k in ("cfg2_plain", "cfg3_proposal")}}
+    out["proposal_eval_rays_per_s_vs_plain_32"] = (out["cfg3_proposal"]["render_32"]["eval_400x400"]["rays_per_s"] /
+                                                   out["cfg2_plain"]["eval_400x400"]["rays_per_s"])
+    seeds = {0: {"cfg2_plain": out["cfg2_plain"]["psnr_db"], "cfg3_proposal": out["cfg3_proposal"]["psnr_db"],
+                 "cfg3_proposal_32": out["cfg3_proposal"]["render_32"]["psnr_db"]}}
     if args.psnr_seeds > 1:
         for seed in range(1, args.psnr_seeds):
-            seeds[seed] = {k: _train_radiance(k, seed, iters, pool, gt, dev)[2].psnr(test, gtt)
-                           for k in ("cfg2_plain", "cfg3_proposal")}
+            seeds[seed] = {"cfg2_plain": _train_radiance("cfg2_plain", seed, iters, pool, gt, dev)[2].psnr(test, gtt)}
+            _, sam, trp, _ = _train_radiance("cfg3_proposal", seed, iters, pool, gt, dev)
+            seeds[seed]["cfg3_proposal"] = trp.psnr(test, gtt)
+            sam.render_fine = 32
+            seeds[seed]["cfg3_proposal_32"] = trp.psnr(test, gtt)
     diffs = [v["cfg3_proposal"] - v["cfg2_plain"] for v in seeds.values()]
+    diffs32 = [v["cfg3_proposal_32"] - v["cfg2_plain"] for v in seeds.values()]
     out["psnr_db_by_seed"] = {str(k): v for k, v in seeds.items()}
     out["proposal_psnr_minus_plain_db"] = float(np.mean(diffs))
     out["proposal_psnr_minus_plain_db_by_seed"] = diffs
+    out["proposal_32_psnr_minus_plain_db_by_seed"] = diffs32
     out["scene"] = "seeded 32 Gaussian density blobs in [-1.5,1.5]^3, 100 views 400x400 focal 555, white bg"
     return out
 

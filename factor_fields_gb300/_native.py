@@ -23,6 +23,7 @@ FF_F32, FF_BF16 = 0, 1
 FF_LOSS = {"l1": 0, "mse": 1}
 FF_FIT_ZERO_GRADS = 1
 FF_FIT_MEAN_LOSS = 2
+FF_FIT_LEVEL0_SHARED = 4
 FF_ADAM_ZERO_GRAD = 1
 
 c_i32, c_i64, c_f32, c_vp = ctypes.c_int32, ctypes.c_int64, ctypes.c_float, ctypes.c_void_p

@@ -297,7 +297,7 @@ static int validate_fit_on_bins(const FFField* f, const void* basis, const void*
   if (loss_kind != FF_LOSS_L1 && loss_kind != FF_LOSS_MSE) return set_error(FF_ERR_ARG, "loss_kind must be L1 or MSE");
   if (!grad_basis || !grad_coeff_grid || !aligned(grad_basis, 16) || !aligned(grad_coeff_grid, 16))
     return set_error(FF_ERR_ARG, "grid gradient buffers must be non-NULL and 16-byte aligned");
-  if (flags & ~FF_FIT_MEAN_LOSS) return set_error(FF_ERR_ARG, "unknown flags");
+  if (flags & ~(FF_FIT_MEAN_LOSS | FF_FIT_LEVEL0_SHARED)) return set_error(FF_ERR_ARG, "unknown flags");
   const int64_t need = ff_field_fit_binned_workspace_bytes(f, n, m->out_dim);
   if (need < 0) return set_error((int)need, "coefficient grid too large to bin by cell");
   if (!workspace) return set_error(FF_ERR_ARG, "workspace is NULL");
@@ -310,9 +310,10 @@ int ff_field_fit_step_binned(const FFField* f, const void* basis, const void* co
                              const float* target, int64_t n, int32_t loss_kind, float loss_scale, float* loss_sum,
                              float* grad_basis, float* grad_coeff_grid, const FFMlpGrad* g, int32_t flags,
                              void* workspace, int64_t workspace_bytes, void* stream) {
-  if (flags & ~(FF_FIT_ZERO_GRADS | FF_FIT_MEAN_LOSS)) return set_error(FF_ERR_ARG, "unknown flags");
+  if (flags & ~(FF_FIT_ZERO_GRADS | FF_FIT_MEAN_LOSS | FF_FIT_LEVEL0_SHARED))
+    return set_error(FF_ERR_ARG, "unknown flags");
   int rc = validate_fit_on_bins(f, basis, coeff, m, n, loss_kind, grad_basis, grad_coeff_grid,
-                                flags & FF_FIT_MEAN_LOSS, workspace, workspace_bytes);
+                                flags & (FF_FIT_MEAN_LOSS | FF_FIT_LEVEL0_SHARED), workspace, workspace_bytes);
   if (rc) return rc;
   rc = validate_fit_bin(f, m, x, target, n, grad_basis, grad_coeff_grid, flags & FF_FIT_ZERO_GRADS, workspace,
                         workspace_bytes);
@@ -321,7 +322,8 @@ int ff_field_fit_step_binned(const FFField* f, const void* basis, const void* co
   return cuda_status(launch_fused_fit_binned(*f, basis, coeff, *m, x, target, n, loss_kind, loss_scale, loss_sum,
                                              grad_basis, grad_coeff_grid, g ? *g : none, workspace,
                                              (flags & FF_FIT_ZERO_GRADS) != 0,
-                                             (flags & FF_FIT_MEAN_LOSS) ? loss_scale : 1.f, (cudaStream_t)stream),
+                                             (flags & FF_FIT_MEAN_LOSS) ? loss_scale : 1.f,
+                                             (flags & FF_FIT_LEVEL0_SHARED) != 0, (cudaStream_t)stream),
                      "ff_field_fit_step_binned launch");
 }
 
@@ -348,7 +350,8 @@ int ff_field_fit_step_on_bins(const FFField* f, const void* basis, const void* c
   FFMlpGrad none = {};
   return cuda_status(launch_fit_on_bins(*f, basis, coeff, *m, n, loss_kind, loss_scale, loss_sum, grad_basis,
                                         grad_coeff_grid, g ? *g : none, workspace,
-                                        (flags & FF_FIT_MEAN_LOSS) ? loss_scale : 1.f, (cudaStream_t)stream),
+                                        (flags & FF_FIT_MEAN_LOSS) ? loss_scale : 1.f,
+                                        (flags & FF_FIT_LEVEL0_SHARED) != 0, (cudaStream_t)stream),
                      "ff_field_fit_step_on_bins launch");
 }
 
@@ -672,7 +675,7 @@ int ff_proposal_resample(const FFProposal* p, const float* rays, int64_t n_rays,
                          void* stream) {
   int rc = validate_proposal(p, rays, n_rays);
   if (rc) return rc;
-  if (n_rays > 0 && (!w_prop || !xyz || !zd || !bin_of)) return set_error(FF_ERR_ARG, "buffers are NULL");
+  if (n_rays > 0 && (!xyz || !zd)) return set_error(FF_ERR_ARG, "xyz/zd are NULL");
   return cuda_status(launch_proposal_resample(*p, rays, n_rays, o_prop, jitter, u, w_prop, xyz, zd, bin_of,
                                               (cudaStream_t)stream),
                      "ff_proposal_resample launch");

@@ -56,14 +56,16 @@ cudaError_t launch_fused_fit_rows(const FFField& f, const void* basis, const voi
 cudaError_t launch_fused_fit_binned(const FFField& f, const void* basis, const void* coeff, const FFMlp& m,
                                     const float* x, const float* target, int64_t n, int loss_kind, float loss_scale,
                                     float* loss_sum, float* grad_basis, float* grad_coeff, const FFMlpGrad& g,
-                                    void* workspace, bool zero_grads, float loss_mul, cudaStream_t st);
+                                    void* workspace, bool zero_grads, float loss_mul, bool level0_shared,
+                                    cudaStream_t st);
 // its two halves: binning (with the gradient zeroing) and the fit kernel on the binned rows
 cudaError_t launch_fit_bin_phase(const FFField& f, const FFMlp& m, const float* x, const float* target, int64_t n,
                                  float* loss_sum, float* grad_basis, float* grad_coeff, const FFMlpGrad& g,
                                  void* workspace, bool zero_grads, cudaStream_t st);
 cudaError_t launch_fit_on_bins(const FFField& f, const void* basis, const void* coeff, const FFMlp& m, int64_t n,
                                int loss_kind, float loss_scale, float* loss_sum, float* grad_basis, float* grad_coeff,
-                               const FFMlpGrad& g, const void* workspace, float loss_mul, cudaStream_t st);
+                               const FFMlpGrad& g, const void* workspace, float loss_mul, bool level0_shared,
+                               cudaStream_t st);
 
 // fit_bin_kernels.cu
 int64_t fit_bin_keys(const FFField& f);

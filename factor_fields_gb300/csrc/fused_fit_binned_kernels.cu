@@ -27,7 +27,8 @@ cudaError_t launch_fit_bin_phase(const FFField& f, const FFMlp& m, const float* 
 
 cudaError_t launch_fit_on_bins(const FFField& f, const void* basis, const void* coeff, const FFMlp& m, int64_t n,
                                int loss_kind, float loss_scale, float* loss_sum, float* grad_basis, float* grad_coeff,
-                               const FFMlpGrad& g, const void* workspace, float loss_mul, cudaStream_t st) {
+                               const FFMlpGrad& g, const void* workspace, float loss_mul, bool level0_shared,
+                               cudaStream_t st) {
   if (n == 0) return cudaSuccess;
   int64_t stride = 0;
   const float* rows = fit_bin_rows(f, n, m.out_dim, workspace, &stride);
@@ -48,18 +49,20 @@ cudaError_t launch_fit_on_bins(const FFField& f, const void* basis, const void* 
   a.grad_w0 = g.weight[0];
   a.grad_b0 = g.bias[0];
   a.grad_w1 = g.weight[1];
+  a.level0_shared = level0_shared ? 1 : 0;
   return dispatch_bf16<kFitBinned>(a, st);
 }
 
 cudaError_t launch_fused_fit_binned(const FFField& f, const void* basis, const void* coeff, const FFMlp& m,
                                     const float* x, const float* target, int64_t n, int loss_kind, float loss_scale,
                                     float* loss_sum, float* grad_basis, float* grad_coeff, const FFMlpGrad& g,
-                                    void* workspace, bool zero_grads, float loss_mul, cudaStream_t st) {
+                                    void* workspace, bool zero_grads, float loss_mul, bool level0_shared,
+                                    cudaStream_t st) {
   cudaError_t e = launch_fit_bin_phase(f, m, x, target, n, loss_sum, grad_basis, grad_coeff, g, workspace, zero_grads,
                                        st);
   if (e != cudaSuccess) return e;
   return launch_fit_on_bins(f, basis, coeff, m, n, loss_kind, loss_scale, loss_sum, grad_basis, grad_coeff, g,
-                            workspace, loss_mul, st);
+                            workspace, loss_mul, level0_shared, st);
 }
 
 }  // namespace ffgb

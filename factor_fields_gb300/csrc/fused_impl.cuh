@@ -24,6 +24,9 @@
 //            entry per block at exit.
 //   scatter dL/dbasis = dX * coeff, dL/dcoeff = dX * basis with float4 / float2 atomics into
 //            the float32 gradient grids (interpolation weights recomputed, never stored).
+//            Binned 2-D fits can keep the level-0 basis gradients (<= 32^2 cells x 4 channels)
+//            block-private in shared memory instead: shared-memory atomics per point and one
+//            float4 atomic per touched cell when the block ends (FF_FIT_LEVEL0_SHARED).
 //
 // Level structure is compile-time: basis_dims = [4, 4, 4, 2, 2, 2] (sum 18), which keeps each
 // point's 18 basis and 18 coefficient values in registers between the gather and the scatter.
@@ -98,7 +101,11 @@ struct FusedArgs {
   float* grad_w0;
   float* grad_b0;
   float* grad_w1;
+  int level0_shared;  // binned 2-D fits: level-0 basis gradients accumulated in shared memory
 };
+
+// Level-0 gradients in shared memory: at most this many float32 values (32^2 cells x 4 channels).
+constexpr int kL0Floats = 4096;
 
 // A-fragment register pair (hi, lo) for two consecutive float32 features of the X tile;
 // columns at or past LD_XF read as zero.
@@ -126,18 +133,20 @@ struct Smem {
   __nv_bfloat16* dh;    // [kWarps][32][LD_H]        (out_dim == 1)
   __nv_bfloat16* h;     // [kWarps][32][LD_H]        (out_dim > 1)
   __nv_bfloat16* dout;  // [kWarps][32][ld_do]       (out_dim > 1)
+  float* g0;            // [kL0Floats] level-0 basis gradients (level0-shared variant)
 };
 
-template <int MODE, int OUTT>
+template <int MODE, int OUTT, bool L0S = false>
 __host__ __device__ constexpr int64_t smem_bytes() {
   int64_t b = 64 * LD_W0 * 2 + 32 * LD_W0T * 2 + 32 * LD_W1 * 2 + 64 * LD_W1T * 2 + 64 * 4;
   b += (int64_t)kWarps * 32 * LD_XF * 4;
   if (MODE != kFwd && OUTT == 1) b += (int64_t)kWarps * 32 * LD_H * 2;                  // dH
   if (MODE != kFwd && OUTT > 1) b += (int64_t)kWarps * 32 * (LD_H + ld_do<OUTT>()) * 2;  // H, dO
+  if (L0S) b += (int64_t)kL0Floats * 4;
   return b;
 }
 
-template <int MODE, int OUTT>
+template <int MODE, int OUTT, bool L0S = false>
 __device__ __forceinline__ Smem carve(unsigned char* base) {
   Smem s;
   unsigned char* p = base;
@@ -154,7 +163,23 @@ __device__ __forceinline__ Smem carve(unsigned char* base) {
     s.h = (__nv_bfloat16*)take((int64_t)kWarps * 32 * LD_H * 2);
     s.dout = (__nv_bfloat16*)take((int64_t)kWarps * 32 * ld_do<OUTT>() * 2);
   }
+  s.g0 = L0S ? (float*)take((int64_t)kL0Floats * 4) : nullptr;
   return s;
+}
+
+// Level-0 basis gradients (4 channels) of one point into the block's shared-memory copy; the
+// corner set lies inside the level (basis_corners_fast), so every index is below the level's
+// cell count.
+template <int D>
+__device__ __forceinline__ void scatter_shared4(float* g0, const Corners<D>& cn, const float* g) {
+#pragma unroll
+  for (int k = 0; k < Corners<D>::K; ++k) {
+    if (cn.w[k] != 0.f) {
+      float* p = g0 + cn.idx[k] * 4;
+#pragma unroll
+      for (int v = 0; v < 4; ++v) atomicAdd(p + v, g[v] * cn.w[k]);
+    }
+  }
 }
 
 // ---- segment-cooperative coefficient scatter (binned batches) ----------------------------
@@ -223,11 +248,11 @@ __device__ __forceinline__ void coop_coeff_scatter(float* __restrict__ grad, int
 
 // ---- the kernel -------------------------------------------------------------------------
 
-template <int MODE, int BD, int CD, int OUTT, typename T>
+template <int MODE, int BD, int CD, int OUTT, typename T, bool L0S = false>
 __global__ void __launch_bounds__(kThreads, MODE == kFwd ? 4 : 3) fused_field_mlp_kernel(const FusedArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, g = lane >> 2, t = lane & 3;
-  const Smem s = carve<MODE, OUTT>(smem_raw);
+  const Smem s = carve<MODE, OUTT, L0S>(smem_raw);
   const FFField& f = a.f;
   const int out = a.out_dim;
   // fits of one output on packed 16-byte rows (x, y, z, target): one load per point
@@ -250,6 +275,9 @@ __global__ void __launch_bounds__(kThreads, MODE == kFwd ? 4 : 3) fused_field_ml
     s.w1t[hh * LD_W1T + o] = v;
   }
   for (int j = tid; j < 64; j += kThreads) s.b0[j] = a.b0[j];
+  if constexpr (L0S) {
+    for (int e = tid; e < kL0Floats / 4; e += kThreads) reinterpret_cast<float4*>(s.g0)[e] = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
   __syncthreads();
 
   float loss_acc = 0.f;
@@ -597,7 +625,10 @@ __global__ void __launch_bounds__(kThreads, MODE == kFwd ? 4 : 3) fused_field_ml
             Corners<BD> bc;
             basis_corners_fast<BD>(f, l, p, bc);
             constexpr int C = kLevelC[l], OFF = kLevelOff[l];
-            scatter_inside<C, BD>(a.grad_basis + f.level_offset[l], f.level_stride[l], bc, bv + OFF);
+            if constexpr (L0S && l == 0)
+              scatter_shared4<BD>(s.g0, bc, bv + OFF);
+            else
+              scatter_inside<C, BD>(a.grad_basis + f.level_offset[l], f.level_stride[l], bc, bv + OFF);
           });
         } else {
 #pragma unroll
@@ -628,13 +659,27 @@ __global__ void __launch_bounds__(kThreads, MODE == kFwd ? 4 : 3) fused_field_ml
           Corners<BD> bc;
           basis_corners_fast<BD>(f, l, p, bc);
           constexpr int C = kLevelC[l], OFF = kLevelOff[l];
-          scatter_inside<C, BD>(a.grad_basis + f.level_offset[l], f.level_stride[l], bc, bv + OFF);
+          if constexpr (L0S && l == 0)
+            scatter_shared4<BD>(s.g0, bc, bv + OFF);
+          else
+            scatter_inside<C, BD>(a.grad_basis + f.level_offset[l], f.level_stride[l], bc, bv + OFF);
         });
       }
       __syncwarp();
     }
   }
 
+  if constexpr (L0S) {
+    // the block's level-0 gradients: one float4 atomic per touched cell (every block runs the
+    // same number of tile iterations, so all threads reach this barrier)
+    __syncthreads();
+    const int cells = f.level_reso[0] * f.level_reso[0];
+    float4* dst = reinterpret_cast<float4*>(a.grad_basis + f.level_offset[0]);
+    for (int e = tid; e < cells; e += kThreads) {
+      const float4 v = reinterpret_cast<const float4*>(s.g0)[e];
+      if (v.x != 0.f || v.y != 0.f || v.z != 0.f || v.w != 0.f) atomicAdd(dst + e, v);
+    }
+  }
   if constexpr (MODE != kFwd) {
     if constexpr (is_fit<MODE>()) {
 #pragma unroll
@@ -682,10 +727,10 @@ __global__ void __launch_bounds__(kThreads, MODE == kFwd ? 4 : 3) fused_field_ml
   }
 }
 
-template <int MODE, int BD, int CD, int OUTT, typename T>
-cudaError_t launch_one(const FusedArgs& a, cudaStream_t st) {
-  constexpr int64_t smem = smem_bytes<MODE, OUTT>();
-  auto kern = fused_field_mlp_kernel<MODE, BD, CD, OUTT, T>;
+template <int MODE, int BD, int CD, int OUTT, typename T, bool L0S>
+cudaError_t launch_kernel(const FusedArgs& a, cudaStream_t st) {
+  constexpr int64_t smem = smem_bytes<MODE, OUTT, L0S>();
+  auto kern = fused_field_mlp_kernel<MODE, BD, CD, OUTT, T, L0S>;
   // the shared-memory opt-in and the occupancy query, once per process and device (atomic cache
   // entries: threads racing on the first launch repeat the same idempotent set-up)
   static std::atomic<int> per_sm_cache[64];
@@ -707,6 +752,20 @@ cudaError_t launch_one(const FusedArgs& a, cudaStream_t st) {
   const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>(tiles, (int64_t)sm_count() * per_sm));
   kern<<<blocks, kThreads, smem, st>>>(a);
   return cudaGetLastError();
+}
+
+// Level-0 gradients in shared memory: binned BF16 fits of a 2-D basis whose level 0 (4 channels,
+// stride 4) has at most kL0Floats / 4 cells.
+inline bool level0_fits_shared(const FFField& f) {
+  return f.basis_dim == 2 && f.level_stride[0] == 4 && (int64_t)f.level_reso[0] * f.level_reso[0] * 4 <= kL0Floats;
+}
+
+template <int MODE, int BD, int CD, int OUTT, typename T>
+cudaError_t launch_one(const FusedArgs& a, cudaStream_t st) {
+  if constexpr (MODE == kFitBinned && BD == 2 && std::is_same<T, __nv_bfloat16>::value) {
+    if (a.level0_shared && level0_fits_shared(a.f)) return launch_kernel<MODE, BD, CD, OUTT, T, true>(a, st);
+  }
+  return launch_kernel<MODE, BD, CD, OUTT, T, false>(a, st);
 }
 
 template <int MODE, int OUTT, typename T>

@@ -229,7 +229,7 @@ __global__ void __launch_bounds__(256) proposal_resample_kernel(
 #pragma unroll
     for (int b = 0; b < kMaxBinsPerLane; ++b)
       if (b < B) {
-        if constexpr (MODE == kResampleAll) w_prop[ray * nb + lane * B + b] = st.w[b];
+        if (MODE == kResampleAll && w_prop) w_prop[ray * nb + lane * B + b] = st.w[b];
         lsum += st.w[b] + 1e-5f;
       }
     const float tot = warp_sum_f(lsum);
@@ -275,7 +275,7 @@ __global__ void __launch_bounds__(256) proposal_resample_kernel(
       const float t = inv_cdf(u, bin);
       ts[i] = t;
       if constexpr (MODE == kResampleAll) {
-        bin_of[ray * nf + i] = bin;
+        if (bin_of) bin_of[ray * nf + i] = bin;
         float x[3];
         sample_pos(s, t, x);
 #pragma unroll

@@ -94,8 +94,9 @@ class ProposalRenderFunction(torch.autograd.Function):
                 if pdesc is sam.desc:
                     pdesc = N.FFProposal.from_buffer_copy(sam.desc)
                 pdesc.u_stratified = 1
-            w_p = torch.empty(n * nb, device=dev)
-            bin_of = torch.empty(n * nf, dtype=torch.int32, device=dev)
+            if job["is_train"]:  # the proposal loss reads the weights and bins; a render does not
+                w_p = torch.empty(n * nb, device=dev)
+                bin_of = torch.empty(n * nf, dtype=torch.int32, device=dev)
             N.call("ff_proposal_resample", ctypes.byref(pdesc), N.ptr(rays), n, N.ptr(o_sample),
                    N.ptr(job["jitter"]), N.ptr(u), N.ptr(w_p), N.ptr(xyz), N.ptr(zd), N.ptr(bin_of), st)
             offsets = torch.arange(n + 1, device=dev, dtype=torch.int64) * nf
@@ -224,8 +225,7 @@ class ProposalSampler:
         if job is None or not self.learned:
             return self.loss_buf[0]
         if job["bin_of"] is None:
-            raise RuntimeError("the proposal loss needs a training render (is_train=True); the last render "
-                               "left out unoccupied samples")
+            raise RuntimeError("the proposal loss needs a training render (is_train=True)")
         rays = job["rays"]
         n, nb = rays.shape[0], self.n_bins
         st = N.stream_ptr()

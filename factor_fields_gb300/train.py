@@ -154,13 +154,17 @@ class FieldFitRunner:
     in PyTorch. Gradients land in the model's .grad buffers; step() returns the mean loss as a
     0-d device tensor (no host synchronisation)."""
 
-    def __init__(self, model, loss="l1", fused=True, binned=None):
+    def __init__(self, model, loss="l1", fused=True, binned=None, level0_shared=False):
         if loss not in N.FF_LOSS:
             raise ValueError("loss must be 'l1' or 'mse'")
         self.m, self.loss, self.fused = model, loss, fused
         self.binned = fused if binned is None else bool(binned)
         if self.binned and not fused:
             raise ValueError("binned=True needs fused=True")
+        # binned 2-D fits: level-0 basis gradients summed per block in shared memory
+        # (FF_FIT_LEVEL0_SHARED; no effect where the kernel does not support it)
+        self.level0_shared = bool(level0_shared)
+        self._l0 = N.FF_FIT_LEVEL0_SHARED if self.level0_shared else 0
         self._ws = None
         self._ws_gen = 0
         # the fused kernel's template arguments: mode, basis dim, coordinate dim, 8-wide output tiles
@@ -327,14 +331,14 @@ class FieldFitRunner:
                 ev[1].record()
                 N.call("ff_field_fit_step_on_bins", ctypes.byref(desc), N.ptr(basis_r), N.ptr(coeff_r),
                        ctypes.byref(mlp), n, N.FF_LOSS[self.loss], scale, N.ptr(lbuf), gb, gc, ctypes.byref(g),
-                       N.FF_FIT_MEAN_LOSS, N.ptr(ws), ws.numel(), st)
+                       N.FF_FIT_MEAN_LOSS | self._l0, N.ptr(ws), ws.numel(), st)
             else:
                 if ev:
                     ev[1].record()
                 common = (ctypes.byref(desc), N.ptr(basis_r), N.ptr(coeff_r), ctypes.byref(mlp), N.ptr(x), N.ptr(y),
                           n, N.FF_LOSS[self.loss], scale, N.ptr(lbuf), gb, gc, ctypes.byref(g))
                 if self.binned:  # kernels: bin (+ gradient and loss zeroing), alloc, permute, fit (mean loss)
-                    N.call("ff_field_fit_step_binned", *common, N.FF_FIT_ZERO_GRADS | N.FF_FIT_MEAN_LOSS,
+                    N.call("ff_field_fit_step_binned", *common, N.FF_FIT_ZERO_GRADS | N.FF_FIT_MEAN_LOSS | self._l0,
                            N.ptr(ws), ws.numel(), st, kernels=4)
                 else:
                     N.call("ff_field_fit_step", *common, st)

@@ -60,7 +60,7 @@ enum { FF_INTERP_LINEAR = 0, FF_INTERP_NEAREST = 1 };
 enum { FF_F32 = 0, FF_BF16 = 1 };
 enum { FF_LOSS_L1 = 0, FF_LOSS_MSE = 1 };
 /* ff_field_fit_step_binned flags */
-enum { FF_FIT_ZERO_GRADS = 1, FF_FIT_MEAN_LOSS = 2 };
+enum { FF_FIT_ZERO_GRADS = 1, FF_FIT_MEAN_LOSS = 2, FF_FIT_LEVEL0_SHARED = 4 };
 
 /*
  * Description of one grid/grid factor field (models/FactorFields.py:262-309 setup_params,
@@ -201,6 +201,11 @@ FF_API int ff_field_fit_step(const FFField* f, const void* basis, const void* co
  * zero_grad without a launch of its own); otherwise they are accumulated into (+=).
  * FF_FIT_MEAN_LOSS: *loss_sum accumulates loss_scale * sum of the per-element losses (with
  * loss_scale = 1 / (n * out_dim) the mean loss itself) instead of the plain sum.
+ * FF_FIT_LEVEL0_SHARED (BF16 grids, 2-D basis whose level 0 has 4 channels and at most 32^2
+ * cells; without effect otherwise): each block of the fit kernel accumulates its level-0 basis
+ * gradients in shared memory and adds them to grad_basis once, one float4 atomic per touched
+ * cell, instead of one global atomic per point and corner. Same gradients up to float32
+ * summation order.
  * workspace: device memory of at least ff_field_fit_binned_workspace_bytes(f, n, out_dim)
  * bytes, 256-byte aligned, not shared with a call in flight. */
 FF_API int64_t ff_field_fit_binned_workspace_bytes(const FFField* f, int64_t n, int32_t out_dim);
@@ -216,7 +221,7 @@ FF_API int ff_field_fit_step_binned(const FFField* f, const void* basis, const v
  * (grad_basis, grad_coeff_grid, g and loss_sum are touched only by that zeroing; the grids' values
  * are not read, so f alone describes them). ff_field_fit_step_on_bins: the fit on the rows that the
  * last ff_field_fit_bin call on this workspace wrote for the same f, n and m->out_dim, in stream
- * order; flags: FF_FIT_MEAN_LOSS. */
+ * order; flags: FF_FIT_MEAN_LOSS, FF_FIT_LEVEL0_SHARED. */
 FF_API int ff_field_fit_bin(const FFField* f, const FFMlp* m, const float* x, const float* target, int64_t n,
                             float* loss_sum, float* grad_basis, float* grad_coeff_grid, const FFMlpGrad* g,
                             int32_t flags, void* workspace, int64_t workspace_bytes, void* stream);
@@ -464,7 +469,8 @@ FF_API int ff_proposal_encode(const FFProposal* p, const void* grid, const float
  * zd [n_rays * n_fine, 2] (z, the width of the sample's CDF stratum [F^-1(i / n_fine), F^-1((i+1) / n_fine)]
  * for stratified u; with u given, the distance to the next sample / the segment end), bin_of [.] int32.
  * u: optional [n_rays * n_fine] uniforms; else u_i = (i + jitter[ray]) / n_fine (jitter
- * optional, 0.5 when NULL). o_prop NULL: a flat histogram (stratified samples over the segment). */
+ * optional, 0.5 when NULL). o_prop NULL: a flat histogram (stratified samples over the segment).
+ * w_prop and bin_of (needed by ff_proposal_loss only) may be NULL: not written. */
 FF_API int ff_proposal_resample(const FFProposal* p, const float* rays, int64_t n_rays, const float* o_prop,
                                 const float* jitter, const float* u, float* w_prop, float* xyz, float* zd,
                                 int32_t* bin_of, void* stream);

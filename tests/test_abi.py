@@ -114,7 +114,7 @@ def test_binned_fit_halves_validate_their_flags(lib):
     assert lib.ff_field_fit_step_on_bins(*args_fit, N.FF_FIT_MEAN_LOSS, ws, need - 1, None) == N.FF_ERR_SIZE
     assert lib.ff_field_fit_step_on_bins(*args_fit, N.FF_FIT_MEAN_LOSS, vp(128), need, None) == N.FF_ERR_ALIGN
     assert lib.ff_field_fit_step_binned(ctypes.byref(desc), vp(16), vp(16), ctypes.byref(mlp), vp(16), vp(16), n,
-                                        N.FF_LOSS["l1"], 1.0 / n, vp(16), vp(16), vp(16), ctypes.byref(g), 4, ws, need,
+                                        N.FF_LOSS["l1"], 1.0 / n, vp(16), vp(16), vp(16), ctypes.byref(g), 8, ws, need,
                                         None) == N.FF_ERR_ARG
 
 

@@ -88,6 +88,47 @@ def test_field_mlp_fwd_bwd_golden(case, precision):
 @pytest.mark.parametrize("loss", ["l1", "mse"])
 @pytest.mark.parametrize("key", ["cfg0", "cfg1", "cfg2", "cfg4"])
 def test_fit_step_full_size(key, loss, binned):
+    _fit_step_full_size(key, loss, binned)
+
+
+@pytest.mark.parametrize("loss", ["l1", "mse"])
+@pytest.mark.parametrize("key", ["cfg0", "cfg4"])
+def test_fit_step_level0_shared_full_size(key, loss):
+    """The binned 2-D fit with the level-0 basis gradients summed per block in shared memory
+    (FF_FIT_LEVEL0_SHARED) against the FP64 oracle, like the global-atomic fit."""
+    _fit_step_full_size(key, loss, True, level0_shared=True)
+
+
+def test_level0_shared_equals_global_atomics():
+    """FF_FIT_LEVEL0_SHARED changes only where the level-0 gradient sums are formed: loss and every
+    gradient equal the global-atomic binned fit's up to float32 summation order (1e-5 of the
+    largest entry, element-wise above a 1e-6 floor)."""
+    from factor_fields_gb300 import FactorFields
+    from factor_fields_gb300 import workloads as W
+    from factor_fields_gb300.train import FieldFitRunner
+    from gpu_util import assert_close
+    xs, ys = W.image_set_batch(5, 65536)
+    x, y = torch.from_numpy(xs).cuda(), torch.from_numpy(ys).cuda()
+    res = []
+    for l0 in (False, True):
+        torch.manual_seed(0)
+        m = FactorFields(W.field_cfg("cfg4"), device="cuda", precision="bf16")
+        with torch.no_grad():
+            m.coeff_flat.copy_(torch.rand(m.coeff_flat.shape, generator=torch.Generator().manual_seed(3)).cuda() * 2 - 1)
+        r = FieldFitRunner(m, loss="mse", level0_shared=l0)
+        loss = float(r.step(x, y))
+        res.append((loss, m.basis_flat.grad.clone(), m.coeff_flat.grad.clone(),
+                    [p.grad.clone() for p in m.linear_mat.parameters()]))
+    (l_a, gb_a, gc_a, gw_a), (l_b, gb_b, gc_b, gw_b) = res
+    assert abs(l_a - l_b) <= 1e-5 * abs(l_a)
+    assert float(gb_a.abs().max()) > 0
+    assert_close(gb_b, gb_a.cpu().numpy(), 1e-5, 1e-6)
+    assert_close(gc_b, gc_a.cpu().numpy(), 1e-5, 1e-6)
+    for a, b in zip(gw_a, gw_b):
+        assert_close(b, a.cpu().numpy(), 1e-5, 1e-6)
+
+
+def _fit_step_full_size(key, loss, binned, level0_shared=False):
     from factor_fields_gb300 import FactorFields
     from factor_fields_gb300 import workloads as W
     from factor_fields_gb300.train import FieldFitRunner
@@ -119,7 +160,7 @@ def test_fit_step_full_size(key, loss, binned):
         g_out = 2 * err / err.size
         loss_ref = (err * err).mean()
     _, ref = oracle_fwd_bwd(m, x, g_out)
-    runner = FieldFitRunner(m, loss=loss, fused=True, binned=binned)
+    runner = FieldFitRunner(m, loss=loss, fused=True, binned=binned, level0_shared=level0_shared)
     lv = runner.step(torch.from_numpy(x).cuda(), torch.from_numpy(y).cuda())
     torch.cuda.synchronize()
     assert abs(float(lv) - loss_ref) <= FWD_TOL * abs(loss_ref)
