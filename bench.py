@@ -791,6 +791,71 @@ def run_reference_arm(args, ws):
             "e2e": {"value": value, "unit": "samples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+def run_profile_case(case, level0_shared, dev):
+    """One small workload for an ncu capture (ncu --profile-from-start off): the launches to capture
+    run between torch.cuda.profiler.start() and stop(), after warm-up launches outside them.
+      fit:cfg0 / fit:cfg1 / fit:cfg4  one binned fit step of the configuration (its batch size)
+      radiance_fwd    the 28-wide field forward on a 4,096-ray batch's live samples (plain sampler,
+                      300 training steps, occupancy volume updated at step 100)
+      proposal_render the proposal head and resampling of a 400x400 view (160,000 rays, 32 samples)"""
+    from factor_fields_gb300 import workloads as W
+    from factor_fields_gb300 import train as T
+    if case.startswith("fit:"):
+        key = case[4:]
+        fc = FIELD_CONFIGS[key]
+        x, y = field_batches(key, 0, 1)[0]
+        x, y = torch.from_numpy(x).to(dev), torch.from_numpy(y).to(dev)
+        r = T.FieldFitRunner(make_model("bf16", key), loss=fc["loss"], level0_shared=level0_shared)
+        for _ in range(3):
+            r.step(x, y)
+        torch.cuda.synchronize()
+        torch.cuda.profiler.start()
+        r.step(x, y)
+    elif case == "radiance_fwd":
+        from factor_fields_gb300 import FactorFields
+        from factor_fields_gb300.renderer import field_eval, march, render_desc
+        scene = W.BlobScene(0)
+        pool = torch.from_numpy(scene.ray_pool(1 << 16, 5)).float()
+        gt = scene.render_gt(pool.double().numpy(), n_steps=256).to(dev)
+        pool = pool.to(dev)
+        torch.manual_seed(0)
+        m = FactorFields(W.field_cfg("cfg2"), device=dev, precision="bf16")
+        tr = T.RadianceFieldTrainer(m, n_samples=1024, n_iters=300)
+        g = torch.Generator(device=dev).manual_seed(0)
+        for it in range(300):
+            idx = torch.randint(0, pool.shape[0], (4096,), device=dev, generator=g)
+            tr.step(pool[idx], gt[idx])
+            if it == 100:
+                m.updateAlphaMask((128, 128, 128), is_update_alphaMask=True, times=1)
+        idx = torch.randint(0, pool.shape[0], (4096,), device=dev, generator=g)
+        _, xyz, _ = march(m, pool[idx], None, render_desc(m, 1024, True))
+        basis_r, coeff_r, dt = m._read_buffers()
+        job = {"fused": True, "fdesc": m.descriptor(dt), "basis_r": basis_r, "coeff_r": coeff_r}
+        for _ in range(3):
+            field_eval(m, job, xyz)
+        torch.cuda.synchronize()
+        torch.cuda.profiler.start()
+        field_eval(m, job, xyz)
+    elif case == "proposal_render":
+        from factor_fields_gb300 import FactorFields
+        from factor_fields_gb300.proposal import ProposalSampler
+        torch.manual_seed(0)
+        m = FactorFields(W.field_cfg("cfg2"), device=dev, precision="bf16")
+        s = ProposalSampler(m, seed=0, render_fine=32)
+        rays = torch.from_numpy(W.BlobScene(0).ray_pool(160000, 6, views=[7])).float().to(dev)
+        with torch.no_grad():
+            for _ in range(3):
+                s.render(rays, is_train=False)
+            torch.cuda.synchronize()
+            torch.cuda.profiler.start()
+            s.render(rays, is_train=False)
+    else:
+        raise SystemExit(f"unknown --profile-case {case!r}")
+    torch.cuda.synchronize()
+    torch.cuda.profiler.stop()
+    print(json.dumps({"profile_case": case, "level0_shared": level0_shared, "ok": True}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -806,7 +871,15 @@ def main():
                     help="measure the MLPRender_Fea tensor-core head alone (prints its JSON record)")
     ap.add_argument("--render-iters", type=int, default=1500)
     ap.add_argument("--psnr-seeds", type=int, default=3, help="training seeds of the PSNR comparison")
+    ap.add_argument("--profile-case", default=None,
+                    help="run one small workload for an ncu capture and exit (see run_profile_case)")
+    ap.add_argument("--level0-shared", action="store_true", help="--profile-case fit:*: FF_FIT_LEVEL0_SHARED")
     args = ap.parse_args()
+    if args.profile_case:
+        dev = torch.device("cuda", 0)
+        torch.cuda.set_device(dev)
+        run_profile_case(args.profile_case, args.level0_shared, dev)
+        return 0
     ws, rank, local = dist_env()
     if args.impl == "reference":
         if rank != 0:

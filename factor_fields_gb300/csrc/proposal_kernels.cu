@@ -286,7 +286,7 @@ __global__ void __launch_bounds__(256) proposal_resample_kernel(
     // stands for its CDF stratum [F^-1(i / n), F^-1((i + 1) / n)]; the strata tile
     // [t_in, t_out]. Other given u: the distance to the next sample (the last one to t_out).
     const bool strata = !u_given || p.u_stratified;
-    if (strata) {
+    if (strata && MODE != kResampleCount) {  // the counting pass needs positions only
       for (int i = lane; i <= nf; i += 32) {
         int bin;
         es[i] = i == 0 ? s.t_in : (i == nf ? s.t_out : inv_cdf((float)i / (float)nf, bin));
@@ -317,11 +317,13 @@ __global__ void __launch_bounds__(256) proposal_resample_kernel(
         bool live = false;
         if (i < nf) {
           t = ts[i];
-          if (!strata) {
-            const float nxt = (i + 1 < nf) ? ts[i + 1] : s.t_out;
-            d = nxt - t;
-          } else {
-            d = es[i + 1] - es[i];
+          if constexpr (MODE == kResampleEmit) {
+            if (!strata) {
+              const float nxt = (i + 1 < nf) ? ts[i + 1] : s.t_out;
+              d = nxt - t;
+            } else {
+              d = es[i + 1] - es[i];
+            }
           }
           sample_pos(s, t, x);
           live = occupied(occ, x);

@@ -56,6 +56,28 @@ def test_no_alloc_scan_matches_workspace_scan_twice():
         assert torch.equal(got, ref), n
 
 
+def test_no_alloc_scan_leaves_device_memory_unchanged():
+    """After a first call on the device (which may load the library's module and with it the
+    scratch array), a call changes neither the free device memory nor torch's allocations."""
+    lib = _lib()
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    n = 300_001
+    counts = torch.randint(0, 50, (n,), dtype=torch.int32, device="cuda")
+    out = torch.empty(n + 1, dtype=torch.int64, device="cuda")
+    assert lib.ff_scan_counts_noalloc(ctypes.c_void_p(counts.data_ptr()), n, ctypes.c_void_p(out.data_ptr()), stream) == 0
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    alloc0 = torch.cuda.memory_allocated()
+    counts.random_(0, 50)
+    assert lib.ff_scan_counts_noalloc(ctypes.c_void_p(counts.data_ptr()), n, ctypes.c_void_p(out.data_ptr()), stream) == 0
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
+    assert torch.cuda.memory_allocated() == alloc0
+    ref = torch.zeros(n + 1, dtype=torch.int64, device="cuda")
+    ref[1:] = torch.cumsum(counts.long(), 0)
+    assert torch.equal(out, ref)
+
+
 def test_no_alloc_scan_limits():
     lib = _lib()
     stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
