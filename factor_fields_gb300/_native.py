@@ -141,6 +141,9 @@ SIGNATURES = {
     "ff_proposal_loss": (c_i32, [_P(FFProposal), c_vp, c_i64, c_vp, c_vp, c_vp, c_f32, c_vp, c_vp, c_vp]),
     "ff_proposal_scatter": (c_i32, [_P(FFProposal), c_vp, c_i64, c_vp, c_vp, c_vp]),
     "ff_proposal_head_forward": (c_i32, [_P(FFProposal), c_vp, _P(FFMlp), c_vp, c_i64, c_vp, c_vp]),
+    "ff_field_render_fixed": (c_i32, [_P(FFField), c_vp, c_vp, _P(FFMlp), _P(FFRender), c_vp, c_vp, c_vp, c_i64,
+                                      c_i32, c_vp, c_vp, c_vp]),
+    "ff_proposal_head_infer": (c_i32, [_P(FFProposal), c_vp, _P(FFMlp), c_vp, c_i64, c_vp, c_vp]),
     "ff_proposal_head_backward": (c_i32, [_P(FFProposal), c_vp, _P(FFMlp), c_vp, c_i64, c_vp, c_vp,
                                           _P(FFMlpGrad), c_vp]),
 }

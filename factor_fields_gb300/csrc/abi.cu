@@ -207,6 +207,26 @@ int ff_field_mlp_forward(const FFField* f, const void* basis, const void* coeff,
                      "ff_field_mlp_forward launch");
 }
 
+int ff_field_render_fixed(const FFField* f, const void* basis, const void* coeff, const FFMlp* m, const FFRender* r,
+                          const float* rays, const float* xyz, const float* zd, int64_t n_rays, int32_t n_fine,
+                          float* rgb, float* depth, void* stream) {
+  if (n_fine != 32 && n_fine != 64 && n_fine != 128)
+    return set_error(FF_ERR_UNSUPPORTED, "ff_field_render_fixed: n_fine must be 32, 64 or 128");
+  if (n_rays < 0 || n_rays > (int64_t(1) << 40)) return set_error(FF_ERR_ARG, "bad ray count");
+  int rc = validate_fused(f, basis, coeff, m, xyz, n_rays * n_fine);
+  if (rc) return rc;
+  if (m->out_dim != 28 || f->coord_dim != 3)
+    return set_error(FF_ERR_UNSUPPORTED,
+                     "ff_field_render_fixed composites 3-D points with a 28-wide head (density + degree-2 SH colour)");
+  rc = validate_render(r, rays, n_rays);
+  if (rc) return rc;
+  if (n_rays > 0 && (!zd || !rgb)) return set_error(FF_ERR_ARG, "zd/rgb are NULL");
+  if (!aligned(zd, 8)) return set_error(FF_ERR_ALIGN, "zd must be 8-byte aligned");
+  return cuda_status(launch_fused_render_fixed(*f, basis, coeff, *m, *r, rays, xyz, zd, n_rays, n_fine, rgb, depth,
+                                               (cudaStream_t)stream),
+                     "ff_field_render_fixed launch");
+}
+
 int ff_field_mlp_backward(const FFField* f, const void* basis, const void* coeff, const FFMlp* m, const float* x,
                           int64_t n, const float* grad_out, float* grad_basis, float* grad_coeff_grid,
                           const FFMlpGrad* g, void* stream) {
@@ -738,6 +758,16 @@ int ff_proposal_head_forward(const FFProposal* p, const void* grid, const FFMlp*
   if (n_rays > 0 && !o_prop) return set_error(FF_ERR_ARG, "o_prop is NULL");
   return cuda_status(launch_proposal_head_forward(*p, grid, *m, rays, n_rays, o_prop, (cudaStream_t)stream),
                      "ff_proposal_head_forward launch");
+}
+
+int ff_proposal_head_infer(const FFProposal* p, const void* grid, const FFMlp* m, const float* rays, int64_t n_rays,
+                           float* o_prop, void* stream) {
+  int rc = validate_head(p, grid, m, rays, n_rays);
+  if (rc) return rc;
+  if (p->param_dtype != FF_BF16) return set_error(FF_ERR_UNSUPPORTED, "ff_proposal_head_infer reads a BF16 grid");
+  if (n_rays > 0 && !o_prop) return set_error(FF_ERR_ARG, "o_prop is NULL");
+  return cuda_status(launch_proposal_head_infer(*p, grid, *m, rays, n_rays, o_prop, (cudaStream_t)stream),
+                     "ff_proposal_head_infer launch");
 }
 
 int ff_proposal_head_backward(const FFProposal* p, const void* grid, const FFMlp* m, const float* rays,

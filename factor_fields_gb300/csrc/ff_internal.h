@@ -58,6 +58,10 @@ cudaError_t launch_fused_fit_binned(const FFField& f, const void* basis, const v
                                     float* loss_sum, float* grad_basis, float* grad_coeff, const FFMlpGrad& g,
                                     void* workspace, bool zero_grads, float loss_mul, bool level0_shared,
                                     cudaStream_t st);
+// fused_render_kernels.cu: field forward + compositing of rays with exactly nf samples each
+cudaError_t launch_fused_render_fixed(const FFField& f, const void* basis, const void* coeff, const FFMlp& m,
+                                      const FFRender& r, const float* rays, const float* xyz, const float* zd,
+                                      int64_t n_rays, int nf, float* rgb, float* depth, cudaStream_t st);
 // its two halves: binning (with the gradient zeroing) and the fit kernel on the binned rows
 cudaError_t launch_fit_bin_phase(const FFField& f, const FFMlp& m, const float* x, const float* target, int64_t n,
                                  float* loss_sum, float* grad_basis, float* grad_coeff, const FFMlpGrad& g,
@@ -163,6 +167,8 @@ cudaError_t launch_render_head_tc_backward(const FFRenderMlp& h, const float* fe
 // proposal_kernels.cu
 cudaError_t launch_proposal_head_forward(const FFProposal& p, const void* grid, const FFMlp& m, const float* rays,
                                          int64_t n, float* o_out, cudaStream_t s);
+cudaError_t launch_proposal_head_infer(const FFProposal& p, const void* grid, const FFMlp& m, const float* rays,
+                                       int64_t n, float* o_out, cudaStream_t s);
 cudaError_t launch_proposal_head_backward(const FFProposal& p, const void* grid, const FFMlp& m, const float* rays,
                                           int64_t n, const float* g_o, float* grad_grid, const FFMlpGrad& gr,
                                           cudaStream_t s);

@@ -37,6 +37,7 @@
 #include <type_traits>
 #include <utility>
 
+#include "composite_common.cuh"
 #include "ff_common.cuh"
 #include "ff_internal.h"
 #include "mma_util.cuh"
@@ -70,10 +71,18 @@ constexpr int ld_do() { return OUTT == 2 ? 24 : 40; }
 
 // kFitBinned: kFit on a batch binned by coefficient cell (fit_bin_kernels.cu); only the
 // coefficient scatter differs (segment-cooperative, see coop_coeff_scatter).
-enum { kFwd = 0, kBwd = 1, kFit = 2, kFitBinned = 3 };
+// kRender: kFwd on rays of exactly nf samples each (ray-major points), the outputs composited in
+// the epilogue instead of written out (see the render epilogue below).
+enum { kFwd = 0, kBwd = 1, kFit = 2, kFitBinned = 3, kRender = 4 };
 
 template <int MODE>
 constexpr bool is_fit() { return MODE == kFit || MODE == kFitBinned; }
+
+template <int MODE>
+constexpr bool is_fwd() { return MODE == kFwd || MODE == kRender; }
+
+constexpr int LD_OUT = 29;  // kRender: float32 output tile [32 samples][29] per warp (odd: conflict-free rows)
+constexpr int kPartStride = 8;  // kRender: per-warp chunk partials (product, acc, depth, rgb) in shared memory
 
 struct FusedArgs {
   FFField f;
@@ -102,6 +111,14 @@ struct FusedArgs {
   float* grad_b0;
   float* grad_w1;
   int level0_shared;  // binned 2-D fits: level-0 basis gradients accumulated in shared memory
+  // kRender: the points are the samples of rays of exactly nf samples (32, 64 or 128), ray r at
+  // rows [r nf, (r + 1) nf); rd's density and colour rules, each sample's (z, dist) in zd
+  FFRender rd;
+  const float* rays;  // [n / nf, 6]
+  const float* zd;    // [n, 2]
+  int nf;
+  float* rgb;    // [n / nf, 3]
+  float* depth;  // [n / nf] or NULL
 };
 
 // Level-0 gradients in shared memory: at most this many float32 values (32^2 cells x 4 channels).
@@ -134,15 +151,18 @@ struct Smem {
   __nv_bfloat16* h;     // [kWarps][32][LD_H]        (out_dim > 1)
   __nv_bfloat16* dout;  // [kWarps][32][ld_do]       (out_dim > 1)
   float* g0;            // [kL0Floats] level-0 basis gradients (level0-shared variant)
+  float* ob;            // kRender: [kWarps][32][LD_OUT] MLP outputs
+  float* part;          // kRender: [kWarps][kPartStride] chunk partials
 };
 
 template <int MODE, int OUTT, bool L0S = false>
 __host__ __device__ constexpr int64_t smem_bytes() {
   int64_t b = 64 * LD_W0 * 2 + 32 * LD_W0T * 2 + 32 * LD_W1 * 2 + 64 * LD_W1T * 2 + 64 * 4;
   b += (int64_t)kWarps * 32 * LD_XF * 4;
-  if (MODE != kFwd && OUTT == 1) b += (int64_t)kWarps * 32 * LD_H * 2;                  // dH
-  if (MODE != kFwd && OUTT > 1) b += (int64_t)kWarps * 32 * (LD_H + ld_do<OUTT>()) * 2;  // H, dO
+  if (!is_fwd<MODE>() && OUTT == 1) b += (int64_t)kWarps * 32 * LD_H * 2;                  // dH
+  if (!is_fwd<MODE>() && OUTT > 1) b += (int64_t)kWarps * 32 * (LD_H + ld_do<OUTT>()) * 2;  // H, dO
   if (L0S) b += (int64_t)kL0Floats * 4;
+  if (MODE == kRender) b += (int64_t)kWarps * 32 * LD_OUT * 4 + (int64_t)kWarps * kPartStride * 4;
   return b;
 }
 
@@ -158,12 +178,17 @@ __device__ __forceinline__ Smem carve(unsigned char* base) {
   s.b0 = (float*)take(64 * 4);
   s.xf = (float*)take((int64_t)kWarps * 32 * LD_XF * 4);
   s.dh = s.h = s.dout = nullptr;
-  if (MODE != kFwd && OUTT == 1) s.dh = (__nv_bfloat16*)take((int64_t)kWarps * 32 * LD_H * 2);
-  if (MODE != kFwd && OUTT > 1) {
+  if (!is_fwd<MODE>() && OUTT == 1) s.dh = (__nv_bfloat16*)take((int64_t)kWarps * 32 * LD_H * 2);
+  if (!is_fwd<MODE>() && OUTT > 1) {
     s.h = (__nv_bfloat16*)take((int64_t)kWarps * 32 * LD_H * 2);
     s.dout = (__nv_bfloat16*)take((int64_t)kWarps * 32 * ld_do<OUTT>() * 2);
   }
   s.g0 = L0S ? (float*)take((int64_t)kL0Floats * 4) : nullptr;
+  s.ob = s.part = nullptr;
+  if (MODE == kRender) {
+    s.ob = (float*)take((int64_t)kWarps * 32 * LD_OUT * 4);
+    s.part = (float*)take((int64_t)kWarps * kPartStride * 4);
+  }
   return s;
 }
 
@@ -249,7 +274,7 @@ __device__ __forceinline__ void coop_coeff_scatter(float* __restrict__ grad, int
 // ---- the kernel -------------------------------------------------------------------------
 
 template <int MODE, int BD, int CD, int OUTT, typename T, bool L0S = false>
-__global__ void __launch_bounds__(kThreads, MODE == kFwd ? 4 : 3) fused_field_mlp_kernel(const FusedArgs a) {
+__global__ void __launch_bounds__(kThreads, is_fwd<MODE>() ? 4 : 3) fused_field_mlp_kernel(const FusedArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, g = lane >> 2, t = lane & 3;
   const Smem s = carve<MODE, OUTT, L0S>(smem_raw);
@@ -386,7 +411,7 @@ __global__ void __launch_bounds__(kThreads, MODE == kFwd ? 4 : 3) fused_field_ml
           }
         }
       }
-      if constexpr (MODE != kFwd && OUTT > 1) {
+      if constexpr (!is_fwd<MODE>() && OUTT > 1) {
         __nv_bfloat16* hw = s.h + warp * 32 * LD_H;
 #pragma unroll
         for (int ks = 0; ks < 4; ++ks) {
@@ -405,6 +430,19 @@ __global__ void __launch_bounds__(kThreads, MODE == kFwd ? 4 : 3) fused_field_ml
             if (c0 + j < out) {
               if (row0 < n_pts) a.out[row0 * out + c0 + j] = oc[nt][j];
               if (row1 < n_pts) a.out[row1 * out + c0 + j] = oc[nt][2 + j];
+            }
+          }
+        }
+      } else if constexpr (MODE == kRender) {
+        float* ob = s.ob + warp * 32 * LD_OUT;
+#pragma unroll
+        for (int nt = 0; nt < OUTT; ++nt) {
+          const int c0 = nt * 8 + 2 * t;
+#pragma unroll
+          for (int j = 0; j < 2; ++j) {
+            if (c0 + j < out) {
+              ob[r0 * LD_OUT + c0 + j] = oc[nt][j];
+              ob[r1 * LD_OUT + c0 + j] = oc[nt][2 + j];
             }
           }
         }
@@ -529,6 +567,69 @@ __global__ void __launch_bounds__(kThreads, MODE == kFwd ? 4 : 3) fused_field_ml
     }
     if constexpr (MODE == kFwd) {
       __syncwarp();
+      continue;
+    } else if constexpr (MODE == kRender) {
+      // ---------------- compositing (ff_composite_forward_zd's rules) ----------------
+      // Lane j takes sample j of the warp's tile. A ray's nf samples fill nf / 32 consecutive
+      // warps of the block (tiles are 128-aligned and nf divides 128); its chunks chain their
+      // transmittance through shared memory in chunk order, as the compositing kernel does.
+      __syncwarp();
+      const int64_t i = base + warp * 32 + lane;
+      const bool live = base + warp * 32 < n_pts;  // n_pts is a multiple of nf, hence of 32
+      const int wpr = a.nf >> 5;                   // warps per ray
+      const int chunk = warp & (wpr - 1);
+      const int64_t ray = (base + warp * 32) / a.nf;
+      const float* row = s.ob + (warp * 32 + lane) * LD_OUT;
+      SampleVals sv = {0.f, 0.f, 0.f, 0.f, 0.f, 1.f};
+      float yb[9];
+      if (live) {
+        const float2 zd = *reinterpret_cast<const float2*>(a.zd + 2 * i);
+        sv = sample_vals_at(a.rd, zd.x, zd.y, row[0]);
+        const float dir[3] = {a.rays[ray * 6 + 3], a.rays[ray * 6 + 4], a.rays[ray * 6 + 5]};
+        sh2_basis(dir, yb);
+      }
+      float excl;
+      const float prod = excl_trans(sv.fac, lane, excl);
+      float T = 1.f;  // transmittance entering this chunk
+      if (wpr > 1) {
+        if (lane == 0) s.part[warp * kPartStride] = prod;
+        __syncthreads();
+        for (int q = warp - chunk; q < warp; ++q) T *= s.part[q * kPartStride];
+      }
+      const float w = live ? sv.alpha * (T * excl) : 0.f;
+      float acc = w, dep = w * sv.z, col[3] = {0.f, 0.f, 0.f};
+      if (live && w > a.rd.weight_thres) {
+        float c[3], lin[3];
+        sample_rgb(row, yb, c, lin);
+        col[0] = w * c[0]; col[1] = w * c[1]; col[2] = w * c[2];
+      }
+      acc = warp_sum(acc);
+      dep = warp_sum(dep);
+      col[0] = warp_sum(col[0]); col[1] = warp_sum(col[1]); col[2] = warp_sum(col[2]);
+      if (wpr > 1) {
+        if (lane == 0) {
+          float* pp = s.part + warp * kPartStride;
+          pp[1] = acc; pp[2] = dep; pp[3] = col[0]; pp[4] = col[1]; pp[5] = col[2];
+        }
+        __syncthreads();
+        if (chunk == 0) {
+          acc = dep = col[0] = col[1] = col[2] = 0.f;
+          for (int q = warp; q < warp + wpr; ++q) {
+            const float* pp = s.part + q * kPartStride;
+            acc += pp[1]; dep += pp[2]; col[0] += pp[3]; col[1] += pp[4]; col[2] += pp[5];
+          }
+        }
+      }
+      if (live && chunk == 0 && lane == 0) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          float v = col[c];
+          if (a.rd.white_bg) v = v + (1.f - acc);
+          a.rgb[ray * 3 + c] = fminf(fmaxf(v, 0.f), 1.f);
+        }
+        if (a.depth) a.depth[ray] = dep;
+      }
+      if (wpr > 1) __syncthreads();  // the partials are read before the next tile writes them
       continue;
     } else {
       __syncthreads();  // every warp's X and dH (and H, dO) tiles are complete
@@ -680,7 +781,7 @@ __global__ void __launch_bounds__(kThreads, MODE == kFwd ? 4 : 3) fused_field_ml
       if (v.x != 0.f || v.y != 0.f || v.z != 0.f || v.w != 0.f) atomicAdd(dst + e, v);
     }
   }
-  if constexpr (MODE != kFwd) {
+  if constexpr (!is_fwd<MODE>()) {
     if constexpr (is_fit<MODE>()) {
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) loss_acc += __shfl_xor_sync(0xffffffffu, loss_acc, o);

@@ -49,6 +49,44 @@ __device__ __forceinline__ Segment segment(const FFProposal& p, const float* ray
   return s;
 }
 
+// segment() for a warp whose 32 lanes share `ray` (all lanes call it): lane k < 3 computes axis
+// k's two slab distances, the others read them by shuffles. The same float32 operations as
+// segment() (min / max are exact), so the same Segment, with two divisions per warp instead of six.
+__device__ __forceinline__ Segment segment_warp(const FFProposal& p, const float* rays, int64_t ray, int lane) {
+  const int k = lane < 3 ? lane : 0;
+  const float o = rays[ray * 6 + k], d = rays[ray * 6 + 3 + k];
+  const float amax = k == 0 ? p.aabb_max[0] : (k == 1 ? p.aabb_max[1] : p.aabb_max[2]);
+  const float amin = k == 0 ? p.aabb_min[0] : (k == 1 ? p.aabb_min[1] : p.aabb_min[2]);
+  const float vec = (d == 0.f) ? 1e-6f : d;
+  const float ra = (amax - o) / vec, rb = (amin - o) / vec;
+  const float lo = fminf(ra, rb), hi = fmaxf(ra, rb);
+  Segment s;
+  float tin = -INFINITY, tout = INFINITY;
+#pragma unroll
+  for (int q = 0; q < 3; ++q) {
+    s.o[q] = __shfl_sync(0xffffffffu, o, q);
+    s.d[q] = __shfl_sync(0xffffffffu, d, q);
+    tin = fmaxf(tin, __shfl_sync(0xffffffffu, lo, q));
+    tout = fminf(tout, __shfl_sync(0xffffffffu, hi, q));
+  }
+  s.t_in = fmaxf(tin, 0.05f);
+  s.t_out = fmaxf(tout, s.t_in);
+  s.len = (s.t_out - s.t_in) / (float)p.n_bins;
+  return s;
+}
+
+// Coarse sample e = ray * nb + bin (shifts when nb is a power of two).
+__device__ __forceinline__ void ray_bin(int64_t e, int nb, int64_t& ray, int& bin) {
+  if ((nb & (nb - 1)) == 0) {
+    const int sh = __ffs(nb) - 1;
+    ray = e >> sh;
+    bin = (int)(e & (nb - 1));
+  } else {
+    ray = e / nb;
+    bin = (int)(e - ray * nb);
+  }
+}
+
 // Trilinear corners of x in the proposal grid (align_corners over the aabb, zero padding).
 __device__ __forceinline__ void grid_corners(const FFProposal& p, const float* x, Corners<3>& c) {
   float ix[3];
@@ -221,7 +259,7 @@ __global__ void __launch_bounds__(256) proposal_resample_kernel(
   float* es = e_s[wib];
   for (int64_t ray = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; ray < n_rays;
        ray += ((int64_t)gridDim.x * blockDim.x) >> 5) {
-    const Segment s = segment(p, rays, ray);
+    const Segment s = segment_warp(p, rays, ray, lane);
     BinState st;
     bin_weights(p, o_prop ? o_prop + ray * nb : nullptr, s.len, lane, B, st);
     // pdf = (w + 1e-5) / sum, cdf with a leading zero (sample_pdf, ray_utils.py:135-138)
@@ -436,6 +474,11 @@ int grid_blocks(int64_t total, int threads) {
 // Backward: dH = g_o * w1 * [H > 0], dX = dH W0 (tensor cores), dW1 in registers, dW0 and the
 // bias gradient (constant-1 feature column) by a block-wide MMA over the block's 128 samples,
 // the grid gradient scattered with float4 atomics.
+// MODE 0: the forward of training (the proposal loss and its backward read these outputs);
+// MODE 1: the backward; MODE 2: the forward of rendering, one BF16 MMA pass per layer (features
+// and hidden activations rounded to BF16, ReLU fused into the rounding) with the 64 -> 1 output
+// layer on the tensor cores as well: a histogram to sample from needs no more precision.
+// n_bins is a multiple of 32 and tiles are 32-aligned, so each warp's 32 samples lie on one ray.
 constexpr int kHW = 4;            // warps per block
 constexpr int kHT = kHW * 32;     // samples per block iteration
 constexpr int HLD_X = 12;         // float32 feature tile [32][12]: 8 features, 1.0, 0, 0, 0
@@ -452,7 +495,32 @@ struct HeadSmem {
 template <int MODE>
 __host__ __device__ constexpr int64_t head_smem_bytes() {
   return 2 * 64 * HLD_W0 * 2 + 8 * HLD_W0T * 2 + 64 * 4 + 64 * 4 + (int64_t)kHW * 32 * HLD_X * 4 +
-         (MODE ? (int64_t)kHW * 32 * HLD_H * 2 : 0);
+         (MODE == 1 ? (int64_t)kHW * 32 * HLD_H * 2 : 0);
+}
+
+// Two float32 values as a BF16 pair after a ReLU, in one conversion (the first value in the low
+// half, as pack_bf16).
+__device__ __forceinline__ uint32_t pack_bf16_relu(float lo, float hi) {
+  uint32_t r;
+  asm("cvt.rn.relu.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(hi), "f"(lo));
+  return r;
+}
+
+// A fragment (rows r, r + 8; columns c, c + 1 and c + 8, c + 9) of the float32 feature tile,
+// rounded to BF16; columns at or past HLD_X read as zero.
+__device__ __forceinline__ void head_frag_bf16(const float* xf, int r0, int c, uint32_t* a) {
+  const float2 v00 = *reinterpret_cast<const float2*>(xf + r0 * HLD_X + c);
+  const float2 v10 = *reinterpret_cast<const float2*>(xf + (r0 + 8) * HLD_X + c);
+  a[0] = pack_bf16(v00.x, v00.y);
+  a[1] = pack_bf16(v10.x, v10.y);
+  if (c + 8 < HLD_X) {
+    const float2 v01 = *reinterpret_cast<const float2*>(xf + r0 * HLD_X + c + 8);
+    const float2 v11 = *reinterpret_cast<const float2*>(xf + (r0 + 8) * HLD_X + c + 8);
+    a[2] = pack_bf16(v01.x, v01.y);
+    a[3] = pack_bf16(v11.x, v11.y);
+  } else {
+    a[2] = a[3] = 0u;
+  }
 }
 
 __device__ __forceinline__ void head_pair(const float* xf, int row, int col, uint32_t& hi, uint32_t& lo) {
@@ -481,7 +549,7 @@ __global__ void __launch_bounds__(kHT) proposal_head_kernel(const FFProposal p, 
     s.b0 = (float*)q; q += 64 * 4;
     s.w1 = (float*)q; q += 64 * 4;
     s.x = (float*)q; q += kHW * 32 * HLD_X * 4;
-    s.dh = MODE ? (__nv_bfloat16*)q : nullptr;
+    s.dh = MODE == 1 ? (__nv_bfloat16*)q : nullptr;
   }
   for (int e = tid; e < 64 * 16; e += kHT) {
     const int j = e >> 4, k = e & 15;
@@ -496,6 +564,17 @@ __global__ void __launch_bounds__(kHT) proposal_head_kernel(const FFProposal p, 
     s.w1[j] = m.weight[1][j];
   }
   __syncthreads();
+  // MODE 2: W1 as the B fragments of the output layer (n-tile column 0 = the single output;
+  // lanes of the other columns hold zeros), k-steps of 16 hidden units
+  uint32_t w1b[MODE == 2 ? 4 : 1][2];
+  if constexpr (MODE == 2) {
+#pragma unroll
+    for (int ks = 0; ks < 4; ++ks) {
+      const int k0 = 16 * ks + 2 * t;
+      w1b[ks][0] = g == 0 ? pack_bf16(s.w1[k0], s.w1[k0 + 1]) : 0u;
+      w1b[ks][1] = g == 0 ? pack_bf16(s.w1[k0 + 8], s.w1[k0 + 9]) : 0u;
+    }
+  }
   float* xf = s.x + warp * 32 * HLD_X;
   const int64_t total = n_rays * p.n_bins;
   float acc_w0[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
@@ -505,13 +584,22 @@ __global__ void __launch_bounds__(kHT) proposal_head_kernel(const FFProposal p, 
 
   for (int64_t base = (int64_t)blockIdx.x * kHT; base < total; base += (int64_t)gridDim.x * kHT) {
     const int64_t e = base + warp * 32 + lane;
-    const bool valid = e < total;
+    // total is a multiple of 32, so a warp's samples are all valid or all past the end
+    const bool valid = base + warp * 32 < total;
     float pos[3] = {0.f, 0.f, 0.f};
     float feat[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     if (valid) {
-      const int64_t ray = e / p.n_bins;
-      const int k = (int)(e % p.n_bins);
-      const Segment sg = segment(p, rays, ray);
+      int64_t ray;
+      int k;
+      Segment sg;
+      if constexpr (MODE == 2) {  // the same values with fewer instructions (more registers)
+        ray_bin(e, p.n_bins, ray, k);
+        sg = segment_warp(p, rays, ray, lane);
+      } else {
+        ray = e / p.n_bins;
+        k = (int)(e % p.n_bins);
+        sg = segment(p, rays, ray);
+      }
       const float tt = sg.t_in + ((float)k + 0.5f) * sg.len;
 #pragma unroll
       for (int q = 0; q < 3; ++q) pos[q] = sg.o[q] + sg.d[q] * tt;
@@ -534,6 +622,41 @@ __global__ void __launch_bounds__(kHT) proposal_head_kernel(const FFProposal p, 
       xr[2] = make_float4(valid ? 1.f : 0.f, 0.f, 0.f, 0.f);
     }
     __syncwarp();
+    if constexpr (MODE == 2) {
+#pragma unroll
+      for (int mt = 0; mt < 2; ++mt) {
+        const int r0 = 16 * mt + g;
+        uint32_t a[4];
+        head_frag_bf16(xf, r0, 2 * t, a);
+        float oc[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+        for (int ks = 0; ks < 4; ++ks) {  // hidden units [16 ks, 16 ks + 16): two n-tiles of layer 0
+          float hc[2][4];
+          uint32_t ha[4];
+#pragma unroll
+          for (int hh = 0; hh < 2; ++hh) {
+            const int nt = 2 * ks + hh;
+            const float bl = s.b0[nt * 8 + 2 * t], bh = s.b0[nt * 8 + 2 * t + 1];
+            hc[hh][0] = bl; hc[hh][1] = bh; hc[hh][2] = bl; hc[hh][3] = bh;
+            const __nv_bfloat16* wp = s.w0 + (nt * 8 + g) * HLD_W0 + 2 * t;
+            mma_bf16(hc[hh], a, lds32(wp), lds32(wp + 8));
+          }
+          ha[0] = pack_bf16_relu(hc[0][0], hc[0][1]);
+          ha[1] = pack_bf16_relu(hc[0][2], hc[0][3]);
+          ha[2] = pack_bf16_relu(hc[1][0], hc[1][1]);
+          ha[3] = pack_bf16_relu(hc[1][2], hc[1][3]);
+          mma_bf16(oc, ha, w1b[ks][0], w1b[ks][1]);
+        }
+        // output column 0: rows r0 (oc[0]) and r0 + 8 (oc[2]) in the t == 0 lanes
+        const int64_t row0 = base + warp * 32 + r0;
+        if (t == 0 && valid) {
+          o_out[row0] = oc[0];
+          o_out[row0 + 8] = oc[2];
+        }
+      }
+      __syncwarp();
+      continue;
+    }
     float dx[2][4];
 #pragma unroll
     for (int mt = 0; mt < 2; ++mt) {
@@ -728,6 +851,12 @@ cudaError_t launch_proposal_head_forward(const FFProposal& p, const void* grid, 
                                          int64_t n, float* o_out, cudaStream_t s) {
   FFMlpGrad none = {};
   return launch_head<0>(p, grid, rays, n, m, o_out, nullptr, nullptr, none, s);
+}
+
+cudaError_t launch_proposal_head_infer(const FFProposal& p, const void* grid, const FFMlp& m, const float* rays,
+                                       int64_t n, float* o_out, cudaStream_t s) {
+  FFMlpGrad none = {};
+  return launch_head<2>(p, grid, rays, n, m, o_out, nullptr, nullptr, none, s);
 }
 
 cudaError_t launch_proposal_head_backward(const FFProposal& p, const void* grid, const FFMlp& m, const float* rays,

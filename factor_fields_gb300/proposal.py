@@ -56,8 +56,10 @@ class ProposalRenderFunction(torch.autograd.Function):
         feat_p = None
         if sam.learned and sam.fused_head:
             o_p = torch.empty(n * nb, 1, device=dev)
-            N.call("ff_proposal_head_forward", ctypes.byref(sam.desc), N.ptr(sam.grid_read()),
-                   ctypes.byref(sam.mlp_struct()), N.ptr(rays), n, N.ptr(o_p), st)
+            # rendering: the single-pass BF16 form of the head (a histogram to sample from)
+            head = "ff_proposal_head_forward" if job["is_train"] else "ff_proposal_head_infer"
+            N.call(head, ctypes.byref(sam.desc), N.ptr(sam.grid_read()), ctypes.byref(sam.mlp_struct()), N.ptr(rays),
+                   n, N.ptr(o_p), st)
         elif sam.learned:
             feat_p = torch.empty(n * nb, 8, device=dev)
             N.call("ff_proposal_encode", ctypes.byref(sam.desc), N.ptr(sam.grid_read()), N.ptr(rays), n,
@@ -100,6 +102,20 @@ class ProposalRenderFunction(torch.autograd.Function):
             N.call("ff_proposal_resample", ctypes.byref(pdesc), N.ptr(rays), n, N.ptr(o_sample),
                    N.ptr(job["jitter"]), N.ptr(u), N.ptr(w_p), N.ptr(xyz), N.ptr(zd), N.ptr(bin_of), st)
             offsets = torch.arange(n + 1, device=dev, dtype=torch.int64) * nf
+            if job.get("fuse_render") and nf in (32, 64, 128) and m.linear_mat.out_dim == 28:
+                # rendering only (no gradients wanted): field forward and compositing in one
+                # launch, the feature rows stay on chip
+                rgb = torch.empty(n, 3, device=dev)
+                depth = torch.empty(n, device=dev)
+                lm = m.linear_mat
+                ws, bs = lm.weights()
+                mlp = FN.mlp_struct(ws, bs, lm.in_dim, lm.hidden_dim, lm.out_dim)
+                N.call("ff_field_render_fixed", ctypes.byref(job["fdesc"]), N.ptr(job["basis_r"]),
+                       N.ptr(job["coeff_r"]), ctypes.byref(mlp), ctypes.byref(job["rdesc"]), N.ptr(rays),
+                       N.ptr(xyz), N.ptr(zd), n, nf, N.ptr(rgb), N.ptr(depth), st)
+                ctx.mark_non_differentiable(rgb, depth)
+                job.update(feat_p=feat_p, o_p=o_p, w_p=None, w_f=None, bin_of=None, rays=rays)
+                return rgb, depth
         feat = field_eval(m, job, xyz)
         rgb = torch.empty(n, 3, device=dev)
         depth = torch.empty(n, device=dev)
@@ -127,7 +143,7 @@ class ProposalRenderFunction(torch.autograd.Function):
 class ProposalSampler:
     def __init__(self, model, reso=64, n_bins=64, n_fine=48, hidden=64, lr_grid=2e-2, lr_mlp=1e-3,
                  density_shift=-4.0, precision="bf16", learned=True, seed=0, uniform_mix=0.0, fused_adam=True,
-                 train_uniform=True, render_fine=None, sample_jitter=True, cull_render=False):
+                 train_uniform=True, render_fine=None, sample_jitter=True, cull_render=False, fuse_render=True):
         self.m, self.learned, self.train_uniform = model, learned, train_uniform
         # cull_render: rendering (not training) on the fused path leaves out the samples that fail
         # the model's alpha mask (ff_proposal_resample_occupied). Off by default: a mask built by
@@ -135,6 +151,9 @@ class ProposalSampler:
         # regions that are still visible along a ray; on the blob scene a mask of the final field
         # cost 3.5-3.8 dB for 9-12% less render time.
         self.cull_render = cull_render
+        # fuse_render: renders without gradients at 32, 64 or 128 samples per ray run the field
+        # forward and the compositing as one launch (ff_field_render_fixed)
+        self.fuse_render = fuse_render
         self.render_fine = render_fine or n_fine  # samples per ray when rendering (not training)
         self.sample_jitter = sample_jitter  # training: jitter each sample in its stratum (else per ray)
         self.reso, self.n_bins, self.n_fine, self.precision = reso, n_bins, n_fine, precision
@@ -208,7 +227,9 @@ class ProposalSampler:
             self._rdesc, self._rdesc_key = render_desc(m, self.n_fine, white_bg), key
         job = {"model": m, "sampler": self, "rdesc": self._rdesc, "is_train": bool(is_train),
                "fdesc": m.descriptor(dt), "basis_r": basis_r, "coeff_r": coeff_r, "coeff_param": m.coeff_flat,
-               "fused": fused, "jitter": jitter}
+               "fused": fused, "jitter": jitter,
+               # a render without gradients may composite inside the field kernel (ff_field_render_fixed)
+               "fuse_render": self.fuse_render and fused and not is_train and not torch.is_grad_enabled()}
         l0, l1 = m.linear_mat.backbone
         rgb, depth = ProposalRenderFunction.apply(rays, m.basis_flat, m.coeff_flat, l0.weight, l0.bias, l1.weight, job)
         self._job = job

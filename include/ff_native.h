@@ -363,6 +363,18 @@ FF_API int ff_composite_backward_zd(const FFRender* r, const float* rays, int64_
                                     const float* zd, const float* feat, int32_t feat_stride,
                                     const float* grad_rgb, float* grad_feat, void* stream);
 
+/* Rendering of rays that carry exactly n_fine samples each (32, 64 or 128; ray k's samples at rows
+ * [k n_fine, (k + 1) n_fine) of xyz [n_rays * n_fine, 3] and zd, e.g. ff_proposal_resample's
+ * output): ff_field_mlp_forward (the fused path, 3-D points, out_dim 28: density + degree-2 SH
+ * colour) and ff_composite_forward_zd with offsets k * n_fine, in one launch. The compositing
+ * runs in the field kernel's epilogue, so the [n, 28] feature rows never reach memory.
+ * rgb [n_rays, 3], depth [n_rays] (optional). Equals the two calls up to float32 summation order
+ * of the per-ray sums (rays longer than 32 samples are summed per 32-sample chunk). Forward only:
+ * the training step keeps the two calls, whose backward needs the feature rows. */
+FF_API int ff_field_render_fixed(const FFField* f, const void* basis, const void* coeff, const FFMlp* m,
+                                 const FFRender* r, const float* rays, const float* xyz, const float* zd,
+                                 int64_t n_rays, int32_t n_fine, float* rgb, float* depth, void* stream);
+
 /* ---- MLPRender_Fea colour head (models/FactorFields.py:162-203) ------------------------------
  * rgb = sigmoid(MLP([feat, dir, PE(feat, fea_pe), PE(dir, view_pe)])) for the samples whose
  * compositing weight passes renderer.rayMarch_weight_thres (:879-885), with
@@ -507,6 +519,13 @@ FF_API int ff_proposal_scatter(const FFProposal* p, const float* rays, int64_t n
  * by ff_mlp_forward up to split-BF16 rounding (first layer: features and weights as hi + lo). */
 FF_API int ff_proposal_head_forward(const FFProposal* p, const void* grid, const FFMlp* m, const float* rays,
                                     int64_t n_rays, float* o_prop, void* stream);
+/* ff_proposal_head_forward for rendering (a BF16 grid): one BF16 tensor-core pass per layer,
+ * features and hidden activations rounded to BF16 and the 64 -> 1 layer on the tensor cores too,
+ * about 45% fewer instructions. o_prop differs from ff_proposal_head_forward's by BF16
+ * rounding (~1e-2 relative). Training keeps ff_proposal_head_forward, whose outputs the loss
+ * and the backward are consistent with. */
+FF_API int ff_proposal_head_infer(const FFProposal* p, const void* grid, const FFMlp* m, const float* rays,
+                                  int64_t n_rays, float* o_prop, void* stream);
 /* Backward of ff_proposal_head_forward for grad_o [n_rays * n_bins]: the grid gradient
  * (float32 [reso^3][8], +=) and the MLP gradients g (+=; NULL entries skipped) in one launch.
  * Equals ff_mlp_backward followed by ff_proposal_scatter up to BF16 rounding. */

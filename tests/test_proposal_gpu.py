@@ -116,6 +116,45 @@ def test_fused_head_matches_encode_mlp_scatter(precision, n_rays, n_bins):
            0, None, st)
 
 
+@pytest.mark.parametrize("n_rays,n_bins", [(61, 64), (33, 96), (1, 32), (257, 128)])
+def test_head_infer_matches_fp64_composition(n_rays, n_bins):
+    """ff_proposal_head_infer (the rendering form: one BF16 MMA pass per layer) against the FP64
+    MLP of the grid lookup (ff_proposal_encode, pinned to trilinear grid_sample): within 2e-2 of
+    the largest output, the BF16 tolerance; 96 bins take the division path of the bin index."""
+    from factor_fields_gb300 import _native as N
+    m, s = make_sampler(reso=12, n_bins=n_bins, precision="bf16")
+    gen = torch.Generator().manual_seed(8)
+    with torch.no_grad():
+        s.grid.copy_(torch.randn(s.grid.shape, generator=gen).cuda() * 0.5)
+        l0, l1 = s.mlp.backbone
+        l0.bias.copy_(torch.randn(64, generator=gen).cuda() * 0.2)
+    st = N.stream_ptr()
+    rt = torch.from_numpy(rays_np(n_rays, 10)).cuda()
+    n, nb = n_rays, n_bins
+    grid_r = s.grid_read()
+    o = torch.full((n * nb + 64, 1), float("nan"), device="cuda")  # rows past n * nb stay untouched
+    N.call("ff_proposal_head_infer", ctypes.byref(s.desc), N.ptr(grid_r), ctypes.byref(s.mlp_struct()), N.ptr(rt),
+           n, N.ptr(o), st)
+    feat = torch.empty(n * nb, 8, device="cuda")
+    N.call("ff_proposal_encode", ctypes.byref(s.desc), N.ptr(grid_r), N.ptr(rt), n, N.ptr(feat), st)
+    torch.cuda.synchronize()
+    x = feat.double().cpu()
+    ref = torch.relu(x @ l0.weight.detach().double().cpu().T + l0.bias.detach().double().cpu()) @ \
+        l1.weight.detach().double().cpu().T
+    assert rel_err(o[:n * nb], ref.numpy()) < 2e-2
+    assert torch.isnan(o[n * nb:]).all()
+    # the training form agrees to its own (tighter) tolerance, so the two forms differ by rounding
+    o_fwd = torch.empty(n * nb, 1, device="cuda")
+    N.call("ff_proposal_head_forward", ctypes.byref(s.desc), N.ptr(grid_r), ctypes.byref(s.mlp_struct()), N.ptr(rt),
+           n, N.ptr(o_fwd), st)
+    assert rel_err(o_fwd, ref.numpy()) < 1e-3
+    # float32 grids are refused (the rendering form reads a BF16 grid)
+    m32, s32 = make_sampler(reso=12, n_bins=n_bins, precision="fp32")
+    with pytest.raises(N.NativeError):
+        N.call("ff_proposal_head_infer", ctypes.byref(s32.desc), N.ptr(s32.grid_read()),
+               ctypes.byref(s32.mlp_struct()), N.ptr(rt), n, N.ptr(o), st)
+
+
 def test_resample_is_sample_pdf():
     from factor_fields_gb300 import _native as N
     m, s = make_sampler()
@@ -272,9 +311,73 @@ def test_render_through_the_mask_equals_zero_density_samples():
            feat.shape[1], N.ptr(rgb_ref), N.ptr(depth_ref), N.ptr(w_f), st)
     torch.cuda.synchronize()
     acc = w_f.view(n, nf).sum(1).cpu().numpy()
+    assert (acc > 0.1).mean() > 0.2 and (acc < 0.9).mean() > 0.2, (shift, acc.mean())  # partly opaque rays
+    assert float((rgb - rgb_ref).abs().max()) < 1e-5
+    assert float((depth - depth_ref).abs().max()) < 1e-5 * float(depth_ref.abs().max())
+
+
+@pytest.mark.parametrize("nf", [32, 64, 128])
+def test_fused_render_equals_field_forward_and_compositing(nf):
+    """ff_field_render_fixed (field forward with the compositing in its epilogue) against
+    ff_field_mlp_forward + ff_composite_forward_zd on the same resampled rays: rgb and depth
+    within 1e-5 (rays of 64 and 128 samples are summed per 32-sample chunk). 301 rays: the last
+    tile is partly past the end. Through the sampler, a render without gradients takes the fused
+    path and gives the unfused render's colours."""
+    from factor_fields_gb300 import _native as N
+    from factor_fields_gb300 import functional as FN
+    from factor_fields_gb300.renderer import field_eval, render_desc
+    m, s = make_sampler(n_fine=nf, precision="bf16")
+    gen = torch.Generator().manual_seed(12)
+    rays = rays_np(301, 11)
+    rt = torch.from_numpy(rays).cuda()
+    n, nb = rays.shape[0], s.n_bins
+    st = N.stream_ptr()
+    o_t = (torch.randn(n * nb, generator=gen) * 3).cuda()
+    xyz = torch.empty(n * nf, 3, device="cuda")
+    zd = torch.empty(n * nf, 2, device="cuda")
+    N.call("ff_proposal_resample", ctypes.byref(s.desc), N.ptr(rt), n, N.ptr(o_t), None, None, None, N.ptr(xyz),
+           N.ptr(zd), None, st)
+    basis_r, coeff_r, dt = m._read_buffers()
+    job = {"fused": True, "fdesc": m.descriptor(dt), "basis_r": basis_r, "coeff_r": coeff_r}
+    feat = field_eval(m, job, xyz)
+    offsets = torch.arange(n + 1, device="cuda", dtype=torch.int64) * nf
+    rgb_ref = torch.empty(n, 3, device="cuda")
+    depth_ref = torch.empty(n, device="cuda")
+    w_f = torch.empty(n * nf, device="cuda")
+    for shift in (0.0, -2.0, -3.0, -4.0, -5.0, -6.0, -7.0, -8.0, -10.0):  # a density with partly opaque rays
+        m.cfg.renderer.density_shift = shift
+        rd = render_desc(m, nf, True)
+        N.call("ff_composite_forward_zd", ctypes.byref(rd), N.ptr(rt), n, N.ptr(offsets), N.ptr(zd), N.ptr(feat),
+               feat.shape[1], N.ptr(rgb_ref), N.ptr(depth_ref), N.ptr(w_f), st)
+        if 0.3 < float(w_f.view(n, nf).sum(1).mean()) < 0.7:
+            break
+    lm = m.linear_mat
+    ws, bs = lm.weights()
+    mlp = FN.mlp_struct(ws, bs, lm.in_dim, lm.hidden_dim, lm.out_dim)
+    rgb = torch.full((n, 3), float("nan"), device="cuda")
+    depth = torch.full((n,), float("nan"), device="cuda")
+    N.call("ff_field_render_fixed", ctypes.byref(job["fdesc"]), N.ptr(basis_r), N.ptr(coeff_r), ctypes.byref(mlp),
+           ctypes.byref(rd), N.ptr(rt), N.ptr(xyz), N.ptr(zd), n, nf, N.ptr(rgb), N.ptr(depth), st)
+    torch.cuda.synchronize()
+    acc = w_f.view(n, nf).sum(1).cpu().numpy()
     assert (acc > 0.2).mean() > 0.2 and (acc < 0.8).mean() > 0.2  # partly opaque rays
     assert float((rgb - rgb_ref).abs().max()) < 1e-5
     assert float((depth - depth_ref).abs().max()) < 1e-5 * float(depth_ref.abs().max())
+    # the sampler: fused when no gradients are wanted, the same colours as the two-call render
+    s.render_fine = nf
+    with torch.no_grad():
+        rgb_f, depth_f = s.render(rt, is_train=False)
+        assert s._job["w_f"] is None  # the fused path ran
+        s.fuse_render = False
+        rgb_u, depth_u = s.render(rt, is_train=False)
+        assert s._job["w_f"] is not None
+    assert float((rgb_f - rgb_u).abs().max()) < 1e-5
+    assert float((depth_f - depth_u).abs().max()) < 1e-5 * float(depth_u.abs().max())
+    # unsupported sample counts and heads are refused
+    with pytest.raises(N.NativeError):
+        N.call("ff_field_render_fixed", ctypes.byref(job["fdesc"]), N.ptr(basis_r), N.ptr(coeff_r),
+               ctypes.byref(mlp), ctypes.byref(rd), N.ptr(rt), N.ptr(xyz), N.ptr(zd), n // 2, 48, N.ptr(rgb),
+               N.ptr(depth), st)
 
 
 def test_proposal_loss_gradient_matches_finite_differences():
