@@ -589,6 +589,16 @@ def run_radiance(args, dev):
     out["proposal_psnr_minus_plain_db"] = float(np.mean(diffs))
     out["proposal_psnr_minus_plain_db_by_seed"] = diffs
     out["proposal_32_psnr_minus_plain_db_by_seed"] = diffs32
+    # the target for the learned sampler: rendering within 0.1 dB of the plain sampler's PSNR (3-view
+    # test set, each seed) at >= 3x its rays/s (a full 400x400 image through the evaluation renderer)
+    r32, r48 = out["proposal_eval_rays_per_s_vs_plain_32"], out["proposal_eval_rays_per_s_vs_plain"]
+    out["proposal_target"] = {
+        "target": "PSNR within 0.1 dB of the plain sampler at >= 3x its rays/s",
+        "render_samples_32": {"rays_per_s_vs_plain": r32, "psnr_minus_plain_db_by_seed": diffs32,
+                              "met": bool(r32 >= 3.0 and min(diffs32) >= -0.1)},
+        "render_samples_48": {"rays_per_s_vs_plain": r48, "psnr_minus_plain_db_by_seed": diffs,
+                              "met": bool(r48 >= 3.0 and min(diffs) >= -0.1)},
+    }
     out["scene"] = "seeded 32 Gaussian density blobs in [-1.5,1.5]^3, 100 views 400x400 focal 555, white bg"
     return out
 
