@@ -554,6 +554,9 @@ def run_radiance(args, dev):
                                                  "ssim": x32["ssim"][0],
                                                  "rays_per_s": 400 * 400 / (x32["ms_per_image"][0] / 1e3)}}
             sampler.render_fine = sampler.n_fine
+        if sampler is None and not args.no_cpu_baseline:
+            rec["cpu_baseline"] = run_cpu_baseline_render(m, pool, gt)
+            rec["rays_per_s_vs_cpu_baseline"] = rec["rays_per_s"] / rec["cpu_baseline"]["value"]
         if sampler is None:
             offs, _, _ = march(m, test, None, render_desc(m, 1024, True))
             rec["live_samples_per_ray"] = float(offs[-1]) / test.shape[0]
@@ -752,6 +755,36 @@ def measure_mlp_head(args, dev, flush):
                                      "rays_per_s": 4096 / (float(np.mean(ts)) / 1e3),
                                      "note": "untrained field (random-init), fwd+bwd, no optimizer"}
     return out
+
+
+def run_cpu_baseline_render(m, pool, gt, n_rays=1024, steps=3, warmup=1):
+    """The reference's render path on the host cores (oracle/ref_torch.py RefRender: sample_point,
+    the alpha mask, get_coding + MLPMixer on the live samples, raw2alpha, the SH-2 colour head,
+    compositing; fwd+bwd with the MSE loss) holding the trained configuration-2 model's parameters
+    and occupancy volume, on a bounded sample of its training rays: rays/s, best step."""
+    from oracle.ref_torch import RefRender, from_model
+    cores = os.cpu_count() or 1
+    torch.set_num_threads(cores)
+    r = m.cfg.renderer
+    vol = m.alphaMask.alpha_volume[0, 0].cpu() if m.alphaMask is not None else None
+    rr = RefRender(from_model(m), float(m.stepSize), 1024, vol, r.density_shift, r.distance_scale,
+                   r.rayMarch_weight_thres, r.fea2denseAct or "softplus")
+    g = torch.Generator().manual_seed(5)
+    idx = torch.randint(0, pool.shape[0], (n_rays,), generator=g)
+    rays, rgb = pool[idx.to(pool.device)].cpu(), gt[idx.to(gt.device)].cpu().float()
+    jit = torch.rand(n_rays, 1, generator=g)
+    for _ in range(warmup):
+        rr.train_step(rays, rgb, jit)
+    best = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        rr.train_step(rays, rgb, jit)
+        best.append(time.perf_counter() - t0)
+    return {"value": n_rays / min(best), "unit": "rays/s", "cores": cores, "kind": CPU_KIND,
+            "sample": f"{n_rays} training rays x up to 1024 samples with the trained model's occupancy volume, "
+                      f"fwd+bwd (MSE), best of {steps} after {warmup} warm-up (torch CPU restatement of the "
+                      "reference's FactorFields.forward render path with the SH-2 head (oracle/ref_torch.py "
+                      "RefRender, pinned to renders of the reference itself))"}
 
 
 def run_cpu_baseline_model(m, key, steps, warmup=1):

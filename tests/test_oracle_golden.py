@@ -249,3 +249,31 @@ def test_torch_cpu_baseline_matches_reference(case):
     for i in range(meta["n_levels"]):
         assert rel_err(r.basises[i].grad.numpy(), d[f"grad_basis{i}"]) < 1e-6
     assert rel_err(r.coeff.grad.numpy(), d["grad_coeffs0"]) < 1e-6
+
+
+@pytest.mark.parametrize("case", [c for c in RENDER_CASES if "sh" in c])
+def test_torch_cpu_render_matches_reference(case):
+    """oracle/ref_torch.py's render (the radiance configurations' timed CPU baseline) reproduces the
+    reference's own render of the golden SH-head fixtures: rgb, depth and the gradients of
+    sum(rgb * g_rgb)."""
+    import torch
+    from oracle.ref_torch import RefField, RefRender
+    d, meta = load(case)
+    ws, bs = mlp_params(d)
+    cfg = meta["cfg"]
+    f = RefField(cfg["defaults"]["mode"], cfg["dataset"]["aabb"], [d[f"basis{i}"] for i in range(6)], d["coeffs0"],
+                 ws, bs, meta["freq_bands"], cfg["model"]["basis_mapping"], cfg["model"]["basis_mode"],
+                 cfg["model"]["coef_mode"])
+    r = cfg["renderer"]
+    rr = RefRender(f, float(d["step_size"]), int(d["n_samples"]), d.get("alpha_volume"), r["density_shift"],
+                   r["distance_scale"], r["rayMarch_weight_thres"], r["fea2denseAct"])
+    jitter = torch.from_numpy(d["u"]) if meta["jitter"] else None
+    rgb, depth = rr.forward(torch.from_numpy(d["rays"]), white_bg=meta["white_bg"], jitter=jitter)
+    assert rel_err(rgb.detach().numpy(), d["rgb"]) < 1e-6
+    assert rel_err(depth.numpy(), d["depth"]) < 1e-6
+    (rgb * torch.from_numpy(d["g_rgb"])).sum().backward()
+    for i in range(6):
+        assert rel_err(f.basises[i].grad.numpy(), d[f"grad_basis{i}"]) < 1e-5, i
+    assert rel_err(f.coeff.grad.numpy(), d["grad_coeffs0"]) < 1e-5
+    for i in range(len(ws)):
+        assert rel_err(f.weights[i].grad.numpy(), d[f"grad_mlp_w{i}"]) < 1e-5
