@@ -141,3 +141,49 @@ def test_render_head_validation(lib):
     assert lib.ff_render_head_forward_tc(ctypes.byref(h), *args, None, None, None) == N.FF_ERR_UNSUPPORTED
     assert b"hidden_dim" in lib.ff_last_error()
     assert lib.ff_render_head_workspace_bytes(ctypes.byref(h), 100) > 0
+
+
+def test_rendering_forms_validate_before_any_launch(lib):
+    """The proposal's rendering entry points reject what they do not implement before any CUDA
+    call: ff_field_render_fixed takes 32, 64 or 128 samples per ray and the 28-wide SH head,
+    ff_proposal_head_infer a BF16 grid, ff_proposal_resample_occupied an occupancy volume and a
+    large enough scan workspace."""
+    from factor_fields_gb300 import FactorFields
+    from factor_fields_gb300 import functional as FN
+    from factor_fields_gb300 import workloads as W
+    from factor_fields_gb300 import _native as N
+    from factor_fields_gb300.renderer import render_desc
+    vp = ctypes.c_void_p
+    m = FactorFields(W.field_cfg("cfg2"), device="cpu", precision="bf16")
+    desc = m.descriptor(N.FF_BF16)
+    ws_, bs_ = m.linear_mat.weights()
+    mlp = FN.mlp_struct(ws_, bs_, m.linear_mat.in_dim, m.linear_mat.hidden_dim, m.linear_mat.out_dim)
+    rd = render_desc(m, 32, True)
+    args = (ctypes.byref(desc), vp(256), vp(256), ctypes.byref(mlp), ctypes.byref(rd), vp(256), vp(256), vp(256))
+    assert lib.ff_field_render_fixed(*args, 100, 48, vp(256), None, None) == N.FF_ERR_UNSUPPORTED
+    assert lib.ff_field_render_fixed(*args, 100, 32, None, None, None) == N.FF_ERR_ARG  # rgb NULL
+    assert lib.ff_field_render_fixed(*args, -1, 32, vp(256), None, None) == N.FF_ERR_ARG
+    mlp.out_dim = 3
+    assert lib.ff_field_render_fixed(*args, 100, 32, vp(256), None, None) == N.FF_ERR_UNSUPPORTED
+    assert b"28-wide" in lib.ff_last_error()
+    # the proposal head's rendering form reads a BF16 grid
+    p = N.FFProposal()
+    for k in range(3):
+        p.aabb_min[k], p.aabb_max[k], p.inv_cell[k] = -1.5, 1.5, 21.0
+    p.reso, p.n_bins, p.n_fine, p.param_dtype = 64, 64, 32, N.FF_F32
+    head = N.FFMlp()
+    head.n_layers, head.in_dim, head.hidden_dim, head.out_dim = 2, 8, 64, 1
+    head.weight[0], head.weight[1], head.bias[0] = 256, 256, 256
+    assert lib.ff_proposal_head_infer(ctypes.byref(p), vp(256), ctypes.byref(head), vp(256), 10, vp(256),
+                                      None) == N.FF_ERR_UNSUPPORTED
+    # occupancy-culled resampling needs occ_bits and the scan workspace
+    p.param_dtype = N.FF_BF16
+    need = lib.ff_scan_workspace_bytes(10)
+    rd.occ_bits = None
+    assert lib.ff_proposal_resample_occupied(ctypes.byref(p), ctypes.byref(rd), vp(256), 10, vp(256), None, vp(256),
+                                             vp(256), vp(256), need, vp(256), vp(256), None) == N.FF_ERR_ARG
+    rd.occ_bits = 256
+    for k in range(3):
+        rd.occ_reso[k] = 8
+    assert lib.ff_proposal_resample_occupied(ctypes.byref(p), ctypes.byref(rd), vp(256), 10, vp(256), None, vp(256),
+                                             vp(256), vp(256), need - 1, vp(256), vp(256), None) == N.FF_ERR_ARG
