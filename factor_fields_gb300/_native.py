@@ -208,7 +208,8 @@ _NON_LAUNCHING = {"ff_abi_version", "ff_last_error", "ff_device_info", "ff_struc
 _KERNELS_PER_CALL = {"ff_scan_counts": 3, "ff_scan_counts_noalloc": 3,
                      "ff_field_fit_bin": 3,  # bin (+ zeroing), alloc, permute
                      "ff_occupancy_mask": 5,  # init, pool, unite, size, filter (3 when min_size <= 1)
-                     "ff_image_metrics": 2}
+                     "ff_image_metrics": 2,
+                     "ff_proposal_resample_occupied": 5}  # count, scan (3), emit
 
 
 def reset_launch_count():
