@@ -468,6 +468,61 @@ def measure_radiance_field_kernels(m, rays, dev, flush, steps, warmup, seed=3):
                          "l2": "flushed (256 MB write) before every timed launch"}}
 
 
+def measure_adam(opt, steps, warmup):
+    """The fused Adam update (ff_adam_step) over an optimizer's parameters alone: CUDA events
+    around 5 back-to-back updates (entries built beforehand; the ~0.5 GB working set of the
+    configuration-2 model is larger than L2), against the HBM roofline with 32 algorithmic bytes
+    per element (param, grad, both moments: read and written; the gradient zeroed) + 2 for each
+    element with a BF16 read copy."""
+    import ctypes
+    from factor_fields_gb300 import _native as N
+    opt.step()  # the moments exist
+    by_hyper, n, n_sh = {}, 0, 0
+    for group in opt.param_groups:
+        b1, b2 = group["betas"]
+        for p in group["params"]:
+            if p.grad is None:
+                continue
+            st = opt.state[p]
+            e = N.FFAdamParam()
+            e.param, e.grad = p.data_ptr(), p.grad.data_ptr()
+            e.exp_avg, e.exp_avg_sq = st["exp_avg"].data_ptr(), st["exp_avg_sq"].data_ptr()
+            sh = getattr(opt, "_shadows", {}).get(p)
+            e.param_bf16 = sh.data_ptr() if sh is not None else None
+            e.n, e.step, e.lr = p.numel(), int(st["step"].item()) + 1, float(group["lr"])
+            by_hyper.setdefault((float(b1), float(b2), float(group["eps"])), []).append(e)
+            n += p.numel()
+            n_sh += p.numel() if sh is not None else 0
+    calls = [((N.FFAdamParam * len(es))(*es), len(es), hyper) for hyper, es in by_hyper.items()]
+
+    def launch():
+        for arr, k, (b1, b2, eps) in calls:
+            N.call("ff_adam_step", ctypes.cast(arr, ctypes.c_void_p), k, b1, b2, eps, N.FF_ADAM_ZERO_GRAD,
+                   N.stream_ptr(), kernels=-(-k // 8))
+
+    for _ in range(warmup):
+        launch()
+    ts = []
+    for _ in range(steps):
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(5):
+            launch()
+        e1.record()
+        torch.cuda.synchronize()
+        ts.append(e0.elapsed_time(e1) / 5)
+    ms = float(np.median(ts))
+    nbytes = 32 * n + 2 * n_sh
+    peaks = load_peaks()
+    peak = peaks.get("hbm_gbs", 6800.0)
+    achieved = nbytes / (ms / 1e3) / 1e9
+    return {"ms": ms, "elements": n, "elements_with_bf16_copy": n_sh, "bytes_per_step": nbytes,
+            "roofline": {"bound": "hbm", "kernel": "adam_kernel", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "l2": "working set larger than L2 (not flushed)",
+                         "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if "hbm_gbs" in peaks else "fallback"}}
+
+
 def run_radiance(args, dev):
     """Configurations 2 and 3 on the synthetic blob scene: rays/s of one fwd+bwd training step
     (plain sampler: 4,096 rays x up to 1,024 samples with 128^3 occupancy-bitfield pruning;
@@ -564,6 +619,8 @@ def run_radiance(args, dev):
             idx = torch.randint(0, pool.shape[0], (batch,), device=dev, generator=g)
             rec["field_kernels"] = measure_radiance_field_kernels(m, pool[idx], dev, flush, args.steps,
                                                                   max(args.warmup, 3))
+            # the optimizer update of the same model (last: it moves the parameters one step)
+            rec["adam"] = measure_adam(tr.opt, args.steps, max(args.warmup, 3))
         else:
             rec["samples_per_ray"] = sampler.n_fine
         out[kind] = rec
