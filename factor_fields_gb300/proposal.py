@@ -144,6 +144,10 @@ class ProposalSampler:
     def __init__(self, model, reso=64, n_bins=64, n_fine=48, hidden=64, lr_grid=2e-2, lr_mlp=1e-3,
                  density_shift=-4.0, precision="bf16", learned=True, seed=0, uniform_mix=0.0, fused_adam=True,
                  train_uniform=True, render_fine=None, sample_jitter=True, cull_render=False, fuse_render=True):
+        from .renderer import MLPRender_Fea
+        if isinstance(model.renderModule, MLPRender_Fea):
+            raise NotImplementedError("the proposal sampler composites with the degree-2 SH colour head "
+                                      "(renderer.shadingMode: SH); MLP_Fea shading is not supported here")
         self.m, self.learned, self.train_uniform = model, learned, train_uniform
         # cull_render: rendering (not training) on the fused path leaves out the samples that fail
         # the model's alpha mask (ff_proposal_resample_occupied). Off by default: a mask built by

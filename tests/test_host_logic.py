@@ -208,3 +208,17 @@ def test_save_averages_scene_coefficients(tmp_path):
     for c in m2.coeffs:
         assert torch.allclose(c, mean, rtol=1e-6, atol=1e-7)
     assert m2.gridSize.tolist() == n_to_reso(300 ** 3, m2.aabb.cpu())
+
+
+def test_proposal_sampler_refuses_mlp_fea_shading():
+    """The proposal sampler composites with the degree-2 SH head; a model shaded by MLPRender_Fea
+    is refused instead of being rendered with the wrong colour head."""
+    import pytest
+    from factor_fields_gb300 import FactorFields
+    from factor_fields_gb300 import workloads as W
+    from factor_fields_gb300.proposal import ProposalSampler
+    cfg = W.field_cfg("cfg2")
+    cfg.renderer.shadingMode = "MLP_Fea"
+    m = FactorFields(cfg, device="cpu")
+    with pytest.raises(NotImplementedError, match="SH"):
+        ProposalSampler(m)
