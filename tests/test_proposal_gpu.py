@@ -380,6 +380,24 @@ def test_fused_render_equals_field_forward_and_compositing(nf):
                N.ptr(depth), st)
 
 
+def test_fused_render_full_view_equals_two_call_render():
+    """At the evaluation shape (one 400x400 view: 160,000 rays x 32 samples), the sampler's fused
+    render (ff_field_render_fixed) gives the two-call render's colours and depths (1e-5)."""
+    from factor_fields_gb300 import workloads as W
+    m, s = make_sampler(reso=64, n_fine=48, precision="bf16")
+    m.cfg.renderer.density_shift = -4.0  # a denser initial field: some rays opaque, some not
+    s.render_fine = 32
+    rays = torch.from_numpy(W.BlobScene(0).ray_pool(160000, 6, views=[7])).float().cuda()
+    with torch.no_grad():
+        rgb_f, depth_f = s.render(rays, is_train=False)
+        assert s._job["w_f"] is None
+        s.fuse_render = False
+        rgb_u, depth_u = s.render(rays, is_train=False)
+    assert float((rgb_f - rgb_u).abs().max()) < 1e-5
+    assert float((depth_f - depth_u).abs().max()) < 1e-5 * float(depth_u.abs().max())
+    assert float(rgb_u.std()) > 1e-3  # not a blank image
+
+
 def test_proposal_loss_gradient_matches_finite_differences():
     from factor_fields_gb300 import _native as N
     m, s = make_sampler()
