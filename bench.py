@@ -604,7 +604,11 @@ def run_radiance(args, dev):
             sampler.render_fine = 32
             evaluation(eval_ds, m, N_vis=-1, N_samples=1024, white_bg=True, sampler=sampler)  # warm-up
             p32, x32 = evaluation(eval_ds, m, N_vis=-1, N_samples=1024, white_bg=True, sampler=sampler)
+            with torch.no_grad():
+                dep32 = torch.cat([tr.render(test[s0:s0 + 16384], is_train=False)[1]
+                                   for s0 in range(0, test.shape[0], 16384)])
             rec["render_32"] = {"psnr_db": tr.psnr(test, gtt), "samples_per_ray": 32,
+                                "depth_mae": float((dep32 - gtd).abs().mean()),
                                 "eval_400x400": {"ms_per_image": x32["ms_per_image"][0], "psnr_db": p32[0],
                                                  "ssim": x32["ssim"][0],
                                                  "rays_per_s": 400 * 400 / (x32["ms_per_image"][0] / 1e3)}}
@@ -655,9 +659,12 @@ def run_radiance(args, dev):
     out["proposal_target"] = {
         "target": "PSNR within 0.1 dB of the plain sampler at >= 3x its rays/s",
         "render_samples_32": {"rays_per_s_vs_plain": r32, "psnr_minus_plain_db_by_seed": diffs32,
+                              "depth_mae": out["cfg3_proposal"]["render_32"]["depth_mae"],
                               "met": bool(r32 >= 3.0 and min(diffs32) >= -0.1)},
         "render_samples_48": {"rays_per_s_vs_plain": r48, "psnr_minus_plain_db_by_seed": diffs,
+                              "depth_mae": out["cfg3_proposal"]["depth_mae"],
                               "met": bool(r48 >= 3.0 and min(diffs) >= -0.1)},
+        "plain_depth_mae": out["cfg2_plain"]["depth_mae"],
     }
     out["scene"] = "seeded 32 Gaussian density blobs in [-1.5,1.5]^3, 100 views 400x400 focal 555, white bg"
     return out
