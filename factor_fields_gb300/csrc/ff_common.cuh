@@ -5,6 +5,7 @@
 // order as the reference's PyTorch ops, so that the compiler cannot contract it into FMAs and
 // indices / interpolation weights come out bit-identical to the reference's float32 values.
 #pragma once
+#include <utility>
 
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -503,5 +504,28 @@ __device__ __forceinline__ float occupancy_value(const FFRender& r, const float*
 
 // The alpha-mask test of FactorFields.forward (models/FactorFields.py:866): sample_alpha > 0.5.
 __device__ __forceinline__ bool occupied(const FFRender& r, const float* p) { return occupancy_value(r, p) > 0.5f; }
+
+// Programmatic dependent launch (the binned fit step's chain: bin -> alloc -> permute -> fit). A
+// kernel launched with launch_pdl may start while the kernel before it in the stream still runs,
+// once that kernel has executed pdl_launch_dependents (or ended); it does its independent prologue,
+// then pdl_wait() returns when the kernel before it has completed and its memory is visible.
+// Without a programmatic launch both are no-ops.
+__device__ __forceinline__ void pdl_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+template <typename... KArgs, typename... Args>
+cudaError_t launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...);
+}
 
 }  // namespace ffgb

@@ -69,7 +69,7 @@ cudaError_t launch_fit_bin_phase(const FFField& f, const FFMlp& m, const float* 
 cudaError_t launch_fit_on_bins(const FFField& f, const void* basis, const void* coeff, const FFMlp& m, int64_t n,
                                int loss_kind, float loss_scale, float* loss_sum, float* grad_basis, float* grad_coeff,
                                const FFMlpGrad& g, const void* workspace, float loss_mul, bool level0_shared,
-                               cudaStream_t st);
+                               cudaStream_t st, bool after_bin = false);
 
 // fit_bin_kernels.cu
 int64_t fit_bin_keys(const FFField& f);

@@ -38,6 +38,7 @@ __global__ void __launch_bounds__(kBinThreads) fit_bin_kernel(const FFField f, c
                                                               int64_t n, int32_t n_keys, int32_t* __restrict__ count,
                                                               int2* __restrict__ key_rank,
                                                               const __grid_constant__ ZeroSet zs) {
+  pdl_launch_dependents();  // the alloc kernel may start; it waits for this one before reading counts
   const int64_t t0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t i = t0; i < n; i += stride) {
     float p[CD];
@@ -63,6 +64,8 @@ __global__ void __launch_bounds__(kBinThreads) fit_bin_kernel(const FFField f, c
 __global__ void __launch_bounds__(kBinThreads) fit_alloc_kernel(const int32_t* __restrict__ count, int64_t n_keys,
                                                                 int64_t* __restrict__ cursor,
                                                                 int64_t* __restrict__ start) {
+  pdl_launch_dependents();
+  pdl_wait();  // the counts are complete
   const int lane = threadIdx.x & 31;
   const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   for (int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; w * 32 < n_keys; w += warps) {
@@ -89,6 +92,7 @@ __global__ void __launch_bounds__(kBinThreads) fit_permute_kernel(const float* _
                                                                   int64_t n, const int2* __restrict__ key_rank,
                                                                   const int64_t* __restrict__ start, int stride,
                                                                   float* __restrict__ rows) {
+  pdl_wait();  // the ranges are complete
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const int2 kr = key_rank[i];
     float4* dst = reinterpret_cast<float4*>(rows + (start[kr.x] + kr.y) * stride);
@@ -106,6 +110,8 @@ __global__ void __launch_bounds__(kBinThreads) fit_permute_kernel(const float* _
       }
     }
   }
+  // the fit kernel (3 blocks per SM fill the register file) launches once every block is past here
+  pdl_launch_dependents();
 }
 
 int bin_blocks(int64_t n) {
@@ -184,15 +190,16 @@ cudaError_t launch_fit_bin(const FFField& f, const float* x, const float* target
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   const int ablocks = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(keys, kBinThreads), (int64_t)sm_count() * 8));
-  fit_alloc_kernel<<<ablocks, kBinThreads, 0, st>>>(count, keys, cursor, start);
-  e = cudaGetLastError();
+  e = launch_pdl(fit_alloc_kernel, dim3(ablocks), dim3(kBinThreads), 0, st, (const int32_t*)count, keys, cursor, start);
   if (e != cudaSuccess) return e;
   const int pblocks = bin_blocks(n);
   if (f.coord_dim == 3)
-    fit_permute_kernel<3><<<pblocks, kBinThreads, 0, st>>>(x, target, out_dim, n, key_rank, start, stride, rows);
+    e = launch_pdl(fit_permute_kernel<3>, dim3(pblocks), dim3(kBinThreads), 0, st, x, target, out_dim, n,
+                   (const int2*)key_rank, (const int64_t*)start, stride, rows);
   else
-    fit_permute_kernel<2><<<pblocks, kBinThreads, 0, st>>>(x, target, out_dim, n, key_rank, start, stride, rows);
-  return cudaGetLastError();
+    e = launch_pdl(fit_permute_kernel<2>, dim3(pblocks), dim3(kBinThreads), 0, st, x, target, out_dim, n,
+                   (const int2*)key_rank, (const int64_t*)start, stride, rows);
+  return e;
 }
 
 }  // namespace ffgb

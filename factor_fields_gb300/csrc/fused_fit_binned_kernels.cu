@@ -28,7 +28,7 @@ cudaError_t launch_fit_bin_phase(const FFField& f, const FFMlp& m, const float* 
 cudaError_t launch_fit_on_bins(const FFField& f, const void* basis, const void* coeff, const FFMlp& m, int64_t n,
                                int loss_kind, float loss_scale, float* loss_sum, float* grad_basis, float* grad_coeff,
                                const FFMlpGrad& g, const void* workspace, float loss_mul, bool level0_shared,
-                               cudaStream_t st) {
+                               cudaStream_t st, bool after_bin) {
   if (n == 0) return cudaSuccess;
   int64_t stride = 0;
   const float* rows = fit_bin_rows(f, n, m.out_dim, workspace, &stride);
@@ -50,6 +50,7 @@ cudaError_t launch_fit_on_bins(const FFField& f, const void* basis, const void* 
   a.grad_b0 = g.bias[0];
   a.grad_w1 = g.weight[1];
   a.level0_shared = level0_shared ? 1 : 0;
+  a.programmatic = after_bin ? 1 : 0;
   return dispatch_bf16<kFitBinned>(a, st);
 }
 
@@ -62,7 +63,7 @@ cudaError_t launch_fused_fit_binned(const FFField& f, const void* basis, const v
                                        st);
   if (e != cudaSuccess) return e;
   return launch_fit_on_bins(f, basis, coeff, m, n, loss_kind, loss_scale, loss_sum, grad_basis, grad_coeff, g,
-                            workspace, loss_mul, level0_shared, st);
+                            workspace, loss_mul, level0_shared, st, /*after_bin=*/true);
 }
 
 }  // namespace ffgb

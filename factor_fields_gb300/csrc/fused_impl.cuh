@@ -111,6 +111,7 @@ struct FusedArgs {
   float* grad_b0;
   float* grad_w1;
   int level0_shared;  // binned 2-D fits: level-0 basis gradients accumulated in shared memory
+  int programmatic;   // binned fits launched right after their row permutation: start during it
   // kRender: the points are the samples of rays of exactly nf samples (32, 64 or 128), ray r at
   // rows [r nf, (r + 1) nf); rd's density and colour rules, each sample's (z, dist) in zd
   FFRender rd;
@@ -303,6 +304,10 @@ __global__ void __launch_bounds__(kThreads, is_fwd<MODE>() ? 4 : 3) fused_field_
   if constexpr (L0S) {
     for (int e = tid; e < kL0Floats / 4; e += kThreads) reinterpret_cast<float4*>(s.g0)[e] = make_float4(0.f, 0.f, 0.f, 0.f);
   }
+  // a binned fit launched programmatically starts during the permutation of its rows: the weights
+  // and shared memory above do not depend on it (the weights were final before the binning
+  // started); the rows and the gradient buffers below do
+  if constexpr (MODE == kFitBinned) pdl_wait();
   __syncthreads();
 
   float loss_acc = 0.f;
@@ -590,13 +595,13 @@ __global__ void __launch_bounds__(kThreads, is_fwd<MODE>() ? 4 : 3) fused_field_
       }
       float excl;
       const float prod = excl_trans(sv.fac, lane, excl);
-      float T = 1.f;  // transmittance entering this chunk
+      float t_in = 1.f;  // transmittance entering this chunk
       if (wpr > 1) {
         if (lane == 0) s.part[warp * kPartStride] = prod;
         __syncthreads();
-        for (int q = warp - chunk; q < warp; ++q) T *= s.part[q * kPartStride];
+        for (int q = warp - chunk; q < warp; ++q) t_in *= s.part[q * kPartStride];
       }
-      const float w = live ? sv.alpha * (T * excl) : 0.f;
+      const float w = live ? sv.alpha * (t_in * excl) : 0.f;
       float acc = w, dep = w * sv.z, col[3] = {0.f, 0.f, 0.f};
       if (live && w > a.rd.weight_thres) {
         float c[3], lin[3];
@@ -851,6 +856,7 @@ cudaError_t launch_kernel(const FusedArgs& a, cudaStream_t st) {
   }
   const int64_t tiles = ceil_div(a.n, kTile);
   const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>(tiles, (int64_t)sm_count() * per_sm));
+  if (MODE == kFitBinned && a.programmatic) return launch_pdl(kern, dim3(blocks), dim3(kThreads), (size_t)smem, st, a);
   kern<<<blocks, kThreads, smem, st>>>(a);
   return cudaGetLastError();
 }
