@@ -251,10 +251,13 @@ def measure_field(key, args, ws, rank, local, flush, with_dropin):
 
     def e2e_step(i):
         x, y = host[i % nb]
-        loss = runner.graph_step(x, y)  # H2D copies from pinned host memory into the graph's inputs
+        # one replay per step: the captured call copies the pinned host batch into its workspace
+        # (FF_FIT_HOST_BATCH) before the binning; then the loss is read back to pinned host memory
+        loss = runner.graph_step(x, y)
         loss_host.copy_(loss.reshape(1), non_blocking=True)
         return None
 
+    runner.capture_graphs(host)  # setup: one graph per pinned host batch, as for the device ring
     for i in range(args.warmup):
         e2e_step(i)
     t_e2e, _ = timed(e2e_step, args.steps, False)

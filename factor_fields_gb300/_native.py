@@ -24,6 +24,7 @@ FF_LOSS = {"l1": 0, "mse": 1}
 FF_FIT_ZERO_GRADS = 1
 FF_FIT_MEAN_LOSS = 2
 FF_FIT_LEVEL0_SHARED = 4
+FF_FIT_HOST_BATCH = 8
 FF_ADAM_ZERO_GRAD = 1
 
 c_i32, c_i64, c_f32, c_vp = ctypes.c_int32, ctypes.c_int64, ctypes.c_float, ctypes.c_void_p
@@ -190,6 +191,13 @@ def ptr(t):
         return None
     if not t.is_cuda:
         raise NativeError("expected a CUDA tensor")
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def host_ptr(t):
+    """Address of a page-locked host tensor (the FF_FIT_HOST_BATCH inputs)."""
+    if t.is_cuda or not t.is_pinned():
+        raise NativeError("expected a page-locked host tensor")
     return ctypes.c_void_p(t.data_ptr())
 
 

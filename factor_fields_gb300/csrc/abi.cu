@@ -297,7 +297,7 @@ static int validate_fit_bin(const FFField* f, const FFMlp* m, const float* x, co
   if (rc) return rc;
   if (n < 0 || (n > 0 && !x)) return set_error(FF_ERR_ARG, "bad points pointer or count");
   if (n > 0 && !target) return set_error(FF_ERR_ARG, "target is NULL");
-  if (flags & ~FF_FIT_ZERO_GRADS) return set_error(FF_ERR_ARG, "unknown flags");
+  if (flags & ~(FF_FIT_ZERO_GRADS | FF_FIT_HOST_BATCH)) return set_error(FF_ERR_ARG, "unknown flags");
   if ((flags & FF_FIT_ZERO_GRADS) &&
       (!grad_basis || !grad_coeff_grid || !aligned(grad_basis, 16) || !aligned(grad_coeff_grid, 16)))
     return set_error(FF_ERR_ARG, "grid gradient buffers must be non-NULL and 16-byte aligned");
@@ -330,14 +330,18 @@ int ff_field_fit_step_binned(const FFField* f, const void* basis, const void* co
                              const float* target, int64_t n, int32_t loss_kind, float loss_scale, float* loss_sum,
                              float* grad_basis, float* grad_coeff_grid, const FFMlpGrad* g, int32_t flags,
                              void* workspace, int64_t workspace_bytes, void* stream) {
-  if (flags & ~(FF_FIT_ZERO_GRADS | FF_FIT_MEAN_LOSS | FF_FIT_LEVEL0_SHARED))
+  if (flags & ~(FF_FIT_ZERO_GRADS | FF_FIT_MEAN_LOSS | FF_FIT_LEVEL0_SHARED | FF_FIT_HOST_BATCH))
     return set_error(FF_ERR_ARG, "unknown flags");
   int rc = validate_fit_on_bins(f, basis, coeff, m, n, loss_kind, grad_basis, grad_coeff_grid,
                                 flags & (FF_FIT_MEAN_LOSS | FF_FIT_LEVEL0_SHARED), workspace, workspace_bytes);
   if (rc) return rc;
-  rc = validate_fit_bin(f, m, x, target, n, grad_basis, grad_coeff_grid, flags & FF_FIT_ZERO_GRADS, workspace,
-                        workspace_bytes);
+  rc = validate_fit_bin(f, m, x, target, n, grad_basis, grad_coeff_grid, flags & (FF_FIT_ZERO_GRADS | FF_FIT_HOST_BATCH),
+                        workspace, workspace_bytes);
   if (rc) return rc;
+  if ((flags & FF_FIT_HOST_BATCH) &&
+      cuda_status(fit_bin_stage_host(*f, &x, &target, m->out_dim, n, workspace, (cudaStream_t)stream),
+                  "ff_field_fit_step_binned host batch copy"))
+    return FF_ERR_CUDA;
   FFMlpGrad none = {};
   return cuda_status(launch_fused_fit_binned(*f, basis, coeff, *m, x, target, n, loss_kind, loss_scale, loss_sum,
                                              grad_basis, grad_coeff_grid, g ? *g : none, workspace,
@@ -354,6 +358,10 @@ int ff_field_fit_bin(const FFField* f, const FFMlp* m, const float* x, const flo
   if (rc) return rc;
   rc = validate_fit_bin(f, m, x, target, n, grad_basis, grad_coeff_grid, flags, workspace, workspace_bytes);
   if (rc) return rc;
+  if ((flags & FF_FIT_HOST_BATCH) &&
+      cuda_status(fit_bin_stage_host(*f, &x, &target, m->out_dim, n, workspace, (cudaStream_t)stream),
+                  "ff_field_fit_bin host batch copy"))
+    return FF_ERR_CUDA;
   FFMlpGrad none = {};
   return cuda_status(launch_fit_bin_phase(*f, *m, x, target, n, loss_sum, grad_basis, grad_coeff_grid, g ? *g : none,
                                           workspace, (flags & FF_FIT_ZERO_GRADS) != 0, (cudaStream_t)stream),

@@ -74,6 +74,10 @@ cudaError_t launch_fit_on_bins(const FFField& f, const void* basis, const void* 
 // fit_bin_kernels.cu
 int64_t fit_bin_keys(const FFField& f);
 int64_t fit_bin_workspace_bytes(const FFField& f, int64_t n, int out_dim);
+// FF_FIT_HOST_BATCH: copies (x, target) from host memory into the workspace on the stream and
+// points *x, *target at the copies
+cudaError_t fit_bin_stage_host(const FFField& f, const float** x, const float** target, int out_dim, int64_t n,
+                               void* workspace, cudaStream_t st);
 // Gradient buffers the binning pass zeroes (NULL entries skipped): the grid gradients (16-byte
 // aligned, sizes from the descriptor) and up to 4 small float buffers with explicit sizes.
 struct FitZero {

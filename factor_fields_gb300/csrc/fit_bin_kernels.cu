@@ -142,10 +142,30 @@ int64_t field_basis_elems(const FFField& f) {
 
 int64_t fit_bin_workspace_bytes(const FFField& f, int64_t n, int out_dim) {
   const int64_t keys = fit_bin_keys(f);
-  return align_up(keys * 4 + 16) + align_up(n * 8) + align_up(keys * 8) + align_up(n * row_stride(f, out_dim) * 4);
+  return align_up(keys * 4 + 16) + align_up(n * 8) + align_up(keys * 8) + align_up(n * row_stride(f, out_dim) * 4) +
+         align_up(n * f.coord_dim * 4) + align_up(n * out_dim * 4);
 }
 
-// Workspace layout: count[keys] + cursor | key_rank[n] | start[keys] | rows[n][stride].
+// Workspace layout: count[keys] + cursor | key_rank[n] | start[keys] | rows[n][stride] |
+// x[n][coord_dim] | target[n][out_dim] (the last two: a host batch's device copy).
+cudaError_t fit_bin_stage_host(const FFField& f, const float** x, const float** target, int out_dim, int64_t n,
+                               void* workspace, cudaStream_t st) {
+  const int64_t keys = fit_bin_keys(f);
+  unsigned char* w = static_cast<unsigned char*>(workspace) + align_up(keys * 4 + 16) + align_up(n * 8) +
+                     align_up(keys * 8) + align_up(n * row_stride(f, out_dim) * 4);
+  float* xs = reinterpret_cast<float*>(w);
+  float* ts = reinterpret_cast<float*>(w + align_up(n * f.coord_dim * 4));
+  if (n > 0) {
+    // cudaMemcpyDefault: the direction comes from the pointers (unified addressing)
+    cudaError_t e = cudaMemcpyAsync(xs, *x, n * f.coord_dim * 4, cudaMemcpyDefault, st);
+    if (e != cudaSuccess) return e;
+    e = cudaMemcpyAsync(ts, *target, n * out_dim * 4, cudaMemcpyDefault, st);
+    if (e != cudaSuccess) return e;
+  }
+  *x = xs;
+  *target = ts;
+  return cudaSuccess;
+}
 const float* fit_bin_rows(const FFField& f, int64_t n, int out_dim, const void* workspace, int64_t* stride_out) {
   const int64_t keys = fit_bin_keys(f);
   *stride_out = row_stride(f, out_dim);

@@ -217,7 +217,7 @@ class FieldFitRunner:
         N.call("ff_zero_f32", self._zero_ptrs, self._zero_counts, len(bufs), N.stream_ptr(),
                kernels=-(-len(bufs) // 8))
 
-    _GRAPHS_KEPT = 8  # graphs of device input pairs read in place (least recently used first out)
+    _GRAPHS_KEPT = 8  # graphs per kind of input pair read in place (device, host; least recently used first out)
 
     def graph_step(self, x, y):
         """step() replayed from a CUDA graph, one host call for all its launches (the binning with
@@ -225,26 +225,28 @@ class FieldFitRunner:
 
         Device batches (contiguous float32 on the model's device) are read in place: a graph is
         captured per input buffer pair and kept (up to 8), so that a ring of batches resident in
-        HBM replays without copies. Any other batch (host memory, other dtypes or strides) is
-        copied into static buffers whose graph then replays. Graphs are re-captured when the batch
-        shape, a parameter buffer or the binning workspace changes. The returned 0-d loss belongs
-        to the replayed graph: the next replay of the same graph overwrites it."""
-        key, in_place = self._graph_key(x, y)
+        HBM replays without copies. Page-locked host batches (contiguous float32, pin_memory())
+        get a graph per buffer pair too (up to 8), which holds the step's own host-to-device
+        copies (FF_FIT_HOST_BATCH): the replay reads the host buffers' contents at that time. Any
+        other batch (pageable host memory, other dtypes or strides) is copied into static
+        buffers whose graph then replays. Graphs are re-captured when the batch shape, a parameter
+        buffer or the binning workspace changes. The returned 0-d loss belongs to the replayed
+        graph: the next replay of the same graph overwrites it."""
+        key, kind = self._graph_key(x, y)
         graphs = self.__dict__.setdefault("_graphs", OrderedDict())
         ent = graphs.get(key)
         if ent is not None and ent["ws_gen"] != self._ws_gen:  # captured with a workspace since freed
             del graphs[key]
             ent = None
         if ent is None:
-            ent = self._capture(x, y, in_place)
+            ent = self._capture(x, y, kind)
             graphs[key] = ent
             for k in [k for k, e in graphs.items() if e["ws_gen"] != self._ws_gen]:
                 del graphs[k]
-            while len(graphs) > self._GRAPHS_KEPT + 1:
-                graphs.popitem(last=False)
+            self._evict(graphs, kind)
         graphs.move_to_end(key)
         self.m._read_buffers()  # refresh the BF16 grid copies in place if the masters changed
-        if not in_place:
+        if kind == "static":
             ent["x"].copy_(x, non_blocking=True)
             ent["y"].copy_(y, non_blocking=True)
         ent["graph"].replay()
@@ -256,24 +258,58 @@ class FieldFitRunner:
         graphs = self.__dict__.setdefault("_graphs", OrderedDict())
         if len(batches) > self._GRAPHS_KEPT:
             raise ValueError(f"at most {self._GRAPHS_KEPT} batches keep their graphs")
+        kinds = set()
         for x, y in batches:
-            key, in_place = self._graph_key(x, y)
+            key, kind = self._graph_key(x, y)
+            kinds.add(kind)
             if key not in graphs or graphs[key]["ws_gen"] != self._ws_gen:
-                graphs[key] = self._capture(x, y, in_place)
+                graphs[key] = self._capture(x, y, kind)
+            graphs.move_to_end(key)
         for k in [k for k, e in graphs.items() if e["ws_gen"] != self._ws_gen]:
             del graphs[k]
+        for kind in kinds:
+            self._evict(graphs, kind)
+
+    def _evict(self, graphs, kind):
+        """Keep at most _GRAPHS_KEPT graphs of this kind (one for "static"), oldest out first."""
+        cap = 1 if kind == "static" else self._GRAPHS_KEPT
+        same = [k for k, e in graphs.items() if e["kind"] == kind]
+        for k in same[:max(0, len(same) - cap)]:
+            del graphs[k]
+
+    def _host_batch(self, x, y):
+        """FF_FIT_HOST_BATCH for a page-locked float32 host batch on the binned path, else 0
+        (device batches; anything else on the host is refused)."""
+        if x.device.type != "cpu" and y.device.type != "cpu":
+            return 0
+        if not (self.fused and self.binned):
+            raise ValueError("host batches need the binned fused path; copy the batch to the device first")
+        if not (x.device.type == y.device.type == "cpu" and x.dtype == y.dtype == torch.float32
+                and x.is_contiguous() and y.is_contiguous() and x.is_pinned() and y.is_pinned()):
+            raise ValueError("a host batch must be contiguous float32 in page-locked memory (tensor.pin_memory())")
+        return N.FF_FIT_HOST_BATCH
 
     def _graph_key(self, x, y):
+        """(key, kind): kind "device" reads a device batch in place, "host" copies a pinned host
+        batch inside the graph (FF_FIT_HOST_BATCH), "static" copies anything else into static
+        device buffers before the replay."""
         dev = self.m.basis_flat.device
-        in_place = (x.device == dev and y.device == dev and x.dtype == torch.float32 and y.dtype == torch.float32
-                    and x.is_contiguous() and y.is_contiguous())
+        if (x.device == dev and y.device == dev and x.dtype == torch.float32 and y.dtype == torch.float32
+                and x.is_contiguous() and y.is_contiguous()):
+            kind, tag = "device", (x.data_ptr(), y.data_ptr())
+        elif (self.fused and self.binned and x.device.type == y.device.type == "cpu"
+              and x.dtype == y.dtype == torch.float32 and x.is_contiguous() and y.is_contiguous()
+              and x.is_pinned() and y.is_pinned()):
+            kind, tag = "host", ("host", x.data_ptr(), y.data_ptr())
+        else:
+            kind, tag = "static", ("static",)
         key = (tuple(x.shape), tuple(y.shape), self.m.basis_flat.data_ptr(), self.m.coeff_flat.data_ptr(),
-               self.m.precision) + ((x.data_ptr(), y.data_ptr()) if in_place else ("static",))
-        return key, in_place
+               self.m.precision) + tag
+        return key, kind
 
-    def _capture(self, x, y, in_place):
+    def _capture(self, x, y, kind):
         dev = self.m.basis_flat.device
-        if in_place:
+        if kind != "static":  # read in place: the device batch, or the host batch by the call's own copies
             xs, ys = x, y
         else:
             xs = torch.empty(x.shape, dtype=torch.float32, device=dev)
@@ -289,7 +325,8 @@ class FieldFitRunner:
         graph = torch.cuda.CUDAGraph()
         with torch.cuda.graph(graph):
             loss = self.step(xs, ys, _loss_buf=loss_buf)
-        return {"graph": graph, "loss": loss, "x": xs, "y": ys, "buf": loss_buf, "ws_gen": self._ws_gen}
+        return {"graph": graph, "loss": loss, "x": xs, "y": ys, "buf": loss_buf, "ws_gen": self._ws_gen,
+                "kind": kind}
 
     def _workspace(self, desc, n):
         """Device workspace of ff_field_fit_step_binned for n points, kept across steps."""
@@ -302,7 +339,10 @@ class FieldFitRunner:
         return self._ws
 
     def step(self, x, y, kernel_events=False, _loss_buf=None):
+        """One step on (x, y): device tensors, or (binned path) page-locked host tensors that the
+        call copies into its workspace itself (FF_FIT_HOST_BATCH)."""
         m = self.m
+        host = self._host_batch(x, y)
         if not (self.fused and self.binned):  # the binned call zeroes them in its binning pass
             self.zero_grad(_loss_buf)
         basis_r, coeff_r, dt = m._read_buffers()
@@ -325,9 +365,10 @@ class FieldFitRunner:
             lbuf = self.loss_buf if _loss_buf is None else _loss_buf
             scale = 1.0 / max(n * m.linear_mat.out_dim, 1)
             gb, gc = N.ptr(m.basis_flat.grad), N.ptr(m.coeff_flat.grad)
+            xp, yp = (N.host_ptr(x), N.host_ptr(y)) if host else (N.ptr(x), N.ptr(y))
             if self.binned and split:  # the same launches as one ff_field_fit_step_binned call, in two calls
-                N.call("ff_field_fit_bin", ctypes.byref(desc), ctypes.byref(mlp), N.ptr(x), N.ptr(y), n, N.ptr(lbuf),
-                       gb, gc, ctypes.byref(g), N.FF_FIT_ZERO_GRADS, N.ptr(ws), ws.numel(), st)
+                N.call("ff_field_fit_bin", ctypes.byref(desc), ctypes.byref(mlp), xp, yp, n, N.ptr(lbuf),
+                       gb, gc, ctypes.byref(g), N.FF_FIT_ZERO_GRADS | host, N.ptr(ws), ws.numel(), st)
                 ev[1].record()
                 N.call("ff_field_fit_step_on_bins", ctypes.byref(desc), N.ptr(basis_r), N.ptr(coeff_r),
                        ctypes.byref(mlp), n, N.FF_LOSS[self.loss], scale, N.ptr(lbuf), gb, gc, ctypes.byref(g),
@@ -335,11 +376,12 @@ class FieldFitRunner:
             else:
                 if ev:
                     ev[1].record()
-                common = (ctypes.byref(desc), N.ptr(basis_r), N.ptr(coeff_r), ctypes.byref(mlp), N.ptr(x), N.ptr(y),
+                common = (ctypes.byref(desc), N.ptr(basis_r), N.ptr(coeff_r), ctypes.byref(mlp), xp, yp,
                           n, N.FF_LOSS[self.loss], scale, N.ptr(lbuf), gb, gc, ctypes.byref(g))
                 if self.binned:  # kernels: bin (+ gradient and loss zeroing), alloc, permute, fit (mean loss)
-                    N.call("ff_field_fit_step_binned", *common, N.FF_FIT_ZERO_GRADS | N.FF_FIT_MEAN_LOSS | self._l0,
-                           N.ptr(ws), ws.numel(), st, kernels=4)
+                    N.call("ff_field_fit_step_binned", *common,
+                           N.FF_FIT_ZERO_GRADS | N.FF_FIT_MEAN_LOSS | self._l0 | host, N.ptr(ws), ws.numel(), st,
+                           kernels=4)
                 else:
                     N.call("ff_field_fit_step", *common, st)
             if ev:

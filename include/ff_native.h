@@ -60,7 +60,7 @@ enum { FF_INTERP_LINEAR = 0, FF_INTERP_NEAREST = 1 };
 enum { FF_F32 = 0, FF_BF16 = 1 };
 enum { FF_LOSS_L1 = 0, FF_LOSS_MSE = 1 };
 /* ff_field_fit_step_binned flags */
-enum { FF_FIT_ZERO_GRADS = 1, FF_FIT_MEAN_LOSS = 2, FF_FIT_LEVEL0_SHARED = 4 };
+enum { FF_FIT_ZERO_GRADS = 1, FF_FIT_MEAN_LOSS = 2, FF_FIT_LEVEL0_SHARED = 4, FF_FIT_HOST_BATCH = 8 };
 
 /*
  * Description of one grid/grid factor field (models/FactorFields.py:262-309 setup_params,
@@ -206,6 +206,12 @@ FF_API int ff_field_fit_step(const FFField* f, const void* basis, const void* co
  * gradients in shared memory and adds them to grad_basis once, one float4 atomic per touched
  * cell, instead of one global atomic per point and corner. Same gradients up to float32
  * summation order.
+ * FF_FIT_HOST_BATCH: x and target are host memory (page-locked, e.g. cudaHostAlloc or a pinned
+ * torch tensor, for an asynchronous copy; pageable memory works but its copy is synchronous
+ * and cannot be captured in a CUDA graph). The call copies them into the workspace
+ * (cudaMemcpyAsync on the stream, in stream order before the binning) and bins from there, so a
+ * captured step holds its own host-to-device copies. The host memory is read when the copies
+ * run, not during the call.
  * workspace: device memory of at least ff_field_fit_binned_workspace_bytes(f, n, out_dim)
  * bytes, 256-byte aligned, not shared with a call in flight. */
 FF_API int64_t ff_field_fit_binned_workspace_bytes(const FFField* f, int64_t n, int32_t out_dim);
@@ -217,8 +223,8 @@ FF_API int ff_field_fit_step_binned(const FFField* f, const void* basis, const v
 
 /* The two halves of ff_field_fit_step_binned, one call each (the same launches in the same
  * order), for callers that time the fit kernel apart from the binning or bin a batch once for
- * several steps. ff_field_fit_bin: bins (x, target) into the workspace; flags: FF_FIT_ZERO_GRADS
- * (grad_basis, grad_coeff_grid, g and loss_sum are touched only by that zeroing; the grids' values
+ * several steps. ff_field_fit_bin: bins (x, target) into the workspace; flags: FF_FIT_ZERO_GRADS,
+ * FF_FIT_HOST_BATCH (grad_basis, grad_coeff_grid, g and loss_sum are touched only by that zeroing; the grids' values
  * are not read, so f alone describes them). ff_field_fit_step_on_bins: the fit on the rows that the
  * last ff_field_fit_bin call on this workspace wrote for the same f, n and m->out_dim, in stream
  * order; flags: FF_FIT_MEAN_LOSS, FF_FIT_LEVEL0_SHARED. */

@@ -88,8 +88,9 @@ def test_argument_validation_before_any_launch(lib):
 
 
 def test_binned_fit_halves_validate_their_flags(lib):
-    """ff_field_fit_bin takes FF_FIT_ZERO_GRADS only, ff_field_fit_step_on_bins FF_FIT_MEAN_LOSS
-    only; both reject a missing or short workspace (all before any launch)."""
+    """ff_field_fit_bin takes FF_FIT_ZERO_GRADS and FF_FIT_HOST_BATCH, ff_field_fit_step_on_bins
+    FF_FIT_MEAN_LOSS and FF_FIT_LEVEL0_SHARED; both reject a missing or short workspace (all
+    before any launch)."""
     from factor_fields_gb300 import FactorFields
     from factor_fields_gb300 import functional as FN
     from factor_fields_gb300 import workloads as W
@@ -114,8 +115,10 @@ def test_binned_fit_halves_validate_their_flags(lib):
     assert lib.ff_field_fit_step_on_bins(*args_fit, N.FF_FIT_MEAN_LOSS, ws, need - 1, None) == N.FF_ERR_SIZE
     assert lib.ff_field_fit_step_on_bins(*args_fit, N.FF_FIT_MEAN_LOSS, vp(128), need, None) == N.FF_ERR_ALIGN
     assert lib.ff_field_fit_step_binned(ctypes.byref(desc), vp(16), vp(16), ctypes.byref(mlp), vp(16), vp(16), n,
-                                        N.FF_LOSS["l1"], 1.0 / n, vp(16), vp(16), vp(16), ctypes.byref(g), 8, ws, need,
+                                        N.FF_LOSS["l1"], 1.0 / n, vp(16), vp(16), vp(16), ctypes.byref(g), 16, ws, need,
                                         None) == N.FF_ERR_ARG
+    # the host batch is the binning half's input: the fit half has none
+    assert lib.ff_field_fit_step_on_bins(*args_fit, N.FF_FIT_HOST_BATCH, ws, need, None) == N.FF_ERR_ARG
 
 
 def test_render_head_validation(lib):

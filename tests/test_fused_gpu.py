@@ -208,9 +208,10 @@ def test_unsupported_shapes_fail_loudly():
 
 
 def test_graph_step_matches_step_and_tracks_updates():
-    """The CUDA-graph replay gives the eager step's loss and gradients, for batches from host
-    memory and from the GPU, also after optimizer updates of the float32 masters (the BF16
-    copies refresh in place)."""
+    """The CUDA-graph replay gives the eager step's loss and gradients, for batches from pageable
+    host memory (static buffers), from page-locked host memory (the graph holds the call's own
+    copies, FF_FIT_HOST_BATCH) and from the GPU, also after optimizer updates of the float32
+    masters (the BF16 copies refresh in place). The eager step takes a page-locked batch too."""
     from factor_fields_gb300 import FactorFields
     from factor_fields_gb300 import workloads as W
     from factor_fields_gb300.train import FieldFitRunner
@@ -220,14 +221,19 @@ def test_graph_step_matches_step_and_tracks_updates():
     opt = torch.optim.Adam(m.parameters(), lr=1e-2)
     batches = [W.sdf_batch(10 + it, 4096) for it in range(2)]
     dev = [(torch.from_numpy(a).cuda(), torch.from_numpy(b).cuda()) for a, b in batches]
+    pinned = [(torch.from_numpy(a).pin_memory(), torch.from_numpy(b).pin_memory()) for a, b in batches]
     for it in range(4):
         xs, ys = batches[it % 2]
         x, y = dev[it % 2]
         l_eager = float(r.step(x, y))
         g_eager = [p.grad.clone() for p in r._params()]
-        for src in ("host", "device"):
+        for src in ("host", "pinned", "pinned eager", "device"):
             if src == "host":
                 l_graph = float(r.graph_step(torch.from_numpy(xs), torch.from_numpy(ys)))
+            elif src == "pinned":
+                l_graph = float(r.graph_step(*pinned[it % 2]))
+            elif src == "pinned eager":
+                l_graph = float(r.step(*pinned[it % 2]))
             else:
                 l_graph = float(r.graph_step(x, y))
             torch.cuda.synchronize()
@@ -243,7 +249,44 @@ def test_graph_step_matches_step_and_tracks_updates():
     torch.cuda.synchronize()
     assert abs(float(la) - eager[0]) <= 1e-6 * max(1.0, abs(eager[0]))
     assert abs(float(lb) - eager[1]) <= 1e-6 * max(1.0, abs(eager[1]))
-    assert len(r._graphs) == 3  # two device pairs + the static buffers of the host batches
+    kinds = sorted(e["kind"] for e in r._graphs.values())
+    assert kinds == ["device", "device", "host", "host", "static"]  # + the static buffers of pageable batches
+    # a page-locked batch refilled in place: the replay reads the buffers' contents at that time
+    px, py = pinned[0]
+    px.copy_(torch.from_numpy(batches[1][0]))
+    py.copy_(torch.from_numpy(batches[1][1]))
+    l_refill = float(r.graph_step(px, py))
+    assert abs(l_refill - eager[1]) <= 1e-6 * max(1.0, abs(eager[1]))
+    # pageable host memory is refused by the eager step (its copy could not be asynchronous)
+    with pytest.raises(ValueError):
+        r.step(torch.from_numpy(batches[0][0]), torch.from_numpy(batches[0][1]))
+
+
+def test_host_batch_graphs_are_kept_per_kind():
+    """Up to 8 graphs of device batches and 8 of page-locked host batches are kept side by side:
+    cycling through 8 of each re-captures nothing."""
+    from factor_fields_gb300 import FactorFields
+    from factor_fields_gb300 import workloads as W
+    from factor_fields_gb300.train import FieldFitRunner
+    m = FactorFields(W.field_cfg("cfg1"), device="cuda", precision="bf16")
+    r = FieldFitRunner(m, loss="l1")
+    batches = [W.sdf_batch(40 + i, 1024) for i in range(9)]
+    dev = [(torch.from_numpy(a).cuda(), torch.from_numpy(b).cuda()) for a, b in batches[:8]]
+    pinned = [(torch.from_numpy(a).pin_memory(), torch.from_numpy(b).pin_memory()) for a, b in batches[:8]]
+    r.capture_graphs(dev)
+    r.capture_graphs(pinned)
+    graphs = dict(r._graphs)
+    for _ in range(2):
+        for d, h in zip(dev, pinned):
+            r.graph_step(*d)
+            r.graph_step(*h)
+    torch.cuda.synchronize()
+    assert len(r._graphs) == 16 and all(graphs[k] is e for k, e in r._graphs.items())
+    # a ninth host pair evicts the least recently used host graph only
+    extra = tuple(torch.from_numpy(t).pin_memory() for t in batches[8])
+    r.graph_step(*extra)
+    kinds = [e["kind"] for e in r._graphs.values()]
+    assert kinds.count("device") == 8 and kinds.count("host") == 8
 
 
 @pytest.mark.parametrize("precision", ["bf16", "fp32"])

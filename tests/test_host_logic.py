@@ -222,3 +222,21 @@ def test_proposal_sampler_refuses_mlp_fea_shading():
     m = FactorFields(cfg, device="cpu")
     with pytest.raises(NotImplementedError, match="SH"):
         ProposalSampler(m)
+
+
+def test_fit_runner_host_batch_rules():
+    """A fit step takes a host batch only on the binned path and only from page-locked memory
+    (FF_FIT_HOST_BATCH copies it asynchronously); anything else is refused before a call."""
+    import pytest
+    import torch
+    from factor_fields_gb300 import FactorFields
+    from factor_fields_gb300 import workloads as W
+    from factor_fields_gb300.train import FieldFitRunner
+    m = FactorFields(W.field_cfg("cfg1"), device="cpu", precision="bf16")
+    x, y = torch.zeros(16, 3), torch.zeros(16, 1)
+    with pytest.raises(ValueError, match="page-locked"):
+        FieldFitRunner(m, loss="l1")._host_batch(x, y)
+    with pytest.raises(ValueError, match="binned"):
+        FieldFitRunner(m, loss="l1", fused=True, binned=False)._host_batch(x, y)
+    with pytest.raises(ValueError, match="binned"):
+        FieldFitRunner(m, loss="l1", fused=False)._host_batch(x, y)
