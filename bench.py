@@ -616,6 +616,25 @@ def run_radiance(args, dev):
                                                  "ssim": x32["ssim"][0],
                                                  "rays_per_s": 400 * 400 / (x32["ms_per_image"][0] / 1e3)}}
             sampler.render_fine = sampler.n_fine
+        # the whole training step (fwd + bwd + the fused Adam updates) replayed from one CUDA
+        # graph (FusedAdam's device schedule), at the training batch: the eager step above is
+        # bound by the host issuing its launches
+        gtimes = []
+        for i in range(max(args.warmup, 3) + args.steps):
+            idx = torch.randint(0, pool.shape[0], (4096,), device=dev, generator=g)
+            rb, gb = pool[idx], gt[idx]
+            flush.zero_()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            tr.graph_step(rb, gb, optimize=True)
+            e1.record()
+            torch.cuda.synchronize()
+            if i >= max(args.warmup, 3):
+                gtimes.append(e0.elapsed_time(e1))
+        gms = float(np.mean(gtimes))
+        rec["train_step_ms_with_adam_graph"] = gms
+        rec["train_rays_per_s_with_adam_graph"] = 4096 / (gms / 1e3)
         if sampler is None and not args.no_cpu_baseline:
             rec["cpu_baseline"] = run_cpu_baseline_render(m, pool, gt)
             rec["rays_per_s_vs_cpu_baseline"] = rec["rays_per_s"] / rec["cpu_baseline"]["value"]
@@ -632,6 +651,9 @@ def run_radiance(args, dev):
             rec["samples_per_ray"] = sampler.n_fine
         out[kind] = rec
     out["proposal_rays_per_s_vs_plain"] = out["cfg3_proposal"]["rays_per_s"] / out["cfg2_plain"]["rays_per_s"]
+    # whole training steps with the optimizer, both from CUDA graphs, 4,096 rays each
+    out["proposal_train_rays_per_s_vs_plain_with_adam_graph"] = (
+        out["cfg3_proposal"]["train_rays_per_s_with_adam_graph"] / out["cfg2_plain"]["train_rays_per_s_with_adam_graph"])
     # like for like: both samplers at 8,192 rays per step, both replayed from CUDA graphs
     out["proposal_rays_per_s_vs_plain_same_batch"] = (out["cfg3_proposal"]["rays_per_s_at_8192"] /
                                                       out["cfg2_plain"]["rays_per_s_at_8192"])

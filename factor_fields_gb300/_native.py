@@ -104,6 +104,7 @@ SIGNATURES = {
                                           _P(FFMlpGrad), c_i32, c_vp, c_i64, c_vp]),
     "ff_zero_f32": (c_i32, [c_vp, c_vp, c_i32, c_vp]),
     "ff_adam_step": (c_i32, [c_vp, c_i32, c_f32, c_f32, c_f32, c_i32, c_vp]),
+    "ff_adam_step_scheduled": (c_i32, [c_vp, c_i32, c_f32, c_f32, c_f32, c_i32, c_vp, c_vp, c_vp]),
     "ff_image_metrics_workspace_bytes": (c_i64, [c_i32, c_i32, c_i32]),
     "ff_image_metrics": (c_i32, [c_vp, c_vp, c_i32, c_i32, c_i32, c_f32, c_vp, c_vp, c_i64, c_vp]),
     "ff_filter_rays": (c_i32, [_P(FFRender), c_vp, c_i64, c_i32, c_i32, c_vp, c_vp]),

@@ -390,8 +390,8 @@ int ff_zero_f32(float* const* ptrs, const int64_t* counts, int32_t n_buffers, vo
   return cuda_status(launch_zero_buffers(ptrs, counts, n_buffers, (cudaStream_t)stream), "ff_zero_f32 launch");
 }
 
-int ff_adam_step(const FFAdamParam* params, int32_t n_params, float beta1, float beta2, float eps, int32_t flags,
-                 void* stream) {
+static int validate_adam(const FFAdamParam* params, int32_t n_params, float beta1, float beta2, float eps,
+                         int32_t flags, bool host_schedule) {
   if (n_params < 0 || (n_params > 0 && !params)) return set_error(FF_ERR_ARG, "bad parameter list");
   if (flags & ~FF_ADAM_ZERO_GRAD) return set_error(FF_ERR_ARG, "unknown flags");
   if (!(beta1 >= 0.f && beta1 < 1.f && beta2 >= 0.f && beta2 < 1.f && eps >= 0.f))
@@ -400,12 +400,30 @@ int ff_adam_step(const FFAdamParam* params, int32_t n_params, float beta1, float
     const FFAdamParam& q = params[b];
     if (q.n < 0 || (q.n > 0 && (!q.param || !q.grad || !q.exp_avg || !q.exp_avg_sq)))
       return set_error(FF_ERR_ARG, "parameter " + std::to_string(b) + ": NULL buffer or negative size");
-    if (q.n > 0 && q.step < 1) return set_error(FF_ERR_ARG, "step must be >= 1");
+    if (host_schedule && q.n > 0 && q.step < 1) return set_error(FF_ERR_ARG, "step must be >= 1");
     if (q.param_bf16 && !aligned(q.param_bf16, 2)) return set_error(FF_ERR_ALIGN, "param_bf16 misaligned");
   }
+  return FF_OK;
+}
+
+int ff_adam_step(const FFAdamParam* params, int32_t n_params, float beta1, float beta2, float eps, int32_t flags,
+                 void* stream) {
+  const int rc = validate_adam(params, n_params, beta1, beta2, eps, flags, true);
+  if (rc) return rc;
   return cuda_status(launch_adam(params, n_params, beta1, beta2, eps, (flags & FF_ADAM_ZERO_GRAD) != 0,
                                  (cudaStream_t)stream),
                      "ff_adam_step launch");
+}
+
+int ff_adam_step_scheduled(const FFAdamParam* params, int32_t n_params, float beta1, float beta2, float eps,
+                           int32_t flags, const double* lr, const int64_t* step, void* stream) {
+  const int rc = validate_adam(params, n_params, beta1, beta2, eps, flags, false);
+  if (rc) return rc;
+  if (n_params > 0 && (!lr || !step)) return set_error(FF_ERR_ARG, "lr and step must be device pointers");
+  if (!aligned(lr, 8) || !aligned(step, 8)) return set_error(FF_ERR_ALIGN, "lr and step must be 8-byte aligned");
+  return cuda_status(launch_adam(params, n_params, beta1, beta2, eps, (flags & FF_ADAM_ZERO_GRAD) != 0,
+                                 (cudaStream_t)stream, lr, step),
+                     "ff_adam_step_scheduled launch");
 }
 
 int64_t ff_image_metrics_workspace_bytes(int32_t height, int32_t width, int32_t channels) {

@@ -100,7 +100,7 @@ cudaError_t launch_zero_buffers(float* const* ptrs, const int64_t* counts, int n
 
 // optim_kernels.cu
 cudaError_t launch_adam(const FFAdamParam* prm, int n, float beta1, float beta2, float eps, bool zero_grad,
-                        cudaStream_t st);
+                        cudaStream_t st, const double* lr_dev = nullptr, const int64_t* step_dev = nullptr);
 
 // metrics_kernels.cu
 int64_t image_metrics_workspace_bytes(int h, int w, int c);

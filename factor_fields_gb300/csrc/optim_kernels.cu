@@ -8,7 +8,10 @@
 //   m = lerp(m, g, 1 - beta1)              (m + w (g - m) for w < 0.5, else g - (g - m)(1 - w))
 //   v = v * beta2 + (1 - beta2) * g * g    (mul_, addcmul_)
 //   p = p - step_size * m / (sqrt(v) / sqrt(bc2) + eps),  step_size = lr / bc1
-// with bc1 = 1 - beta1^t, bc2 = 1 - beta2^t computed on the host in double precision.
+// with bc1 = 1 - beta1^t, bc2 = 1 - beta2^t computed in double precision: on the host from each
+// parameter's step and lr, or (the scheduled form) by each block from the learning rate and the
+// step counter in device memory, so that a captured CUDA graph replays the update with the
+// current values (torch computes them in Python floats, i.e. double precision, too).
 #include "ff_common.cuh"
 #include "ff_internal.h"
 
@@ -26,8 +29,9 @@ struct AdamParamDev {
   float* v;
   __nv_bfloat16* shadow;
   int64_t n;
-  float neg_step_size;  // -lr / bc1
+  float neg_step_size;  // -lr / bc1 (host schedule)
   float bc2_sqrt;
+  const double* lr;     // scheduled form: this parameter's learning rate in device memory
 };
 
 struct AdamJob {
@@ -35,10 +39,16 @@ struct AdamJob {
   float w1;  // 1 - beta1 (lerp weight)
   float beta2, one_minus_beta2, eps;
   int zero_grad;
+  double beta1_d, beta2_d;  // the scheduled form's bias corrections
+  const int64_t* step;      // scheduled form: t after this update, shared by all parameters
+};
+
+struct AdamScale {
+  float neg_step_size, bc2_sqrt;
 };
 
 __device__ __forceinline__ float adam_elem(float& p, float g, float& m, float& v, const AdamJob& j,
-                                           const AdamParamDev& a) {
+                                           const AdamScale& a) {
   const float w = j.w1;
   m = w < 0.5f ? __fadd_rn(m, __fmul_rn(w, __fsub_rn(g, m)))
                : __fsub_rn(g, __fmul_rn(__fsub_rn(g, m), __fsub_rn(1.f, w)));
@@ -51,6 +61,18 @@ __device__ __forceinline__ float adam_elem(float& p, float g, float& m, float& v
 // blockIdx.y: the parameter. float4 path when all four arrays are 16-byte aligned.
 __global__ void __launch_bounds__(kAdamThreads) adam_kernel(const __grid_constant__ AdamJob job) {
   const AdamParamDev& a = job.prm[blockIdx.y];
+  AdamScale sc = {a.neg_step_size, a.bc2_sqrt};
+  if (job.step) {  // scheduled: one thread per block derives the scales from lr and t
+    __shared__ AdamScale s_sc;
+    if (threadIdx.x == 0) {
+      const double t = (double)*job.step;
+      const double bc1 = 1.0 - pow(job.beta1_d, t), bc2 = 1.0 - pow(job.beta2_d, t);
+      s_sc.neg_step_size = (float)(-*a.lr / bc1);
+      s_sc.bc2_sqrt = (float)sqrt(bc2);
+    }
+    __syncthreads();
+    sc = s_sc;
+  }
   const int64_t t0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, stride = (int64_t)gridDim.x * blockDim.x;
   const bool vec = ((reinterpret_cast<uintptr_t>(a.p) | reinterpret_cast<uintptr_t>(a.g) |
                      reinterpret_cast<uintptr_t>(a.m) | reinterpret_cast<uintptr_t>(a.v)) & 15) == 0 &&
@@ -64,10 +86,10 @@ __global__ void __launch_bounds__(kAdamThreads) adam_kernel(const __grid_constan
     float4* v4 = reinterpret_cast<float4*>(a.v);
     for (int64_t i = t0; i < n4; i += stride) {
       float4 p = p4[i], g = g4[i], m = m4[i], v = v4[i];
-      adam_elem(p.x, g.x, m.x, v.x, job, a);
-      adam_elem(p.y, g.y, m.y, v.y, job, a);
-      adam_elem(p.z, g.z, m.z, v.z, job, a);
-      adam_elem(p.w, g.w, m.w, v.w, job, a);
+      adam_elem(p.x, g.x, m.x, v.x, job, sc);
+      adam_elem(p.y, g.y, m.y, v.y, job, sc);
+      adam_elem(p.z, g.z, m.z, v.z, job, sc);
+      adam_elem(p.w, g.w, m.w, v.w, job, sc);
       p4[i] = p;
       m4[i] = m;
       v4[i] = v;
@@ -85,7 +107,7 @@ __global__ void __launch_bounds__(kAdamThreads) adam_kernel(const __grid_constan
   for (int64_t i = done + t0; i < a.n; i += stride) {
     float p = a.p[i], m = a.m[i], v = a.v[i];
     const float g = a.g[i];
-    adam_elem(p, g, m, v, job, a);
+    adam_elem(p, g, m, v, job, sc);
     a.p[i] = p;
     a.m[i] = m;
     a.v[i] = v;
@@ -97,7 +119,7 @@ __global__ void __launch_bounds__(kAdamThreads) adam_kernel(const __grid_constan
 }  // namespace
 
 cudaError_t launch_adam(const FFAdamParam* prm, int n, float beta1, float beta2, float eps, bool zero_grad,
-                        cudaStream_t st) {
+                        cudaStream_t st, const double* lr_dev, const int64_t* step_dev) {
   for (int b0 = 0; b0 < n; b0 += kMaxAdamParams) {
     AdamJob job = {};
     job.w1 = (float)(1.0 - (double)beta1);
@@ -105,6 +127,9 @@ cudaError_t launch_adam(const FFAdamParam* prm, int n, float beta1, float beta2,
     job.one_minus_beta2 = (float)(1.0 - (double)beta2);
     job.eps = eps;
     job.zero_grad = zero_grad ? 1 : 0;
+    job.beta1_d = (double)beta1;
+    job.beta2_d = (double)beta2;
+    job.step = step_dev;
     int cnt = 0;
     int64_t most = 0;
     for (int b = b0; b < n && cnt < kMaxAdamParams; ++b) {
@@ -117,10 +142,14 @@ cudaError_t launch_adam(const FFAdamParam* prm, int n, float beta1, float beta2,
       a.v = q.exp_avg_sq;
       a.shadow = static_cast<__nv_bfloat16*>(q.param_bf16);
       a.n = q.n;
-      const double bc1 = 1.0 - std::pow((double)beta1, (double)q.step);
-      const double bc2 = 1.0 - std::pow((double)beta2, (double)q.step);
-      a.neg_step_size = (float)(-(double)q.lr / bc1);
-      a.bc2_sqrt = (float)std::sqrt(bc2);
+      if (step_dev) {
+        a.lr = lr_dev + b;
+      } else {
+        const double bc1 = 1.0 - std::pow((double)beta1, (double)q.step);
+        const double bc2 = 1.0 - std::pow((double)beta2, (double)q.step);
+        a.neg_step_size = (float)(-(double)q.lr / bc1);
+        a.bc2_sqrt = (float)std::sqrt(bc2);
+      }
       most = std::max(most, q.n);
     }
     if (cnt == 0) continue;

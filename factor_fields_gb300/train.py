@@ -71,13 +71,20 @@ class RadianceFieldTrainer:
         if side is not None:
             torch.cuda.current_stream().wait_stream(side)
         if optimize:
-            self.opt.step()
+            self._update()
+        return loss.detach()
+
+    def _update(self):
+        """Adam on the field (lr decayed by lr_factor per step) and the proposal network."""
+        self.opt.step()
+        if self.fused_adam:
+            self.opt.decay_lr(self.lr_factor)
+        else:
             for g in self.opt.param_groups:
                 g["lr"] = g["lr"] * self.lr_factor
-            if self.sampler is not None:
-                self.sampler.step()
-            self._grads_clean = self.fused_adam and (self.sampler is None or self.sampler.fused_adam)
-        return loss.detach()
+        if self.sampler is not None:
+            self.sampler.step()
+        self._grads_clean = self.fused_adam and (self.sampler is None or self.sampler.fused_adam)
 
     def _plain_step_static(self, rays, rgb_gt):
         """The plain sampler's fwd+bwd training step without autograd and without host reads
@@ -96,41 +103,69 @@ class RadianceFieldTrainer:
         sh_render_backward(job, jitter, saved, diff * (2.0 / diff.numel()))
         return loss
 
-    def graph_step(self, rays, rgb_gt):
-        """step(optimize=False) replayed from a CUDA graph. The batch is copied into static
-        buffers; the capture covers the gradient zeroing, rendering, loss, the field backward and
-        (proposal sampler) the proposal loss/backward. The plain sampler's step is captured as the
-        explicit _plain_step_static (no autograd, no host reads: live-sample buffers sized for all
-        n_rays * n_samples slots, the live count read on the device; fused BF16 path, SH-2 head).
-        The per-ray jitter is drawn inside the graph (or self.jitter). Re-captured when the batch
-        shape changes."""
+    def graph_step(self, rays, rgb_gt, optimize=False):
+        """step(optimize) replayed from a CUDA graph. The batch is copied into static buffers;
+        the capture covers the gradient zeroing, rendering, loss, the field backward and
+        (proposal sampler) the proposal loss/backward, and with optimize=True the fused Adam
+        updates of the field (with its learning-rate decay) and the proposal network. The plain
+        sampler's step is captured as the explicit _plain_step_static (no autograd, no host reads:
+        live-sample buffers sized for all n_rays * n_samples slots, the live count read on the
+        device; fused BF16 path, SH-2 head). The per-ray jitter is drawn inside the graph (or
+        self.jitter). Re-captured when the batch shape changes.
+
+        optimize=True needs FusedAdam for the field and the proposal network (fused_adam=True):
+        the optimizers switch to their device schedule (step counts and learning rates in device
+        memory, FusedAdam.enable_device_schedule) at the first capture, and the update zeroes the
+        gradients for the next replay."""
         static = self.sampler is None
-        key = (tuple(rays.shape), tuple(rgb_gt.shape))
-        if getattr(self, "_gkey", None) != key:
+        if optimize and not (self.fused_adam and (self.sampler is None or self.sampler.fused_adam)):
+            raise ValueError("graph_step(optimize=True) needs fused_adam=True")
+        key = (tuple(rays.shape), tuple(rgb_gt.shape), bool(optimize))
+        graphs = self.__dict__.setdefault("_rgraphs", {})
+        ent = graphs.get(key)
+        if ent is None:
             dev = self.m.basis_flat.device
-            self._gr = torch.empty(rays.shape, dtype=torch.float32, device=dev)
-            self._gg = torch.empty(rgb_gt.shape, dtype=torch.float32, device=dev)
-            self._gr.copy_(rays)
-            self._gg.copy_(rgb_gt)
+            gr = torch.empty(rays.shape, dtype=torch.float32, device=dev)
+            gg = torch.empty(rgb_gt.shape, dtype=torch.float32, device=dev)
+            gr.copy_(rays)
+            gg.copy_(rgb_gt)
+            fwd_bwd = (lambda: self._plain_step_static(gr, gg)) if static else \
+                (lambda: self.step(gr, gg, optimize=False))
             side = torch.cuda.Stream()
             side.wait_stream(torch.cuda.current_stream())
-            body = (lambda: self._plain_step_static(self._gr, self._gg)) if static else \
-                (lambda: self.step(self._gr, self._gg, optimize=False))
-            with torch.cuda.stream(side):
+            with torch.cuda.stream(side):  # warm-up (kernel attributes, workspaces) without updates
                 for _ in range(2):
-                    body()
+                    fwd_bwd()
             torch.cuda.current_stream().wait_stream(side)
-            self._graph = torch.cuda.CUDAGraph()
-            with torch.cuda.graph(self._graph):
-                self._gloss = body()
-            self._gkey = key
+            if optimize:
+                self.opt.enable_device_schedule()
+                if self.sampler is not None:
+                    self.sampler.opt.enable_device_schedule()
+                self._zero_grads()  # the warm-up's gradients; each replay's update zeroes its own
+                self._grads_clean = True
+
+                def body():
+                    loss = fwd_bwd()
+                    self._update()
+                    return loss
+            else:
+                body = fwd_bwd
+            graph = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(graph):
+                loss = body()
+            # the captured body zeroes the gradients first unless an update leaves them clean
+            ent = {"graph": graph, "loss": loss, "rays": gr, "gt": gg, "clean_after": bool(optimize)}
+            graphs[key] = ent
         self.m._read_buffers()
         if self.sampler is not None:
             self.sampler.grid_read()
-        self._gr.copy_(rays, non_blocking=True)
-        self._gg.copy_(rgb_gt, non_blocking=True)
-        self._graph.replay()
-        return self._gloss
+        if optimize and not self._grads_clean:  # the captured update step does not zero first
+            self._zero_grads()
+        ent["rays"].copy_(rays, non_blocking=True)
+        ent["gt"].copy_(rgb_gt, non_blocking=True)
+        ent["graph"].replay()
+        self._grads_clean = ent["clean_after"]
+        return ent["loss"]
 
     @torch.no_grad()
     def psnr(self, rays, rgb_gt, chunk=16384):

@@ -262,6 +262,15 @@ enum { FF_ADAM_ZERO_GRAD = 1 };
  * BF16 copy, and with FF_ADAM_ZERO_GRAD the gradient set to 0 (the next step's zero_grad). */
 FF_API int ff_adam_step(const FFAdamParam* params, int32_t n_params, float beta1, float beta2, float eps,
                         int32_t flags, void* stream);
+/* ff_adam_step with the schedule in device memory, for a training step captured in a CUDA graph
+ * (a replay reads the current values; the launch arguments hold only pointers): lr[b] (float64)
+ * is parameter b's learning rate and *step (int64, >= 1 when the kernels run) the step number t
+ * after this update, shared by all n_params parameters; the entries' lr and step fields are not
+ * read. The bias corrections 1 - beta^t are formed in double precision on the device, as
+ * torch.optim.Adam forms them in Python floats. The caller advances *step (and decays lr) on the
+ * stream before the call. */
+FF_API int ff_adam_step_scheduled(const FFAdamParam* params, int32_t n_params, float beta1, float beta2, float eps,
+                                  int32_t flags, const double* lr, const int64_t* step, void* stream);
 
 /* ---- evaluation metrics (renderer.py:30-98, utils.py:110-156) ------------------------------ */
 /* Mean squared error and SSIM of two [height][width][channels] float32 device images, SSIM as

@@ -65,6 +65,9 @@ def test_argument_validation_before_any_launch(lib):
     arr[0].step = 0
     assert lib.ff_adam_step(ctypes.cast(arr, vp), 1, 0.9, 0.99, 1e-8, 0, None) == N.FF_ERR_ARG
     assert b"step" in lib.ff_last_error()
+    # the scheduled form reads lr and step from device memory: both pointers are required
+    assert lib.ff_adam_step_scheduled(ctypes.cast(arr, vp), 1, 0.9, 0.99, 1e-8, 0, None, vp(16), None) == N.FF_ERR_ARG
+    assert lib.ff_adam_step_scheduled(ctypes.cast(arr, vp), 1, 0.9, 0.99, 1e-8, 0, vp(16), vp(12), None) == N.FF_ERR_ALIGN
     # ff_zero_f32: NULL buffer with a count
     ptrs = (vp * 1)(None)
     counts = (ctypes.c_int64 * 1)(5)
