@@ -929,7 +929,9 @@ def run_profile_case(case, level0_shared, dev):
       fit:cfg0 / fit:cfg1 / fit:cfg4  one binned fit step of the configuration (its batch size)
       radiance_fwd    the 28-wide field forward on a 4,096-ray batch's live samples (plain sampler,
                       300 training steps, occupancy volume updated at step 100)
-      proposal_render the proposal head and resampling of a 400x400 view (160,000 rays, 32 samples)"""
+      proposal_render the proposal head and resampling of a 400x400 view (160,000 rays, 32 samples)
+      train:plain / train:proposal  two whole training steps (4,096 rays, fwd + bwd + the fused
+                      Adam updates) replayed from their CUDA graph after 300 eager training steps"""
     from factor_fields_gb300 import workloads as W
     from factor_fields_gb300 import train as T
     if case.startswith("fit:"):
@@ -981,6 +983,31 @@ def run_profile_case(case, level0_shared, dev):
             torch.cuda.synchronize()
             torch.cuda.profiler.start()
             s.render(rays, is_train=False)
+    elif case in ("train:plain", "train:proposal"):
+        from factor_fields_gb300 import FactorFields
+        from factor_fields_gb300.proposal import ProposalSampler
+        scene = W.BlobScene(0)
+        pool = torch.from_numpy(scene.ray_pool(1 << 16, 5)).float()
+        gt = scene.render_gt(pool.double().numpy(), n_steps=256).to(dev)
+        pool = pool.to(dev)
+        torch.manual_seed(0)
+        m = FactorFields(W.field_cfg("cfg2"), device=dev, precision="bf16")
+        sampler = ProposalSampler(m, seed=0) if case == "train:proposal" else None
+        tr = T.RadianceFieldTrainer(m, n_samples=1024, n_iters=300, sampler=sampler)
+        g = torch.Generator(device=dev).manual_seed(0)
+        for it in range(300):
+            idx = torch.randint(0, pool.shape[0], (4096,), device=dev, generator=g)
+            tr.step(pool[idx], gt[idx])
+            if it == 100 and sampler is None:
+                m.updateAlphaMask((128, 128, 128), is_update_alphaMask=True, times=1)
+        for it in range(5):
+            idx = torch.randint(0, pool.shape[0], (4096,), device=dev, generator=g)
+            tr.graph_step(pool[idx], gt[idx], optimize=True)
+        torch.cuda.synchronize()
+        torch.cuda.profiler.start()
+        for it in range(2):
+            idx = torch.randint(0, pool.shape[0], (4096,), device=dev, generator=g)
+            tr.graph_step(pool[idx], gt[idx], optimize=True)
     else:
         raise SystemExit(f"unknown --profile-case {case!r}")
     torch.cuda.synchronize()

@@ -266,8 +266,9 @@ FF_API int ff_adam_step(const FFAdamParam* params, int32_t n_params, float beta1
  * (a replay reads the current values; the launch arguments hold only pointers): lr[b] (float64)
  * is parameter b's learning rate and *step (int64, >= 1 when the kernels run) the step number t
  * after this update, shared by all n_params parameters; the entries' lr and step fields are not
- * read. The bias corrections 1 - beta^t are formed in double precision on the device, as
- * torch.optim.Adam forms them in Python floats. The caller advances *step (and decays lr) on the
+ * read. The bias corrections 1 - beta^t are formed on the device in float32 (beta^t =
+ * exp2(t log2 beta)): the step size is within a few ulp of ff_adam_step's, which forms them in
+ * double precision as torch.optim.Adam does. The caller advances *step (and decays lr) on the
  * stream before the call. */
 FF_API int ff_adam_step_scheduled(const FFAdamParam* params, int32_t n_params, float beta1, float beta2, float eps,
                                   int32_t flags, const double* lr, const int64_t* step, void* stream);

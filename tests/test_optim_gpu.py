@@ -87,9 +87,9 @@ def test_trainer_with_fused_adam_trains_like_torch_adam():
 def test_scheduled_adam_matches_host_schedule():
     """FusedAdam under its device schedule (ff_adam_step_scheduled: step count and learning rates
     in device memory, decayed on the device) against the host schedule (ff_adam_step): five steps
-    with an lr decay after each, two groups; parameters and moments agree to the rounding of the
-    bias corrections (formed in double precision on either side), and sync_host() returns the
-    host schedule's step counts and learning rates exactly."""
+    with an lr decay after each, two groups; the moments agree exactly, the parameters to the
+    rounding of the step size (float32 bias corrections on the device, double on the host), and
+    sync_host() returns the host schedule's step counts and learning rates exactly."""
     from factor_fields_gb300.optim import FusedAdam
     gen = torch.Generator().manual_seed(1)
     sizes = [5, 1024, 4099]
@@ -114,7 +114,8 @@ def test_scheduled_adam_matches_host_schedule():
         opt_d.decay_lr(0.93)
     torch.cuda.synchronize()
     for a, b in zip(host, devs):
-        assert torch.allclose(a, b, rtol=1e-6, atol=0)
+        # a few ulp of a step of at most lr = 2e-2 per step
+        assert torch.allclose(a, b, rtol=1e-6, atol=1e-7)
         assert torch.allclose(opt_h.state[a]["exp_avg"], opt_d.state[b]["exp_avg"], rtol=0, atol=0)
         assert torch.allclose(opt_h.state[a]["exp_avg_sq"], opt_d.state[b]["exp_avg_sq"], rtol=0, atol=0)
         assert float(b.grad.abs().max()) == 0.0
