@@ -412,3 +412,39 @@ def test_trained_state_against_unrounded_reference():
     assert abs(loss - float((err * err).mean())) <= 2e-2 * float((err * err).mean())
     _, ref = oracle_fwd_bwd(m, x, 2 * (oracle_fwd_bwd(m, x, None)[0] - y) / err.size)  # the stored model
     check_grads(m, ref)
+
+
+def test_host_batch_from_pageable_memory_through_the_abi():
+    """ff_field_fit_step_binned with FF_FIT_HOST_BATCH on pageable host arrays (numpy, as a
+    binding would hand them over; the copy is then synchronous) gives the device batch's loss
+    and gradients."""
+    import ctypes
+    from factor_fields_gb300 import FactorFields
+    from factor_fields_gb300 import _native as N
+    from factor_fields_gb300 import functional as FN
+    from factor_fields_gb300 import workloads as W
+    from factor_fields_gb300.train import FieldFitRunner
+    torch.manual_seed(0)
+    m = FactorFields(W.field_cfg("cfg1"), device="cuda", precision="bf16")
+    r = FieldFitRunner(m, loss="l1")
+    xs, ys = W.sdf_batch(7, 5000)
+    xs, ys = np.ascontiguousarray(xs, dtype=np.float32), np.ascontiguousarray(ys, dtype=np.float32)
+    l_dev = float(r.step(torch.from_numpy(xs).cuda(), torch.from_numpy(ys).cuda()))
+    g_dev = [p.grad.clone() for p in r._params()]
+    basis_r, coeff_r, dt = m._read_buffers()
+    desc = m.descriptor(dt)
+    ws_, bs_ = m.linear_mat.weights()
+    mlp = FN.mlp_struct(ws_, bs_, m.linear_mat.in_dim, m.linear_mat.hidden_dim, m.linear_mat.out_dim)
+    n = xs.shape[0]
+    ws = r._workspace(desc, n)
+    lbuf = torch.zeros(1, device="cuda")
+    g = r._grad_struct()
+    N.call("ff_field_fit_step_binned", ctypes.byref(desc), N.ptr(basis_r), N.ptr(coeff_r), ctypes.byref(mlp),
+           xs.ctypes.data_as(ctypes.c_void_p), ys.ctypes.data_as(ctypes.c_void_p), n, N.FF_LOSS["l1"], 1.0 / n,
+           N.ptr(lbuf), N.ptr(m.basis_flat.grad), N.ptr(m.coeff_flat.grad), ctypes.byref(g),
+           N.FF_FIT_ZERO_GRADS | N.FF_FIT_MEAN_LOSS | N.FF_FIT_HOST_BATCH, N.ptr(ws), ws.numel(), N.stream_ptr(),
+           kernels=4)
+    torch.cuda.synchronize()
+    assert abs(float(lbuf[0]) - l_dev) <= 1e-6 * max(1.0, abs(l_dev))
+    for a, p in zip(g_dev, r._params()):
+        assert torch.allclose(a, p.grad, rtol=1e-5, atol=1e-9)
