@@ -408,14 +408,18 @@ __device__ __forceinline__ void scatter_inside(float* __restrict__ grad, int str
 // All 18 coefficient channels of every valid corner with 16-byte loads (channels 0..15) and
 // one 4- (BF16) or 8-byte (float32) load for channels 16, 17. Needs coeff_stride % 8 == 0.
 // Corner sets as in gather_inside (all: every corner; else slot 0 only).
-template <int D>
+// kSkipZero: corners of zero weight are not loaded. For image-set lookups (a 2-D basis with a 3-D
+// coefficient volume over (x, y, image)) the image coordinate sits on a voxel centre, so half of
+// the 8 corners carry weight 0; elsewhere zero weights are rare and the test costs more than it
+// saves.
+template <int D, bool kSkipZero = false>
 __device__ __forceinline__ void gather_coeff18(const __nv_bfloat16* __restrict__ grid, int stride, const Corners<D>& cn,
                                                bool all, float* acc) {
 #pragma unroll
   for (int v = 0; v < 18; ++v) acc[v] = 0.f;
 #pragma unroll
   for (int k = 0; k < Corners<D>::K; ++k) {
-    if (k == 0 || all) {
+    if ((k == 0 || all) && (!kSkipZero || cn.w[k] != 0.f)) {
       const __nv_bfloat16* p = grid + (int64_t)cn.idx[k] * stride;
       const uint4 a = __ldg(reinterpret_cast<const uint4*>(p));
       const uint4 b = __ldg(reinterpret_cast<const uint4*>(p + 8));
@@ -431,14 +435,14 @@ __device__ __forceinline__ void gather_coeff18(const __nv_bfloat16* __restrict__
   }
 }
 
-template <int D>
+template <int D, bool kSkipZero = false>
 __device__ __forceinline__ void gather_coeff18(const float* __restrict__ grid, int stride, const Corners<D>& cn,
                                                bool all, float* acc) {
 #pragma unroll
   for (int v = 0; v < 18; ++v) acc[v] = 0.f;
 #pragma unroll
   for (int k = 0; k < Corners<D>::K; ++k) {
-    if (k == 0 || all) {
+    if ((k == 0 || all) && (!kSkipZero || cn.w[k] != 0.f)) {
       const float* p = grid + (int64_t)cn.idx[k] * stride;
       const float wk = cn.w[k];
 #pragma unroll

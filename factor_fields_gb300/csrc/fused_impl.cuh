@@ -216,7 +216,7 @@ __device__ __forceinline__ void scatter_shared4(float* g0, const Corners<D>& cn,
 // atomics per corner, so a cell's corners take one atomic per segment instead of one per point.
 // On an unbinned batch every segment has length 1 and this is the plain per-point scatter.
 // gs: this warp's [32][LD_XF] float tile (free: dX has been read), ws: [32][8] floats.
-template <int CD>
+template <int CD, bool kSkipZero = false>
 __device__ __forceinline__ void coop_coeff_scatter(float* __restrict__ grad, int stride, const Corners<CD>& cc,
                                                    const float* gc, bool valid, float* gs, float* ws, int lane) {
   constexpr int K = Corners<CD>::K;
@@ -241,8 +241,10 @@ __device__ __forceinline__ void coop_coeff_scatter(float* __restrict__ grad, int
 #pragma unroll
   for (int k = 0; k < 18; ++k) acc[k] = 0.f;
   int c = lane - s0, j = 0;
+  bool any = !kSkipZero;  // kSkipZero: a corner of zero weight over the whole segment gets no atomics
   while (c < K) {
     const float w = ws[(s0 + j) * 8 + c];
+    if (kSkipZero) any |= w != 0.f;
     const float* g = gs + (s0 + j) * LD_XF;
 #pragma unroll
     for (int k = 0; k < 16; k += 4) {
@@ -257,7 +259,7 @@ __device__ __forceinline__ void coop_coeff_scatter(float* __restrict__ grad, int
 #pragma unroll
       for (int q = 0; q < K; ++q)
         if (q == c) idx = cc.idx[q];
-      if (idx >= 0) {
+      if (idx >= 0 && any) {
         float* p = grad + (int64_t)idx * stride;
 #pragma unroll
         for (int k = 0; k < 4; ++k)
@@ -267,6 +269,7 @@ __device__ __forceinline__ void coop_coeff_scatter(float* __restrict__ grad, int
 #pragma unroll
       for (int k = 0; k < 18; ++k) acc[k] = 0.f;
       j = 0;
+      any = !kSkipZero;
       c += L;
     }
   }
@@ -340,7 +343,8 @@ __global__ void __launch_bounds__(kThreads, is_fwd<MODE>() ? 4 : 3) fused_field_
       }
       Corners<CD> cc;
       coeff_corners<CD, true>(f, p, cc);
-      gather_coeff18<CD>(coeff, f.coeff_stride, cc, f.coeff_interp != FF_INTERP_NEAREST, cv);
+      // image sets (2-D basis, coefficient volume over (x, y, image)): half the corners weigh 0
+      gather_coeff18<CD, BD == 2 && CD == 3>(coeff, f.coeff_stride, cc, f.coeff_interp != FF_INTERP_NEAREST, cv);
       const bool all_b = f.basis_interp != FF_INTERP_NEAREST;
       for_levels(std::make_integer_sequence<int, 6>{}, [&](auto lc) {
         constexpr int l = decltype(lc)::value;
@@ -746,7 +750,7 @@ __global__ void __launch_bounds__(kThreads, is_fwd<MODE>() ? 4 : 3) fused_field_
           }
         }
         // scratch for the segment weights: this warp's dH (out_dim 1) or H tile, both consumed
-        coop_coeff_scatter<CD>(a.grad_coeff, f.coeff_stride, cc, gc, valid, xf,
+        coop_coeff_scatter<CD, BD == 2 && CD == 3>(a.grad_coeff, f.coeff_stride, cc, gc, valid, xf,
                                reinterpret_cast<float*>((OUTT == 1 ? s.dh : s.h) + warp * 32 * LD_H), lane);
       } else if (valid) {
         float gc[kF];
