@@ -117,6 +117,12 @@ class FusedAdam(torch.optim.Optimizer):
         self.sync_host()
         return super().state_dict()
 
+    def load_state_dict(self, state_dict):
+        """Loads as torch's optimizers do; a device schedule is dropped (its step count and learning
+        rates would be stale) and must be enabled again, which rebuilds it from the loaded state."""
+        super().load_state_dict(state_dict)
+        self._dev = None
+
     @torch.no_grad()
     def step(self, closure=None):
         loss = None

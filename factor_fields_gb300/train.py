@@ -86,6 +86,11 @@ class RadianceFieldTrainer:
             self.sampler.step()
         self._grads_clean = self.fused_adam and (self.sampler is None or self.sampler.fused_adam)
 
+    def _schedules(self):
+        """The optimizers' device schedules (what a captured update step reads; compared by identity)."""
+        return (getattr(self.opt, "_dev", None),
+                getattr(self.sampler.opt, "_dev", None) if self.sampler is not None else None)
+
     def _plain_step_static(self, rays, rgb_gt):
         """The plain sampler's fwd+bwd training step without autograd and without host reads
         (the body of its CUDA graph): gradients zeroed, static render forward, MSE, its gradient
@@ -116,13 +121,18 @@ class RadianceFieldTrainer:
         optimize=True needs FusedAdam for the field and the proposal network (fused_adam=True):
         the optimizers switch to their device schedule (step counts and learning rates in device
         memory, FusedAdam.enable_device_schedule) at the first capture, and the update zeroes the
-        gradients for the next replay."""
+        gradients for the next replay. A load_state_dict of either optimizer (which drops its
+        device schedule and replaces the moment buffers) makes the next call capture again. The
+        captured decay multiplies by the lr_factor of capture time: after changing lr_factor, drop
+        self._rgraphs."""
         static = self.sampler is None
         if optimize and not (self.fused_adam and (self.sampler is None or self.sampler.fused_adam)):
             raise ValueError("graph_step(optimize=True) needs fused_adam=True")
         key = (tuple(rays.shape), tuple(rgb_gt.shape), bool(optimize))
         graphs = self.__dict__.setdefault("_rgraphs", {})
         ent = graphs.get(key)
+        if ent is not None and optimize and any(a is not b for a, b in zip(ent["sched"], self._schedules())):
+            ent = None  # an optimizer dropped its device schedule (load_state_dict): capture again
         if ent is None:
             dev = self.m.basis_flat.device
             gr = torch.empty(rays.shape, dtype=torch.float32, device=dev)
@@ -154,7 +164,8 @@ class RadianceFieldTrainer:
             with torch.cuda.graph(graph):
                 loss = body()
             # the captured body zeroes the gradients first unless an update leaves them clean
-            ent = {"graph": graph, "loss": loss, "rays": gr, "gt": gg, "clean_after": bool(optimize)}
+            ent = {"graph": graph, "loss": loss, "rays": gr, "gt": gg, "clean_after": bool(optimize),
+                   "sched": self._schedules() if optimize else None}
             graphs[key] = ent
         self.m._read_buffers()
         if self.sampler is not None:

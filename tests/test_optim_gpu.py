@@ -177,3 +177,36 @@ def test_graph_step_with_update_trains_like_eager_step(proposal):
     for a, b in ((0, 10), (25, 35), (50, 60)):
         assert abs(lg[a:b].mean() - le[a:b].mean()) < 0.02 * le[a:b].mean(), (a, lg[a:b].mean(), le[a:b].mean())
     assert lg[-10:].mean() < lg[:10].mean()  # it trains
+
+
+def test_graph_step_with_update_after_load_state_dict():
+    """A load_state_dict of the optimizer drops its device schedule and replaces its moment
+    buffers; the next graph_step(optimize=True) captures again and continues from the loaded
+    step count and learning rates."""
+    import copy
+    from factor_fields_gb300 import FactorFields
+    from factor_fields_gb300 import workloads as W
+    from factor_fields_gb300.train import RadianceFieldTrainer
+    scene = W.BlobScene(0)
+    pool = torch.from_numpy(scene.ray_pool(1 << 12, 5)).float().cuda()
+    gt = torch.rand(pool.shape[0], 3, device="cuda")
+    torch.manual_seed(0)
+    m = FactorFields(W.field_cfg("cfg2"), device="cuda", precision="bf16")
+    m.cfg.renderer.density_shift = -4.0
+    tr = RadianceFieldTrainer(m, n_samples=128, n_iters=50)
+    rays, rgb = pool[:1024], gt[:1024]
+    for _ in range(5):
+        tr.graph_step(rays, rgb, optimize=True)
+    sd = copy.deepcopy(tr.opt.state_dict())  # step 5
+    lr5 = [g["lr"] for g in sd["param_groups"]]
+    for _ in range(3):
+        tr.graph_step(rays, rgb, optimize=True)
+    tr.opt.load_state_dict(sd)
+    assert not tr.opt.device_schedule
+    loss = tr.graph_step(rays, rgb, optimize=True)  # captured again from the loaded state
+    torch.cuda.synchronize()
+    assert torch.isfinite(loss)
+    tr.opt.sync_host()
+    assert sorted({int(s["step"]) for s in tr.opt.state.values()}) == [6]
+    for g, lr in zip(tr.opt.param_groups, lr5):
+        assert g["lr"] == lr * tr.lr_factor
