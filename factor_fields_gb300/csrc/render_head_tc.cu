@@ -4,7 +4,8 @@
 // of a tile = TMEM lane r):
 //
 // head_fwd16_kernel (the forward): FP16 operands, one MMA pass per layer, two tiles in flight
-// (two 8-warp groups with their own buffers, TMEM columns and barriers); described above it.
+// (512 threads software-pipelined over two tile buffers and their TMEM accumulators: the MMAs of
+// one tile run while the CUDA cores work on the other); described above it.
 //
 // head_tc_kernel (the backward, with the forward recomputed): 512 threads, warp w serves TMEM
 // lane quadrant w % 4 (rows 32 (w % 4) .. + 31) and the 32-column slice w / 4 of every 128-wide
