@@ -262,6 +262,16 @@ def measure_field(key, args, ws, rank, local, flush, with_dropin):
         e2e_step(i)
     t_e2e, _ = timed(e2e_step, args.steps, False)
 
+    # the notebooks' whole training step: the same graph-replayed fit with the fused Adam update
+    # (lr 1e-2) captured after it (FusedAdam's device schedule; it moves the parameters)
+    from factor_fields_gb300.optim import FusedAdam
+    opt = FusedAdam(m.parameters(), lr=1e-2, zero_grad=False, shadows=m.bf16_shadows())
+    trainer = T.FieldFitRunner(m, loss=fc["loss"], optimizer=opt)
+    trainer.capture_graphs(devb, optimize=True)
+    for i in range(args.warmup):
+        trainer.graph_step(*devb[i % nb], optimize=True)
+    t_adam, _ = timed(lambda i: trainer.graph_step(*devb[i % nb], optimize=True), args.steps, False)
+
     ms_drop = None
     if with_dropin:  # the float32 drop-in path (autograd through get_coding / linear_mat)
         md = make_model("fp32", key)
@@ -280,8 +290,8 @@ def measure_field(key, args, ws, rank, local, flush, with_dropin):
         t_drop, _ = timed(dropin_step, args.steps, False)
         ms_drop = float(np.sum(t_drop))
 
-    vals = max_over_ranks([ms, float(np.sum(t_e2e))] + ([ms_drop] if with_dropin else []))
-    ms, ms_e2e = vals[0], vals[1]
+    vals = max_over_ranks([ms, float(np.sum(t_e2e)), float(np.sum(t_adam))] + ([ms_drop] if with_dropin else []))
+    ms, ms_e2e, ms_adam = vals[0], vals[1], vals[2]
     pts = n * args.steps * ws
     kern_ms = float(np.mean(k_fast)) if k_fast else None  # the fit kernel alone
     # the whole ff_field_fit_step_binned call (binning with the gradient zeroing + the fit kernel):
@@ -309,9 +319,12 @@ def measure_field(key, args, ws, rank, local, flush, with_dropin):
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if "hbm_gbs" in peaks else "fallback"},
         "gpu_launches": per_step * args.steps,
         "clocks": ck,
+        # the notebooks' training step (fit + Adam), resident batches, L2 flushed per step as above
+        "train_with_adam": {"mode": "CUDA graph replay: binned fit + fused Adam (lr 1e-2, device schedule)",
+                            "value": pts / (ms_adam / 1e3), "unit": "samples/s", "ms_per_step": ms_adam / args.steps},
     }
     if with_dropin:
-        out["fp32_dropin"] = {"value": pts / (vals[2] / 1e3), "unit": "samples/s", "ms_per_step": vals[2] / args.steps}
+        out["fp32_dropin"] = {"value": pts / (vals[3] / 1e3), "unit": "samples/s", "ms_per_step": vals[3] / args.steps}
     return out, m
 
 
@@ -341,7 +354,7 @@ def run_native(args, ws, rank, local):
         "data": "synthetic (seeded analytic SDF: 16 spheres + 8 boxes)",
         "config": bench_config(ws), "path": r1["path"],
         "e2e": r1["e2e"], "fp32_dropin": r1["fp32_dropin"], "roofline": roof,
-        "gpu_launches": r1["gpu_launches"], "clocks": r1["clocks"],
+        "gpu_launches": r1["gpu_launches"], "clocks": r1["clocks"], "train_with_adam": r1["train_with_adam"],
     }
     if not args.no_field_configs:
         # the 2-D configurations: the image fit and the image set (shared basis, per-image coefficients)

@@ -198,9 +198,13 @@ class FieldFitRunner:
     coefficient gradients of points sharing a cell are summed on chip. fused=False: the drop-in
     kernels launched one after the other (field fwd, MLP fwd, MLP bwd, field bwd) with the loss
     in PyTorch. Gradients land in the model's .grad buffers; step() returns the mean loss as a
-    0-d device tensor (no host synchronisation)."""
+    0-d device tensor (no host synchronisation).
 
-    def __init__(self, model, loss="l1", fused=True, binned=None, level0_shared=False):
+    optimizer: a FusedAdam over the model's parameters (the notebooks' torch.optim.Adam), run by
+    step(..., optimize=True) and graph_step(..., optimize=True) after the backward. With the
+    binned path, FusedAdam(zero_grad=False) avoids a second zeroing: the step zeroes first."""
+
+    def __init__(self, model, loss="l1", fused=True, binned=None, level0_shared=False, optimizer=None):
         if loss not in N.FF_LOSS:
             raise ValueError("loss must be 'l1' or 'mse'")
         self.m, self.loss, self.fused = model, loss, fused
@@ -211,6 +215,7 @@ class FieldFitRunner:
         # (FF_FIT_LEVEL0_SHARED; no effect where the kernel does not support it)
         self.level0_shared = bool(level0_shared)
         self._l0 = N.FF_FIT_LEVEL0_SHARED if self.level0_shared else 0
+        self.opt = optimizer
         self._ws = None
         self._ws_gen = 0
         # the fused kernel's template arguments: mode, basis dim, coordinate dim, 8-wide output tiles
@@ -265,9 +270,11 @@ class FieldFitRunner:
 
     _GRAPHS_KEPT = 8  # graphs per kind of input pair read in place (device, host; least recently used first out)
 
-    def graph_step(self, x, y):
+    def graph_step(self, x, y, optimize=False):
         """step() replayed from a CUDA graph, one host call for all its launches (the binning with
-        the gradient zeroing, the fit kernel; the loss is the mean, accumulated by the kernel).
+        the gradient zeroing, the fit kernel; the loss is the mean, accumulated by the kernel;
+        with optimize=True the optimizer's update too, its step count and learning rates moved to
+        device memory at the first capture: FusedAdam.enable_device_schedule).
 
         Device batches (contiguous float32 on the model's device) are read in place: a graph is
         captured per input buffer pair and kept (up to 8), so that a ring of batches resident in
@@ -278,14 +285,15 @@ class FieldFitRunner:
         buffers whose graph then replays. Graphs are re-captured when the batch shape, a parameter
         buffer or the binning workspace changes. The returned 0-d loss belongs to the replayed
         graph: the next replay of the same graph overwrites it."""
-        key, kind = self._graph_key(x, y)
+        key, kind = self._graph_key(x, y, optimize)
         graphs = self.__dict__.setdefault("_graphs", OrderedDict())
         ent = graphs.get(key)
-        if ent is not None and ent["ws_gen"] != self._ws_gen:  # captured with a workspace since freed
+        if ent is not None and (ent["ws_gen"] != self._ws_gen  # captured with a workspace since freed
+                                or (optimize and ent["sched"] is not getattr(self.opt, "_dev", None))):
             del graphs[key]
             ent = None
         if ent is None:
-            ent = self._capture(x, y, kind)
+            ent = self._capture(x, y, kind, optimize)
             graphs[key] = ent
             for k in [k for k, e in graphs.items() if e["ws_gen"] != self._ws_gen]:
                 del graphs[k]
@@ -298,7 +306,7 @@ class FieldFitRunner:
         ent["graph"].replay()
         return ent["loss"]
 
-    def capture_graphs(self, batches):
+    def capture_graphs(self, batches, optimize=False):
         """Capture (without replaying) the graphs graph_step will use for these (x, y) batches,
         e.g. a ring of batches resident in HBM, so that no step pays for a capture."""
         graphs = self.__dict__.setdefault("_graphs", OrderedDict())
@@ -306,10 +314,10 @@ class FieldFitRunner:
             raise ValueError(f"at most {self._GRAPHS_KEPT} batches keep their graphs")
         kinds = set()
         for x, y in batches:
-            key, kind = self._graph_key(x, y)
+            key, kind = self._graph_key(x, y, optimize)
             kinds.add(kind)
             if key not in graphs or graphs[key]["ws_gen"] != self._ws_gen:
-                graphs[key] = self._capture(x, y, kind)
+                graphs[key] = self._capture(x, y, kind, optimize)
             graphs.move_to_end(key)
         for k in [k for k, e in graphs.items() if e["ws_gen"] != self._ws_gen]:
             del graphs[k]
@@ -335,7 +343,7 @@ class FieldFitRunner:
             raise ValueError("a host batch must be contiguous float32 in page-locked memory (tensor.pin_memory())")
         return N.FF_FIT_HOST_BATCH
 
-    def _graph_key(self, x, y):
+    def _graph_key(self, x, y, optimize=False):
         """(key, kind): kind "device" reads a device batch in place, "host" copies a pinned host
         batch inside the graph (FF_FIT_HOST_BATCH), "static" copies anything else into static
         device buffers before the replay."""
@@ -350,10 +358,10 @@ class FieldFitRunner:
         else:
             kind, tag = "static", ("static",)
         key = (tuple(x.shape), tuple(y.shape), self.m.basis_flat.data_ptr(), self.m.coeff_flat.data_ptr(),
-               self.m.precision) + tag
+               self.m.precision, bool(optimize)) + tag
         return key, kind
 
-    def _capture(self, x, y, kind):
+    def _capture(self, x, y, kind, optimize=False):
         dev = self.m.basis_flat.device
         if kind != "static":  # read in place: the device batch, or the host batch by the call's own copies
             xs, ys = x, y
@@ -368,11 +376,15 @@ class FieldFitRunner:
         with torch.cuda.stream(side):
             self.step(xs, ys, _loss_buf=loss_buf)  # warm-up outside the capture (kernel attributes, workspace)
         torch.cuda.current_stream().wait_stream(side)
+        if optimize:
+            if self.opt is None or not hasattr(self.opt, "enable_device_schedule"):
+                raise ValueError("graph_step(optimize=True) needs FieldFitRunner(..., optimizer=FusedAdam(...))")
+            self.opt.enable_device_schedule()
         graph = torch.cuda.CUDAGraph()
         with torch.cuda.graph(graph):
-            loss = self.step(xs, ys, _loss_buf=loss_buf)
+            loss = self.step(xs, ys, _loss_buf=loss_buf, optimize=optimize)
         return {"graph": graph, "loss": loss, "x": xs, "y": ys, "buf": loss_buf, "ws_gen": self._ws_gen,
-                "kind": kind}
+                "kind": kind, "sched": getattr(self.opt, "_dev", None) if optimize else None}
 
     def _workspace(self, desc, n):
         """Device workspace of ff_field_fit_step_binned for n points, kept across steps."""
@@ -384,9 +396,18 @@ class FieldFitRunner:
             self._ws_gen += 1
         return self._ws
 
-    def step(self, x, y, kernel_events=False, _loss_buf=None):
+    def step(self, x, y, kernel_events=False, _loss_buf=None, optimize=False):
         """One step on (x, y): device tensors, or (binned path) page-locked host tensors that the
-        call copies into its workspace itself (FF_FIT_HOST_BATCH)."""
+        call copies into its workspace itself (FF_FIT_HOST_BATCH). optimize=True: then the
+        optimizer's update (not with kernel_events)."""
+        if optimize and self.opt is None:
+            raise ValueError("optimize=True needs FieldFitRunner(..., optimizer=FusedAdam(...))")
+        loss = self._fwd_bwd(x, y, kernel_events, _loss_buf)
+        if optimize and not kernel_events:
+            self.opt.step()
+        return loss
+
+    def _fwd_bwd(self, x, y, kernel_events, _loss_buf):
         m = self.m
         host = self._host_batch(x, y)
         if not (self.fused and self.binned):  # the binned call zeroes them in its binning pass
