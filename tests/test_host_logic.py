@@ -240,3 +240,33 @@ def test_fit_runner_host_batch_rules():
         FieldFitRunner(m, loss="l1", fused=True, binned=False)._host_batch(x, y)
     with pytest.raises(ValueError, match="binned"):
         FieldFitRunner(m, loss="l1", fused=False)._host_batch(x, y)
+
+
+def test_fused_adam_device_schedule_host_logic():
+    """FusedAdam's device schedule bookkeeping without a GPU: enable_device_schedule takes every
+    parameter with a gradient (creating its Adam state), refuses mixed step counts, decays the
+    learning rates as float64 products exactly like the host schedule, and sync_host /
+    state_dict write them back; load_state_dict drops the schedule."""
+    import pytest
+    import torch
+    from factor_fields_gb300.optim import FusedAdam
+    ps = [torch.nn.Parameter(torch.zeros(5)), torch.nn.Parameter(torch.zeros(3)), torch.nn.Parameter(torch.zeros(2))]
+    for p in ps[:2]:
+        p.grad = torch.zeros_like(p)  # ps[2] has no gradient: not scheduled
+    opt = FusedAdam([{"params": ps[:1], "lr": 2e-2}, {"params": ps[1:], "lr": 1e-3}], betas=(0.9, 0.99))
+    opt.enable_device_schedule()
+    assert opt.device_schedule and len(opt.state) == 2
+    lrs = [2e-2, 1e-3]
+    for _ in range(7):
+        opt.decay_lr(0.93)
+        lrs = [v * 0.93 for v in lrs]
+    opt._dev["t"] += 7  # what seven replayed updates would have counted
+    sd = opt.state_dict()  # synchronises first
+    assert [g["lr"] for g in sd["param_groups"]] == lrs
+    assert all(int(s["step"]) == 7 for s in sd["state"].values())
+    opt.load_state_dict(sd)
+    assert not opt.device_schedule
+    # mixed step counts cannot share one device counter
+    opt.state[ps[0]]["step"] = torch.tensor(3.0)
+    with pytest.raises(ValueError, match="same step"):
+        opt.enable_device_schedule()
