@@ -270,3 +270,15 @@ def test_fused_adam_device_schedule_host_logic():
     opt.state[ps[0]]["step"] = torch.tensor(3.0)
     with pytest.raises(ValueError, match="same step"):
         opt.enable_device_schedule()
+
+
+def test_fit_runner_optimize_needs_an_optimizer():
+    import pytest
+    import torch
+    from factor_fields_gb300 import FactorFields
+    from factor_fields_gb300 import workloads as W
+    from factor_fields_gb300.train import FieldFitRunner
+    m = FactorFields(W.field_cfg("cfg1"), device="cpu", precision="bf16")
+    r = FieldFitRunner(m, loss="l1")
+    with pytest.raises(ValueError, match="optimizer"):
+        r.step(torch.zeros(4, 3), torch.zeros(4, 1), optimize=True)
