@@ -942,6 +942,7 @@ def run_profile_case(case, level0_shared, dev):
       fit:cfg0 / fit:cfg1 / fit:cfg4  one binned fit step of the configuration (its batch size)
       radiance_fwd    the 28-wide field forward on a 4,096-ray batch's live samples (plain sampler,
                       300 training steps, occupancy volume updated at step 100)
+      radiance_bwd    the 28-wide field backward on the same samples
       proposal_render the proposal head and resampling of a 400x400 view (160,000 rays, 32 samples)
       train:plain / train:proposal  two whole training steps (4,096 rays, fwd + bwd + the fused
                       Adam updates) replayed from their CUDA graph after 300 eager training steps"""
@@ -958,8 +959,11 @@ def run_profile_case(case, level0_shared, dev):
         torch.cuda.synchronize()
         torch.cuda.profiler.start()
         r.step(x, y)
-    elif case == "radiance_fwd":
+    elif case in ("radiance_fwd", "radiance_bwd"):
+        import ctypes
         from factor_fields_gb300 import FactorFields
+        from factor_fields_gb300 import _native as N
+        from factor_fields_gb300 import functional as FN
         from factor_fields_gb300.renderer import field_eval, march, render_desc
         scene = W.BlobScene(0)
         pool = torch.from_numpy(scene.ray_pool(1 << 16, 5)).float()
@@ -978,11 +982,29 @@ def run_profile_case(case, level0_shared, dev):
         _, xyz, _ = march(m, pool[idx], None, render_desc(m, 1024, True))
         basis_r, coeff_r, dt = m._read_buffers()
         job = {"fused": True, "fdesc": m.descriptor(dt), "basis_r": basis_r, "coeff_r": coeff_r}
+        if case == "radiance_fwd":
+            run = lambda: field_eval(m, job, xyz)  # noqa: E731
+        else:  # the field backward (ff_field_mlp_backward) on the same samples, scratch gradients
+            lm = m.linear_mat
+            ws_, bs_ = lm.weights()
+            mlp = FN.mlp_struct(ws_, bs_, lm.in_dim, lm.hidden_dim, lm.out_dim)
+            n = xyz.shape[0]
+            g_out = torch.randn(n, lm.out_dim, device=dev, generator=g) * 1e-3
+            gbas, gcoef = torch.zeros_like(m.basis_flat), torch.zeros_like(m.coeff_flat)
+            gw = [torch.zeros_like(w) for w in ws_]
+            gbias = [torch.zeros_like(b) if b is not None else None for b in bs_]
+            grad = N.FFMlpGrad()
+            for i in range(len(ws_)):
+                grad.weight[i] = gw[i].data_ptr()
+                grad.bias[i] = gbias[i].data_ptr() if gbias[i] is not None else None
+            run = lambda: N.call("ff_field_mlp_backward", ctypes.byref(job["fdesc"]), N.ptr(basis_r),  # noqa: E731
+                                 N.ptr(coeff_r), ctypes.byref(mlp), N.ptr(xyz), n, N.ptr(g_out), N.ptr(gbas),
+                                 N.ptr(gcoef), ctypes.byref(grad), N.stream_ptr())
         for _ in range(3):
-            field_eval(m, job, xyz)
+            run()
         torch.cuda.synchronize()
         torch.cuda.profiler.start()
-        field_eval(m, job, xyz)
+        run()
     elif case == "proposal_render":
         from factor_fields_gb300 import FactorFields
         from factor_fields_gb300.proposal import ProposalSampler
