@@ -209,9 +209,12 @@ def measure_field(key, args, ws, rank, local, flush, with_dropin):
         times, ktimes = [], []
         for i in range(k):
             if with_kernel_events and ws == 1:
-                # no host sync after the flush: the GPU is still writing the 256 MB while the
-                # host enqueues the step, so the kernel events see device time, not enqueue gaps
+                # no host sync after the flush: the GPU is still busy (a ~1 ms spin, then the
+                # 256 MB flush) while the host enqueues the step, so the kernel events see device
+                # time, not enqueue gaps (on a slow host the flush alone did not cover the Python
+                # between the two halves of the call)
                 torch.cuda.synchronize()
+                torch.cuda._sleep(2_000_000)
                 flush_l2(flush)
             else:
                 flush_l2(flush)
@@ -435,6 +438,7 @@ def measure_radiance_field_kernels(m, rays, dev, flush, steps, warmup, seed=3):
         for _ in range(steps):
             flush.zero_()
             torch.cuda.synchronize()
+            torch.cuda._sleep(2_000_000)  # the GPU spins (~1 ms) while the host enqueues: no launch gap timed
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(stream)
             fn()
@@ -521,6 +525,7 @@ def measure_adam(opt, steps, warmup):
     ts = []
     for _ in range(steps):
         torch.cuda.synchronize()
+        torch.cuda._sleep(2_000_000)  # the GPU stays busy while the host enqueues the five updates
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
         for _ in range(5):
@@ -789,6 +794,7 @@ def measure_mlp_head(args, dev, flush):
         ts = []
         for _ in range(k):
             torch.cuda.synchronize()
+            torch.cuda._sleep(2_000_000)  # the GPU stays busy while the host enqueues the timed launch
             flush.zero_()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record()
